@@ -1,0 +1,255 @@
+// Batched small-block linear algebra (9x9 camera and 3x3 point blocks), the
+// damped point-block inverse, the point back-substitution, the LM gain
+// denominator and the trial-parameter update.
+//
+// Reference counterparts: schur.cuh:23-116 (chol9 factor/solve, inverse3_spd,
+// batch kernels), src/lm.cu:289-302 (damp_invert_v_kernel) and the host loops
+// src/lm.cu:606-654 (back-substitution, denominator, trial parameters), which
+// here run on the device with deterministic reductions.
+
+#include "blocks.cuh"
+#include "common.cuh"
+#include "solver.hpp"
+
+namespace gba {
+namespace {
+
+constexpr int kTB = 256;
+
+// V' = V + lambda * max(diag V, 1e-12) on the diagonal; Vinv = V'^-1 (packed).
+__global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __restrict__ V, double lambda, int P,
+                                                           double* __restrict__ Vinv,
+                                                           unsigned long long* __restrict__ nonspd) {
+    __shared__ unsigned long long redu[kTB / 32];
+    unsigned long long bad = 0;
+    for (int p = blockIdx.x * kTB + threadIdx.x; p < P; p += gridDim.x * kTB) {
+        double a[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a[k] = V[6ll * p + k];
+        a[0] += lambda * (a[0] > 0.0 ? a[0] : 1e-12);
+        a[2] += lambda * (a[2] > 0.0 ? a[2] : 1e-12);
+        a[5] += lambda * (a[5] > 0.0 ? a[5] : 1e-12);
+        double inv[6];
+        if (!blk::inverse3_packed(a, inv)) {
+            ++bad;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) inv[k] = 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) Vinv[6ll * p + k] = inv[k];
+    }
+    const unsigned long long nb = block_sum_u64<kTB>(bad, redu);
+    if (threadIdx.x == 0 && nb) atomicAdd(nonspd, nb);
+}
+
+__global__ void batch_chol9_kernel(const double* __restrict__ A, const double* __restrict__ b, double* __restrict__ x,
+                                   int* __restrict__ ok, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double L[45];
+    const bool good = blk::chol9_factor(A + 81ll * i, L);
+    ok[i] = good ? 1 : 0;
+    if (good) {
+        double xi[9], bi[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) bi[k] = b[9ll * i + k];
+        blk::chol9_solve(L, bi, xi);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) x[9ll * i + k] = xi[k];
+    }
+}
+
+__global__ void batch_inverse3_kernel(const double* __restrict__ A, double* __restrict__ Ainv, int* __restrict__ ok,
+                                      int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = A + 9ll * i;
+    const double pk[6] = {a[0], a[3], a[4], a[6], a[7], a[8]};  // lower triangle, row-major
+    double inv[6];
+    const bool good = blk::inverse3_packed(pk, inv);
+    ok[i] = good ? 1 : 0;
+    if (good) {
+        double* o = Ainv + 9ll * i;
+        o[0] = inv[0]; o[1] = inv[1]; o[2] = inv[3];
+        o[3] = inv[1]; o[4] = inv[2]; o[5] = inv[4];
+        o[6] = inv[3]; o[7] = inv[4]; o[8] = inv[5];
+    }
+}
+
+// Point back-substitution, FP64 W records (plain form):
+//   dp_p = V'^-1_p (bp_p - sum_{e in p} W_e^T dc_{c(e)}),  tpts = pts + dp,
+// and the point part of the gain denominator sum dp (lambda d dp + bp).
+__global__ void __launch_bounds__(kTB) backsub_points_w64(
+    const int* __restrict__ pt_off, const int* __restrict__ s_cam, const double* __restrict__ W,
+    const double* __restrict__ dc, const double* __restrict__ V, const double* __restrict__ Vinv,
+    const double* __restrict__ bp, const double* __restrict__ pts, double lambda, int P, double* __restrict__ dp,
+    double* __restrict__ tpts, double* __restrict__ part) {
+    __shared__ double red[kTB / 32];
+    double den = 0.0;
+    const int p = blockIdx.x * kTB + threadIdx.x;
+    if (p < P) {
+        double m0 = bp[3ll * p], m1 = bp[3ll * p + 1], m2 = bp[3ll * p + 2];
+        const double b0 = m0, b1 = m1, b2 = m2;
+        for (int s = pt_off[p]; s < pt_off[p + 1]; ++s) {
+            const double* We = W + 27ll * s;
+            const double* d = dc + 9ll * s_cam[s];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const double di = d[i];
+                m0 -= We[3 * i] * di;
+                m1 -= We[3 * i + 1] * di;
+                m2 -= We[3 * i + 2] * di;
+            }
+        }
+        const double* Vi = Vinv + 6ll * p;  // packed (00,10,11,20,21,22)
+        const double d0 = Vi[0] * m0 + Vi[1] * m1 + Vi[3] * m2;
+        const double d1 = Vi[1] * m0 + Vi[2] * m1 + Vi[4] * m2;
+        const double d2 = Vi[3] * m0 + Vi[4] * m1 + Vi[5] * m2;
+        dp[3ll * p] = d0;
+        dp[3ll * p + 1] = d1;
+        dp[3ll * p + 2] = d2;
+        tpts[3ll * p] = pts[3ll * p] + d0;
+        tpts[3ll * p + 1] = pts[3ll * p + 1] + d1;
+        tpts[3ll * p + 2] = pts[3ll * p + 2] + d2;
+        const double v0 = V[6ll * p], v1 = V[6ll * p + 2], v2 = V[6ll * p + 5];
+        den = d0 * (lambda * (v0 > 0.0 ? v0 : 1e-12) * d0 + b0) + d1 * (lambda * (v1 > 0.0 ? v1 : 1e-12) * d1 + b1) +
+              d2 * (lambda * (v2 > 0.0 ? v2 : 1e-12) * d2 + b2);
+    }
+    const double t = block_sum<kTB>(den, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Same, from the FP32 Jacobian records of the mixed form (FP64 arithmetic):
+// W_e^T dc = Jp^T (Jc dc).
+__global__ void __launch_bounds__(kTB) backsub_points_j32(
+    const int* __restrict__ pt_off, const int* __restrict__ s_cam, const float* __restrict__ J32,
+    const double* __restrict__ dc, const double* __restrict__ V, const double* __restrict__ Vinv,
+    const double* __restrict__ bp, const double* __restrict__ pts, double lambda, int P, double* __restrict__ dp,
+    double* __restrict__ tpts, double* __restrict__ part) {
+    __shared__ double red[kTB / 32];
+    double den = 0.0;
+    const int p = blockIdx.x * kTB + threadIdx.x;
+    if (p < P) {
+        double m0 = bp[3ll * p], m1 = bp[3ll * p + 1], m2 = bp[3ll * p + 2];
+        const double b0 = m0, b1 = m1, b2 = m2;
+        for (int s = pt_off[p]; s < pt_off[p + 1]; ++s) {
+            const float* J = J32 + 24ll * s;
+            const double* d = dc + 9ll * s_cam[s];
+            double y0 = 0.0, y1 = 0.0;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                y0 += static_cast<double>(J[i]) * d[i];
+                y1 += static_cast<double>(J[9 + i]) * d[i];
+            }
+            m0 -= static_cast<double>(J[18]) * y0 + static_cast<double>(J[21]) * y1;
+            m1 -= static_cast<double>(J[19]) * y0 + static_cast<double>(J[22]) * y1;
+            m2 -= static_cast<double>(J[20]) * y0 + static_cast<double>(J[23]) * y1;
+        }
+        const double* Vi = Vinv + 6ll * p;
+        const double d0 = Vi[0] * m0 + Vi[1] * m1 + Vi[3] * m2;
+        const double d1 = Vi[1] * m0 + Vi[2] * m1 + Vi[4] * m2;
+        const double d2 = Vi[3] * m0 + Vi[4] * m1 + Vi[5] * m2;
+        dp[3ll * p] = d0;
+        dp[3ll * p + 1] = d1;
+        dp[3ll * p + 2] = d2;
+        tpts[3ll * p] = pts[3ll * p] + d0;
+        tpts[3ll * p + 1] = pts[3ll * p + 1] + d1;
+        tpts[3ll * p + 2] = pts[3ll * p + 2] + d2;
+        const double v0 = V[6ll * p], v1 = V[6ll * p + 2], v2 = V[6ll * p + 5];
+        den = d0 * (lambda * (v0 > 0.0 ? v0 : 1e-12) * d0 + b0) + d1 * (lambda * (v1 > 0.0 ? v1 : 1e-12) * d1 + b1) +
+              d2 * (lambda * (v2 > 0.0 ? v2 : 1e-12) * d2 + b2);
+    }
+    const double t = block_sum<kTB>(den, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Camera part of the denominator and the trial cameras (tcams = cams + dc).
+__global__ void __launch_bounds__(kTB) camera_step_kernel(const double* __restrict__ dc, const double* __restrict__ U,
+                                                         const double* __restrict__ bc,
+                                                         const double* __restrict__ cams, double lambda, int C,
+                                                         double* __restrict__ tcams, double* __restrict__ part) {
+    __shared__ double red[kTB / 32];
+    double den = 0.0;
+    const int i = blockIdx.x * kTB + threadIdx.x;
+    if (i < 9 * C) {
+        const int c = i / 9, k = i % 9;
+        const double dg = U[81ll * c + 10 * k];
+        const double d = dc[i];
+        den = d * (lambda * (dg > 0.0 ? dg : 1e-12) * d + bc[i]);
+        tcams[i] = cams[i] + d;
+    }
+    const double t = block_sum<kTB>(den, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// denom = (camera partials in order) + (point partials in order).
+__global__ void __launch_bounds__(256) denom_finalize(const double* __restrict__ part, int ncam, int npt,
+                                                     double* __restrict__ out) {
+    __shared__ double red[8];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < ncam; i += 256) s += part[i];
+    const double a = block_sum<256>(s, red);
+    s = 0.0;
+    for (int i = threadIdx.x; i < npt; i += 256) s += part[ncam + i];
+    const double b = block_sum<256>(s, red);
+    if (threadIdx.x == 0) *out = a + b;
+}
+
+}  // namespace
+
+unsigned long long Solver::damp_invert_v(double lambda) {
+    GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get() + 3, 0, sizeof(unsigned long long), stream_));
+    const int grid = std::min(ceil_div(P_, kTB), 8 * device_sm_count());
+    damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), counters_.get() + 3);
+    GBA_LAUNCH_CHECK();
+    unsigned long long bad = 0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&bad, counters_.get() + 3, sizeof bad, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    if (bad) {
+        // keep the cumulative non-SPD count (reference counters[1])
+        unsigned long long h[2];
+        GBA_CUDA_CHECK(cudaMemcpyAsync(h, counters_.get(), sizeof h, cudaMemcpyDeviceToHost, stream_));
+        sync();
+        h[1] += bad;
+        GBA_CUDA_CHECK(cudaMemcpyAsync(counters_.get(), h, sizeof h, cudaMemcpyHostToDevice, stream_));
+        sync();
+    }
+    return bad;
+}
+
+double Solver::back_substitute(double lambda) {
+    const int ncam = ceil_div(9ll * C_, kTB), npt = ceil_div(P_, kTB);
+    double* part = red_part_.get();
+    camera_step_kernel<<<ncam, kTB, 0, stream_>>>(dc_.get(), U_.get(), bc_.get(), cams_.get(), lambda, C_,
+                                                  tcams_.get(), part);
+    GBA_LAUNCH_CHECK();
+    if (form_ == SolverForm::Plain)
+        backsub_points_w64<<<npt, kTB, 0, stream_>>>(pt_off_.get(), s_cam_.get(), W_.get(), dc_.get(), V_.get(),
+                                                     Vinv_.get(), bp_.get(), pts_.get(), lambda, P_, dp_.get(),
+                                                     tpts_.get(), part + ncam);
+    else
+        backsub_points_j32<<<npt, kTB, 0, stream_>>>(pt_off_.get(), s_cam_.get(), J32_.get(), dc_.get(), V_.get(),
+                                                     Vinv_.get(), bp_.get(), pts_.get(), lambda, P_, dp_.get(),
+                                                     tpts_.get(), part + ncam);
+    GBA_LAUNCH_CHECK();
+    denom_finalize<<<1, 256, 0, stream_>>>(part, ncam, npt, scal_.get() + 2);
+    GBA_LAUNCH_CHECK();
+    double denom = 0.0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&denom, scal_.get() + 2, sizeof denom, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    return denom;
+}
+
+void launch_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    batch_chol9_kernel<<<ceil_div(n, 128), 128, 0, s>>>(A, b, x, ok, n);
+    GBA_LAUNCH_CHECK();
+}
+
+void launch_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    batch_inverse3_kernel<<<ceil_div(n, 128), 128, 0, s>>>(A, Ainv, ok, n);
+    GBA_LAUNCH_CHECK();
+}
+
+}  // namespace gba

@@ -1,0 +1,462 @@
+// extern "C" layer over the C++ library: status codes instead of exceptions.
+
+#include "gba_capi.h"
+
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "common.cuh"
+#include "gba/bal_problem.hpp"
+#include "gba/lm.hpp"
+#include "lm_internal.hpp"
+#include "solver.hpp"
+#include "synthetic.hpp"
+
+struct gba_host_problem {
+    gba::BALProblem p;
+};
+
+struct gba_solver {
+    std::unique_ptr<gba::Solver> s;
+    cudaStream_t own_stream = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        f();
+        return GBA_OK;
+    } catch (const gba::CudaError& e) {
+        g_err = e.what();
+        return GBA_ERR_CUDA;
+    } catch (const std::invalid_argument& e) {
+        g_err = e.what();
+        return GBA_ERR_INVALID;
+    } catch (const std::bad_alloc& e) {
+        g_err = "host allocation failed";
+        return GBA_ERR_INTERNAL;
+    } catch (const std::runtime_error& e) {
+        g_err = e.what();
+        return GBA_ERR_IO;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return GBA_ERR_INTERNAL;
+    } catch (...) {
+        g_err = "unknown exception";
+        return GBA_ERR_INTERNAL;
+    }
+}
+
+void need(bool ok, const char* what) {
+    if (!ok) throw std::invalid_argument(what);
+}
+
+gba::LMOptions to_options(const gba_lm_options* o) {
+    gba::LMOptions r;
+    if (!o) return r;
+    r.max_iterations = o->max_iterations;
+    r.initial_lambda = o->initial_lambda;
+    r.rel_decrease_tol = o->rel_decrease_tol;
+    r.max_inner_trials = o->max_inner_trials;
+    r.verbose = o->verbose != 0;
+    need(o->form >= GBA_FORM_PLAIN && o->form <= GBA_FORM_MIXED_LEARNED, "bad solver form");
+    r.form = static_cast<gba::SolverForm>(o->form);
+    r.refine_tol = o->refine_tol;
+    r.refine_max_steps = o->refine_max_steps;
+    r.pcg_tol = o->pcg_tol;
+    r.pcg_max_iters = o->pcg_max_iters;
+    r.model_path = o->model_path ? o->model_path : "";
+    r.target_cost = o->target_cost;
+    return r;
+}
+
+void fill_result(const gba::LMResult& r, gba_lm_result* out) {
+    out->initial_cost = r.initial_cost;
+    out->final_cost = r.final_cost;
+    out->iterations = r.iterations;
+    out->termination = r.termination == "CONVERGENCE" ? GBA_TERM_CONVERGENCE
+                       : r.termination == "FAILURE"   ? GBA_TERM_FAILURE
+                                                      : GBA_TERM_MAX_ITERATIONS;
+    out->anomalies = r.anomalies;
+    out->total_time_s = r.total_time_s;
+    out->trials = r.trials;
+    out->pcg_iterations = r.pcg_iterations;
+    out->refine_steps = r.refine_steps;
+    out->time_to_target_s = r.time_to_target_s;
+    out->t_setup = r.t_setup;
+    out->t_accumulate = r.t_accumulate;
+    out->t_damp = r.t_damp;
+    out->t_schur = r.t_schur;
+    out->t_backsub = r.t_backsub;
+    out->t_cost = r.t_cost;
+    out->trajectory_len = static_cast<int>(r.trajectory.size());
+    const int n = std::min<int>(out->trajectory_len, std::max(0, out->trajectory_capacity));
+    for (int i = 0; i < n; ++i) {
+        if (out->trajectory) out->trajectory[i] = r.trajectory[i];
+        if (out->trajectory_time_s) out->trajectory_time_s[i] = r.trajectory_time_s[i];
+    }
+}
+
+gba::Solver& S(gba_solver* s) {
+    need(s && s->s, "null solver");
+    return *s->s;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gba_last_error(void) { return g_err.c_str(); }
+const char* gba_version(void) { return "gba-gb300 1.0 (sm_103a)"; }
+
+void gba_lm_options_default(gba_lm_options* o) {
+    if (!o) return;
+    const gba::LMOptions d;
+    o->max_iterations = d.max_iterations;
+    o->initial_lambda = d.initial_lambda;
+    o->rel_decrease_tol = d.rel_decrease_tol;
+    o->max_inner_trials = d.max_inner_trials;
+    o->verbose = d.verbose ? 1 : 0;
+    o->form = GBA_FORM_PLAIN;
+    o->refine_tol = d.refine_tol;
+    o->refine_max_steps = d.refine_max_steps;
+    o->pcg_tol = d.pcg_tol;
+    o->pcg_max_iters = d.pcg_max_iters;
+    o->model_path = nullptr;
+    o->target_cost = d.target_cost;
+}
+
+int gba_solve_bal(int C, int P, int E, double* cameras, double* points, const int* obs_camera,
+                  const int* obs_point, const double* obs_pixel, const gba_lm_options* opts, gba_lm_result* result) {
+    return guarded([&] {
+        need(cameras && points && obs_camera && obs_point && obs_pixel && result, "null argument");
+        gba::validate_problem(C, P, E, cameras, points, obs_camera, obs_point, obs_pixel);
+        const gba::LMOptions o = to_options(opts);
+        const auto t0 = std::chrono::steady_clock::now();
+        cudaStream_t stream = nullptr;
+        GBA_CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        struct Guard {
+            cudaStream_t s;
+            ~Guard() { cudaStreamDestroy(s); }
+        } g{stream};
+        gba::LMResult r;
+        {
+            gba::Solver s(C, P, E, cameras, points, obs_camera, obs_point, obs_pixel, o.form, stream);
+            if (o.form == gba::SolverForm::MixedLearned) s.load_model(o.model_path);
+            const double t_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            r = gba::run_lm(s, o, t0);
+            r.t_setup = t_setup;
+            s.get_params(cameras, points);
+        }
+        r.total_time_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_result(r, result);
+    });
+}
+
+int gba_edge_residual_jacobian_host(const double* cam, const double* pt, const double* obs, double* r, double* Jc,
+                                    double* Jp) {
+    return guarded([&] {
+        need(cam && pt && obs && r && Jc && Jp, "null argument");
+        gba::edge_residual_jacobian_host(cam, pt, obs, r, Jc, Jp);
+    });
+}
+
+int gba_snavely_residual(const double* cam, const double* pt, const double* obs, double* out2) {
+    return guarded([&] {
+        need(cam && pt && obs && out2, "null argument");
+        gba::snavely_residual(cam, pt, obs, out2);
+    });
+}
+
+int gba_total_squared_error(int C, int P, int E, const double* cams, const double* pts, const int* oc, const int* op,
+                            const double* px, double* out) {
+    return guarded([&] {
+        need(cams && pts && oc && op && px && out, "null argument");
+        need(C > 0 && P > 0 && E >= 0, "bad sizes");
+        double sum = 0.0, r[2];
+        for (int i = 0; i < E; ++i) {
+            need(oc[i] >= 0 && oc[i] < C && op[i] >= 0 && op[i] < P, "observation index out of range");
+            gba::snavely_residual(cams + 9ll * oc[i], pts + 3ll * op[i], px + 2ll * i, r);
+            sum += r[0] * r[0] + r[1] * r[1];
+        }
+        *out = sum;
+    });
+}
+
+int gba_host_problem_load(const char* path, gba_host_problem** out) {
+    return guarded([&] {
+        need(path && out, "null argument");
+        auto h = std::make_unique<gba_host_problem>();
+        h->p = gba::load_bal(path);
+        *out = h.release();
+    });
+}
+
+int gba_host_problem_synthetic(int workload, uint64_t seed, gba_host_problem** out, gba_host_problem** truth) {
+    return guarded([&] {
+        need(out != nullptr, "null argument");
+        const gba::SyntheticConfig cfg = gba::synthetic_config(workload);
+        auto h = std::make_unique<gba_host_problem>();
+        std::unique_ptr<gba_host_problem> t;
+        if (truth) t = std::make_unique<gba_host_problem>();
+        h->p = gba::make_synthetic(cfg, seed, t ? &t->p : nullptr);
+        *out = h.release();
+        if (truth) *truth = t.release();
+    });
+}
+
+int gba_host_problem_synthetic_custom(int C, int P, int kmin, int kmax, double alpha, double ofrac, double osig,
+                                      uint64_t seed, gba_host_problem** out) {
+    return guarded([&] {
+        need(out != nullptr, "null argument");
+        const gba::SyntheticConfig cfg{C, P, kmin, kmax, alpha, ofrac, osig};
+        auto h = std::make_unique<gba_host_problem>();
+        h->p = gba::make_synthetic(cfg, seed, nullptr);
+        *out = h.release();
+    });
+}
+
+int gba_host_problem_launch_bounds(int num_points, gba_host_problem** out) {
+    return guarded([&] {
+        need(out != nullptr && num_points > 0, "bad argument");
+        auto h = std::make_unique<gba_host_problem>();
+        h->p = gba::make_launch_bounds_problem(num_points);
+        *out = h.release();
+    });
+}
+
+int gba_host_problem_dims(const gba_host_problem* p, int* C, int* P, int* E) {
+    return guarded([&] {
+        need(p != nullptr, "null problem");
+        if (C) *C = p->p.num_cameras;
+        if (P) *P = p->p.num_points;
+        if (E) *E = p->p.num_observations;
+    });
+}
+
+int gba_host_problem_copy(const gba_host_problem* h, double* cams, double* pts, int* oc, int* op, double* px) {
+    return guarded([&] {
+        need(h != nullptr, "null problem");
+        const auto& p = h->p;
+        if (cams) std::memcpy(cams, p.cameras.data(), p.cameras.size() * sizeof(double));
+        if (pts) std::memcpy(pts, p.points.data(), p.points.size() * sizeof(double));
+        if (oc) std::memcpy(oc, p.obs_camera.data(), p.obs_camera.size() * sizeof(int));
+        if (op) std::memcpy(op, p.obs_point.data(), p.obs_point.size() * sizeof(int));
+        if (px) std::memcpy(px, p.obs_pixel.data(), p.obs_pixel.size() * sizeof(double));
+    });
+}
+
+int gba_host_problem_save(const gba_host_problem* h, const char* path) {
+    return guarded([&] {
+        need(h && path, "null argument");
+        gba::write_bal(path, h->p);
+    });
+}
+
+void gba_host_problem_free(gba_host_problem* p) { delete p; }
+
+int gba_solver_create(int C, int P, int E, const double* cams, const double* pts, const int* oc, const int* op,
+                      const double* px, int form, void* stream, gba_solver** out) {
+    return guarded([&] {
+        need(out != nullptr, "null argument");
+        need(form >= GBA_FORM_PLAIN && form <= GBA_FORM_MIXED_LEARNED, "bad solver form");
+        gba::validate_problem(C, P, E, cams, pts, oc, op, px);
+        auto h = std::make_unique<gba_solver>();
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (!st) {
+            GBA_CUDA_CHECK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+            st = h->own_stream;
+        }
+        try {
+            h->s = std::make_unique<gba::Solver>(C, P, E, cams, pts, oc, op, px, static_cast<gba::SolverForm>(form), st);
+        } catch (...) {
+            if (h->own_stream) cudaStreamDestroy(h->own_stream);
+            throw;
+        }
+        *out = h.release();
+    });
+}
+
+void gba_solver_destroy(gba_solver* s) {
+    if (!s) return;
+    s->s.reset();
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+}
+
+int gba_solver_set_params(gba_solver* s, const double* cams, const double* pts) {
+    return guarded([&] {
+        need(cams && pts, "null argument");
+        S(s).set_params(cams, pts);
+        S(s).sync();
+    });
+}
+
+int gba_solver_get_params(gba_solver* s, double* cams, double* pts) {
+    return guarded([&] { S(s).get_params(cams, pts); });
+}
+
+int gba_solver_accumulate(gba_solver* s, double* out_sse) {
+    return guarded([&] {
+        const double v = S(s).accumulate();
+        if (out_sse) *out_sse = v;
+    });
+}
+
+int gba_solver_damp_invert_v(gba_solver* s, double lambda, unsigned long long* out) {
+    return guarded([&] {
+        const unsigned long long v = S(s).damp_invert_v(lambda);
+        if (out) *out = v;
+    });
+}
+
+int gba_solver_schur_dense(gba_solver* s, double lambda, int* out_info) {
+    return guarded([&] {
+        need(S(s).form() == gba::SolverForm::Plain, "schur_dense needs the plain form");
+        const int v = S(s).schur_dense(lambda);
+        if (out_info) *out_info = v;
+    });
+}
+
+int gba_solver_schur_pcg(gba_solver* s, double lambda, const gba_lm_options* opts, int learned, long long* iters,
+                         int* steps, double* relres) {
+    return guarded([&] {
+        need(S(s).form() != gba::SolverForm::Plain, "schur_pcg needs a mixed form");
+        const gba::LMOptions o = to_options(opts);
+        const gba::PcgStats st = S(s).schur_pcg(lambda, o, learned != 0);
+        if (iters) *iters = st.pcg_iterations;
+        if (steps) *steps = st.refine_steps;
+        if (relres) *relres = st.rel_residual;
+    });
+}
+
+int gba_solver_back_substitute(gba_solver* s, double lambda, double* out_denom) {
+    return guarded([&] {
+        const double v = S(s).back_substitute(lambda);
+        if (out_denom) *out_denom = v;
+    });
+}
+
+int gba_solver_trial_cost(gba_solver* s, double* out_sse) {
+    return guarded([&] {
+        const double v = S(s).trial_cost();
+        if (out_sse) *out_sse = v;
+    });
+}
+
+int gba_solver_accept(gba_solver* s) {
+    return guarded([&] { S(s).accept(); });
+}
+
+int gba_solver_counters(gba_solver* s, unsigned long long* a, unsigned long long* n) {
+    return guarded([&] {
+        if (a) *a = S(s).anomalies();
+        if (n) *n = S(s).nonspd_total();
+    });
+}
+
+int gba_solver_load_model(gba_solver* s, const char* path) {
+    return guarded([&] {
+        need(path != nullptr, "null path");
+        S(s).load_model(path);
+    });
+}
+
+int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out) {
+    return guarded([&] {
+        need(out != nullptr, "null argument");
+        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_TRIAL_PTS, "bad buffer id");
+        size_t bytes = 0;
+        S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &bytes);
+        *out = bytes;
+    });
+}
+
+int gba_solver_download(gba_solver* s, int buffer, void* dst, size_t bytes) {
+    return guarded([&] {
+        need(dst != nullptr, "null destination");
+        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_TRIAL_PTS, "bad buffer id");
+        size_t have = 0;
+        const void* src = S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &have);
+        need(src != nullptr, "buffer not held by this solver form");
+        need(bytes <= have, "download larger than the buffer");
+        GBA_CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, S(s).stream()));
+        S(s).sync();
+    });
+}
+
+int gba_solver_device_ptr(gba_solver* s, int buffer, void** out) {
+    return guarded([&] {
+        need(out != nullptr, "null argument");
+        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_TRIAL_PTS, "bad buffer id");
+        size_t have = 0;
+        *out = const_cast<void*>(S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &have));
+    });
+}
+
+int gba_solver_dims(gba_solver* s, int* C, int* P, int* E, int* n_pad) {
+    return guarded([&] {
+        if (C) *C = S(s).C();
+        if (P) *P = S(s).P();
+        if (E) *E = S(s).E();
+        if (n_pad) *n_pad = S(s).n_pad();
+    });
+}
+
+int gba_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n, void* stream) {
+    return guarded([&] {
+        need(n >= 0, "negative batch");
+        need(n == 0 || (A && b && x && ok), "null argument");
+        gba::launch_batch_chol9_factor_solve(A, b, x, ok, n, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, void* stream) {
+    return guarded([&] {
+        need(n >= 0, "negative batch");
+        need(n == 0 || (A && Ainv && ok), "null argument");
+        gba::launch_batch_inverse3_spd(A, Ainv, ok, n, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_dense_potrf(double* A, int n, int lda, int* info, void* stream) {
+    return guarded([&] {
+        need(A && info, "null argument");
+        need(n > 0 && n % 64 == 0 && lda >= n, "n must be a positive multiple of 64 and lda >= n");
+        gba::dense_potrf(A, n, lda, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info, void* stream) {
+    return guarded([&] {
+        need(L && b && info, "null argument");
+        need(n > 0 && n % 64 == 0 && lda >= n, "n must be a positive multiple of 64 and lda >= n");
+        gba::dense_potrs(L, n, lda, b, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_eval_edges(int precision, const double* cams, const double* pts, const int* oc, const int* op,
+                   const double* px, int E, void* r, void* Jc, void* Jp, void* stream) {
+    return guarded([&] {
+        need(precision == 64 || precision == 32, "precision must be 64 or 32");
+        need(E >= 0, "negative count");
+        if (E == 0) return;
+        need(cams && pts && oc && op && px && r, "null argument");
+        if (precision == 64)
+            gba::launch_eval_edges_f64(cams, pts, oc, op, px, E, static_cast<double*>(r), static_cast<double*>(Jc),
+                                       static_cast<double*>(Jp), static_cast<cudaStream_t>(stream));
+        else
+            gba::launch_eval_edges_f32(cams, pts, oc, op, px, E, static_cast<float*>(r), static_cast<float*>(Jc),
+                                       static_cast<float*>(Jp), static_cast<cudaStream_t>(stream));
+    });
+}
+
+}  // extern "C"

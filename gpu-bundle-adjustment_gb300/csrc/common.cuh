@@ -1,0 +1,84 @@
+#pragma once
+// Shared device/host utilities: error handling, launch helpers and the
+// deterministic reduction primitives used by every kernel in this library.
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace gba {
+
+// Thrown by the host driver on CUDA failure (the C-ABI layer converts it to a
+// status code; nothing throws across the ABI).
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define GBA_CUDA_CHECK(call)                                                            \
+    do {                                                                                \
+        cudaError_t err_ = (call);                                                      \
+        if (err_ != cudaSuccess)                                                        \
+            throw ::gba::CudaError(std::string("CUDA error at ") + __FILE__ + ":" +     \
+                                   std::to_string(__LINE__) + ": " +                    \
+                                   cudaGetErrorString(err_));                           \
+    } while (0)
+
+#define GBA_LAUNCH_CHECK() GBA_CUDA_CHECK(cudaGetLastError())
+
+inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
+
+// Number of SMs of the current device (152 on GB300), cached per process.
+int device_sm_count();
+
+#ifdef __CUDACC__
+// Deterministic block-wide sum of one double per thread. Fixed shuffle tree
+// within each warp, then warp partials summed in warp order by warp 0.
+// `shared` holds at least blockDim.x/32 doubles. Result valid in thread 0.
+template <int kThreads>
+__device__ __forceinline__ double block_sum(double v, double* shared) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) shared[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) r += shared[w];
+    }
+    __syncthreads();
+    return r;
+}
+
+template <int kThreads>
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v,
+                                                            unsigned long long* shared) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) shared[warp] = v;
+    __syncthreads();
+    unsigned long long r = 0;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) r += shared[w];
+    }
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+#endif
+
+}  // namespace gba

@@ -1,0 +1,404 @@
+// Plain form: on-device assembly of the dense reduced camera system and its
+// blocked FP64 Cholesky on the DMMA tensor cores.
+//
+// Reference: the host assembly src/lm.cu:488-594 (T_e = W_e V'^-1, privatised
+// S -= T_e W_f^T over edge pairs of each point, merge, rhs, damped U blocks) and
+// the host Eigen LLT src/lm.cu:598-604. Here:
+//   * T_e is computed per slot on the device;
+//   * S is assembled output-stationary: the edge pairs (e, f) of every point
+//     with cam(e) >= cam(f) are sorted once by camera-pair block, and each
+//     9x9 block is written once as the ordered sum of its pairs (no atomics,
+//     deterministic), then the damped U blocks are added;
+//   * the factorisation is right-looking blocked Cholesky (panel width 64):
+//     diagonal-block potrf in shared memory, panel triangular solve, and the
+//     trailing update C -= A B^T with mma.sync.m8n8k4 FP64 (DMMA).
+// S is column-major, n_pad x n_pad (n_pad = 9C rounded up to 64, identity on
+// the padding), lower triangle meaningful; the upper triangle is never read.
+
+#include "common.cuh"
+#include "solver.hpp"
+
+namespace gba {
+namespace {
+
+constexpr int NB = 64;       // panel width / tile size
+constexpr int kSP = NB + 8;  // shared-memory stride (doubles) of K-major tiles: conflict-free DMMA fragments
+
+__global__ void compute_T_kernel(const double* __restrict__ W, const double* __restrict__ Vinv,
+                                 const int* __restrict__ s_pt, int E, double* __restrict__ T) {
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < E; s += (long long)gridDim.x * blockDim.x) {
+        const double* Vi = Vinv + 6ll * s_pt[s];
+        const double v00 = Vi[0], v10 = Vi[1], v11 = Vi[2], v20 = Vi[3], v21 = Vi[4], v22 = Vi[5];
+        const double* We = W + 27 * s;
+        double* Te = T + 27 * s;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const double w0 = We[3 * i], w1 = We[3 * i + 1], w2 = We[3 * i + 2];
+            Te[3 * i] = w0 * v00 + w1 * v10 + w2 * v20;
+            Te[3 * i + 1] = w0 * v10 + w1 * v11 + w2 * v21;
+            Te[3 * i + 2] = w0 * v20 + w1 * v21 + w2 * v22;
+        }
+    }
+}
+
+// One thread per (block, row i): S(9ce+i, 9cf+j) = -sum_{(e,f) in block} T_e(i,:) . W_f(j,:)
+__global__ void __launch_bounds__(288) assemble_kernel(const int* __restrict__ block_off,
+                                                      const int* __restrict__ block_ce,
+                                                      const int* __restrict__ block_cf, const int* __restrict__ pe,
+                                                      const int* __restrict__ pf, const double* __restrict__ T,
+                                                      const double* __restrict__ W, int nblocks, int lda,
+                                                      double* __restrict__ S) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long b = t / 9;
+    const int i = static_cast<int>(t % 9);
+    if (b >= nblocks) return;
+    double acc[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) acc[j] = 0.0;
+    for (int q = block_off[b]; q < block_off[b + 1]; ++q) {
+        const double* Te = T + 27ll * pe[q] + 3 * i;
+        const double t0 = Te[0], t1 = Te[1], t2 = Te[2];
+        const double* Wf = W + 27ll * pf[q];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) acc[j] += t0 * Wf[3 * j] + t1 * Wf[3 * j + 1] + t2 * Wf[3 * j + 2];
+    }
+    const long long row = 9ll * block_ce[b] + i;
+    const long long col0 = 9ll * block_cf[b];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) S[row + (col0 + j) * lda] = -acc[j];
+}
+
+// Diagonal blocks += U_c + lambda * max(diag U_c, 1e-12); identity on padding.
+__global__ void add_damped_u_kernel(const double* __restrict__ U, double lambda, int C, int n_pad, int lda,
+                                    double* __restrict__ S) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 81 * C) {
+        const int c = t / 81, i = (t % 81) / 9, j = t % 9;
+        double v = U[t];
+        if (i == j) v += lambda * (v > 0.0 ? v : 1e-12);
+        S[(9ll * c + i) + (9ll * c + j) * lda] += v;
+    } else if (t < 81 * C + (n_pad - 9 * C)) {
+        const long long r = 9ll * C + (t - 81 * C);
+        S[r + r * lda] = 1.0;
+    }
+}
+
+// rhs_c = bc_c - sum_{e in c} T_e bp_{p(e)}; one CTA per camera, ordered sums.
+__global__ void __launch_bounds__(128) rhs_kernel(const int* __restrict__ cam_off, const int* __restrict__ cam_slots,
+                                                 const int* __restrict__ s_pt, const double* __restrict__ T,
+                                                 const double* __restrict__ bp, const double* __restrict__ bc,
+                                                 double* __restrict__ rhs) {
+    __shared__ double wpart[4][9];
+    const int c = blockIdx.x;
+    double acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    for (int i = cam_off[c] + threadIdx.x; i < cam_off[c + 1]; i += 128) {
+        const int s = cam_slots[i];
+        const double* Te = T + 27ll * s;
+        const double* b = bp + 3ll * s_pt[s];
+        const double b0 = b[0], b1 = b[1], b2 = b[2];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] += Te[3 * k] * b0 + Te[3 * k + 1] * b1 + Te[3 * k + 2] * b2;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const double v = warp_sum(acc[k]);
+        if (lane == 0) wpart[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        const double v = wpart[0][threadIdx.x] + wpart[1][threadIdx.x] + wpart[2][threadIdx.x] + wpart[3][threadIdx.x];
+        rhs[9ll * c + threadIdx.x] = bc[9ll * c + threadIdx.x] - v;
+    }
+}
+
+// ---------------------------------------------------------------- Cholesky
+
+// Factor the NB x NB diagonal block at (j0, j0) in shared memory.
+__global__ void __launch_bounds__(256) potrf_diag_kernel(double* __restrict__ A, int j0, int lda, int* __restrict__ info) {
+    __shared__ double a[NB][NB + 1];  // a[col][row]
+    __shared__ int failed;
+    if (*info) return;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < NB * NB; idx += 256) {
+        const int r = idx % NB, c = idx / NB;
+        a[c][r] = r >= c ? A[(j0 + r) + (long long)(j0 + c) * lda] : 0.0;
+    }
+    if (tid == 0) failed = 0;
+    __syncthreads();
+    for (int k = 0; k < NB; ++k) {
+        const double piv = a[k][k];
+        if (!(piv > 0.0)) {
+            if (tid == 0) {
+                failed = 1;
+                *info = j0 + k + 1;
+            }
+            break;  // every thread read the same pivot
+        }
+        const double lkk = sqrt(piv);
+        __syncthreads();
+        for (int r = k + 1 + tid; r < NB; r += 256) a[k][r] /= lkk;
+        if (tid == 0) a[k][k] = lkk;
+        __syncthreads();
+        for (int idx = tid; idx < NB * NB; idx += 256) {
+            const int r = idx % NB, c = idx / NB;
+            if (c > k && r >= c) a[c][r] -= a[k][r] * a[k][c];
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (failed) return;
+    for (int idx = tid; idx < NB * NB; idx += 256) {
+        const int r = idx % NB, c = idx / NB;
+        if (r >= c) A[(j0 + r) + (long long)(j0 + c) * lda] = a[c][r];
+    }
+}
+
+// Panel solve: rows [j0+NB, n) of columns [j0, j0+NB) := B L_jj^{-T}.
+__global__ void __launch_bounds__(256) trsm_panel_kernel(double* __restrict__ A, int j0, int lda,
+                                                        const int* __restrict__ info) {
+    extern __shared__ double tsm[];
+    double(*L)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(tsm);                  // L[col][row]
+    double(*X)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(tsm + NB * (NB + 1));  // X[col][row]
+    if (*info) return;
+    const int tid = threadIdx.x;
+    const long long r0 = j0 + NB + (long long)NB * blockIdx.x;
+    for (int idx = tid; idx < NB * NB; idx += 256) {
+        const int r = idx % NB, c = idx / NB;
+        L[c][r] = r >= c ? A[(j0 + r) + (long long)(j0 + c) * lda] : 0.0;
+        X[c][r] = A[(r0 + r) + (long long)(j0 + c) * lda];
+    }
+    __syncthreads();
+    for (int k = 0; k < NB; ++k) {
+        const double d = L[k][k];
+        for (int r = tid; r < NB; r += 256) X[k][r] /= d;
+        __syncthreads();
+        for (int idx = tid; idx < NB * NB; idx += 256) {
+            const int r = idx % NB, c = idx / NB;
+            if (c > k) X[c][r] -= X[k][r] * L[k][c];
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < NB * NB; idx += 256) {
+        const int r = idx % NB, c = idx / NB;
+        A[(r0 + r) + (long long)(j0 + c) * lda] = X[c][r];
+    }
+}
+
+__device__ __forceinline__ void dmma_m8n8k4(double (&d)[2], double a, double b) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                 : "+d"(d[0]), "+d"(d[1])
+                 : "d"(a), "d"(b));
+}
+
+// Trailing update of the lower tiles: C(ti,tj) -= A(ti) A(tj)^T, K = NB (the
+// panel). 8 warps per 64x64 tile, each warp 32x16 = 4x2 DMMA tiles.
+__global__ void __launch_bounds__(256) syrk_update_kernel(double* __restrict__ A, int j0, int ntiles, int lda,
+                                                         const int* __restrict__ info) {
+    extern __shared__ double smem[];
+    double* As = smem;             // [k][row], stride kSP
+    double* Bs = smem + NB * kSP;  // [k][col]
+    if (*info) return;
+    // lower-triangular tile index from the linear block index
+    const long long bidx = blockIdx.x;
+    int ti = static_cast<int>((sqrt(8.0 * (double)bidx + 1.0) - 1.0) * 0.5);
+    while ((long long)(ti + 1) * (ti + 2) / 2 <= bidx) ++ti;
+    while ((long long)ti * (ti + 1) / 2 > bidx) --ti;
+    const int tj = static_cast<int>(bidx - (long long)ti * (ti + 1) / 2);
+    if (ti >= ntiles) return;
+    const long long R0 = j0 + NB + (long long)NB * ti, C0 = j0 + NB + (long long)NB * tj;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < NB * NB; idx += 256) {
+        const int r = idx % NB, k = idx / NB;
+        As[k * kSP + r] = A[(R0 + r) + (long long)(j0 + k) * lda];
+        Bs[k * kSP + r] = A[(C0 + r) + (long long)(j0 + k) * lda];
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+    const int fr = lane >> 2, fk = lane & 3;
+    double acc[4][2][2];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int n = 0; n < 2; ++n) acc[m][n][0] = acc[m][n][1] = 0.0;
+#pragma unroll 4
+    for (int kk = 0; kk < NB; kk += 4) {
+        const double* ak = As + (kk + fk) * kSP + wm + fr;
+        const double* bk = Bs + (kk + fk) * kSP + wn + fr;
+        double af[4], bf[2];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) af[m] = ak[8 * m];
+#pragma unroll
+        for (int n = 0; n < 2; ++n) bf[n] = bk[8 * n];
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int n = 0; n < 2; ++n) dmma_m8n8k4(acc[m][n], af[m], bf[n]);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int n = 0; n < 2; ++n) {
+            const long long row = R0 + wm + 8 * m + fr;
+            const long long col = C0 + wn + 8 * n + 2 * fk;
+            A[row + col * lda] -= acc[m][n][0];
+            A[row + (col + 1) * lda] -= acc[m][n][1];
+        }
+}
+
+// ---------------------------------------------------------------- triangular solves
+
+// y_j = L_jj^{-1} b_j (forward) for the diagonal block at j0; one CTA.
+__global__ void trsv_lower_diag(const double* __restrict__ L, int j0, int lda, double* __restrict__ b,
+                                const int* __restrict__ info) {
+    __shared__ double x[NB];
+    if (*info) return;
+    const int t = threadIdx.x;  // NB threads
+    x[t] = b[j0 + t];
+    __syncthreads();
+    for (int k = 0; k < NB; ++k) {
+        if (t == k) x[k] /= L[(j0 + k) + (long long)(j0 + k) * lda];
+        __syncthreads();
+        if (t > k) x[t] -= L[(j0 + t) + (long long)(j0 + k) * lda] * x[k];
+        __syncthreads();
+    }
+    b[j0 + t] = x[t];
+}
+
+// b[j0+NB : n) -= L[j0+NB:n, j0:j0+NB] b[j0 : j0+NB); thread per row.
+__global__ void gemv_lower_below(const double* __restrict__ L, int j0, int n, int lda, double* __restrict__ b,
+                                 const int* __restrict__ info) {
+    __shared__ double x[NB];
+    if (*info) return;
+    if (threadIdx.x < NB) x[threadIdx.x] = b[j0 + threadIdx.x];
+    __syncthreads();
+    const long long r = j0 + NB + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double s = 0.0;
+#pragma unroll 8
+    for (int k = 0; k < NB; ++k) s += L[r + (long long)(j0 + k) * lda] * x[k];
+    b[r] -= s;
+}
+
+// x_j = L_jj^{-T} y_j (backward) for the diagonal block at j0; one CTA.
+__global__ void trsv_upper_diag(const double* __restrict__ L, int j0, int lda, double* __restrict__ b,
+                                const int* __restrict__ info) {
+    __shared__ double x[NB];
+    if (*info) return;
+    const int t = threadIdx.x;
+    x[t] = b[j0 + t];
+    __syncthreads();
+    for (int k = NB - 1; k >= 0; --k) {
+        if (t == k) x[k] /= L[(j0 + k) + (long long)(j0 + k) * lda];
+        __syncthreads();
+        // row t of L^T is column t of L: (L^T)(t, k) = L(k, t), k > t
+        if (t < k) x[t] -= L[(j0 + k) + (long long)(j0 + t) * lda] * x[k];
+        __syncthreads();
+    }
+    b[j0 + t] = x[t];
+}
+
+// y[0 : j0) -= L[j0:j0+NB, 0:j0]^T x_j; one warp per output row i (reads column i of L).
+__global__ void gemv_upper_above(const double* __restrict__ L, int j0, int lda, double* __restrict__ b,
+                                 const int* __restrict__ info) {
+    __shared__ double x[NB];
+    if (*info) return;
+    if (threadIdx.x < NB) x[threadIdx.x] = b[j0 + threadIdx.x];
+    __syncthreads();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= j0) return;
+    const double* col = L + (long long)warp * lda + j0;
+    double s = col[lane] * x[lane] + col[lane + 32] * x[lane + 32];
+    s = warp_sum(s);
+    if (lane == 0) b[warp] -= s;
+}
+
+}  // namespace
+
+void dense_potrf(double* A, int n, int lda, int* info, cudaStream_t s) {
+    if (n % NB != 0 || lda < n) throw std::invalid_argument("dense_potrf: n must be a multiple of 64, lda >= n");
+    GBA_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
+    static bool attr = false;
+    const int smem = 2 * NB * kSP * sizeof(double);
+    const int tsmem = 2 * NB * (NB + 1) * sizeof(double);
+    if (!attr) {
+        GBA_CUDA_CHECK(cudaFuncSetAttribute(syrk_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        GBA_CUDA_CHECK(cudaFuncSetAttribute(trsm_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
+        attr = true;
+    }
+    const int nt = n / NB;
+    for (int jb = 0; jb < nt; ++jb) {
+        const int j0 = jb * NB;
+        potrf_diag_kernel<<<1, 256, 0, s>>>(A, j0, lda, info);
+        GBA_LAUNCH_CHECK();
+        const int below = nt - jb - 1;
+        if (below == 0) break;
+        trsm_panel_kernel<<<below, 256, tsmem, s>>>(A, j0, lda, info);
+        GBA_LAUNCH_CHECK();
+        const long long tiles = (long long)below * (below + 1) / 2;
+        syrk_update_kernel<<<static_cast<unsigned>(tiles), 256, smem, s>>>(A, j0, below, lda, info);
+        GBA_LAUNCH_CHECK();
+    }
+}
+
+void dense_potrs(const double* L, int n, int lda, double* b, const int* info, cudaStream_t s) {
+    if (n % NB != 0 || lda < n) throw std::invalid_argument("dense_potrs: n must be a multiple of 64, lda >= n");
+    const int nt = n / NB;
+    for (int jb = 0; jb < nt; ++jb) {
+        const int j0 = jb * NB;
+        trsv_lower_diag<<<1, NB, 0, s>>>(L, j0, lda, b, info);
+        GBA_LAUNCH_CHECK();
+        if (j0 + NB < n) {
+            gemv_lower_below<<<ceil_div(n - j0 - NB, 256), 256, 0, s>>>(L, j0, n, lda, b, info);
+            GBA_LAUNCH_CHECK();
+        }
+    }
+    for (int jb = nt - 1; jb >= 0; --jb) {
+        const int j0 = jb * NB;
+        trsv_upper_diag<<<1, NB, 0, s>>>(L, j0, lda, b, info);
+        GBA_LAUNCH_CHECK();
+        if (j0 > 0) {
+            gemv_upper_above<<<ceil_div(32ll * j0, 256), 256, 0, s>>>(L, j0, lda, b, info);
+            GBA_LAUNCH_CHECK();
+        }
+    }
+}
+
+int Solver::schur_dense(double lambda) {
+    const int lda = n_pad_;
+    compute_T_kernel<<<std::min(ceil_div(E_, 256), 32 * device_sm_count()), 256, 0, stream_>>>(
+        W_.get(), Vinv_.get(), s_pt_.get(), E_, T_.get());
+    GBA_LAUNCH_CHECK();
+    GBA_CUDA_CHECK(cudaMemsetAsync(S_.get(), 0, S_.size() * sizeof(double), stream_));
+    if (n_blocks_ > 0) {
+        assemble_kernel<<<ceil_div(9ll * n_blocks_, 288), 288, 0, stream_>>>(
+            block_off_.get(), block_ce_.get(), block_cf_.get(), pair_e_.get(), pair_f_.get(), T_.get(), W_.get(),
+            n_blocks_, lda, S_.get());
+        GBA_LAUNCH_CHECK();
+    }
+    add_damped_u_kernel<<<ceil_div(81ll * C_ + (n_pad_ - 9 * C_), 256), 256, 0, stream_>>>(U_.get(), lambda, C_,
+                                                                                        n_pad_, lda, S_.get());
+    GBA_LAUNCH_CHECK();
+    GBA_CUDA_CHECK(cudaMemsetAsync(rhs_.get(), 0, rhs_.size() * sizeof(double), stream_));
+    rhs_kernel<<<C_, 128, 0, stream_>>>(cam_off_.get(), cam_slots_.get(), s_pt_.get(), T_.get(), bp_.get(),
+                                        bc_.get(), rhs_.get());
+    GBA_LAUNCH_CHECK();
+    dense_potrf(S_.get(), n_pad_, lda, info_.get(), stream_);
+    int info = 0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&info, info_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    sync();
+    if (info != 0) return info;
+    // solve in a copy so rhs stays the assembled right-hand side
+    GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), rhs_.get(), n_pad_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   stream_));
+    dense_potrs(S_.get(), n_pad_, lda, pcg_x_.get(), info_.get(), stream_);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(dc_.get(), pcg_x_.get(), 9ull * C_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   stream_));
+    sync();
+    return 0;
+}
+
+}  // namespace gba

@@ -1,0 +1,179 @@
+#pragma once
+// Device-resident LM state for one BAL problem and the stage functions the
+// LM driver (lm.cpp) and the C-ABI (capi.cpp) call. Host-only header: the
+// kernels live in structure.cu, edge.cu, blocks.cu, dense.cu, pcg.cu, mlp.cu.
+//
+// HBM layout (all device buffers owned by Solver, RAII):
+//   parameters     cams[9C], pts[3P] (FP64, BAL layout) + trial copies
+//   structure      observations stably sorted by point ("slots" s = 0..E-1):
+//                  order[s] (original index), s_cam[s], s_pt[s], s_px[2s..2s+1],
+//                  pt_off[P+1] (CSR), and a camera-major view cam_slots[] / cam_off[C+1]
+//   work chunks    point chunks (whole points, <= 256 slots) for the point pass;
+//                  camera chunks (<= kCamChunk slots of one camera) for the camera pass
+//   normal eqs     U[81C] (full symmetric 9x9), bc[9C], V[6P] (packed lower 3x3),
+//                  bp[3P], W[27 E] (FP64, slot order) or J32[28 E] (FP32: Jc, Jp, r)
+//   Schur (plain)  pair list sorted by camera-pair block, dense S (n_pad x n_pad,
+//                  column-major, lower triangle), rhs, dc, dp
+//   Schur (mixed)  PCG vectors (9C) and block-Jacobi factors (81C)
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gba/lm.hpp"
+
+namespace gba {
+
+template <typename T>
+class DevBuf {
+public:
+    DevBuf() = default;
+    explicit DevBuf(size_t n) { alloc(n); }
+    ~DevBuf() { release(); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p_ = o.p_; n_ = o.n_; o.p_ = nullptr; o.n_ = 0; }
+        return *this;
+    }
+    void alloc(size_t n);   // defined in structure.cu (throws CudaError)
+    void release();
+    T* get() const { return p_; }
+    size_t size() const { return n_; }
+    void swap(DevBuf& o) { std::swap(p_, o.p_); std::swap(n_, o.n_); }
+
+private:
+    T* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+struct PcgStats {
+    int refine_steps = 0;
+    long long pcg_iterations = 0;
+    double rel_residual = 0.0;  // final ||rhs - S dc|| / ||rhs|| (FP64)
+    bool converged = false;
+};
+
+struct PhaseTimes {
+    double setup = 0, accumulate = 0, damp = 0, schur = 0, backsub = 0, cost = 0;
+};
+
+class LearnedPreconditioner;  // mlp.cu
+
+class Solver {
+public:
+    // Copies the problem to the device and builds the slot structure. Host arrays
+    // in the BAL layout; observation indices are bounds-checked on the host.
+    Solver(int C, int P, int E, const double* cams, const double* pts, const int* obs_cam,
+           const int* obs_pt, const double* obs_px, SolverForm form, cudaStream_t stream);
+    ~Solver();
+
+    int C() const { return C_; }
+    int P() const { return P_; }
+    int E() const { return E_; }
+    int n_pad() const { return n_pad_; }
+    SolverForm form() const { return form_; }
+    cudaStream_t stream() const { return stream_; }
+
+    void set_params(const double* cams, const double* pts);
+    void get_params(double* cams, double* pts) const;
+
+    // Normal equations at the current parameters: FP64 (plain) or FP32
+    // Jacobians with FP64 accumulation (mixed). Returns the SSE; adds non-finite
+    // edges to the anomaly counter.
+    double accumulate();
+    // V' = V + lambda * max(diag V, 1e-12), inverted per point. Returns the number
+    // of non-SPD blocks found by this call.
+    unsigned long long damp_invert_v(double lambda);
+    // Plain form: assemble dense S and rhs, Cholesky-factor, solve for dc.
+    // Returns 0 on success, else the (1-based) failed pivot column.
+    int schur_dense(double lambda);
+    // Mixed form: solve S dc = rhs by FP32 PCG inside FP64 iterative refinement.
+    PcgStats schur_pcg(double lambda, const LMOptions& opts, bool learned);
+    // dp = V'^-1 (bp - sum_e W_e^T dc), the gain denominator, and the trial
+    // parameters (current + step). Returns the denominator (SSE units).
+    double back_substitute(double lambda);
+    // SSE at the trial parameters (FP64); adds non-finite residuals to the
+    // anomaly counter.
+    double trial_cost();
+    // Trial parameters become current.
+    void accept();
+
+    unsigned long long anomalies() const;     // cumulative counter[0]
+    unsigned long long nonspd_total() const;  // cumulative counter[1]
+
+    // Learned preconditioner (MixedLearned form).
+    void load_model(const std::string& path);
+    LearnedPreconditioner* model() { return model_; }
+
+    // Raw views for the C-ABI download/inspection entry points.
+    enum Buf { kU, kV, kBc, kBp, kW, kVinv, kS, kRhs, kDc, kDp, kOrder, kJ32, kSdiag, kCams, kPts,
+               kTrialCams, kTrialPts };
+    const void* buffer(Buf b, size_t* bytes) const;
+
+    PhaseTimes times;
+    bool timing = false;  // synchronise after each stage and accumulate phase wall times
+
+    // ---- internal state (public for the kernel translation units) ----
+    int C_, P_, E_, n_pad_ = 0;
+    SolverForm form_;
+    cudaStream_t stream_;
+    LearnedPreconditioner* model_ = nullptr;
+
+    DevBuf<double> cams_, pts_, tcams_, tpts_;
+    // structure
+    DevBuf<int> order_, pt_off_, s_cam_, s_pt_, cam_off_, cam_slots_;
+    DevBuf<double> s_px_;
+    int n_pchunk_ = 0, n_cchunk_ = 0;
+    DevBuf<int> pchunk_, cchunk_begin_, cchunk_cam_, cam_chunk_off_;
+    // normal equations
+    DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
+    DevBuf<float> J32_;
+    DevBuf<double> sse_part_, cam_part_, scal_;  // scal_: [0] sse, [1] trial sse, [2] denom, [3..] scratch
+    DevBuf<unsigned long long> counters_;        // [0] anomalies, [1] non-SPD V blocks
+    // plain Schur
+    long long n_pairs_ = 0;
+    int n_blocks_ = 0;
+    DevBuf<int> pair_e_, pair_f_, block_off_, block_ce_, block_cf_;
+    DevBuf<double> T_, S_, rhs_, dc_, dp_, red_part_;
+    DevBuf<int> info_;
+    // mixed Schur
+    DevBuf<double> Sdiag_, Pfac_;  // S diagonal blocks (81C), preconditioner factors (81C)
+    DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_;
+    DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or FP64)
+    DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
+    DevBuf<float> mlp_in_;   // learned form: per-camera features
+
+    void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px);
+    void build_pairs();
+    void sync() const;
+};
+
+// Host-side checks of a BAL problem (sizes, null arrays, index ranges); throws
+// std::invalid_argument. Runs before any device work.
+void validate_problem(int C, int P, int E, const double* cams, const double* pts, const int* obs_cam,
+                      const int* obs_pt, const double* obs_px);
+
+// Standalone kernels with raw device pointers (C-ABI entry points wrap these).
+void launch_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n,
+                                     cudaStream_t s);
+void launch_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, cudaStream_t s);
+// Blocked dense Cholesky (lower, column-major). n must be a multiple of 64,
+// lda >= n. info (device int) = 0 on success, else the 1-based failed column.
+void dense_potrf(double* A, int n, int lda, int* info, cudaStream_t s);
+// Solves L L^T x = b in place (b on the device, length n), L from dense_potrf.
+void dense_potrs(const double* L, int n, int lda, double* b, const int* info, cudaStream_t s);
+// Residual + Jacobian for E independent observations (device pointers, original
+// layout). Jc, Jp may be null. FP64 or FP32 arithmetic.
+void launch_eval_edges_f64(const double* cams, const double* pts, const int* oc, const int* op,
+                           const double* px, int E, double* r, double* Jc, double* Jp,
+                           cudaStream_t s);
+void launch_eval_edges_f32(const double* cams, const double* pts, const int* oc, const int* op,
+                           const double* px, int E, float* r, float* Jc, float* Jp,
+                           cudaStream_t s);
+
+}  // namespace gba

@@ -1,0 +1,446 @@
+// Problem upload and slot structure: observations stably sorted by point
+// (CSR over points), a camera-major view of the same slots, the work chunks of
+// the point and camera passes, and (plain form) the list of edge pairs that
+// feed each camera-pair block of the reduced camera system.
+//
+// The reference keeps observations in file order and builds a host adjacency
+// list point -> edges (src/lm.cu:380-381); there is no sorted layout there. This
+// layout is what lets every reduction in this library run without atomics.
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_run_length_encode.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <climits>
+#include <vector>
+
+#include "common.cuh"
+#include "solver.hpp"
+
+namespace gba {
+
+template <typename T>
+void DevBuf<T>::alloc(size_t n) {
+    release();
+    if (n == 0) return;
+    GBA_CUDA_CHECK(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)));
+    n_ = n;
+}
+template <typename T>
+void DevBuf<T>::release() {
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+}
+template class DevBuf<double>;
+template class DevBuf<float>;
+template class DevBuf<int>;
+template class DevBuf<unsigned long long>;
+template class DevBuf<unsigned int>;
+template class DevBuf<unsigned char>;
+template class DevBuf<long long>;
+
+int device_sm_count() {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0;
+        GBA_CUDA_CHECK(cudaGetDevice(&dev));
+        GBA_CUDA_CHECK(cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev));
+    }
+    return cached;
+}
+
+namespace {
+
+constexpr int kPointChunk = 256;   // max slots (and max points) per point-pass CTA
+constexpr int kCamChunk = 1024;    // max slots per camera-pass CTA
+
+__global__ void iota_kernel(int* v, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
+__global__ void gather_obs_kernel(const int* __restrict__ order, const int* __restrict__ oc,
+                                  const double* __restrict__ px, int E, int* __restrict__ s_cam,
+                                  double2* __restrict__ s_px) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+        const int e = order[s];
+        s_cam[s] = oc[e];
+        s_px[s] = make_double2(px[2 * e], px[2 * e + 1]);
+    }
+}
+
+// offsets[k] = first position i with keys[i] >= k, for k = 0..nk (keys sorted).
+__global__ void csr_offsets_kernel(const int* __restrict__ keys, int n, int nk, int* __restrict__ off) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int prev = i == 0 ? -1 : keys[i - 1];
+        const int cur = keys[i];
+        for (int k = prev + 1; k <= cur; ++k) off[k] = i;
+        if (i == n - 1)
+            for (int k = cur + 1; k <= nk; ++k) off[k] = n;
+    }
+}
+
+// Number of ordered slot pairs (e, f) of point p with cam(e) >= cam(f).
+__global__ void pair_count_kernel(const int* __restrict__ pt_off, const int* __restrict__ s_cam, int P,
+                                  long long* __restrict__ cnt) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const int b = pt_off[p], e = pt_off[p + 1];
+        long long n = 0;
+        for (int i = b; i < e; ++i) {
+            const int ci = s_cam[i];
+            for (int j = b; j < e; ++j) n += (s_cam[j] <= ci);
+        }
+        cnt[p] = n;
+    }
+}
+
+__global__ void pair_fill_kernel(const int* __restrict__ pt_off, const int* __restrict__ s_cam, int P,
+                                 int C, const long long* __restrict__ base,
+                                 unsigned long long* __restrict__ key, unsigned long long* __restrict__ val) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const int b = pt_off[p], e = pt_off[p + 1];
+        long long o = base[p];
+        for (int i = b; i < e; ++i) {
+            const int ci = s_cam[i];
+            for (int j = b; j < e; ++j) {
+                const int cj = s_cam[j];
+                if (cj <= ci) {
+                    key[o] = static_cast<unsigned long long>(ci) * static_cast<unsigned long long>(C) + cj;
+                    val[o] = (static_cast<unsigned long long>(static_cast<unsigned>(i)) << 32) |
+                             static_cast<unsigned>(j);
+                    ++o;
+                }
+            }
+        }
+    }
+}
+
+__global__ void pair_split_kernel(const unsigned long long* __restrict__ val, long long n, int* __restrict__ pe,
+                                  int* __restrict__ pf) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long v = val[i];
+        pe[i] = static_cast<int>(v >> 32);
+        pf[i] = static_cast<int>(v & 0xffffffffu);
+    }
+}
+
+__global__ void block_split_kernel(const unsigned long long* __restrict__ ukey, int nb, int C,
+                                   int* __restrict__ ce, int* __restrict__ cf) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
+        const unsigned long long k = ukey[i];
+        ce[i] = static_cast<int>(k / static_cast<unsigned long long>(C));
+        cf[i] = static_cast<int>(k % static_cast<unsigned long long>(C));
+    }
+}
+
+int bits_for(long long n) {
+    int b = 1;
+    while ((1LL << b) < n) ++b;
+    return b;
+}
+
+int grid_for(long long n, int threads = 256) {
+    const long long want = (n + threads - 1) / threads;
+    const long long cap = 32LL * device_sm_count();
+    return static_cast<int>(std::max<long long>(1, std::min(want, cap)));
+}
+
+}  // namespace
+
+void validate_problem(int C, int P, int E, const double* cams, const double* pts, const int* obs_cam,
+                      const int* obs_pt, const double* obs_px) {
+    if (C <= 0 || P <= 0 || E <= 0) throw std::invalid_argument("empty BAL problem");
+    if (!cams || !pts || !obs_cam || !obs_pt || !obs_px) throw std::invalid_argument("null problem array");
+    for (int e = 0; e < E; ++e)
+        if (obs_cam[e] < 0 || obs_cam[e] >= C || obs_pt[e] < 0 || obs_pt[e] >= P)
+            throw std::invalid_argument("observation index out of range");
+    if (static_cast<long long>(C) * 9 > INT_MAX / 2) throw std::invalid_argument("too many cameras");
+}
+
+Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const int* obs_cam,
+               const int* obs_pt, const double* obs_px, SolverForm form, cudaStream_t stream)
+    : C_(C), P_(P), E_(E), form_(form), stream_(stream) {
+    validate_problem(C, P, E, cams, pts, obs_cam, obs_pt, obs_px);
+
+    cams_.alloc(9ull * C);
+    pts_.alloc(3ull * P);
+    tcams_.alloc(9ull * C);
+    tpts_.alloc(3ull * P);
+    counters_.alloc(4);  // [0] anomalies, [1] non-SPD V blocks, [2] scratch, [3] per-call non-SPD
+    scal_.alloc(8);
+    GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get(), 0, 4 * sizeof(unsigned long long), stream_));
+    set_params(cams, pts);
+    build_structure(obs_cam, obs_pt, obs_px);
+
+    // normal equations (both forms)
+    U_.alloc(81ull * C);
+    bc_.alloc(9ull * C);
+    V_.alloc(6ull * P);
+    bp_.alloc(3ull * P);
+    Vinv_.alloc(6ull * P);
+    dc_.alloc(9ull * C);
+    dp_.alloc(3ull * P);
+    sse_part_.alloc(std::max(n_pchunk_, 1));
+    cam_part_.alloc(54ull * std::max(n_cchunk_, 1));
+    red_part_.alloc(ceil_div(P, 256) + 2 * ceil_div(9ll * C, 256) + 64);
+    if (form_ == SolverForm::Plain) {
+        W_.alloc(27ull * E);
+        JcR_.alloc(20ull * E);
+        T_.alloc(27ull * E);
+        n_pad_ = ((9 * C + 63) / 64) * 64;
+        S_.alloc(static_cast<size_t>(n_pad_) * n_pad_);
+        rhs_.alloc(n_pad_);
+        pcg_x_.alloc(n_pad_);  // dense solve work vector
+        info_.alloc(1);
+        build_pairs();
+    } else {
+        J32_.alloc(24ull * E);
+        Sdiag_.alloc(81ull * C);
+        Pfac_.alloc(81ull * C);
+        rhs_.alloc(9ull * C);
+        pcg_x_.alloc(9ull * C);
+        pcg_r_.alloc(9ull * C);
+        pcg_z_.alloc(9ull * C);
+        pcg_p_.alloc(9ull * C);
+        pcg_q_.alloc(9ull * C);
+        ref_r_.alloc(9ull * C);
+        u_.alloc(2ull * E);
+        pcg_s_.alloc(16);
+    }
+    sync();
+}
+
+void Solver::sync() const { GBA_CUDA_CHECK(cudaStreamSynchronize(stream_)); }
+
+void Solver::set_params(const double* cams, const double* pts) {
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cams_.get(), cams, 9ull * C_ * sizeof(double), cudaMemcpyHostToDevice,
+                                   stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(pts_.get(), pts, 3ull * P_ * sizeof(double), cudaMemcpyHostToDevice,
+                                   stream_));
+}
+
+void Solver::get_params(double* cams, double* pts) const {
+    if (cams)
+        GBA_CUDA_CHECK(cudaMemcpyAsync(cams, cams_.get(), 9ull * C_ * sizeof(double), cudaMemcpyDeviceToHost,
+                                       stream_));
+    if (pts)
+        GBA_CUDA_CHECK(cudaMemcpyAsync(pts, pts_.get(), 3ull * P_ * sizeof(double), cudaMemcpyDeviceToHost,
+                                       stream_));
+    sync();
+}
+
+void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px) {
+    const int E = E_, P = P_, C = C_;
+    DevBuf<int> d_oc(E), d_op(E), keys_sorted(E), iota(E);
+    DevBuf<double> d_px(2ull * E);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(d_oc.get(), obs_cam, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(d_op.get(), obs_pt, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    GBA_CUDA_CHECK(
+        cudaMemcpyAsync(d_px.get(), obs_px, 2ull * E * sizeof(double), cudaMemcpyHostToDevice, stream_));
+
+    order_.alloc(E);
+    s_cam_.alloc(E);
+    s_pt_.alloc(E);
+    s_px_.alloc(2ull * E);
+    pt_off_.alloc(P + 1ull);
+    cam_off_.alloc(C + 1ull);
+    cam_slots_.alloc(E);
+
+    iota_kernel<<<grid_for(E), 256, 0, stream_>>>(iota.get(), E);
+    GBA_LAUNCH_CHECK();
+
+    // 1. stable sort of observations by point
+    size_t tmp_bytes = 0, tmp2 = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, d_op.get(), s_pt_.get(), iota.get(), order_.get(), E,
+                                    0, bits_for(P + 1), stream_);
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp2, d_oc.get(), keys_sorted.get(), iota.get(),
+                                    cam_slots_.get(), E, 0, bits_for(C + 1), stream_);
+    DevBuf<unsigned char> tmp(std::max(tmp_bytes, tmp2));
+    size_t tb = tmp.size();
+    GBA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tmp.get(), tb, d_op.get(), s_pt_.get(), iota.get(),
+                                                   order_.get(), E, 0, bits_for(P + 1), stream_));
+    gather_obs_kernel<<<grid_for(E), 256, 0, stream_>>>(order_.get(), d_oc.get(), d_px.get(), E, s_cam_.get(),
+                                                        reinterpret_cast<double2*>(s_px_.get()));
+    GBA_LAUNCH_CHECK();
+    csr_offsets_kernel<<<grid_for(E), 256, 0, stream_>>>(s_pt_.get(), E, P, pt_off_.get());
+    GBA_LAUNCH_CHECK();
+
+    // 2. camera-major view of the slots (stable: slot order within a camera)
+    tb = tmp.size();
+    GBA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tmp.get(), tb, s_cam_.get(), keys_sorted.get(), iota.get(),
+                                                   cam_slots_.get(), E, 0, bits_for(C + 1), stream_));
+    csr_offsets_kernel<<<grid_for(E), 256, 0, stream_>>>(keys_sorted.get(), E, C, cam_off_.get());
+    GBA_LAUNCH_CHECK();
+
+    // 3. work chunks, built on the host from the CSR offsets
+    std::vector<int> h_pt_off(P + 1), h_cam_off(C + 1);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(h_pt_off.data(), pt_off_.get(), (P + 1) * sizeof(int),
+                                   cudaMemcpyDeviceToHost, stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(h_cam_off.data(), cam_off_.get(), (C + 1) * sizeof(int),
+                                   cudaMemcpyDeviceToHost, stream_));
+    sync();
+
+    std::vector<int> pchunk;
+    pchunk.reserve(E / 64 + 16);
+    pchunk.push_back(0);
+    int edges = 0, pts_in = 0;
+    for (int p = 0; p < P; ++p) {
+        const int k = h_pt_off[p + 1] - h_pt_off[p];
+        if (pts_in > 0 && (edges + k > kPointChunk || pts_in >= kPointChunk)) {
+            pchunk.push_back(p);
+            edges = 0;
+            pts_in = 0;
+        }
+        edges += k;
+        ++pts_in;
+    }
+    pchunk.push_back(P);
+    n_pchunk_ = static_cast<int>(pchunk.size()) - 1;
+
+    std::vector<int> cbeg, ccam, cam_chunk_off(C + 1);
+    for (int c = 0; c < C; ++c) {
+        cam_chunk_off[c] = static_cast<int>(cbeg.size());
+        for (int b = h_cam_off[c]; b < h_cam_off[c + 1]; b += kCamChunk) {
+            cbeg.push_back(b);
+            ccam.push_back(c);
+        }
+    }
+    cam_chunk_off[C] = static_cast<int>(cbeg.size());
+    n_cchunk_ = static_cast<int>(cbeg.size());
+
+    pchunk_.alloc(pchunk.size());
+    cchunk_begin_.alloc(std::max<size_t>(cbeg.size(), 1));
+    cchunk_cam_.alloc(std::max<size_t>(ccam.size(), 1));
+    cam_chunk_off_.alloc(C + 1ull);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(pchunk_.get(), pchunk.data(), pchunk.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice, stream_));
+    if (!cbeg.empty()) {
+        GBA_CUDA_CHECK(cudaMemcpyAsync(cchunk_begin_.get(), cbeg.data(), cbeg.size() * sizeof(int),
+                                       cudaMemcpyHostToDevice, stream_));
+        GBA_CUDA_CHECK(cudaMemcpyAsync(cchunk_cam_.get(), ccam.data(), ccam.size() * sizeof(int),
+                                       cudaMemcpyHostToDevice, stream_));
+    }
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cam_chunk_off_.get(), cam_chunk_off.data(), (C + 1) * sizeof(int),
+                                   cudaMemcpyHostToDevice, stream_));
+    sync();  // host vectors die at scope exit
+}
+
+void Solver::build_pairs() {
+    const int P = P_, C = C_;
+    DevBuf<long long> cnt(P + 1ull), base(P + 1ull);
+    pair_count_kernel<<<grid_for(P), 256, 0, stream_>>>(pt_off_.get(), s_cam_.get(), P, cnt.get());
+    GBA_LAUNCH_CHECK();
+    GBA_CUDA_CHECK(cudaMemsetAsync(cnt.get() + P, 0, sizeof(long long), stream_));
+    size_t tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt.get(), base.get(), P + 1, stream_);
+    {
+        DevBuf<unsigned char> tmp(tb);
+        GBA_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(tmp.get(), tb, cnt.get(), base.get(), P + 1, stream_));
+    }
+    long long npairs = 0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&npairs, base.get() + P, sizeof(long long), cudaMemcpyDeviceToHost, stream_));
+    sync();
+    if (npairs <= 0 || npairs > INT_MAX) throw std::invalid_argument("Schur pair list size out of range");
+    n_pairs_ = npairs;
+
+    DevBuf<unsigned long long> key(npairs), key2(npairs), val(npairs), val2(npairs);
+    pair_fill_kernel<<<grid_for(P), 256, 0, stream_>>>(pt_off_.get(), s_cam_.get(), P, C, base.get(), key.get(),
+                                                       val.get());
+    GBA_LAUNCH_CHECK();
+    const int kb = bits_for(static_cast<long long>(C) * C + 1);
+    tb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, key.get(), key2.get(), val.get(), val2.get(), npairs, 0, kb,
+                                    stream_);
+    {
+        DevBuf<unsigned char> tmp(tb);
+        GBA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tmp.get(), tb, key.get(), key2.get(), val.get(), val2.get(),
+                                                       npairs, 0, kb, stream_));
+    }
+    pair_e_.alloc(npairs);
+    pair_f_.alloc(npairs);
+    pair_split_kernel<<<grid_for(npairs), 256, 0, stream_>>>(val2.get(), npairs, pair_e_.get(), pair_f_.get());
+    GBA_LAUNCH_CHECK();
+    val.release();
+    val2.release();
+
+    // run-length encode the block keys -> blocks and their pair ranges
+    DevBuf<unsigned long long> ukey(npairs);
+    DevBuf<int> counts(npairs + 1), nruns(1);
+    tb = 0;
+    cub::DeviceRunLengthEncode::Encode(nullptr, tb, key2.get(), ukey.get(), counts.get(), nruns.get(),
+                                       static_cast<int>(npairs), stream_);
+    {
+        DevBuf<unsigned char> tmp(tb);
+        GBA_CUDA_CHECK(cub::DeviceRunLengthEncode::Encode(tmp.get(), tb, key2.get(), ukey.get(), counts.get(),
+                                                          nruns.get(), static_cast<int>(npairs), stream_));
+    }
+    int nb = 0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&nb, nruns.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    sync();
+    n_blocks_ = nb;
+    block_off_.alloc(nb + 1ull);
+    block_ce_.alloc(nb);
+    block_cf_.alloc(nb);
+    GBA_CUDA_CHECK(cudaMemsetAsync(counts.get() + nb, 0, sizeof(int), stream_));
+    tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, counts.get(), block_off_.get(), nb + 1, stream_);
+    {
+        DevBuf<unsigned char> tmp(tb);
+        GBA_CUDA_CHECK(
+            cub::DeviceScan::ExclusiveSum(tmp.get(), tb, counts.get(), block_off_.get(), nb + 1, stream_));
+    }
+    block_split_kernel<<<grid_for(nb), 256, 0, stream_>>>(ukey.get(), nb, C, block_ce_.get(), block_cf_.get());
+    GBA_LAUNCH_CHECK();
+    sync();
+}
+
+unsigned long long Solver::anomalies() const {
+    unsigned long long h[2];
+    GBA_CUDA_CHECK(cudaMemcpyAsync(h, counters_.get(), sizeof h, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    return h[0];
+}
+
+unsigned long long Solver::nonspd_total() const {
+    unsigned long long h[2];
+    GBA_CUDA_CHECK(cudaMemcpyAsync(h, counters_.get(), sizeof h, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    return h[1];
+}
+
+void Solver::accept() {
+    cams_.swap(tcams_);
+    pts_.swap(tpts_);
+}
+
+const void* Solver::buffer(Buf b, size_t* bytes) const {
+    auto ret = [&](const auto& buf) -> const void* {
+        *bytes = buf.size() * sizeof(*buf.get());
+        return buf.get();
+    };
+    switch (b) {
+        case kU: return ret(U_);
+        case kV: return ret(V_);
+        case kBc: return ret(bc_);
+        case kBp: return ret(bp_);
+        case kW: return ret(W_);
+        case kVinv: return ret(Vinv_);
+        case kS: return ret(S_);
+        case kRhs: return ret(rhs_);
+        case kDc: return ret(dc_);
+        case kDp: return ret(dp_);
+        case kOrder: return ret(order_);
+        case kJ32: return ret(J32_);
+        case kSdiag: return ret(Sdiag_);
+        case kCams: return ret(cams_);
+        case kPts: return ret(pts_);
+        case kTrialCams: return ret(tcams_);
+        case kTrialPts: return ret(tpts_);
+    }
+    *bytes = 0;
+    return nullptr;
+}
+
+}  // namespace gba

@@ -1,0 +1,82 @@
+#pragma once
+// Drop-in public interface of the GB300 Levenberg-Marquardt solver.
+//
+// The reference declarations (include/gba/lm.hpp:13-42) are kept: LMOptions with
+// the same five fields and defaults, LMResult with the same six fields, the same
+// solve_bal_gpu and edge_residual_jacobian_host signatures. Everything after the
+// "additive" markers is new, defaulted, and ignorable by reference callers.
+//
+// Parameters live in the caller's BALProblem (host, FP64) and are updated in place.
+
+#include <string>
+#include <vector>
+
+#include "gba/bal_problem.hpp"
+
+namespace gba {
+
+// How the reduced camera system S dc = rhs is solved each trial.
+enum class SolverForm {
+    // All FP64: FP64 residuals/Jacobians, dense S assembled on the device and
+    // factored by the blocked FP64 tensor-core (DMMA) Cholesky. The drop-in.
+    Plain = 0,
+    // FP32 residuals/Jacobians with FP64 accumulation; S never formed: FP32
+    // implicit matvecs inside block-Jacobi PCG, wrapped in FP64 iterative
+    // refinement. Cost evaluation, refinement residual and 3x3 inverses FP64.
+    Mixed = 1,
+    // Mixed, with the block-Jacobi preconditioner corrected by the learned
+    // per-camera MLP (weights from LMOptions::model_path).
+    MixedLearned = 2,
+};
+
+struct LMOptions {
+    int max_iterations = 50;
+    double initial_lambda = 1e-3;    // Marquardt diagonal damping
+    double rel_decrease_tol = 1e-6;  // convergence: relative cost decrease
+    int max_inner_trials = 16;       // lambda escalations per outer iteration
+    bool verbose = false;            // per-trial log to stderr
+
+    // ---- additive ----
+    SolverForm form = SolverForm::Plain;
+    double refine_tol = 1e-8;     // mixed: FP64 refinement stops at ||rhs - S dc|| <= tol ||rhs||
+    int refine_max_steps = 8;     // mixed: FP64 refinement steps per trial
+    double pcg_tol = 1e-2;        // mixed: relative residual target of each inner FP32 PCG solve
+    int pcg_max_iters = 200;      // mixed: PCG iteration cap per inner solve
+    std::string model_path;       // learned form: MLP weights file (gba_mlp binary)
+    double target_cost = 0.0;     // if > 0: record the wall time at which cost first <= target
+};
+
+struct LMResult {
+    double initial_cost = 0.0;
+    double final_cost = 0.0;
+    int iterations = 0;               // accepted outer iterations
+    std::string termination;          // "CONVERGENCE" | "MAX_ITERATIONS" | "FAILURE"
+    unsigned long long anomalies = 0; // cumulative non-finite edge / trial-residual count
+    double total_time_s = 0.0;        // wall time of the solve, device setup included
+
+    // ---- additive ----
+    std::vector<double> trajectory;        // cost at start and after every accepted iteration
+    std::vector<double> trajectory_time_s; // wall time (from solve start) of each trajectory entry
+    int trials = 0;                        // inner trials evaluated (accepted + rejected)
+    long long pcg_iterations = 0;          // mixed: total inner PCG iterations
+    int refine_steps = 0;                  // mixed: total FP64 refinement steps
+    double time_to_target_s = -1.0;        // first time cost <= LMOptions::target_cost, or -1
+    // Phase wall times (device-synchronised): setup, accumulate, damp+V^-1,
+    // Schur solve (assembly+factor or PCG), back-substitution, trial cost.
+    double t_setup = 0, t_accumulate = 0, t_damp = 0, t_schur = 0, t_backsub = 0, t_cost = 0;
+};
+
+// Runs LM on the current CUDA device. Modifies prob's cameras and points to the
+// solution. Throws std::runtime_error on CUDA failure or invalid input
+// (reference: include/gba/lm.hpp:34, src/lm.cu:371-724).
+LMResult solve_bal_gpu(BALProblem& prob, const LMOptions& opts = {});
+
+// Host entry point to the same residual + analytic Jacobian that the FP64 edge
+// kernel evaluates (one __host__ __device__ template). Jc is 2x9 row-major
+// (rodrigues[3], t[3], f, k1, k2), Jp is 2x3 row-major
+// (reference: include/gba/lm.hpp:40-42, src/lm.cu:365-369).
+void edge_residual_jacobian_host(const double* camera9, const double* point3,
+                                 const double* observed2, double* out_residual2,
+                                 double* out_Jc, double* out_Jp);
+
+}  // namespace gba

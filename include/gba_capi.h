@@ -1,0 +1,221 @@
+/*
+ * gba_capi.h — C ABI of the GB300 bundle-adjustment library (libgba_gb300.so).
+ *
+ * Plain C types only: pointers, sizes, an opaque solver handle and a
+ * cudaStream_t passed as void*. Every function returns an int status
+ * (GBA_OK = 0) and never throws; gba_last_error() returns the message of the
+ * last failure on the calling thread.
+ *
+ * The reference exposes a C++ API only (include/gba/lm.hpp, bal_problem.hpp,
+ * schur.cuh); each entry point below names the reference interface it stands in
+ * for. Pointers marked [host] are host memory; [device] are device memory of
+ * the current CUDA device.
+ */
+#ifndef GBA_CAPI_H
+#define GBA_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GBA_OK = 0,
+    GBA_ERR_INVALID = 1,  /* bad argument / malformed input */
+    GBA_ERR_CUDA = 2,     /* CUDA runtime failure */
+    GBA_ERR_NOT_SPD = 3,  /* a factorisation met a non-positive pivot */
+    GBA_ERR_IO = 4,       /* file read / write failure */
+    GBA_ERR_INTERNAL = 5
+};
+
+enum { GBA_FORM_PLAIN = 0, GBA_FORM_MIXED = 1, GBA_FORM_MIXED_LEARNED = 2 };
+enum { GBA_TERM_CONVERGENCE = 0, GBA_TERM_MAX_ITERATIONS = 1, GBA_TERM_FAILURE = 2 };
+
+const char* gba_last_error(void);
+const char* gba_version(void);
+
+/* ------------------------------------------------------------ whole solve */
+
+/* Mirrors gba::LMOptions (reference include/gba/lm.hpp:13-19) plus the
+ * additive fields of this library. Fill with gba_lm_options_default. */
+typedef struct gba_lm_options {
+    int max_iterations;       /* 50 */
+    double initial_lambda;    /* 1e-3 */
+    double rel_decrease_tol;  /* 1e-6 */
+    int max_inner_trials;     /* 16 */
+    int verbose;              /* 0 */
+    int form;                 /* GBA_FORM_* (plain) */
+    double refine_tol;        /* 1e-8 */
+    int refine_max_steps;     /* 8 */
+    double pcg_tol;           /* 1e-2 */
+    int pcg_max_iters;        /* 200 */
+    const char* model_path;   /* learned-form weights, or NULL */
+    double target_cost;       /* 0 = off */
+} gba_lm_options;
+
+/* Mirrors gba::LMResult (reference include/gba/lm.hpp:21-29) plus additive
+ * fields. trajectory / trajectory_time_s may be NULL; otherwise they hold
+ * trajectory_capacity doubles and receive min(len, capacity) entries. */
+typedef struct gba_lm_result {
+    double initial_cost;
+    double final_cost;
+    int iterations;
+    int termination;                 /* GBA_TERM_* */
+    unsigned long long anomalies;
+    double total_time_s;
+    int trials;
+    long long pcg_iterations;
+    int refine_steps;
+    double time_to_target_s;
+    double t_setup, t_accumulate, t_damp, t_schur, t_backsub, t_cost;
+    double* trajectory;              /* [host] out */
+    double* trajectory_time_s;       /* [host] out */
+    int trajectory_capacity;
+    int trajectory_len;
+} gba_lm_result;
+
+void gba_lm_options_default(gba_lm_options* opts);
+
+/* LM solve of a BAL problem held in host arrays (BAL layout); cameras and
+ * points are updated in place. Replaces gba::solve_bal_gpu
+ * (reference include/gba/lm.hpp:34, src/lm.cu:371-724). [host] all arrays. */
+int gba_solve_bal(int num_cameras, int num_points, int num_observations, double* cameras, double* points,
+                  const int* obs_camera, const int* obs_point, const double* obs_pixel,
+                  const gba_lm_options* opts, gba_lm_result* result);
+
+/* ------------------------------------------------------------ CPU model / IO */
+
+/* Replaces gba::edge_residual_jacobian_host (reference include/gba/lm.hpp:40-42).
+ * [host] cam9, pt3, obs2 in; r2, Jc18 (2x9 row-major), Jp6 (2x3 row-major) out. */
+int gba_edge_residual_jacobian_host(const double* camera9, const double* point3, const double* observed2,
+                                    double* out_residual2, double* out_Jc, double* out_Jp);
+
+/* Replaces gba::snavely_residual (reference include/gba/bal_problem.hpp:45-46). [host] */
+int gba_snavely_residual(const double* camera9, const double* point3, const double* observed2, double* out2);
+
+/* Replaces gba::total_squared_error (reference include/gba/bal_problem.hpp:50). [host] */
+int gba_total_squared_error(int num_cameras, int num_points, int num_observations, const double* cameras,
+                            const double* points, const int* obs_camera, const int* obs_point,
+                            const double* obs_pixel, double* out_sse);
+
+/* Host-side problem handle: holds a BALProblem produced by the reader or the
+ * synthetic generator until its arrays are copied out. */
+typedef struct gba_host_problem gba_host_problem;
+
+/* Replaces gba::load_bal (reference include/gba/bal_problem.hpp:36). */
+int gba_host_problem_load(const char* path, gba_host_problem** out);
+/* Seeded synthetic workload 1..5 (no reference counterpart: stands in for the
+ * BAL datasets). If truth is non-NULL it receives the unperturbed problem. */
+int gba_host_problem_synthetic(int workload, uint64_t seed, gba_host_problem** out, gba_host_problem** truth);
+/* Same generator with explicit sizes (no reference counterpart). */
+int gba_host_problem_synthetic_custom(int num_cameras, int num_points, int track_min, int track_max,
+                                      double track_alpha, double outlier_fraction, double outlier_sigma,
+                                      uint64_t seed, gba_host_problem** out);
+/* The reference launch-bounds regression problem (tests/test_launch_bounds.cpp:28-80). */
+int gba_host_problem_launch_bounds(int num_points, gba_host_problem** out);
+int gba_host_problem_dims(const gba_host_problem* p, int* num_cameras, int* num_points, int* num_observations);
+/* Copies the arrays out; any destination may be NULL. [host] */
+int gba_host_problem_copy(const gba_host_problem* p, double* cameras, double* points, int* obs_camera,
+                          int* obs_point, double* obs_pixel);
+/* Writes a BAL text file (no reference counterpart in the library). */
+int gba_host_problem_save(const gba_host_problem* p, const char* path);
+void gba_host_problem_free(gba_host_problem* p);
+
+/* ------------------------------------------------------------ device stages */
+
+/* Device-resident LM state for one problem (parameters, sorted observation
+ * slots, normal equations, Schur buffers). The stage functions below are the
+ * steps of one LM trial; gba_solve_bal runs exactly these. They replace the
+ * per-stage code of reference src/lm.cu:371-724. */
+typedef struct gba_solver gba_solver;
+
+/* [host] arrays. stream: a cudaStream_t or NULL (the solver then creates one). */
+int gba_solver_create(int num_cameras, int num_points, int num_observations, const double* cameras,
+                      const double* points, const int* obs_camera, const int* obs_point, const double* obs_pixel,
+                      int form, void* stream, gba_solver** out);
+void gba_solver_destroy(gba_solver* s);
+int gba_solver_set_params(gba_solver* s, const double* cameras, const double* points);   /* [host] in */
+int gba_solver_get_params(gba_solver* s, double* cameras, double* points);               /* [host] out */
+/* Normal equations at the current parameters (reference edge_kernel +
+ * accumulate, src/lm.cu:205-252, 399-422). out_sse: FP64 SSE. */
+int gba_solver_accumulate(gba_solver* s, double* out_sse);
+/* Damped point-block inverses (reference damp_invert_v_kernel, src/lm.cu:289-302).
+ * out_nonspd: number of non-SPD blocks in this call. */
+int gba_solver_damp_invert_v(gba_solver* s, double lambda, unsigned long long* out_nonspd);
+/* Plain form: dense S assembly + FP64 DMMA Cholesky + solve (reference
+ * src/lm.cu:488-604). out_info: 0, or the failed pivot column (1-based). */
+int gba_solver_schur_dense(gba_solver* s, double lambda, int* out_info);
+/* Mixed forms: PCG + FP64 refinement (no reference counterpart). */
+int gba_solver_schur_pcg(gba_solver* s, double lambda, const gba_lm_options* opts, int learned,
+                         long long* out_pcg_iters, int* out_refine_steps, double* out_rel_residual);
+/* Back-substitution, gain denominator, trial parameters (reference src/lm.cu:606-654). */
+int gba_solver_back_substitute(gba_solver* s, double lambda, double* out_denom);
+/* FP64 SSE at the trial parameters (reference cost_kernel, src/lm.cu:255-281). */
+int gba_solver_trial_cost(gba_solver* s, double* out_sse);
+int gba_solver_accept(gba_solver* s);
+int gba_solver_counters(gba_solver* s, unsigned long long* out_anomalies, unsigned long long* out_nonspd);
+/* Loads the learned-preconditioner weights for the MixedLearned form. */
+int gba_solver_load_model(gba_solver* s, const char* path);
+
+enum {
+    GBA_BUF_U = 0,        /* double[81 C]  full symmetric 9x9 per camera */
+    GBA_BUF_V = 1,        /* double[6 P]   packed lower 3x3 per point (00,10,11,20,21,22) */
+    GBA_BUF_BC = 2,       /* double[9 C] */
+    GBA_BUF_BP = 3,       /* double[3 P] */
+    GBA_BUF_W = 4,        /* double[27 E]  9x3 row-major per slot (plain form) */
+    GBA_BUF_VINV = 5,     /* double[6 P]   packed */
+    GBA_BUF_S = 6,        /* double[n_pad^2] column-major (plain form; factor after schur_dense) */
+    GBA_BUF_RHS = 7,      /* double[n_pad] (plain) or [9 C] (mixed) */
+    GBA_BUF_DC = 8,       /* double[9 C] */
+    GBA_BUF_DP = 9,       /* double[3 P] */
+    GBA_BUF_ORDER = 10,   /* int[E]  original observation index of each slot */
+    GBA_BUF_J32 = 11,     /* float[24 E] Jc(18), Jp(6) per slot (mixed form) */
+    GBA_BUF_SDIAG = 12,   /* double[81 C] S diagonal blocks (mixed form) */
+    GBA_BUF_CAMS = 13,    /* double[9 C] current cameras */
+    GBA_BUF_PTS = 14,     /* double[3 P] current points */
+    GBA_BUF_TRIAL_CAMS = 15,
+    GBA_BUF_TRIAL_PTS = 16
+};
+/* Size in bytes of a solver buffer (0 if the form does not hold it). */
+int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out_bytes);
+/* Copies a solver buffer to the host. [host] dst of at least buffer_size bytes. */
+int gba_solver_download(gba_solver* s, int buffer, void* dst, size_t bytes);
+/* Device address of a solver buffer (for zero-copy use by the caller). */
+int gba_solver_device_ptr(gba_solver* s, int buffer, void** out_ptr);
+int gba_solver_dims(gba_solver* s, int* num_cameras, int* num_points, int* num_observations, int* n_pad);
+
+/* ------------------------------------------------------------ standalone kernels */
+
+/* Batched 9x9 SPD factor + solve, one block per thread; ok[i] = 0 where
+ * A_i is not SPD. Replaces gba::batch_chol9_factor_solve (reference
+ * include/gba/schur.cuh:104-109). [device] A (n x 81 row-major, lower read),
+ * b (n x 9), x (n x 9), ok (n). */
+int gba_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n, void* stream);
+
+/* Batched 3x3 SPD inverse. Replaces gba::batch_inverse3_spd (reference
+ * include/gba/schur.cuh:112-116). [device] A (n x 9 row-major, lower read), Ainv (n x 9). */
+int gba_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, void* stream);
+
+/* Blocked FP64 Cholesky (lower, column-major, DMMA trailing update), in place.
+ * Replaces Eigen::LLT<MatrixXd, Lower> (reference src/lm.cu:598-603).
+ * n multiple of 64, lda >= n. [device] A, info (int: 0 or failed column). */
+int gba_dense_potrf(double* A, int n, int lda, int* info, void* stream);
+/* Solves L L^T x = b in place after gba_dense_potrf (reference src/lm.cu:604). [device] */
+int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info, void* stream);
+
+/* Residual + analytic Jacobian of E observations on the device, FP64 or FP32
+ * (precision 64 / 32). [device] cams (9C), pts (3P), obs_camera, obs_point,
+ * obs_pixel (2E) in; r (2E), Jc (18E, may be NULL), Jp (6E, may be NULL) out,
+ * of type double (64) or float (32). Same function as the reference
+ * edge_residual_jacobian (src/lm.cu:93-191). */
+int gba_eval_edges(int precision, const double* cameras, const double* points, const int* obs_camera,
+                   const int* obs_point, const double* obs_pixel, int num_observations, void* r, void* Jc,
+                   void* Jp, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBA_CAPI_H */

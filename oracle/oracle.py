@@ -1,0 +1,148 @@
+"""ORACLE (test infrastructure only): ctypes access to the CPU restatement of
+the reference LM (liboracle.so) and to the reference's own compiled BAL reader
+(_ref/libgba_ref_reader.so, present only where the reference checkout was
+available at build time). Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg use this module, as the checker.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from build_oracle import ORACLE_SO, REF_SO, build_oracle, build_reference_reader
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+build_oracle()
+_lib = C.CDLL(str(ORACLE_SO))
+_lib.oracle_residual_jacobian.argtypes = [_dp] * 6
+_lib.oracle_residual.argtypes = [_dp] * 4
+_lib.oracle_accumulate.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                   C.POINTER(C.c_ulonglong)]
+_lib.oracle_cost.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp]
+_lib.oracle_cost.restype = C.c_double
+_lib.oracle_schur_step.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_int, _dp,
+                                   _dp, _dp, _dp, _dp]
+_lib.oracle_cholesky.argtypes = [_dp, C.c_int, C.c_int]
+_lib.oracle_cholesky_solve.argtypes = [_dp, C.c_int, _dp]
+_lib.oracle_solve.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_int, C.c_double, C.c_double,
+                              C.c_int, C.c_int, _dp, _dp, _ip, _ip, C.POINTER(C.c_ulonglong), _dp, C.c_int, _ip]
+
+TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE"}
+
+
+def residual_jacobian(cam, pt, obs):
+    cam, pt, obs = (np.ascontiguousarray(x, np.float64) for x in (cam, pt, obs))
+    r, jc, jp = np.empty(2), np.empty(18), np.empty(6)
+    _lib.oracle_residual_jacobian(_d(cam), _d(pt), _d(obs), _d(r), _d(jc), _d(jp))
+    return r, jc.reshape(2, 9), jp.reshape(2, 3)
+
+
+def residual(cam, pt, obs):
+    cam, pt, obs = (np.ascontiguousarray(x, np.float64) for x in (cam, pt, obs))
+    r = np.empty(2)
+    _lib.oracle_residual(_d(cam), _d(pt), _d(obs), _d(r))
+    return r
+
+
+def _args(prob):
+    return (prob.num_cameras, prob.num_points, prob.num_observations)
+
+
+def accumulate(prob, cams=None, pts=None):
+    """Normal equations in observation order: dict U (C,9,9), V (P,3,3), W (E,9,3), bc, bp, sse, anomalies."""
+    C_, P_, E_ = _args(prob)
+    cams = prob.cameras if cams is None else cams
+    pts = prob.points if pts is None else pts
+    U, V, W = np.empty(81 * C_), np.empty(9 * P_), np.empty(27 * E_)
+    bc, bp, sse, an = np.empty(9 * C_), np.empty(3 * P_), np.empty(1), C.c_ulonglong()
+    _lib.oracle_accumulate(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
+                           _d(prob.obs_pixel), _d(U), _d(V), _d(W), _d(bc), _d(bp), _d(sse), C.byref(an))
+    return dict(U=U.reshape(C_, 9, 9), V=V.reshape(P_, 3, 3), W=W.reshape(E_, 9, 3), bc=bc, bp=bp, sse=sse[0],
+                anomalies=an.value)
+
+
+def cost(prob, cams=None, pts=None) -> float:
+    cams = prob.cameras if cams is None else cams
+    pts = prob.points if pts is None else pts
+    return _lib.oracle_cost(*_args(prob), _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
+                            _d(prob.obs_pixel))
+
+
+def schur_step(prob, lam, threads=0, want_S=False):
+    C_, P_, E_ = _args(prob)
+    dc, dp, rhs, den = np.zeros(9 * C_), np.zeros(3 * P_), np.zeros(9 * C_), np.zeros(1)
+    S = np.zeros((9 * C_) * (9 * C_)) if want_S else None
+    st = _lib.oracle_schur_step(C_, P_, E_, _d(prob.cameras), _d(prob.points), _i(prob.obs_camera),
+                                _i(prob.obs_point), _d(prob.obs_pixel), lam, threads, _d(dc), _d(dp), _d(rhs),
+                                _d(S) if want_S else None, _d(den))
+    out = dict(status=st, dc=dc, dp=dp, rhs=rhs, denom=den[0])
+    if want_S:
+        out["S"] = S.reshape(9 * C_, 9 * C_).T  # column-major -> row-major view (lower triangle filled)
+    return out
+
+
+def cholesky(A_colmajor: np.ndarray, n: int, threads: int = 0) -> int:
+    return _lib.oracle_cholesky(_d(A_colmajor), n, threads)
+
+
+def solve(prob, max_iterations=50, initial_lambda=1e-3, rel_decrease_tol=1e-6, max_inner_trials=16, threads=0):
+    """Full LM solve on copies of the parameters; returns (result dict, cams, pts)."""
+    C_, P_, E_ = _args(prob)
+    cams, pts = prob.cameras.copy(), prob.points.copy()
+    init, fin, it, term = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+    an, tl = C.c_ulonglong(), C.c_int()
+    cap = max_iterations + 2
+    traj = np.zeros(cap)
+    _lib.oracle_solve(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point), _d(prob.obs_pixel),
+                      max_iterations, initial_lambda, rel_decrease_tol, max_inner_trials, threads, C.byref(init),
+                      C.byref(fin), C.byref(it), C.byref(term), C.byref(an), _d(traj), cap, C.byref(tl))
+    res = dict(initial_cost=init.value, final_cost=fin.value, iterations=it.value,
+               termination=TERMINATION[term.value], anomalies=an.value, trajectory=traj[:min(tl.value, cap)].tolist())
+    return res, cams, pts
+
+
+class ReferenceReader:
+    """The reference's own src/bal_reader.cpp (compiled from source) via ctypes."""
+
+    def __init__(self):
+        path = build_reference_reader()
+        if path is None or not Path(path).exists():
+            raise FileNotFoundError("reference BAL reader not built (reference checkout unavailable)")
+        self.lib = C.CDLL(str(path))
+        self.lib.ref_snavely_residual.argtypes = [_dp] * 4
+        self.lib.ref_total_squared_error.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp]
+        self.lib.ref_total_squared_error.restype = C.c_double
+        self.lib.ref_load_bal_dims.argtypes = [C.c_char_p, _ip, _ip, _ip]
+        self.lib.ref_load_bal.argtypes = [C.c_char_p, _dp, _dp, _ip, _ip, _dp]
+
+    def snavely_residual(self, cam, pt, obs):
+        cam, pt, obs = (np.ascontiguousarray(x, np.float64) for x in (cam, pt, obs))
+        out = np.empty(2)
+        self.lib.ref_snavely_residual(_d(cam), _d(pt), _d(obs), _d(out))
+        return out
+
+    def total_squared_error(self, prob) -> float:
+        return self.lib.ref_total_squared_error(*_args(prob), _d(prob.cameras), _d(prob.points),
+                                                _i(prob.obs_camera), _i(prob.obs_point), _d(prob.obs_pixel))
+
+    def load_bal(self, path):
+        c, p, e = C.c_int(), C.c_int(), C.c_int()
+        if self.lib.ref_load_bal_dims(str(path).encode(), C.byref(c), C.byref(p), C.byref(e)) != 0:
+            raise ValueError("reference load_bal rejected " + str(path))
+        arrs = (np.empty(9 * c.value), np.empty(3 * p.value), np.empty(e.value, np.int32), np.empty(e.value, np.int32),
+                np.empty(2 * e.value))
+        self.lib.ref_load_bal(str(path).encode(), _d(arrs[0]), _d(arrs[1]), _i(arrs[2]), _i(arrs[3]), _d(arrs[4]))
+        return arrs

@@ -1,0 +1,189 @@
+"""CPU: pins the oracle (CPU restatement of the reference LM) to the reference's
+own code and golden cases, and the host side of the library to the oracle.
+
+Reference tests followed: tests/test_vs_ceres.cpp:31-74 (finite-difference
+Jacobian on two golden cases), tests/test_schur.cu (SPD factor / inverse to
+1e-9), the initial-cost identity of benchmarks/bench_bal.cpp:87-94.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_err
+
+
+def _fd_jacobian(fn, cam, pt, obs, eps=1e-6):
+    """Central differences of fn(cam, pt, obs) -> r2 (reference test_vs_ceres.cpp:50-69)."""
+    cam, pt = np.array(cam, float), np.array(pt, float)
+    Jc, Jp = np.zeros((2, 9)), np.zeros((2, 3))
+    for j in range(9):
+        a, b = cam.copy(), cam.copy()
+        a[j] += eps
+        b[j] -= eps
+        Jc[:, j] = (fn(a, pt, obs) - fn(b, pt, obs)) / (2 * eps)
+    for j in range(3):
+        a, b = pt.copy(), pt.copy()
+        a[j] += eps
+        b[j] -= eps
+        Jp[:, j] = (fn(cam, a, obs) - fn(cam, b, obs)) / (2 * eps)
+    return Jc, Jp
+
+
+def _fd_err(J, Jfd):
+    return float(np.max(np.abs(J - Jfd) / np.maximum(1.0, np.abs(J))))
+
+
+def test_oracle_residual_matches_reference_golden(oracle):
+    g = json.loads((GOLDEN / "residual_golden.json").read_text())
+    worst = 0.0
+    for e in g["edges"]:
+        r = oracle.residual(e["cam"], e["pt"], e["obs"])
+        ref = np.array(e["residual"])
+        worst = max(worst, float(np.max(np.abs(r - ref)) / max(1.0, np.max(np.abs(ref)))))
+    # Same model; the CPU reader drops the first-order a x X term below |a| = 1e-12
+    # and uses theta > 1e-12 instead of theta^2 > 1e-24: ~1e-12 px at most.
+    assert worst < 1e-9, worst
+
+
+def test_oracle_residual_matches_reference_compiled(oracle):
+    try:
+        ref = oracle.ReferenceReader()
+    except FileNotFoundError:
+        pytest.skip("reference reader not built here (reference checkout absent)")
+    rng = np.random.default_rng(5)
+    for _ in range(100):
+        cam = np.concatenate([rng.normal(0, 0.5, 3), rng.normal(0, 1, 3), [500.0], rng.normal(0, 0.05, 2)])
+        pt = rng.normal(0, 3, 3) - np.array([0, 0, 8.0])
+        obs = rng.normal(0, 100, 2)
+        np.testing.assert_allclose(oracle.residual(cam, pt, obs), ref.snavely_residual(cam, pt, obs), rtol=1e-13,
+                                   atol=1e-9)
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_oracle_jacobian_vs_finite_differences(oracle, which):
+    case = json.loads((GOLDEN / "fd_cases.json").read_text())["cases"][which]
+    cam, pt, obs = case[:9], case[9:12], case[12:14]
+    _, Jc, Jp = oracle.residual_jacobian(cam, pt, obs)
+    Jc_fd, Jp_fd = _fd_jacobian(oracle.residual, cam, pt, obs)
+    assert max(_fd_err(Jc, Jc_fd), _fd_err(Jp, Jp_fd)) < 1e-5
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_library_host_jacobian_vs_finite_differences(gba, which):
+    """gba_edge_residual_jacobian_host: the reference FD gate (rel err < 1e-5)."""
+    case = json.loads((GOLDEN / "fd_cases.json").read_text())["cases"][which]
+    cam, pt, obs = case[:9], case[9:12], case[12:14]
+    _, Jc, Jp = gba.edge_residual_jacobian_host(cam, pt, obs)
+    fn = lambda c, p, o: gba.edge_residual_jacobian_host(c, p, o)[0]  # noqa: E731
+    Jc_fd, Jp_fd = _fd_jacobian(fn, cam, pt, obs)
+    assert max(_fd_err(Jc, Jc_fd), _fd_err(Jp, Jp_fd)) < 1e-5
+
+
+def test_library_jacobian_matches_oracle_derivation(gba, oracle):
+    """The library's left-Jacobian derivation equals the reference's w-derivative one."""
+    rng = np.random.default_rng(7)
+    worst = 0.0
+    for i in range(500):
+        cam = np.concatenate([rng.normal(0, 0.4, 3), rng.normal(0, 1, 3), [rng.uniform(300, 700)],
+                              rng.normal(0, 0.05, 1), rng.normal(0, 0.005, 1)])
+        if i % 50 == 0:
+            cam[:3] = rng.normal(0, 1e-14, 3)  # first-order branch
+        pt = np.array([rng.uniform(-3, 3), rng.uniform(-3, 3), rng.uniform(-12, -3)])
+        obs = rng.normal(0, 300, 2)
+        r1, jc1, jp1 = gba.edge_residual_jacobian_host(cam, pt, obs)
+        r2, jc2, jp2 = oracle.residual_jacobian(cam, pt, obs)
+        for a, b in ((r1, r2), (jc1, jc2), (jp1, jp2)):
+            worst = max(worst, float(np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b)))))
+    assert worst < 1e-9, worst
+
+
+def test_library_reader_and_sse_match_reference_golden(gba):
+    meta = json.loads((GOLDEN / "tiny_problem.json").read_text())
+    prob = gba.load_bal(GOLDEN / "tiny_problem.txt")
+    assert (prob.num_cameras, prob.num_points, prob.num_observations) == (
+        meta["num_cameras"], meta["num_points"], meta["num_observations"])
+    sse = gba.total_squared_error(prob)
+    assert abs(sse - meta["total_squared_error"]) <= 1e-12 * abs(meta["total_squared_error"])
+
+
+def test_library_reader_matches_reference_reader(gba, oracle, tmp_path):
+    try:
+        ref = oracle.ReferenceReader()
+    except FileNotFoundError:
+        pytest.skip("reference reader not built here")
+    cams, pts, oc, op, px = ref.load_bal(GOLDEN / "tiny_problem.txt")
+    prob = gba.load_bal(GOLDEN / "tiny_problem.txt")
+    for a, b in zip(prob.arrays(), (cams, pts, oc, op, px)):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("text,ok", [
+    ("1 1 1\n0 0 1.5 2.5\n" + "1\n" * 9 + "1\n2\n3\n", True),
+    ("0 1 1\n0 0 1 1\n", False),                       # bad header
+    ("1 1 1\n0 1 1.5 2.5\n" + "1\n" * 12, False),      # point index out of range
+    ("1 1 1\n0 0 1.5 2.5\n" + "1\n" * 12 + "7\n", False),  # trailing garbage
+    ("1 1 1\n0 0 1.5 x\n" + "1\n" * 12, False),        # malformed number
+    ("1 1 1\n0 0 1.5 2.5\n" + "1\n" * 11, False),      # truncated
+])
+def test_reader_validation(gba, tmp_path, text, ok):
+    """Reader error behaviour of the reference (src/bal_reader.cpp:66-98)."""
+    f = tmp_path / "p.txt"
+    f.write_text(text)
+    if ok:
+        prob = gba.load_bal(f)
+        assert prob.num_observations == 1 and prob.obs_pixel.tolist() == [1.5, 2.5]
+    else:
+        with pytest.raises(gba.GbaError):
+            gba.load_bal(f)
+
+
+def test_oracle_cholesky_matches_numpy(oracle):
+    rng = np.random.default_rng(3)
+    n = 150
+    M = rng.normal(size=(n, n))
+    A = M @ M.T + n * np.eye(n)
+    colmajor = np.asfortranarray(A).ravel(order="F").copy()
+    assert oracle.cholesky(colmajor, n, 2) == 0
+    L = np.tril(colmajor.reshape(n, n, order="F"))
+    assert rel_err(L, np.linalg.cholesky(A)) < 1e-12
+    bad = -np.eye(n).ravel()
+    assert oracle.cholesky(bad, n, 1) == 1
+
+
+def test_oracle_schur_step_matches_dense_normal_equations(gba, oracle):
+    """The oracle's Schur step equals the full damped Gauss-Newton solve (numpy)."""
+    prob = gba.synthetic_custom(4, 60, 2, 4, 1.5, seed=3)
+    lam = 1e-2
+    ne = oracle.accumulate(prob)
+    C, P = prob.num_cameras, prob.num_points
+    n = 9 * C + 3 * P
+    H = np.zeros((n, n))
+    b = np.concatenate([ne["bc"], ne["bp"]])
+    for c in range(C):
+        H[9 * c:9 * c + 9, 9 * c:9 * c + 9] = ne["U"][c]
+    for p in range(P):
+        H[9 * C + 3 * p:9 * C + 3 * p + 3, 9 * C + 3 * p:9 * C + 3 * p + 3] = ne["V"][p]
+    for e in range(prob.num_observations):
+        c, p = prob.obs_camera[e], prob.obs_point[e]
+        H[9 * c:9 * c + 9, 9 * C + 3 * p:9 * C + 3 * p + 3] += ne["W"][e]
+        H[9 * C + 3 * p:9 * C + 3 * p + 3, 9 * c:9 * c + 9] += ne["W"][e].T
+    d = np.diag(H).copy()
+    H[np.diag_indices(n)] += lam * np.where(d > 0, d, 1e-12)
+    x = np.linalg.solve(H, b)
+    st = oracle.schur_step(prob, lam, threads=2)
+    assert st["status"] == 0
+    assert rel_err(st["dc"], x[:9 * C]) < 1e-8
+    assert rel_err(st["dp"], x[9 * C:]) < 1e-8
+
+
+def test_oracle_lm_converges_on_small_problem(gba, oracle):
+    prob = gba.synthetic_custom(6, 400, 2, 6, 1.5, seed=4)
+    res, _, _ = oracle.solve(prob, max_iterations=30, threads=2)
+    assert res["anomalies"] == 0
+    assert res["termination"] in ("CONVERGENCE", "MAX_ITERATIONS")
+    traj = res["trajectory"]
+    assert all(b < a for a, b in zip(traj, traj[1:]))
+    # noise is N(0,1) px: the optimum is near E px^2 / 2 per observation
+    assert res["final_cost"] < 0.75 * prob.num_observations
+    assert abs(res["initial_cost"] - gba.total_squared_error(prob) / 2) <= 1e-9 * res["initial_cost"]
