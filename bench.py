@@ -1,0 +1,351 @@
+"""Benchmark: LM solve seconds to reach <= 1.001x the FP64 oracle cost, one GB300.
+
+One step = one full LM solve of the workload's synthetic problem, from the same
+initial parameters, until the cost first reaches the target (1.001 x the FP64
+reference final cost of this workload) or max_iterations. Metric (lower is
+better): seconds per step.
+
+  value  device-resident: the problem (observations, sorted slots, Schur
+         structure) is on the device before the timed region; each step resets
+         the parameters on the device and runs the LM loop (gba_solver_run).
+         Timed with CUDA events on the solver stream, synchronize both sides.
+  e2e    the reference-facing call gba_solve_bal on pinned host buffers: H2D of
+         the problem, setup, the solve, D2H of the parameters, every step.
+
+Default workload: 5 (5,000 cameras / 1,500,000 points / ~8.8M observations,
+power-law tracks 2-200, 5% outliers), form "learned" (mixed precision +
+learned block-Jacobi PCG); --form plain|mixed selects the other forms. Inputs
+(~0.9 GB of observations, 3.8 GB of per-slot Jacobians) exceed the 129 MB L2,
+so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference LM (oracle/,
+all host threads) on a bounded sample of the same workload, scaled to seconds
+per solve (see cpu_sample()).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gpu-bundle-adjustment_gb300"
+GOLDEN = ROOT / "tests" / "golden"
+sys.path.insert(0, str(PKG))
+
+METRIC = "LM solve s to <=1.001x oracle cost: plain FP64 vs mixed+learned PCG, 1 GB300"
+TARGET_FACTOR = 1.001
+MODEL = PKG / "models" / "bj_mlp.bin"
+
+
+def _peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def reference_cost(workload: int, seed: int):
+    """FP64 reference final cost of a workload (committed fixture), or None."""
+    f = GOLDEN / "workload_reference.json"
+    if not f.exists():
+        return None
+    data = json.loads(f.read_text())
+    e = data.get(f"{workload}:{seed}")
+    return None if e is None else e["final_cost"]
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                      f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.splitlines()[0].split(",")])
+            except (OSError, subprocess.SubprocessError):
+                return
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons}
+
+
+def _dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+def algorithmic_bytes(kernel: str, C: int, P: int, E: int) -> float:
+    """Bytes one launch must move (each array once), per the kernel's definition."""
+    if kernel == "schur_point_pass_f32":
+        # J32 (Jc, Jp) 96 B + s_cam 4 + s_pt 4 + u write 8 per slot; V^-1 48 + CSR 4 per point; x 72 per camera
+        return E * 112.0 + P * 52.0 + C * 72.0
+    if kernel == "schur_camera_pass_f32":
+        # cam_slots 4 + Jc 72 (of the 80 B read) + u 8 per slot
+        return E * 84.0
+    if kernel == "point_pass_f32":
+        # s_cam, s_pt, s_px, r_cur (32 B) in, J32 96 B out per slot; point 24 B in, V/bp 72 B out per point
+        return E * 128.0 + P * 96.0 + C * 72.0
+    if kernel == "cost_f64":
+        return E * 32.0 + P * 24.0 + C * 72.0
+    raise KeyError(kernel)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import gba_gb300 as gba
+
+    rank, world = _dist_env()
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", dev))
+
+    prob = gba.synthetic(args.workload, args.seed)
+    C, P, E = prob.num_cameras, prob.num_points, prob.num_observations
+    ref = reference_cost(args.workload, args.seed)
+    target = ref * TARGET_FACTOR if ref else 0.0
+    form = args.form
+    opts = dict(form=form, max_iterations=args.max_iterations, target_cost=target, stop_at_target=1 if ref else 0)
+    if form == "learned":
+        opts["model_path"] = str(MODEL)
+
+    stream = torch.cuda.Stream()
+    solver = gba.Solver(prob, form, stream=stream.cuda_stream)
+    if form == "learned":
+        solver.load_model(MODEL)
+
+    # ---- device-resident steps
+    results = []
+    for _ in range(args.warmup):
+        solver.reset_params()
+        results.append(solver.run(**opts))
+    solver.profile(True)
+    solver.profile_reset()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = gba.launch_count()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    timed = []
+    with ClockSampler() as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            solver.reset_params()
+            timed.append(solver.run(**opts))
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = gba.launch_count() - l0
+    ms_total = start.elapsed_time(end)
+    ms = torch.tensor([ms_total], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+    ms_per_step = float(ms.item()) / args.steps
+
+    # dominant kernel of the form and its live CUDA-event timing
+    dom = "schur_point_pass_f32" if form != "plain" else "dense_potrf"
+    n_launch, k_ms = solver.kernel_stats(dom)
+    peaks, peak_src = _peaks()
+    roofline = None
+    if n_launch:
+        per_launch_s = k_ms / n_launch / 1e3
+        if dom == "dense_potrf":
+            n = 9 * C
+            flops = n ** 3 / 3.0
+            achieved = flops / per_launch_s / 1e12
+            roofline = {"bound": "tensor", "achieved": achieved, "peak": 1.05, "unit": "TFLOP/s",
+                        "frac": achieved / 1.05, "traffic": None,
+                        "peak_note": "FP64 DMMA peak measured on this GB300 (mma.sync m8n8k4 f64 loop)"}
+        else:
+            b = algorithmic_bytes(dom, C, P, E)
+            achieved = b / per_launch_s / 1e9
+            roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
+                        "launches": n_launch, "avg_launch_us": per_launch_s * 1e6, "peak_source": peak_src}
+    solver.profile(False)
+    final = timed[-1]
+
+    # ---- e2e: gba_solve_bal on pinned host buffers, H2D + setup + solve + D2H per step
+    pinned = [torch.from_numpy(a.copy()).pin_memory() for a in prob.arrays()]
+    init_cams, init_pts = pinned[0].clone(), pinned[1].clone()
+    h2d = sum(t.numel() * t.element_size() for t in pinned)
+    d2h = pinned[0].numel() * 8 + pinned[1].numel() * 8
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        pinned[0].copy_(init_cams)
+        pinned[1].copy_(init_pts)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = gba.solve_raw(C, P, E, *(t.data_ptr() for t in pinned), **opts)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+
+    line = {
+        "metric": METRIC,
+        "value": ms_per_step / 1e3,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if form == "plain" else "f32+f64",
+        "data": "synthetic (seeded BAL-shaped generator; the BAL datasets are not available offline)",
+        "config": {
+            "workload": f"workload{args.workload}: {C} cameras / {P} points / {E} observations, seed {args.seed}",
+            "form": form,
+            "target_cost": target or None,
+            "fp64_reference_cost": ref,
+            "max_iterations": args.max_iterations,
+            "l2": "inputs larger than L2 (no flush)",
+            "parallelism": f"replicas x{world}",
+        },
+        "result": {"final_cost": final.final_cost, "iterations": final.iterations, "termination": final.termination,
+                   "time_to_target_s": final.time_to_target_s, "pcg_iterations": final.pcg_iterations,
+                   "trials": final.trials, "anomalies": final.anomalies,
+                   "rel_err_vs_fp64_reference": (final.final_cost - ref) / ref if ref else None},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_sample(prob, args, final.iterations)
+    if rank == 0:
+        print(json.dumps(line))
+    solver.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_sample(prob, args, iterations_to_target: int) -> dict:
+    """CPU restatement of the reference LM (oracle/, all host threads) on a
+    bounded sample of the workload, scaled to seconds per solve:
+      per-iteration = accumulate (all observations, measured)
+                    + Schur assembly + dense Cholesky of the 9C x 9C system,
+                      measured on the camera-subset problem and scaled by
+                      (C / C_sub)^2 (assembly) and (C / C_sub)^3 (factor)
+    times the LM iterations the FP64 solve takes to the target."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+
+    import gba_gb300 as gba
+    import oracle
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.accumulate(prob)
+    t_acc = time.perf_counter() - t0
+    C = prob.num_cameras
+    c_sub = min(C, 600)
+    sub = gba.synthetic_custom(c_sub, max(1000, prob.num_points * c_sub // C), 2, min(200, c_sub), 2.2, seed=3)
+    t0 = time.perf_counter()
+    st = oracle.schur_step(sub, 1e-3, threads=threads)
+    t_step = time.perf_counter() - t0
+    scale3 = (C / c_sub) ** 3
+    per_iter = t_acc + t_step * scale3
+    iters = max(1, iterations_to_target)
+    return {"value": per_iter * iters, "unit": "s", "cores": threads, "kind": "port",
+            "sample": (f"oracle accumulate over all {prob.num_observations} observations ({t_acc:.2f} s) + one "
+                       f"Schur step (assembly + dense Cholesky + back-substitution) on a {c_sub}-camera problem "
+                       f"({t_step:.2f} s, scaled by (C/{c_sub})^3), x {iters} LM iterations"),
+            "status": st["status"]}
+
+
+def run_reference(args):
+    rank, world = _dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import gba_gb300 as gba
+
+    prob = gba.synthetic(args.workload, args.seed)
+    iters = args.reference_iterations
+    vals = []
+    sample = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_sample(prob, args, iters)
+        sample = cb
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = sum(vals) / len(vals)
+    line = {
+        "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded BAL-shaped generator)",
+        "config": {"workload": f"workload{args.workload}: {prob.num_cameras} cameras / {prob.num_points} points / "
+                               f"{prob.num_observations} observations, seed {args.seed}", "form": "plain (CPU)"},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "s", "cores": sample["cores"], "kind": "port",
+                         "sample": sample["sample"]},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", type=int, default=5)
+    ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--form", default="learned", choices=["plain", "mixed", "learned"])
+    ap.add_argument("--max-iterations", type=int, default=50)
+    ap.add_argument("--reference-iterations", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.seed is None:
+        args.seed = args.workload
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

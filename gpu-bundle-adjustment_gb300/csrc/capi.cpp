@@ -13,6 +13,7 @@
 #include "gba/bal_problem.hpp"
 #include "gba/lm.hpp"
 #include "lm_internal.hpp"
+#include "mlp.hpp"
 #include "solver.hpp"
 #include "synthetic.hpp"
 
@@ -75,6 +76,7 @@ gba::LMOptions to_options(const gba_lm_options* o) {
     r.pcg_max_iters = o->pcg_max_iters;
     r.model_path = o->model_path ? o->model_path : "";
     r.target_cost = o->target_cost;
+    r.stop_at_target = o->stop_at_target != 0;
     return r;
 }
 
@@ -82,9 +84,10 @@ void fill_result(const gba::LMResult& r, gba_lm_result* out) {
     out->initial_cost = r.initial_cost;
     out->final_cost = r.final_cost;
     out->iterations = r.iterations;
-    out->termination = r.termination == "CONVERGENCE" ? GBA_TERM_CONVERGENCE
-                       : r.termination == "FAILURE"   ? GBA_TERM_FAILURE
-                                                      : GBA_TERM_MAX_ITERATIONS;
+    out->termination = r.termination == "CONVERGENCE"   ? GBA_TERM_CONVERGENCE
+                       : r.termination == "FAILURE"     ? GBA_TERM_FAILURE
+                       : r.termination == "TARGET_COST" ? GBA_TERM_TARGET_COST
+                                                        : GBA_TERM_MAX_ITERATIONS;
     out->anomalies = r.anomalies;
     out->total_time_s = r.total_time_s;
     out->trials = r.trials;
@@ -132,6 +135,131 @@ void gba_lm_options_default(gba_lm_options* o) {
     o->pcg_max_iters = d.pcg_max_iters;
     o->model_path = nullptr;
     o->target_cost = d.target_cost;
+    o->stop_at_target = 0;
+}
+
+unsigned long long gba_launch_count(void) { return gba::launch_count(); }
+
+int gba_solver_set_harvest(gba_solver* s, int enable) {
+    return guarded([&] {
+        need(S(s).form() == gba::SolverForm::Plain, "harvest needs the plain form");
+        S(s).harvest_ = enable != 0;
+    });
+}
+
+int gba_solver_features(gba_solver* s, double lambda, float* feat) {
+    return guarded([&] {
+        need(feat != nullptr, "null features buffer");
+        need(S(s).Sdiag_.get() != nullptr, "no diagonal blocks yet (run schur_pcg, or schur_dense with harvest)");
+        gba::mlp_features(S(s), lambda, feat);
+        S(s).sync();
+    });
+}
+
+long long gba_mlp_num_params(void) { return gba::kMlpParams; }
+
+int gba_mlp_create(uint64_t seed, int cap, gba_mlp** out) {
+    return guarded([&] {
+        need(out != nullptr && cap > 0, "bad argument");
+        *out = reinterpret_cast<gba_mlp*>(new gba::Mlp(cap, seed));
+    });
+}
+
+int gba_mlp_load(const char* path, int cap, gba_mlp** out) {
+    return guarded([&] {
+        need(path && out && cap > 0, "bad argument");
+        *out = reinterpret_cast<gba_mlp*>(new gba::Mlp(std::string(path), cap));
+    });
+}
+
+int gba_mlp_save(const gba_mlp* m, const char* path) {
+    return guarded([&] {
+        need(m && path, "null argument");
+        reinterpret_cast<const gba::Mlp*>(m)->save(path);
+    });
+}
+
+void gba_mlp_destroy(gba_mlp* m) { delete reinterpret_cast<gba::Mlp*>(m); }
+
+int gba_mlp_get_params(const gba_mlp* m, float* p) {
+    return guarded([&] {
+        need(m && p, "null argument");
+        reinterpret_cast<const gba::Mlp*>(m)->get_params(p);
+    });
+}
+
+int gba_mlp_set_params(gba_mlp* m, const float* p) {
+    return guarded([&] {
+        need(m && p, "null argument");
+        reinterpret_cast<gba::Mlp*>(m)->set_params(p);
+    });
+}
+
+int gba_mlp_get_grads(const gba_mlp* m, float* g) {
+    return guarded([&] {
+        need(m && g, "null argument");
+        reinterpret_cast<const gba::Mlp*>(m)->grads(g);
+    });
+}
+
+int gba_mlp_forward(gba_mlp* m, const float* feat, int B, float* out, void* stream) {
+    return guarded([&] {
+        need(m && feat && out && B > 0, "bad argument");
+        auto st = static_cast<cudaStream_t>(stream);
+        reinterpret_cast<gba::Mlp*>(m)->forward(feat, B, out, st);
+        GBA_CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+int gba_mlp_loss_grad(gba_mlp* m, const float* feat, const double* Shat, const double* Lhat, const double* g,
+                      const double* x, int B, void* stream, double* out_loss, double* out_base) {
+    return guarded([&] {
+        need(m && feat && Shat && Lhat && g && x && B > 0, "bad argument");
+        const double l = reinterpret_cast<gba::Mlp*>(m)->loss_grad(feat, Shat, Lhat, g, x, B,
+                                                                  static_cast<cudaStream_t>(stream), out_base);
+        if (out_loss) *out_loss = l;
+    });
+}
+
+int gba_mlp_adam_step(gba_mlp* m, float lr, float b1, float b2, float eps, void* stream) {
+    return guarded([&] {
+        need(m != nullptr, "null model");
+        auto st = static_cast<cudaStream_t>(stream);
+        reinterpret_cast<gba::Mlp*>(m)->adam_step(lr, b1, b2, eps, st);
+        GBA_CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+int gba_solver_run(gba_solver* s, const gba_lm_options* opts, gba_lm_result* result) {
+    return guarded([&] {
+        need(result != nullptr, "null result");
+        const gba::LMOptions o = to_options(opts);
+        need(o.form == S(s).form(), "options form differs from the solver's form");
+        if (o.form == gba::SolverForm::MixedLearned && !S(s).model()) S(s).load_model(o.model_path);
+        const auto t0 = std::chrono::steady_clock::now();
+        gba::LMResult r = gba::run_lm(S(s), o, t0);
+        r.total_time_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_result(r, result);
+    });
+}
+
+int gba_solver_reset_params(gba_solver* s) {
+    return guarded([&] { S(s).reset_params(); });
+}
+
+int gba_solver_profile(gba_solver* s, int enable) {
+    return guarded([&] { S(s).set_profiling(enable != 0); });
+}
+
+int gba_solver_kernel_stats(gba_solver* s, const char* name, long long* launches, double* ms) {
+    return guarded([&] {
+        need(name != nullptr, "null name");
+        S(s).kernel_stats(name, launches, ms);
+    });
+}
+
+int gba_solver_profile_reset(gba_solver* s) {
+    return guarded([&] { S(s).prof_reset(); });
 }
 
 int gba_solve_bal(int C, int P, int E, double* cameras, double* points, const int* obs_camera,

@@ -25,7 +25,15 @@ struct CudaError : std::runtime_error {
                                    cudaGetErrorString(err_));                           \
     } while (0)
 
-#define GBA_LAUNCH_CHECK() GBA_CUDA_CHECK(cudaGetLastError())
+// Every kernel launch of this library is followed by GBA_LAUNCH_CHECK(), which
+// also counts it (gba_launch_count() in the C ABI reports the total).
+void count_launch();
+unsigned long long launch_count();
+#define GBA_LAUNCH_CHECK()                          \
+    do {                                            \
+        ::gba::count_launch();                      \
+        GBA_CUDA_CHECK(cudaGetLastError());         \
+    } while (0)
 
 inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
 

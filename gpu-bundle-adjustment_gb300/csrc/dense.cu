@@ -83,6 +83,15 @@ __global__ void add_damped_u_kernel(const double* __restrict__ U, double lambda,
     }
 }
 
+// Copies the assembled diagonal blocks S_cc (lower triangle mirrored) to Sdiag.
+__global__ void extract_diag_blocks(const double* __restrict__ S, int C, int lda, double* __restrict__ Sdiag) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 81 * C) return;
+    const int c = t / 81, i = (t % 81) / 9, j = t % 9;
+    const int r = i >= j ? i : j, q = i >= j ? j : i;
+    Sdiag[t] = S[(9ll * c + r) + (9ll * c + q) * lda];
+}
+
 // rhs_c = bc_c - sum_{e in c} T_e bp_{p(e)}; one CTA per camera, ordered sums.
 __global__ void __launch_bounds__(128) rhs_kernel(const int* __restrict__ cam_off, const int* __restrict__ cam_slots,
                                                  const int* __restrict__ s_pt, const double* __restrict__ T,
@@ -374,10 +383,12 @@ int Solver::schur_dense(double lambda) {
     GBA_LAUNCH_CHECK();
     GBA_CUDA_CHECK(cudaMemsetAsync(S_.get(), 0, S_.size() * sizeof(double), stream_));
     if (n_blocks_ > 0) {
+        cudaEvent_t ev = prof_start();
         assemble_kernel<<<ceil_div(9ll * n_blocks_, 288), 288, 0, stream_>>>(
             block_off_.get(), block_ce_.get(), block_cf_.get(), pair_e_.get(), pair_f_.get(), T_.get(), W_.get(),
             n_blocks_, lda, S_.get());
         GBA_LAUNCH_CHECK();
+        prof_stop("schur_assemble", ev);
     }
     add_damped_u_kernel<<<ceil_div(81ll * C_ + (n_pad_ - 9 * C_), 256), 256, 0, stream_>>>(U_.get(), lambda, C_,
                                                                                         n_pad_, lda, S_.get());
@@ -386,7 +397,14 @@ int Solver::schur_dense(double lambda) {
     rhs_kernel<<<C_, 128, 0, stream_>>>(cam_off_.get(), cam_slots_.get(), s_pt_.get(), T_.get(), bp_.get(),
                                         bc_.get(), rhs_.get());
     GBA_LAUNCH_CHECK();
+    if (harvest_) {
+        if (!Sdiag_.get()) Sdiag_.alloc(81ull * C_);
+        extract_diag_blocks<<<ceil_div(81ll * C_, 256), 256, 0, stream_>>>(S_.get(), C_, lda, Sdiag_.get());
+        GBA_LAUNCH_CHECK();
+    }
+    cudaEvent_t ev = prof_start();
     dense_potrf(S_.get(), n_pad_, lda, info_.get(), stream_);
+    prof_stop("dense_potrf", ev);
     int info = 0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&info, info_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
     sync();

@@ -178,11 +178,14 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 
 // Point pass, FP32 arithmetic: per-slot Jacobian record J32 = [Jc(18), Jp(6)];
 // V / bp summed per point in FP32 and stored FP64 (one FP64 conversion per point).
+// The residuals come from r_cur: the FP64 cost pass at these parameters (run
+// anyway to drive accept/reject) stores them rounded to FP32, which keeps the
+// gradient accurate to FP32 rounding of r instead of FP32 rounding of f d u.
 __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
     const int* __restrict__ s_pt, const double2* __restrict__ s_px, const double* __restrict__ cams,
-    const double* __restrict__ pts, float* __restrict__ J32, double* __restrict__ V, double* __restrict__ bp,
-    unsigned long long* __restrict__ counters) {
+    const double* __restrict__ pts, const float2* __restrict__ r_cur, float* __restrict__ J32,
+    double* __restrict__ V, double* __restrict__ bp, unsigned long long* __restrict__ counters) {
     __shared__ float contrib[9][kPT];
     __shared__ unsigned long long redu[kPT / 32];
     const int chunk = blockIdx.x;
@@ -214,6 +217,9 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             obs[0] = static_cast<float>(o.x);
             obs[1] = static_cast<float>(o.y);
             model::residual_jacobian(cam, X, obs, r, J, J + 18);
+            const float2 rf = r_cur[s];  // FP64-evaluated residual, stored FP32
+            r[0] = rf.x;
+            r[1] = rf.y;
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
             float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
             if (fin) {
@@ -261,7 +267,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
 __global__ void __launch_bounds__(kCT) camera_pass_f32(
     const int* __restrict__ cchunk_begin, const int* __restrict__ cchunk_cam, const int* __restrict__ cam_off,
     const int* __restrict__ cam_slots, const int* __restrict__ s_pt, const double2* __restrict__ s_px,
-    const double* __restrict__ cams, const double* __restrict__ pts, double* __restrict__ part) {
+    const double* __restrict__ cams, const double* __restrict__ pts, const float2* __restrict__ r_cur,
+    double* __restrict__ part) {
     const int k = blockIdx.x;
     const int b = cchunk_begin[k], c = cchunk_cam[k];
     const int e = min(b + kCamChunk, cam_off[c + 1]);
@@ -281,6 +288,9 @@ __global__ void __launch_bounds__(kCT) camera_pass_f32(
         obs[0] = static_cast<float>(o.x);
         obs[1] = static_cast<float>(o.y);
         model::residual_jacobian(cam, X, obs, r, Jc, Jp);
+        const float2 rf = r_cur[s];
+        r[0] = rf.x;
+        r[1] = rf.y;
         const bool fin = all_finite(r, 2) && all_finite(Jc, 18) && all_finite(Jp, 6);
         if (!fin) continue;
         int idx = 0;
@@ -328,12 +338,13 @@ __global__ void __launch_bounds__(256) ordered_sum(const double* __restrict__ pa
     if (threadIdx.x == 0) *out = t;
 }
 
-// FP64 SSE of all slots at (cams, pts), one CTA per point chunk.
+// FP64 SSE of all slots at (cams, pts), one CTA per point chunk. If r_out is
+// set, each slot's residual is also stored (FP32; NaN where not finite).
 __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                const double2* __restrict__ s_px, const double* __restrict__ cams,
                                                const double* __restrict__ pts, double* __restrict__ sse_part,
-                                               unsigned long long* __restrict__ counters) {
+                                               unsigned long long* __restrict__ counters, float2* __restrict__ r_out) {
     __shared__ double red[kPT / 32];
     __shared__ unsigned long long redu[kPT / 32];
     const int chunk = blockIdx.x;
@@ -351,7 +362,9 @@ __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, 
         obs[0] = o.x;
         obs[1] = o.y;
         model::residual(cam, X, obs, r);
-        if (!isfinite(r[0]) || !isfinite(r[1])) {
+        const bool fin = isfinite(r[0]) && isfinite(r[1]);
+        if (r_out) r_out[s] = fin ? make_float2(static_cast<float>(r[0]), static_cast<float>(r[1])) : make_float2(NAN, NAN);
+        if (!fin) {
             ++anom;
             continue;
         }
@@ -391,37 +404,51 @@ __global__ void eval_edges_kernel(const double* __restrict__ cams, const double*
 double Solver::accumulate() {
     const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
     if (form_ == SolverForm::Plain) {
+        cudaEvent_t ev = prof_start();
         point_pass_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
                                                        spx, cams_.get(), pts_.get(), W_.get(), JcR_.get(),
                                                        V_.get(), bp_.get(), sse_part_.get(), counters_.get());
         GBA_LAUNCH_CHECK();
+        prof_stop("point_pass_f64", ev);
         if (n_cchunk_ > 0) {
+            ev = prof_start();
             camera_pass_f64<<<n_cchunk_, kCT, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(),
                                                             cam_off_.get(), cam_slots_.get(), JcR_.get(),
                                                             cam_part_.get());
             GBA_LAUNCH_CHECK();
+            prof_stop("camera_pass_f64", ev);
         }
         ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
         GBA_LAUNCH_CHECK();
     } else {
+        // The mixed form keeps the cost FP64: SSE and residuals come from the
+        // FP64 residual pass. After an accepted trial they are already there
+        // (the trial evaluation at these parameters). Its non-finite count goes
+        // to a scratch counter: the FP32 pass counts this evaluation's anomalies.
+        if (!resid_valid_) {
+            cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
+                                                     cams_.get(), pts_.get(), sse_part_.get(), counters_.get() + 2,
+                                                     reinterpret_cast<float2*>(r_cur_.get()));
+            GBA_LAUNCH_CHECK();
+            ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
+            GBA_LAUNCH_CHECK();
+            resid_valid_ = true;
+        }
+        const float2* rc = reinterpret_cast<const float2*>(r_cur_.get());
+        cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
-                                                       spx, cams_.get(), pts_.get(), J32_.get(), V_.get(),
+                                                       spx, cams_.get(), pts_.get(), rc, J32_.get(), V_.get(),
                                                        bp_.get(), counters_.get());
         GBA_LAUNCH_CHECK();
+        prof_stop("point_pass_f32", ev);
         if (n_cchunk_ > 0) {
+            ev = prof_start();
             camera_pass_f32<<<n_cchunk_, kCT, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(),
                                                             cam_off_.get(), cam_slots_.get(), s_pt_.get(), spx,
-                                                            cams_.get(), pts_.get(), cam_part_.get());
+                                                            cams_.get(), pts_.get(), rc, cam_part_.get());
             GBA_LAUNCH_CHECK();
+            prof_stop("camera_pass_f32", ev);
         }
-        // The mixed form keeps the cost FP64: SSE from the FP64 residual pass.
-        // Its non-finite count goes to a scratch counter: the FP32 pass has
-        // already counted this evaluation's anomalies.
-        cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                                 cams_.get(), pts_.get(), sse_part_.get(), counters_.get() + 2);
-        GBA_LAUNCH_CHECK();
-        ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
-        GBA_LAUNCH_CHECK();
     }
     camera_finalize<<<ceil_div(54ll * C_, 256), 256, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), C_,
                                                                  U_.get(), bc_.get());
@@ -434,9 +461,12 @@ double Solver::accumulate() {
 
 double Solver::trial_cost() {
     const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
+    cudaEvent_t ev = prof_start();
     cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                             tcams_.get(), tpts_.get(), sse_part_.get(), counters_.get());
+                                             tcams_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
+                                             reinterpret_cast<float2*>(r_trial_.get()));
     GBA_LAUNCH_CHECK();
+    prof_stop("cost_f64", ev);
     ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get() + 1);
     GBA_LAUNCH_CHECK();
     double sse = 0.0;

@@ -51,11 +51,12 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
     if (opts.target_cost > 0.0 && res.initial_cost <= opts.target_cost) res.time_to_target_s = seconds_since(t0);
 
     double lambda = opts.initial_lambda;
-    bool converged = false, failed = false;
+    bool converged = false, failed = false, at_target = false;
+    if (opts.stop_at_target && res.time_to_target_s >= 0.0) at_target = true;
     double rel_decrease = 0.0;
     unsigned long long anomalies = s.anomalies();
 
-    while (res.iterations < opts.max_iterations && !converged && !failed) {
+    while (res.iterations < opts.max_iterations && !converged && !failed && !at_target) {
         double nu = 2.0;
         bool accepted = false;
         for (int trial = 0; trial < opts.max_inner_trials; ++trial) {
@@ -134,12 +135,16 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
             converged = true;
             break;
         }
+        if (opts.stop_at_target && res.time_to_target_s >= 0.0) {
+            at_target = true;
+            break;
+        }
         phase(res.t_accumulate, [&] { return s.accumulate(); });
     }
 
     res.final_cost = sse / 2.0;
     res.anomalies = s.anomalies();
-    res.termination = converged ? "CONVERGENCE" : failed ? "FAILURE" : "MAX_ITERATIONS";
+    res.termination = converged ? "CONVERGENCE" : failed ? "FAILURE" : at_target ? "TARGET_COST" : "MAX_ITERATIONS";
     return res;
 }
 

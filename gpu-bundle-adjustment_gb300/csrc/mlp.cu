@@ -1,25 +1,542 @@
-// Learned block-Jacobi correction (per-camera MLP).
+// Learned block-Jacobi correction: MLP training and inference kernels.
+//
+//   GEMMs      mma.sync.m16n8k16 BF16 x BF16 -> FP32 (BF16 weights and
+//              activations in shared memory, FP32 accumulation and storage);
+//              one kernel with strided operand loads serves the forward
+//              (X W^T), input-gradient (dY W) and weight-gradient (dY^T X) shapes.
+//   loss       per-camera FP64 thread: the preconditioned block step, its error
+//              in the block norm, and the analytic gradient through the factor
+//              parametrisation (rank-2 form dl/dF_ij = -(c_i a_j + d_i b_j)).
+//   Adam       FP32 masters, BF16 copies refreshed after each step.
+//   inference  features of S_cc -> MLP -> corrected factor L_c F_c.
+// No reference counterpart (the reference has no iterative solver).
 
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#include "blocks.cuh"
 #include "common.cuh"
 #include "mlp.hpp"
 #include "solver.hpp"
 
 namespace gba {
+namespace {
 
-struct LearnedPreconditioner::Impl {};
+constexpr int kGT = 128;  // GEMM threads (4 warps, 2 x 2 warp grid of 32 x 32)
+constexpr long long kW1 = 0, kB1 = kW1 + 1ll * kMlpH * kMlpIn, kW2 = kB1 + kMlpH, kB2 = kW2 + 1ll * kMlpH * kMlpH,
+                    kW3 = kB2 + kMlpH, kB3 = kW3 + 1ll * kMlpOut * kMlpH;
+constexpr long long kBf16Count = 1ll * kMlpH * kMlpIn + 1ll * kMlpH * kMlpH + 1ll * kMlpOut * kMlpH;
 
-LearnedPreconditioner::LearnedPreconditioner(const std::string&) {
-    throw std::invalid_argument("learned preconditioner not available in this build");
+__device__ __forceinline__ __nv_bfloat16 to_bf16(float v) { return __float2bfloat16_rn(v); }
+__device__ __forceinline__ __nv_bfloat16 to_bf16(__nv_bfloat16 v) { return v; }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
-LearnedPreconditioner::~LearnedPreconditioner() { delete impl; }
-void LearnedPreconditioner::correct_factors(Solver&, double) {}
 
-Solver::~Solver() { delete model_; }
+// C(m, n) = epilogue( sum_k A(m, k) B(k, n) ), A(m,k) = A[m*sam + k*sak],
+// B(k,n) = B[k*sbk + n*sbn]; epilogue: + bias[n], ReLU, * (mask(m,n) > 0).
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(kGT) gemm_bf16_kernel(int M, int N, int K, const TA* __restrict__ A, long long sam,
+                                                       long long sak, const TB* __restrict__ B, long long sbk,
+                                                       long long sbn, float* __restrict__ Cm, int ldc,
+                                                       const float* __restrict__ bias, int relu,
+                                                       const float* __restrict__ mask, int ldm) {
+    __shared__ __align__(16) __nv_bfloat16 As[64][24];
+    __shared__ __align__(16) __nv_bfloat16 Bs[64][24];
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
+    const int g = lane >> 2, t = lane & 3;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        for (int idx = tid; idx < 64 * 16; idx += kGT) {
+            const int r = idx >> 4, kk = idx & 15;
+            const int k = k0 + kk;
+            const int m = m0 + r, n = n0 + r;
+            As[r][kk] = (m < M && k < K) ? to_bf16(A[m * sam + k * sak]) : __float2bfloat16_rn(0.f);
+            Bs[r][kk] = (n < N && k < K) ? to_bf16(B[k * sbk + n * sbn]) : __float2bfloat16_rn(0.f);
+        }
+        __syncthreads();
+        uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const int r = wm + 16 * mt + g;
+            af[mt][0] = *reinterpret_cast<const uint32_t*>(&As[r][2 * t]);
+            af[mt][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][2 * t]);
+            af[mt][2] = *reinterpret_cast<const uint32_t*>(&As[r][2 * t + 8]);
+            af[mt][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][2 * t + 8]);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            const int r = wn + 8 * nt + g;
+            bfr[nt][0] = *reinterpret_cast<const uint32_t*>(&Bs[r][2 * t]);
+            bfr[nt][1] = *reinterpret_cast<const uint32_t*>(&Bs[r][2 * t + 8]);
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[mt][nt], af[mt], bfr[nt]);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int m = m0 + wm + 16 * mt + g + ((q >= 2) ? 8 : 0);
+                const int n = n0 + wn + 8 * nt + 2 * t + (q & 1);
+                if (m >= M || n >= N) continue;
+                float v = acc[mt][nt][q];
+                if (bias) v += bias[n];
+                if (relu) v = fmaxf(v, 0.f);
+                if (mask && !(mask[(long long)m * ldm + n] > 0.f)) v = 0.f;
+                Cm[(long long)m * ldc + n] = v;
+            }
+}
+
+template <typename TA, typename TB>
+void gemm(int M, int N, int K, const TA* A, long long sam, long long sak, const TB* B, long long sbk, long long sbn,
+          float* Cm, int ldc, const float* bias, bool relu, const float* mask, int ldm, cudaStream_t s) {
+    dim3 grid(ceil_div(N, 64), ceil_div(M, 64));
+    gemm_bf16_kernel<TA, TB><<<grid, kGT, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, Cm, ldc, bias, relu ? 1 : 0,
+                                                  mask, ldm);
+    GBA_LAUNCH_CHECK();
+}
+
+// db[n] = sum_m dY[m][n] (ordered, deterministic); one CTA per column.
+__global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ dY, int M, int ld, float* __restrict__ db) {
+    __shared__ double sh[8];
+    double s = 0.0;
+    for (int m = threadIdx.x; m < M; m += 256) s += dY[(long long)m * ld + blockIdx.x];
+    const double v = block_sum<256>(s, sh);
+    if (threadIdx.x == 0) db[blockIdx.x] = static_cast<float>(v);
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, long long n, float lr, float b1, float b2, float eps, float c1,
+                            float c2) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+using blk::tri;
+
+// F from the 45 network outputs (packed lower).
+__device__ __forceinline__ void build_F(const float* o, double* F, double* th) {
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j <= i; ++j) {
+            const int k = tri(i, j);
+            const double tk = tanh(static_cast<double>(o[k]));
+            th[k] = tk;
+            F[k] = (i == j) ? exp(0.5 * tk) : 0.5 * tk;
+        }
+}
+
+// Lt = L F (both packed lower).
+__device__ __forceinline__ void lower_mul(const double* L, const double* F, double* Lt) {
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double s = 0.0;
+            for (int k = j; k <= i; ++k) s += L[tri(i, k)] * F[tri(k, j)];
+            Lt[tri(i, j)] = s;
+        }
+}
+
+__device__ __forceinline__ void sym_mul(const double* S, const double* x, double* y) {  // packed symmetric
+    for (int i = 0; i < 9; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < 9; ++j) s += S[i >= j ? tri(i, j) : tri(j, i)] * x[j];
+        y[i] = s;
+    }
+}
+
+__device__ __forceinline__ void lowerT_vec(const double* L, const double* x, double* y) {  // y = L^T x
+    for (int j = 0; j < 9; ++j) {
+        double s = 0.0;
+        for (int i = j; i < 9; ++i) s += L[tri(i, j)] * x[i];
+        y[j] = s;
+    }
+}
+
+// Per-sample loss and gradient w.r.t. the 45 outputs (scaled by inv_b).
+__global__ void loss_kernel(const float* __restrict__ O, const double* __restrict__ Shat,
+                            const double* __restrict__ Lhat, const double* __restrict__ g,
+                            const double* __restrict__ x, int B, double inv_b, float* __restrict__ dO,
+                            double* __restrict__ loss) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    double S[45], L[45], F[45], th[45], Lt[45];
+    for (int k = 0; k < 45; ++k) {
+        S[k] = Shat[45ll * b + k];
+        L[k] = Lhat[45ll * b + k];
+    }
+    double gv[9], xv[9];
+    for (int k = 0; k < 9; ++k) {
+        gv[k] = g[9ll * b + k];
+        xv[k] = x[9ll * b + k];
+    }
+    float o[45];
+    for (int k = 0; k < 45; ++k) o[k] = O[48ll * b + k];
+    build_F(o, F, th);
+    lower_mul(L, F, Lt);
+    double y[9], y0[9], e[9], Se[9], Sx[9];
+    blk::chol9_solve(Lt, gv, y);
+    blk::chol9_solve(L, gv, y0);
+    sym_mul(S, xv, Sx);
+    double den = 0.0;
+    for (int k = 0; k < 9; ++k) den += xv[k] * Sx[k];
+    den = den > 1e-300 ? den : 1e-300;
+    for (int k = 0; k < 9; ++k) e[k] = y[k] - xv[k];
+    sym_mul(S, e, Se);
+    double num = 0.0;
+    for (int k = 0; k < 9; ++k) num += e[k] * Se[k];
+    // baseline (F = I)
+    double e0[9], Se0[9], num0 = 0.0;
+    for (int k = 0; k < 9; ++k) e0[k] = y0[k] - xv[k];
+    sym_mul(S, e0, Se0);
+    for (int k = 0; k < 9; ++k) num0 += e0[k] * Se0[k];
+    loss[2ll * b] = num / den;
+    loss[2ll * b + 1] = num0 / den;
+    if (!dO) return;
+    // gradient: gy = 2 S e / den, z = A^-1 gy, a = Lt^T y, bb = Lt^T z, c = L^T z, d = L^T y,
+    // dl/dF_ij = -(c_i a_j + d_i bb_j) (i >= j)
+    double gy[9], z[9], a[9], bv[9], c[9], d[9];
+    for (int k = 0; k < 9; ++k) gy[k] = 2.0 * Se[k] / den;
+    blk::chol9_solve(Lt, gy, z);
+    lowerT_vec(Lt, y, a);
+    lowerT_vec(Lt, z, bv);
+    lowerT_vec(L, z, c);
+    lowerT_vec(L, y, d);
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j <= i; ++j) {
+            const int k = tri(i, j);
+            const double dF = -(c[i] * a[j] + d[i] * bv[j]);
+            const double dt = 0.5 * (1.0 - th[k] * th[k]);
+            const double dout = (i == j) ? dF * F[k] * dt : dF * dt;
+            dO[48ll * b + k] = static_cast<float>(dout * inv_b);
+        }
+    for (int k = 45; k < 48; ++k) dO[48ll * b + k] = 0.f;
+}
+
+__global__ void __launch_bounds__(256) mean2_kernel(const double* __restrict__ loss, int B, double* __restrict__ out) {
+    __shared__ double sh[8];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < B; i += 256) {
+        a += loss[2ll * i];
+        b += loss[2ll * i + 1];
+    }
+    const double ta = block_sum<256>(a, sh);
+    const double tb = block_sum<256>(b, sh);
+    if (threadIdx.x == 0) {
+        out[0] = ta / B;
+        out[1] = tb / B;
+    }
+}
+
+// ---- inference-side kernels
+
+// Per-camera track statistics: observations, sum of (track length - 1), mean track length.
+__global__ void camera_stats_kernel(const int* __restrict__ cam_off, const int* __restrict__ cam_slots,
+                                    const int* __restrict__ s_pt, const int* __restrict__ pt_off, int C,
+                                    float* __restrict__ stats) {
+    const int c = blockIdx.x;
+    __shared__ double sh[8];
+    double s1 = 0.0;
+    for (int i = cam_off[c] + threadIdx.x; i < cam_off[c + 1]; i += 256) {
+        const int p = s_pt[cam_slots[i]];
+        s1 += pt_off[p + 1] - pt_off[p];
+    }
+    const double sk = block_sum<256>(s1, sh);
+    if (threadIdx.x == 0) {
+        const double n = cam_off[c + 1] - cam_off[c];
+        stats[3 * c] = static_cast<float>(log1p(n) / 10.0);
+        stats[3 * c + 1] = static_cast<float>(log1p(sk - n) / 15.0);
+        stats[3 * c + 2] = static_cast<float>(n > 0 ? sk / n / 10.0 : 0.0);
+    }
+}
+
+__global__ void features_kernel(const double* __restrict__ Sdiag, const double* __restrict__ U,
+                                const float* __restrict__ stats, double lambda, int C, float* __restrict__ feat) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const double* S = Sdiag + 81ll * c;
+    const double* Uc = U + 81ll * c;
+    double isd[9];
+    float* f = feat + 64ll * c;
+    for (int i = 0; i < 9; ++i) {
+        const double d = S[10 * i];
+        isd[i] = d > 1e-300 ? 1.0 / sqrt(d) : 0.0;
+        const double u = Uc[10 * i];
+        const double ud = u + lambda * (u > 0.0 ? u : 1e-12);
+        f[36 + i] = static_cast<float>(ud > 0.0 ? d / ud : 0.0);
+    }
+    int k = 0;
+    for (int i = 1; i < 9; ++i)
+        for (int j = 0; j < i; ++j) f[k++] = static_cast<float>(S[9 * i + j] * isd[i] * isd[j]);
+    f[45] = stats[3 * c];
+    f[46] = stats[3 * c + 1];
+    f[47] = stats[3 * c + 2];
+    f[48] = static_cast<float>(log10(lambda > 1e-300 ? lambda : 1e-300) / 10.0);
+    for (int i = 49; i < 64; ++i) f[i] = 0.f;
+}
+
+// Pfac_c <- L_c F_c (in place; both packed lower).
+__global__ void correct_kernel(const float* __restrict__ O, int C, double* __restrict__ Pfac) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    double L[45], F[45], th[45], Lt[45];
+    for (int k = 0; k < 45; ++k) L[k] = Pfac[45ll * c + k];
+    float o[45];
+    for (int k = 0; k < 45; ++k) o[k] = O[48ll * c + k];
+    build_F(o, F, th);
+    lower_mul(L, F, Lt);
+    for (int k = 0; k < 45; ++k) Pfac[45ll * c + k] = Lt[k];
+}
+
+template <typename T>
+T* dalloc(long long n) {
+    T* p = nullptr;
+    GBA_CUDA_CHECK(cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * n));
+    return p;
+}
+
+const char kMagic[8] = {'G', 'B', 'A', 'M', 'L', 'P', '0', '1'};
+
+}  // namespace
+
+// ------------------------------------------------------------------ Mlp
+
+void Mlp::alloc() {
+    p_ = dalloc<float>(kMlpParams);
+    g_ = dalloc<float>(kMlpParams);
+    m_ = dalloc<float>(kMlpParams);
+    v_ = dalloc<float>(kMlpParams);
+    wb_ = dalloc<__nv_bfloat16>(kBf16Count);
+    GBA_CUDA_CHECK(cudaMemset(g_, 0, sizeof(float) * kMlpParams));
+    GBA_CUDA_CHECK(cudaMemset(m_, 0, sizeof(float) * kMlpParams));
+    GBA_CUDA_CHECK(cudaMemset(v_, 0, sizeof(float) * kMlpParams));
+    ensure_capacity(cap_);
+}
+
+void Mlp::ensure_capacity(int B) {
+    if (B <= cap_ && h1_) return;
+    cap_ = std::max(B, std::max(cap_, 1));
+    for (void* q : {static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(o_), static_cast<void*>(do_),
+                    static_cast<void*>(dh2_), static_cast<void*>(dh1_), static_cast<void*>(loss_)})
+        if (q) cudaFree(q);
+    h1_ = dalloc<float>(1ll * cap_ * kMlpH);
+    h2_ = dalloc<float>(1ll * cap_ * kMlpH);
+    o_ = dalloc<float>(1ll * cap_ * kMlpOut);
+    do_ = dalloc<float>(1ll * cap_ * kMlpOut);
+    dh2_ = dalloc<float>(1ll * cap_ * kMlpH);
+    dh1_ = dalloc<float>(1ll * cap_ * kMlpH);
+    loss_ = dalloc<double>(2ll * cap_ + 2);
+}
+
+Mlp::Mlp(int capacity, uint64_t seed) : cap_(capacity) {
+    alloc();
+    std::vector<float> h(kMlpParams, 0.f);
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd(0.f, 1.f);
+    const float s1 = std::sqrt(2.f / kMlpUsedIn), s2 = std::sqrt(2.f / kMlpH);
+    for (int r = 0; r < kMlpH; ++r)
+        for (int c = 0; c < kMlpUsedIn; ++c) h[kW1 + 1ll * r * kMlpIn + c] = s1 * nd(rng);
+    for (long long i = 0; i < 1ll * kMlpH * kMlpH; ++i) h[kW2 + i] = s2 * nd(rng);
+    set_params(h.data());  // W3 = 0, biases = 0: the network starts as plain block-Jacobi
+}
+
+Mlp::Mlp(const std::string& path, int capacity) : cap_(capacity) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open model " + path);
+    char magic[8];
+    int32_t dims[3];
+    f.read(magic, 8);
+    f.read(reinterpret_cast<char*>(dims), sizeof dims);
+    if (!f || std::memcmp(magic, kMagic, 8) != 0 || dims[0] != kMlpIn || dims[1] != kMlpH || dims[2] != kMlpOut)
+        throw std::runtime_error("not a gba MLP model: " + path);
+    std::vector<float> h(kMlpParams);
+    f.read(reinterpret_cast<char*>(h.data()), sizeof(float) * kMlpParams);
+    if (!f) throw std::runtime_error("truncated model " + path);
+    alloc();
+    set_params(h.data());
+}
+
+Mlp::~Mlp() {
+    for (void* q : {static_cast<void*>(p_), static_cast<void*>(g_), static_cast<void*>(m_), static_cast<void*>(v_), wb_,
+                    static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(o_), static_cast<void*>(do_),
+                    static_cast<void*>(dh2_), static_cast<void*>(dh1_), static_cast<void*>(loss_)})
+        if (q) cudaFree(q);
+}
+
+void Mlp::save(const std::string& path) const {
+    std::vector<float> h(kMlpParams);
+    get_params(h.data());
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write model " + path);
+    const int32_t dims[3] = {kMlpIn, kMlpH, kMlpOut};
+    f.write(kMagic, 8);
+    f.write(reinterpret_cast<const char*>(dims), sizeof dims);
+    f.write(reinterpret_cast<const char*>(h.data()), sizeof(float) * kMlpParams);
+    if (!f) throw std::runtime_error("write failed for " + path);
+}
+
+void Mlp::get_params(float* host) const {
+    GBA_CUDA_CHECK(cudaMemcpy(host, p_, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+}
+
+void Mlp::set_params(const float* host) {
+    GBA_CUDA_CHECK(cudaMemcpy(p_, host, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
+    refresh_bf16(nullptr);
+    GBA_CUDA_CHECK(cudaStreamSynchronize(nullptr));
+}
+
+void Mlp::grads(float* host) const {
+    GBA_CUDA_CHECK(cudaDeviceSynchronize());
+    GBA_CUDA_CHECK(cudaMemcpy(host, g_, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+}
+
+void Mlp::refresh_bf16(cudaStream_t s) {
+    __nv_bfloat16* wb = static_cast<__nv_bfloat16*>(wb_);
+    to_bf16_kernel<<<64, 256, 0, s>>>(p_ + kW1, wb, 1ll * kMlpH * kMlpIn);
+    GBA_LAUNCH_CHECK();
+    to_bf16_kernel<<<64, 256, 0, s>>>(p_ + kW2, wb + 1ll * kMlpH * kMlpIn, 1ll * kMlpH * kMlpH);
+    GBA_LAUNCH_CHECK();
+    to_bf16_kernel<<<64, 256, 0, s>>>(p_ + kW3, wb + 1ll * kMlpH * kMlpIn + 1ll * kMlpH * kMlpH, 1ll * kMlpOut * kMlpH);
+    GBA_LAUNCH_CHECK();
+}
+
+void Mlp::forward(const float* feat, int B, float* out, cudaStream_t s) {
+    ensure_capacity(B);
+    const __nv_bfloat16* wb = static_cast<const __nv_bfloat16*>(wb_);
+    const __nv_bfloat16* w1 = wb;
+    const __nv_bfloat16* w2 = wb + 1ll * kMlpH * kMlpIn;
+    const __nv_bfloat16* w3 = w2 + 1ll * kMlpH * kMlpH;
+    // H1 = relu(X W1^T + b1): A = X [B x 64], B(k, n) = W1[n][k]
+    gemm(B, kMlpH, kMlpIn, feat, kMlpIn, 1, w1, 1, kMlpIn, h1_, kMlpH, p_ + kB1, true, nullptr, 0, s);
+    gemm(B, kMlpH, kMlpH, h1_, kMlpH, 1, w2, 1, kMlpH, h2_, kMlpH, p_ + kB2, true, nullptr, 0, s);
+    gemm(B, kMlpOut, kMlpH, h2_, kMlpH, 1, w3, 1, kMlpH, out, kMlpOut, p_ + kB3, false, nullptr, 0, s);
+}
+
+double Mlp::loss_grad(const float* feat, const double* Shat, const double* Lhat, const double* g, const double* x,
+                      int B, cudaStream_t s, double* baseline_loss) {
+    if (B <= 0) throw std::invalid_argument("empty batch");
+    ensure_capacity(B);
+    forward(feat, B, o_, s);
+    loss_kernel<<<ceil_div(B, 128), 128, 0, s>>>(o_, Shat, Lhat, g, x, B, 1.0 / B, do_, loss_);
+    GBA_LAUNCH_CHECK();
+    mean2_kernel<<<1, 256, 0, s>>>(loss_, B, loss_ + 2ll * cap_);
+    GBA_LAUNCH_CHECK();
+    const __nv_bfloat16* wb = static_cast<const __nv_bfloat16*>(wb_);
+    const __nv_bfloat16* w2 = wb + 1ll * kMlpH * kMlpIn;
+    const __nv_bfloat16* w3 = w2 + 1ll * kMlpH * kMlpH;
+    // layer 3: dW3[n][k] = sum_m dO[m][n] H2[m][k]; db3; dH2 = (dO W3) * (H2 > 0)
+    gemm(kMlpOut, kMlpH, B, do_, 1, kMlpOut, h2_, kMlpH, 1, g_ + kW3, kMlpH, nullptr, false, nullptr, 0, s);
+    colsum_kernel<<<kMlpOut, 256, 0, s>>>(do_, B, kMlpOut, g_ + kB3);
+    GBA_LAUNCH_CHECK();
+    gemm(B, kMlpH, kMlpOut, do_, kMlpOut, 1, w3, kMlpH, 1, dh2_, kMlpH, nullptr, false, h2_, kMlpH, s);
+    // layer 2
+    gemm(kMlpH, kMlpH, B, dh2_, 1, kMlpH, h1_, kMlpH, 1, g_ + kW2, kMlpH, nullptr, false, nullptr, 0, s);
+    colsum_kernel<<<kMlpH, 256, 0, s>>>(dh2_, B, kMlpH, g_ + kB2);
+    GBA_LAUNCH_CHECK();
+    gemm(B, kMlpH, kMlpH, dh2_, kMlpH, 1, w2, kMlpH, 1, dh1_, kMlpH, nullptr, false, h1_, kMlpH, s);
+    // layer 1 (input features need no gradient)
+    gemm(kMlpH, kMlpIn, B, dh1_, 1, kMlpH, feat, kMlpIn, 1, g_ + kW1, kMlpIn, nullptr, false, nullptr, 0, s);
+    colsum_kernel<<<kMlpH, 256, 0, s>>>(dh1_, B, kMlpH, g_ + kB1);
+    GBA_LAUNCH_CHECK();
+    double h[2];
+    GBA_CUDA_CHECK(cudaMemcpyAsync(h, loss_ + 2ll * cap_, sizeof h, cudaMemcpyDeviceToHost, s));
+    GBA_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (baseline_loss) *baseline_loss = h[1];
+    return h[0];
+}
+
+void Mlp::adam_step(float lr, float beta1, float beta2, float eps, cudaStream_t s) {
+    ++step_;
+    const float c1 = 1.f - std::pow(beta1, static_cast<float>(step_));
+    const float c2 = 1.f - std::pow(beta2, static_cast<float>(step_));
+    adam_kernel<<<120, 256, 0, s>>>(p_, g_, m_, v_, kMlpParams, lr, beta1, beta2, eps, c1, c2);
+    GBA_LAUNCH_CHECK();
+    refresh_bf16(s);
+}
+
+// ------------------------------------------------------------------ solver side
+
+void mlp_features(Solver& s, double lambda, float* feat) {
+    if (!s.mlp_stats_.get()) {
+        s.mlp_stats_.alloc(3ull * s.C_);
+        camera_stats_kernel<<<s.C_, 256, 0, s.stream_>>>(s.cam_off_.get(), s.cam_slots_.get(), s.s_pt_.get(),
+                                                          s.pt_off_.get(), s.C_, s.mlp_stats_.get());
+        GBA_LAUNCH_CHECK();
+    }
+    features_kernel<<<ceil_div(s.C_, 128), 128, 0, s.stream_>>>(s.Sdiag_.get(), s.U_.get(), s.mlp_stats_.get(),
+                                                                 lambda, s.C_, feat);
+    GBA_LAUNCH_CHECK();
+}
+
+LearnedPreconditioner::LearnedPreconditioner(const std::string& path) : mlp_(path, 1) {}
+
+LearnedPreconditioner::~LearnedPreconditioner() {
+    if (feat_) cudaFree(feat_);
+    if (out_) cudaFree(out_);
+}
+
+void LearnedPreconditioner::correct_factors(Solver& s, double lambda) {
+    if (cap_ < s.C_) {
+        if (feat_) cudaFree(feat_);
+        if (out_) cudaFree(out_);
+        feat_ = dalloc<float>(64ll * s.C_);
+        out_ = dalloc<float>(1ll * kMlpOut * s.C_);
+        cap_ = s.C_;
+    }
+    mlp_features(s, lambda, feat_);
+    cudaEvent_t ev = s.prof_start();
+    mlp_.forward(feat_, s.C_, out_, s.stream_);
+    s.prof_stop("mlp_forward", ev);
+    correct_kernel<<<ceil_div(s.C_, 128), 128, 0, s.stream_>>>(out_, s.C_, s.Pfac_.get());
+    GBA_LAUNCH_CHECK();
+}
+
+Solver::~Solver() {
+    prof_reset();
+    delete model_;
+}
 
 void Solver::load_model(const std::string& path) {
+    if (form_ == SolverForm::Plain) throw std::invalid_argument("the learned preconditioner needs a mixed form");
+    if (path.empty()) throw std::invalid_argument("learned form: empty model path");
+    auto* m = new LearnedPreconditioner(path);
     delete model_;
-    model_ = nullptr;
-    model_ = new LearnedPreconditioner(path);
+    model_ = m;
 }
 
 }  // namespace gba

@@ -459,9 +459,24 @@ __global__ void __launch_bounds__(kCT) sdiag_camera_pass(const int* __restrict__
     }
 }
 
-// Thread per camera: S_cc (full, FP64) and its packed Cholesky factor. A block
-// that is not SPD in FP64 (round-off with tiny damping) falls back to its
-// diagonal, counted in sc[S_NORM].
+// Packed Cholesky factor of a full 9x9 block; a block that is not SPD in FP64
+// (round-off with tiny damping) falls back to the square root of its diagonal.
+__device__ void factor_block(const double* A, double* Lc) {
+    double f[45];
+    if (!blk::chol9_factor(A, f)) {
+#pragma unroll
+        for (int i = 0; i < 45; ++i) f[i] = 0.0;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const double d = A[10 * i];
+            f[blk::tri(i, i)] = sqrt(d > 1e-300 ? d : 1e-300);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 45; ++i) Lc[i] = f[i];
+}
+
+// Thread per camera: S_cc (full, FP64) and its packed Cholesky factor.
 __global__ void __launch_bounds__(kVT) sdiag_finalize(const int* __restrict__ cam_chunk_off,
                                                      const double* __restrict__ part, const double* __restrict__ U,
                                                      double lambda, int C, double* __restrict__ Sdiag,
@@ -486,19 +501,18 @@ __global__ void __launch_bounds__(kVT) sdiag_finalize(const int* __restrict__ ca
     double* Sd = Sdiag + 81ll * c;
 #pragma unroll
     for (int i = 0; i < 81; ++i) Sd[i] = A[i];
-    double f[45];
-    if (!blk::chol9_factor(A, f)) {
+    factor_block(A, L + 45ll * c);
+}
+
+// Block-Jacobi factors from stored diagonal blocks (the learned form's fallback).
+__global__ void __launch_bounds__(kVT) factor_blocks_kernel(const double* __restrict__ Sdiag, int C,
+                                                           double* __restrict__ L) {
+    const int c = blockIdx.x * kVT + threadIdx.x;
+    if (c >= C) return;
+    double A[81];
 #pragma unroll
-        for (int i = 0; i < 45; ++i) f[i] = 0.0;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) {
-            const double d = A[10 * i];
-            f[blk::tri(i, i)] = sqrt(d > 1e-300 ? d : 1e-300);
-        }
-    }
-    double* Lc = L + 45ll * c;
-#pragma unroll
-    for (int i = 0; i < 45; ++i) Lc[i] = f[i];
+    for (int i = 0; i < 81; ++i) A[i] = Sdiag[81ll * c + i];
+    factor_block(A, L + 45ll * c);
 }
 
 }  // namespace
@@ -508,14 +522,19 @@ __global__ void __launch_bounds__(kVT) sdiag_finalize(const int* __restrict__ ca
 template <typename T>
 static void implicit_parts(Solver& s, const double* x, double a, const double* done) {
     T* u = reinterpret_cast<T*>(s.u_.get());
+    const bool f32 = sizeof(T) == 4;
+    cudaEvent_t ev = s.prof_start();
     schur_point_pass<T><<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
                                                            s.s_pt_.get(), s.J32_.get(), s.Vinv_.get(), s.bp_.get(), x, a, u, done);
     GBA_LAUNCH_CHECK();
+    s.prof_stop(f32 ? "schur_point_pass_f32" : "schur_point_pass_f64", ev);
     if (s.n_cchunk_ > 0) {
+        ev = s.prof_start();
         schur_camera_pass<T><<<s.n_cchunk_, kCT, 0, s.stream_>>>(s.cchunk_begin_.get(), s.cchunk_cam_.get(),
                                                                  s.cam_off_.get(), s.cam_slots_.get(), s.J32_.get(),
                                                                  u, s.cam_part_.get(), done);
         GBA_LAUNCH_CHECK();
+        s.prof_stop(f32 ? "schur_camera_pass_f32" : "schur_camera_pass_f64", ev);
     }
 }
 
@@ -566,8 +585,9 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     }
     double rnorm2 = bnorm2;
     const double tol2 = opts.refine_tol * opts.refine_tol * bnorm2;
-    for (int step = 0; step < opts.refine_max_steps && rnorm2 > tol2; ++step) {
-        // inner PCG on the FP32 operator: S32 e = r
+    // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_). Returns the
+    // iteration count; *ok = reached the inner tolerance without breakdown.
+    auto inner_pcg = [&](bool* ok) -> long long {
         pcg_init<<<ncb, kVT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), ref_r_.get(),
                                            Pfac_.get(), C_, red, red2);
         GBA_LAUNCH_CHECK();
@@ -594,8 +614,28 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             sync();
             if (flag != 0.0) break;
         }
-        double iters = 0.0;
-        GBA_CUDA_CHECK(cudaMemcpyAsync(&iters, sc + S_ITERS, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+        double h[9];
+        GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
+        sync();
+        *ok = h[S_DONE] != 2.0 && h[S_RR] <= h[S_TOL2] * h[S_BB];
+        return static_cast<long long>(h[S_ITERS]);
+    };
+    bool use_learned = learned;
+    for (int step = 0; step < opts.refine_max_steps && rnorm2 > tol2; ++step) {
+        bool ok = false;
+        long long it_count = inner_pcg(&ok);
+        if (use_learned && !ok) {
+            // Block-Jacobi judges the learned factors: an inner solve that breaks
+            // down or misses its tolerance is redone with the plain blocks, which
+            // then serve for the rest of this trial.
+            factor_blocks_kernel<<<ncb, kVT, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+            GBA_LAUNCH_CHECK();
+            use_learned = false;
+            ++st.fallbacks;
+            st.pcg_iterations += it_count;
+            it_count = inner_pcg(&ok);
+        }
+        const double iters = static_cast<double>(it_count);
         // dc += e; FP64 residual r = rhs - S64 dc
         axpy_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_x_.get(), n);
         GBA_LAUNCH_CHECK();

@@ -56,6 +56,7 @@ struct PcgStats {
     long long pcg_iterations = 0;
     double rel_residual = 0.0;  // final ||rhs - S dc|| / ||rhs|| (FP64)
     bool converged = false;
+    int fallbacks = 0;          // learned form: inner solves redone with plain block-Jacobi
 };
 
 struct PhaseTimes {
@@ -115,8 +116,17 @@ public:
                kTrialCams, kTrialPts };
     const void* buffer(Buf b, size_t* bytes) const;
 
-    PhaseTimes times;
-    bool timing = false;  // synchronise after each stage and accumulate phase wall times
+    // Optional per-kernel device timing (CUDA events on the solver stream
+    // around selected launches). prof_start returns null when profiling is off.
+    void set_profiling(bool on);
+    cudaEvent_t prof_start();
+    void prof_stop(const char* name, cudaEvent_t start);
+    // Launch count and total device milliseconds of the named kernel since the
+    // last reset (synchronises the stream).
+    void kernel_stats(const std::string& name, long long* launches, double* total_ms);
+    void prof_reset();
+    // Restores the parameters given at construction (device-to-device copy).
+    void reset_params();
 
     // ---- internal state (public for the kernel translation units) ----
     int C_, P_, E_, n_pad_ = 0;
@@ -124,7 +134,13 @@ public:
     cudaStream_t stream_;
     LearnedPreconditioner* model_ = nullptr;
 
-    DevBuf<double> cams_, pts_, tcams_, tpts_;
+    DevBuf<double> cams_, pts_, tcams_, tpts_, cams0_, pts0_;
+    bool profiling_ = false;
+    struct Timed {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Timed> timed_;
     // structure
     DevBuf<int> order_, pt_off_, s_cam_, s_pt_, cam_off_, cam_slots_;
     DevBuf<double> s_px_;
@@ -133,6 +149,8 @@ public:
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
     DevBuf<float> J32_;
+    DevBuf<float> r_cur_, r_trial_;  // mixed: FP64-evaluated residuals (FP32) at current / trial parameters
+    bool resid_valid_ = false;       // r_cur_ and scal_[0] hold the current parameters' residuals / SSE
     DevBuf<double> sse_part_, cam_part_, scal_;  // scal_: [0] sse, [1] trial sse, [2] denom, [3..] scratch
     DevBuf<unsigned long long> counters_;        // [0] anomalies, [1] non-SPD V blocks
     // plain Schur
@@ -146,7 +164,8 @@ public:
     DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_;
     DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or FP64)
     DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
-    DevBuf<float> mlp_in_;   // learned form: per-camera features
+    DevBuf<float> mlp_stats_;  // learned form: per-camera track statistics (3 per camera)
+    bool harvest_ = false;     // plain form: keep the damped diagonal blocks S_cc in Sdiag_
 
     void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px);
     void build_pairs();

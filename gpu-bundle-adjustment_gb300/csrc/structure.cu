@@ -12,6 +12,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <vector>
 
@@ -40,6 +41,12 @@ template class DevBuf<unsigned long long>;
 template class DevBuf<unsigned int>;
 template class DevBuf<unsigned char>;
 template class DevBuf<long long>;
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int device_sm_count() {
     static int cached = 0;
@@ -172,6 +179,12 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     scal_.alloc(8);
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get(), 0, 4 * sizeof(unsigned long long), stream_));
     set_params(cams, pts);
+    cams0_.alloc(9ull * C);
+    pts0_.alloc(3ull * P);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cams0_.get(), cams_.get(), 9ull * C * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(pts0_.get(), pts_.get(), 3ull * P * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   stream_));
     build_structure(obs_cam, obs_pt, obs_px);
 
     // normal equations (both forms)
@@ -197,6 +210,8 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         build_pairs();
     } else {
         J32_.alloc(24ull * E);
+        r_cur_.alloc(2ull * E);
+        r_trial_.alloc(2ull * E);
         Sdiag_.alloc(81ull * C);
         Pfac_.alloc(81ull * C);
         rhs_.alloc(9ull * C);
@@ -215,6 +230,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
 void Solver::sync() const { GBA_CUDA_CHECK(cudaStreamSynchronize(stream_)); }
 
 void Solver::set_params(const double* cams, const double* pts) {
+    resid_valid_ = false;
     GBA_CUDA_CHECK(cudaMemcpyAsync(cams_.get(), cams, 9ull * C_ * sizeof(double), cudaMemcpyHostToDevice,
                                    stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(pts_.get(), pts, 3ull * P_ * sizeof(double), cudaMemcpyHostToDevice,
@@ -413,6 +429,12 @@ unsigned long long Solver::nonspd_total() const {
 void Solver::accept() {
     cams_.swap(tcams_);
     pts_.swap(tpts_);
+    if (form_ != SolverForm::Plain) {
+        // the trial evaluation is the current one now: residuals and SSE
+        r_cur_.swap(r_trial_);
+        GBA_CUDA_CHECK(cudaMemcpyAsync(scal_.get(), scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+        resid_valid_ = true;
+    }
 }
 
 const void* Solver::buffer(Buf b, size_t* bytes) const {
@@ -441,6 +463,60 @@ const void* Solver::buffer(Buf b, size_t* bytes) const {
     }
     *bytes = 0;
     return nullptr;
+}
+
+}  // namespace gba
+
+namespace gba {
+
+void Solver::reset_params() {
+    resid_valid_ = false;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cams_.get(), cams0_.get(), 9ull * C_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(pts_.get(), pts0_.get(), 3ull * P_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   stream_));
+}
+
+void Solver::set_profiling(bool on) { profiling_ = on; }
+
+cudaEvent_t Solver::prof_start() {
+    if (!profiling_) return nullptr;
+    cudaEvent_t e = nullptr;
+    GBA_CUDA_CHECK(cudaEventCreate(&e));
+    GBA_CUDA_CHECK(cudaEventRecord(e, stream_));
+    return e;
+}
+
+void Solver::prof_stop(const char* name, cudaEvent_t start) {
+    if (!start) return;
+    cudaEvent_t e = nullptr;
+    GBA_CUDA_CHECK(cudaEventCreate(&e));
+    GBA_CUDA_CHECK(cudaEventRecord(e, stream_));
+    timed_.push_back({name, start, e});
+}
+
+void Solver::kernel_stats(const std::string& name, long long* launches, double* total_ms) {
+    sync();
+    long long n = 0;
+    double ms = 0.0;
+    for (const Timed& t : timed_) {
+        if (t.name != name) continue;
+        float v = 0.f;
+        GBA_CUDA_CHECK(cudaEventElapsedTime(&v, t.a, t.b));
+        ms += v;
+        ++n;
+    }
+    if (launches) *launches = n;
+    if (total_ms) *total_ms = ms;
+}
+
+void Solver::prof_reset() {
+    sync();
+    for (Timed& t : timed_) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    timed_.clear();
 }
 
 }  // namespace gba

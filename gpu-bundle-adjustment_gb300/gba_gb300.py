@@ -21,7 +21,7 @@ LIB_PATH = PKG / "lib" / "libgba_gb300.so"
 
 GBA_OK = 0
 FORMS = {"plain": 0, "mixed": 1, "learned": 2}
-TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE"}
+TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE", 3: "TARGET_COST"}
 BUF = {
     "U": 0, "V": 1, "bc": 2, "bp": 3, "W": 4, "Vinv": 5, "S": 6, "rhs": 7, "dc": 8, "dp": 9,
     "order": 10, "J32": 11, "Sdiag": 12, "cams": 13, "pts": 14, "trial_cams": 15, "trial_pts": 16,
@@ -52,6 +52,7 @@ class LMOptions(C.Structure):
         ("pcg_max_iters", C.c_int),
         ("model_path", C.c_char_p),
         ("target_cost", C.c_double),
+        ("stop_at_target", C.c_int),
     ]
 
 
@@ -123,6 +124,26 @@ _SIG = {
     "gba_solver_accept": (C.c_int, [C.c_void_p]),
     "gba_solver_counters": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
     "gba_solver_load_model": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "gba_solver_run": (C.c_int, [C.c_void_p, C.POINTER(LMOptions), C.POINTER(LMResultC)]),
+    "gba_solver_reset_params": (C.c_int, [C.c_void_p]),
+    "gba_solver_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "gba_solver_kernel_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+    "gba_solver_profile_reset": (C.c_int, [C.c_void_p]),
+    "gba_launch_count": (C.c_ulonglong, []),
+    "gba_solver_set_harvest": (C.c_int, [C.c_void_p, C.c_int]),
+    "gba_solver_features": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
+    "gba_mlp_num_params": (C.c_longlong, []),
+    "gba_mlp_create": (C.c_int, [C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]),
+    "gba_mlp_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "gba_mlp_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "gba_mlp_destroy": (None, [C.c_void_p]),
+    "gba_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "gba_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "gba_mlp_get_grads": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "gba_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "gba_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gba_mlp_adam_step": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]),
     "gba_solver_buffer_size": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
     "gba_solver_download": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "gba_solver_device_ptr": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
@@ -280,22 +301,16 @@ class LMResult:
     trajectory_time_s: list = field(default_factory=list)
 
 
-def solve(prob: BALProblem, **opts) -> LMResult:
-    """gba::solve_bal_gpu through the C ABI: updates prob.cameras / prob.points in place."""
-    o = default_options(**opts)
-    cap = max(8, o.max_iterations + 2)
+def _result_struct(cap: int):
     traj, ttime = np.zeros(cap), np.zeros(cap)
     r = LMResultC()
     r.trajectory = _d(traj)
     r.trajectory_time_s = _d(ttime)
     r.trajectory_capacity = cap
-    for a, dt in ((prob.cameras, np.float64), (prob.points, np.float64), (prob.obs_camera, np.int32),
-                  (prob.obs_point, np.int32), (prob.obs_pixel, np.float64)):
-        if a.dtype != dt or not a.flags.c_contiguous:
-            raise TypeError("BALProblem arrays must be contiguous float64 / int32")
-    _check(lib.gba_solve_bal(prob.num_cameras, prob.num_points, prob.num_observations, _d(prob.cameras),
-                             _d(prob.points), _i(prob.obs_camera), _i(prob.obs_point), _d(prob.obs_pixel),
-                             C.byref(o), C.byref(r)))
+    return r, traj, ttime
+
+
+def _to_result(r, traj, ttime, cap) -> "LMResult":
     n = min(r.trajectory_len, cap)
     return LMResult(
         r.initial_cost, r.final_cost, r.iterations, TERMINATION[r.termination], r.anomalies, r.total_time_s,
@@ -304,6 +319,37 @@ def solve(prob: BALProblem, **opts) -> LMResult:
              cost=r.t_cost),
         traj[:n].tolist(), ttime[:n].tolist(),
     )
+
+
+def launch_count() -> int:
+    """Kernels launched by libgba_gb300 in this process so far."""
+    return int(lib.gba_launch_count())
+
+
+def solve(prob: BALProblem, **opts) -> LMResult:
+    """gba::solve_bal_gpu through the C ABI: updates prob.cameras / prob.points in place."""
+    o = default_options(**opts)
+    cap = max(8, o.max_iterations + 2)
+    r, traj, ttime = _result_struct(cap)
+    for a, dt in ((prob.cameras, np.float64), (prob.points, np.float64), (prob.obs_camera, np.int32),
+                  (prob.obs_point, np.int32), (prob.obs_pixel, np.float64)):
+        if a.dtype != dt or not a.flags.c_contiguous:
+            raise TypeError("BALProblem arrays must be contiguous float64 / int32")
+    _check(lib.gba_solve_bal(prob.num_cameras, prob.num_points, prob.num_observations, _d(prob.cameras),
+                             _d(prob.points), _i(prob.obs_camera), _i(prob.obs_point), _d(prob.obs_pixel),
+                             C.byref(o), C.byref(r)))
+    return _to_result(r, traj, ttime, cap)
+
+
+def solve_raw(num_cameras: int, num_points: int, num_observations: int, cams: int, pts: int, oc: int, op: int,
+              px: int, **opts) -> LMResult:
+    """gba_solve_bal on raw host addresses (e.g. pinned torch tensors' data_ptr())."""
+    o = default_options(**opts)
+    cap = max(8, o.max_iterations + 2)
+    r, traj, ttime = _result_struct(cap)
+    _check(lib.gba_solve_bal(num_cameras, num_points, num_observations, C.cast(cams, _dp), C.cast(pts, _dp),
+                             C.cast(oc, _ip), C.cast(op, _ip), C.cast(px, _dp), C.byref(o), C.byref(r)))
+    return _to_result(r, traj, ttime, cap)
 
 
 class Solver:
@@ -392,6 +438,29 @@ class Solver:
     def load_model(self, path) -> None:
         _check(lib.gba_solver_load_model(self.h, str(path).encode()))
 
+    def run(self, **opts) -> LMResult:
+        """Full LM loop on the device-resident problem from the current parameters."""
+        opts.setdefault("form", self.form)
+        o = default_options(**opts)
+        cap = max(8, o.max_iterations + 2)
+        r, traj, ttime = _result_struct(cap)
+        _check(lib.gba_solver_run(self.h, C.byref(o), C.byref(r)))
+        return _to_result(r, traj, ttime, cap)
+
+    def reset_params(self) -> None:
+        _check(lib.gba_solver_reset_params(self.h))
+
+    def profile(self, enable: bool = True) -> None:
+        _check(lib.gba_solver_profile(self.h, int(enable)))
+
+    def kernel_stats(self, name: str):
+        n, ms = C.c_longlong(), C.c_double()
+        _check(lib.gba_solver_kernel_stats(self.h, name.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def profile_reset(self) -> None:
+        _check(lib.gba_solver_profile_reset(self.h))
+
     def download(self, name: str) -> np.ndarray:
         bid = BUF[name]
         size = C.c_size_t()
@@ -429,3 +498,67 @@ def dense_potrs(L: int, n: int, lda: int, b: int, info: int, stream: int = 0) ->
 def eval_edges(precision: int, cams: int, pts: int, oc: int, op: int, px: int, E: int, r: int, Jc: int = 0,
                Jp: int = 0, stream: int = 0) -> None:
     _check(lib.gba_eval_edges(precision, cams, pts, oc, op, px, E, r, Jc or None, Jp or None, stream or None))
+
+
+def solver_set_harvest(solver: "Solver", enable: bool = True) -> None:
+    _check(lib.gba_solver_set_harvest(solver.h, int(enable)))
+
+
+def solver_features(solver: "Solver", lam: float, feat_dev: int) -> None:
+    """Features of the solver's current S_cc blocks into a device buffer (C x 64 float)."""
+    _check(lib.gba_solver_features(solver.h, lam, feat_dev))
+
+
+class Mlp:
+    """The learned block-Jacobi correction network (gba_mlp)."""
+
+    NUM_PARAMS = int(lib.gba_mlp_num_params())
+
+    def __init__(self, seed: int = 0, capacity: int = 4096, path=None):
+        h = C.c_void_p()
+        if path is not None:
+            _check(lib.gba_mlp_load(str(path).encode(), capacity, C.byref(h)))
+        else:
+            _check(lib.gba_mlp_create(seed, capacity, C.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib.gba_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def save(self, path) -> None:
+        _check(lib.gba_mlp_save(self.h, str(path).encode()))
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.NUM_PARAMS, np.float32)
+        _check(lib.gba_mlp_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        _check(lib.gba_mlp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(self.NUM_PARAMS, np.float32)
+        _check(lib.gba_mlp_get_grads(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def forward(self, feat_dev: int, batch: int, out_dev: int, stream: int = 0) -> None:
+        _check(lib.gba_mlp_forward(self.h, feat_dev, batch, out_dev, stream or None))
+
+    def loss_grad(self, feat: int, Shat: int, Lhat: int, g: int, x: int, batch: int, stream: int = 0):
+        loss, base = C.c_double(), C.c_double()
+        _check(lib.gba_mlp_loss_grad(self.h, feat, Shat, Lhat, g, x, batch, stream or None, C.byref(loss),
+                                     C.byref(base)))
+        return loss.value, base.value
+
+    def adam_step(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
+                  stream: int = 0) -> None:
+        _check(lib.gba_mlp_adam_step(self.h, lr, beta1, beta2, eps, stream or None))

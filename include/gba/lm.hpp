@@ -44,6 +44,7 @@ struct LMOptions {
     int pcg_max_iters = 200;      // mixed: PCG iteration cap per inner solve
     std::string model_path;       // learned form: MLP weights file (gba_mlp binary)
     double target_cost = 0.0;     // if > 0: record the wall time at which cost first <= target
+    bool stop_at_target = false;  // end the solve ("TARGET_COST") once cost <= target_cost
 };
 
 struct LMResult {
@@ -51,6 +52,7 @@ struct LMResult {
     double final_cost = 0.0;
     int iterations = 0;               // accepted outer iterations
     std::string termination;          // "CONVERGENCE" | "MAX_ITERATIONS" | "FAILURE"
+                                      // (+ "TARGET_COST" with LMOptions::stop_at_target)
     unsigned long long anomalies = 0; // cumulative non-finite edge / trial-residual count
     double total_time_s = 0.0;        // wall time of the solve, device setup included
 

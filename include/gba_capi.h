@@ -31,7 +31,7 @@ enum {
 };
 
 enum { GBA_FORM_PLAIN = 0, GBA_FORM_MIXED = 1, GBA_FORM_MIXED_LEARNED = 2 };
-enum { GBA_TERM_CONVERGENCE = 0, GBA_TERM_MAX_ITERATIONS = 1, GBA_TERM_FAILURE = 2 };
+enum { GBA_TERM_CONVERGENCE = 0, GBA_TERM_MAX_ITERATIONS = 1, GBA_TERM_FAILURE = 2, GBA_TERM_TARGET_COST = 3 };
 
 const char* gba_last_error(void);
 const char* gba_version(void);
@@ -53,6 +53,7 @@ typedef struct gba_lm_options {
     int pcg_max_iters;        /* 200 */
     const char* model_path;   /* learned-form weights, or NULL */
     double target_cost;       /* 0 = off */
+    int stop_at_target;       /* 0; 1 = end the solve once cost <= target_cost */
 } gba_lm_options;
 
 /* Mirrors gba::LMResult (reference include/gba/lm.hpp:21-29) plus additive
@@ -158,6 +159,58 @@ int gba_solver_accept(gba_solver* s);
 int gba_solver_counters(gba_solver* s, unsigned long long* out_anomalies, unsigned long long* out_nonspd);
 /* Loads the learned-preconditioner weights for the MixedLearned form. */
 int gba_solver_load_model(gba_solver* s, const char* path);
+/* Runs the full LM loop on the solver's device-resident problem from its
+ * current parameters (the stages above, in the reference's order; no host
+ * copies of the problem). Same contract as gba_solve_bal; parameters stay on
+ * the device (gba_solver_get_params). opts->form must match the solver's form. */
+int gba_solver_run(gba_solver* s, const gba_lm_options* opts, gba_lm_result* result);
+/* Restores the parameters the solver was created with (device copy). */
+int gba_solver_reset_params(gba_solver* s);
+/* Per-kernel device timing with CUDA events on the solver stream: enable /
+ * disable, query (launches and total milliseconds of a named kernel since the
+ * last reset), reset. Names: point_pass_f64, camera_pass_f64, point_pass_f32,
+ * camera_pass_f32, cost_f64, schur_point_pass_f32, schur_camera_pass_f32,
+ * schur_point_pass_f64, schur_camera_pass_f64, schur_assemble, dense_potrf. */
+int gba_solver_profile(gba_solver* s, int enable);
+int gba_solver_kernel_stats(gba_solver* s, const char* name, long long* out_launches, double* out_total_ms);
+int gba_solver_profile_reset(gba_solver* s);
+
+/* Number of kernels this library has launched in the process so far. */
+unsigned long long gba_launch_count(void);
+
+/* ------------------------------------------------------------ learned preconditioner
+ * No reference counterpart (the reference has no iterative solver). The MLP
+ * maps per-camera features of the damped diagonal block S_cc (49, padded to
+ * 64 floats) to 45 outputs (padded to 48) that correct the block's Cholesky
+ * factor; see gpu-bundle-adjustment_gb300/csrc/mlp.hpp for the layout. */
+
+/* Plain form: also keep the damped diagonal blocks S_cc (GBA_BUF_SDIAG) at each
+ * gba_solver_schur_dense (training-data harvest). */
+int gba_solver_set_harvest(gba_solver* s, int enable);
+/* Features of the current S_cc blocks at damping lambda. [device] feat (C x 64 float). */
+int gba_solver_features(gba_solver* s, double lambda, float* feat);
+
+typedef struct gba_mlp gba_mlp;
+long long gba_mlp_num_params(void);
+/* New network (He-initialised hidden layers, zero output layer = plain block-Jacobi). */
+int gba_mlp_create(uint64_t seed, int batch_capacity, gba_mlp** out);
+int gba_mlp_load(const char* path, int batch_capacity, gba_mlp** out);
+int gba_mlp_save(const gba_mlp* m, const char* path);
+void gba_mlp_destroy(gba_mlp* m);
+/* FP32 master parameters / last gradients, flat (gba_mlp_num_params floats). [host] */
+int gba_mlp_get_params(const gba_mlp* m, float* params);
+int gba_mlp_set_params(gba_mlp* m, const float* params);
+int gba_mlp_get_grads(const gba_mlp* m, float* grads);
+/* out (B x 48) = network(feat (B x 64)). [device] */
+int gba_mlp_forward(gba_mlp* m, const float* feat, int batch, float* out, void* stream);
+/* Forward + per-camera loss + backward on a batch. [device] feat (B x 64 float),
+ * Shat / Lhat (B x 45 double, packed lower: Jacobi-scaled S_cc and its Cholesky
+ * factor), g / x (B x 9 double: scaled right-hand side and exact step).
+ * out_loss: mean loss; out_baseline: mean loss of plain block-Jacobi. */
+int gba_mlp_loss_grad(gba_mlp* m, const float* feat, const double* Shat, const double* Lhat, const double* g,
+                      const double* x, int batch, void* stream, double* out_loss, double* out_baseline);
+/* One Adam step with the gradients of the last gba_mlp_loss_grad. */
+int gba_mlp_adam_step(gba_mlp* m, float lr, float beta1, float beta2, float eps, void* stream);
 
 enum {
     GBA_BUF_U = 0,        /* double[81 C]  full symmetric 9x9 per camera */

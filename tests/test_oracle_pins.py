@@ -187,3 +187,61 @@ def test_oracle_lm_converges_on_small_problem(gba, oracle):
     # noise is N(0,1) px: the optimum is near E px^2 / 2 per observation
     assert res["final_cost"] < 0.75 * prob.num_observations
     assert abs(res["initial_cost"] - gba.total_squared_error(prob) / 2) <= 1e-9 * res["initial_cost"]
+
+
+def _block_sample(rng, mlp_oracle):
+    M = rng.normal(size=(9, 9))
+    S = M @ M.T + 9 * np.eye(9)
+    S *= np.outer(np.logspace(0, 3, 9), np.logspace(0, 3, 9))  # badly scaled like camera blocks
+    g = rng.normal(size=9)
+    x = np.linalg.solve(S, g) * (1 + 0.3 * rng.normal(size=9))
+    return mlp_oracle.scaled_sample(S, g, x)
+
+
+def test_mlp_oracle_loss_gradient_vs_finite_differences():
+    """The analytic (rank-2) gradient of the block step-error loss that the GPU
+    loss kernel implements, against central differences."""
+    import mlp_oracle
+
+    rng = np.random.default_rng(11)
+    for _ in range(5):
+        Sh, Lh, gh, xh = _block_sample(rng, mlp_oracle)
+        o = rng.normal(0, 0.4, 45)
+        an = mlp_oracle.sample_loss_grad(o, Sh, Lh, gh, xh)
+        fd = np.zeros(45)
+        for k in range(45):
+            e = np.zeros(45)
+            e[k] = 1e-6
+            fd[k] = (mlp_oracle.sample_loss(o + e, Sh, Lh, gh, xh) - mlp_oracle.sample_loss(o - e, Sh, Lh, gh, xh)) / 2e-6
+        assert np.max(np.abs(an - fd)) < 1e-6 * max(1.0, np.max(np.abs(fd)))
+
+
+def test_mlp_oracle_backward_vs_finite_differences():
+    import mlp_oracle
+
+    rng = np.random.default_rng(12)
+    B = 3
+    samples = [_block_sample(rng, mlp_oracle) for _ in range(B)]
+    S, L, g, x = (np.array([s[i] for s in samples]) for i in range(4))
+    feat = np.zeros((B, 64))
+    feat[:, :49] = rng.normal(0, 0.5, (B, 49))
+    p = mlp_oracle.unpack(np.zeros(mlp_oracle.N_PARAMS))
+    p["W1"][:, :49] = rng.normal(0, 0.3, (128, 49))
+    p["b1"][:] = 0.05
+    p["W2"][:] = rng.normal(0, 0.1, (128, 128))
+    p["W3"][:45] = rng.normal(0, 0.05, (45, 128))
+    flat = mlp_oracle.pack(p)
+    _, _, grad = mlp_oracle.loss_and_grads(flat, feat, S, L, g, x, emulate_bf16=False)
+
+    def loss_at(v):
+        o, _ = mlp_oracle.forward(v, feat, emulate_bf16=False)
+        return np.mean([mlp_oracle.sample_loss(o[b, :45], S[b], L[b], g[b], x[b]) for b in range(B)])
+
+    sizes = np.cumsum([0] + [int(np.prod(s)) for _, s in mlp_oracle.SIZES])
+    idx = [sizes[0] + 5, sizes[1] + 3, sizes[2] + 700, sizes[3] + 9, sizes[4] + 129, sizes[5] + 2]
+    for i in idx:
+        e = np.zeros_like(flat)
+        e[i] = 1e-5
+        fd = (loss_at(flat + e) - loss_at(flat - e)) / 2e-5
+        # the forward stores activations in FP32, so differences resolve ~1e-7
+        assert abs(fd - grad[i]) < 1e-4 * max(1.0, abs(fd)) + 1e-6, (i, fd, grad[i])
