@@ -31,6 +31,7 @@ LIB_SOURCES = [
     "dense.cu",
     "pcg.cu",
     "mlp.cu",
+    "noalloc.cu",
     "lm.cpp",
     "capi.cpp",
     "bal_io.cpp",

@@ -14,6 +14,7 @@
 #include "gba/lm.hpp"
 #include "lm_internal.hpp"
 #include "mlp.hpp"
+#include "noalloc.hpp"
 #include "solver.hpp"
 #include "synthetic.hpp"
 
@@ -568,6 +569,16 @@ int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info,
         need(L && b && info, "null argument");
         need(n > 0 && n % 64 == 0 && lda >= n, "n must be a positive multiple of 64 and lda >= n");
         gba::dense_potrs(L, n, lda, b, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_cost_noalloc(const double* cams, const double* pts, const int* oc, const int* op, const double* px, int E,
+                     double* out_sse, unsigned long long* out_nonfinite, void* stream) {
+    return guarded([&] {
+        need(out_sse != nullptr, "null out_sse");
+        need(E >= 0, "negative observation count");
+        need(E == 0 || (cams && pts && oc && op && px), "null argument");
+        gba::cost_noalloc(cams, pts, oc, op, px, E, out_sse, out_nonfinite, static_cast<cudaStream_t>(stream));
     });
 }
 

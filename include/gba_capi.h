@@ -258,6 +258,25 @@ int gba_dense_potrf(double* A, int n, int lda, int* info, void* stream);
 /* Solves L L^T x = b in place after gba_dense_potrf (reference src/lm.cu:604). [device] */
 int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info, void* stream);
 
+/* FP64 reprojection cost that allocates no device memory (no counterpart in the
+ * reference). For callers that cannot let a library allocate: host frameworks
+ * that own the device-memory budget through their own pool, or per-frame loops
+ * that must not call cudaMalloc / cudaFree because those calls synchronise the
+ * device. Computes the sum of squared Snavely residuals of num_observations
+ * observations (the same FP64 function as the solver's trial-cost kernel) and
+ * the number of non-finite residuals. [device] cameras (9C), points (3P),
+ * obs_camera, obs_point (E), obs_pixel (2E) in; out_sse (1 double) and
+ * out_nonfinite (1 unsigned long long, may be NULL) out.
+ * Limit: num_observations <= 67,108,864 (GBA_ERR_INVALID above). Partial sums
+ * go to a fixed 512 KiB file-scope device array that every device loading the
+ * library holds until exit; all calls share it (each call writes every slot it
+ * reads), so calls that overlap on the GPU race and must be serialised by the
+ * caller. The first call on a device looks up that array's device address;
+ * make that first call before any stream capture. */
+int gba_cost_noalloc(const double* cameras, const double* points, const int* obs_camera, const int* obs_point,
+                     const double* obs_pixel, int num_observations, double* out_sse,
+                     unsigned long long* out_nonfinite, void* stream);
+
 /* Residual + analytic Jacobian of E observations on the device, FP64 or FP32
  * (precision 64 / 32). [device] cams (9C), pts (3P), obs_camera, obs_point,
  * obs_pixel (2E) in; r (2E), Jc (18E, may be NULL), Jp (6E, may be NULL) out,
