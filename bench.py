@@ -246,6 +246,9 @@ def run_ours(args):
         "result": {"final_cost": final.final_cost, "iterations": final.iterations, "termination": final.termination,
                    "time_to_target_s": final.time_to_target_s, "pcg_iterations": final.pcg_iterations,
                    "trials": final.trials, "anomalies": final.anomalies,
+                   "learned_choice": {0: None, 1: "learned", 2: "block-Jacobi"}[final.learned_choice],
+                   "judged_first_solve_pcg_iterations": {"block_jacobi": final.judge_iters[0],
+                                                         "learned": final.judge_iters[1]},
                    "rel_err_vs_fp64_reference": (final.final_cost - ref) / ref if ref else None},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

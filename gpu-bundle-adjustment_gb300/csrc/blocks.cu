@@ -17,8 +17,9 @@ namespace {
 constexpr int kTB = 256;
 
 // V' = V + lambda * max(diag V, 1e-12) on the diagonal; Vinv = V'^-1 (packed).
+// Vinv32 (may be null): FP32 copy for the mixed form's FP32 Schur matvec.
 __global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __restrict__ V, double lambda, int P,
-                                                           double* __restrict__ Vinv,
+                                                           double* __restrict__ Vinv, float* __restrict__ Vinv32,
                                                            unsigned long long* __restrict__ nonspd) {
     __shared__ unsigned long long redu[kTB / 32];
     unsigned long long bad = 0;
@@ -37,6 +38,12 @@ __global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __rest
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) Vinv[6ll * p + k] = inv[k];
+        if (Vinv32) {
+            float2* o = reinterpret_cast<float2*>(Vinv32 + 6ll * p);
+            o[0] = make_float2(static_cast<float>(inv[0]), static_cast<float>(inv[1]));
+            o[1] = make_float2(static_cast<float>(inv[2]), static_cast<float>(inv[3]));
+            o[2] = make_float2(static_cast<float>(inv[4]), static_cast<float>(inv[5]));
+        }
     }
     const unsigned long long nb = block_sum_u64<kTB>(bad, redu);
     if (threadIdx.x == 0 && nb) atomicAdd(nonspd, nb);
@@ -76,91 +83,109 @@ __global__ void batch_inverse3_kernel(const double* __restrict__ A, double* __re
     }
 }
 
-// Point back-substitution, FP64 W records (plain form):
+// Point back-substitution, one CTA per point chunk (slots sorted by point):
 //   dp_p = V'^-1_p (bp_p - sum_{e in p} W_e^T dc_{c(e)}),  tpts = pts + dp,
-// and the point part of the gain denominator sum dp (lambda d dp + bp).
-__global__ void __launch_bounds__(kTB) backsub_points_w64(
-    const int* __restrict__ pt_off, const int* __restrict__ s_cam, const double* __restrict__ W,
-    const double* __restrict__ dc, const double* __restrict__ V, const double* __restrict__ Vinv,
-    const double* __restrict__ bp, const double* __restrict__ pts, double lambda, int P, double* __restrict__ dp,
+// and the chunk's part of the gain denominator sum dp (lambda d dp + bp).
+// Plain form: W_e^T dc in FP64 from the W records. Mixed form: Jp^T (Jc dc)
+// in FP32 from the Jacobian records and an FP32 copy of dc, summed per point
+// in FP64 (FP64 V'^-1 and denominator).
+template <bool kMixed>
+__global__ void __launch_bounds__(kTB) backsub_chunk_kernel(
+    const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
+    const double* __restrict__ W, const float* __restrict__ J32, const double* __restrict__ dc,
+    const float* __restrict__ dc32, const double* __restrict__ V, const double* __restrict__ Vinv,
+    const double* __restrict__ bp, const double* __restrict__ pts, double lambda, double* __restrict__ dp,
     double* __restrict__ tpts, double* __restrict__ part) {
+    __shared__ double contrib[3][kTB];
     __shared__ double red[kTB / 32];
-    double den = 0.0;
-    const int p = blockIdx.x * kTB + threadIdx.x;
-    if (p < P) {
-        double m0 = bp[3ll * p], m1 = bp[3ll * p + 1], m2 = bp[3ll * p + 2];
-        const double b0 = m0, b1 = m1, b2 = m2;
-        for (int s = pt_off[p]; s < pt_off[p + 1]; ++s) {
-            const double* We = W + 27ll * s;
-            const double* d = dc + 9ll * s_cam[s];
+    const int chunk = blockIdx.x;
+    const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
+    const int s0 = pt_off[p0], s1 = pt_off[p1];
+    const int my_p = p0 + threadIdx.x;
+    int my_b = 0, my_e = 0;
+    if (my_p < p1) {
+        my_b = pt_off[my_p];
+        my_e = pt_off[my_p + 1];
+    }
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int base = s0; base < s1; base += kTB) {
+        const int s = base + threadIdx.x;
+        double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+        if (s < s1) {
+            const int c = s_cam[s];
+            if (kMixed) {
+                const float4* q = reinterpret_cast<const float4*>(J32 + 24ll * s);
+                float J[24];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                const double di = d[i];
-                m0 -= We[3 * i] * di;
-                m1 -= We[3 * i + 1] * di;
-                m2 -= We[3 * i + 2] * di;
+                for (int k = 0; k < 6; ++k) {
+                    const float4 t = q[k];
+                    J[4 * k] = t.x;
+                    J[4 * k + 1] = t.y;
+                    J[4 * k + 2] = t.z;
+                    J[4 * k + 3] = t.w;
+                }
+                const float* d = dc32 + 9ll * c;
+                float t0 = 0.f, t1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    t0 += J[k] * d[k];
+                    t1 += J[9 + k] * d[k];
+                }
+                v0 = static_cast<double>(J[18] * t0 + J[21] * t1);
+                v1 = static_cast<double>(J[19] * t0 + J[22] * t1);
+                v2 = static_cast<double>(J[20] * t0 + J[23] * t1);
+            } else {
+                const double* We = W + 27ll * s;
+                const double* d = dc + 9ll * c;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) {
+                    const double di = d[i];
+                    v0 += We[3 * i] * di;
+                    v1 += We[3 * i + 1] * di;
+                    v2 += We[3 * i + 2] * di;
+                }
             }
         }
-        const double* Vi = Vinv + 6ll * p;  // packed (00,10,11,20,21,22)
+        contrib[0][threadIdx.x] = v0;
+        contrib[1][threadIdx.x] = v1;
+        contrib[2][threadIdx.x] = v2;
+        __syncthreads();
+        if (my_p < p1) {
+            const int b = max(my_b, base), e = min(my_e, base + kTB);
+            for (int t = b; t < e; ++t) {
+                a0 += contrib[0][t - base];
+                a1 += contrib[1][t - base];
+                a2 += contrib[2][t - base];
+            }
+        }
+        __syncthreads();
+    }
+    double den = 0.0;
+    if (my_p < p1) {
+        const long long p = my_p;
+        const double b0 = bp[3 * p], b1 = bp[3 * p + 1], b2 = bp[3 * p + 2];
+        const double m0 = b0 - a0, m1 = b1 - a1, m2 = b2 - a2;
+        const double* Vi = Vinv + 6 * p;  // packed (00,10,11,20,21,22)
         const double d0 = Vi[0] * m0 + Vi[1] * m1 + Vi[3] * m2;
         const double d1 = Vi[1] * m0 + Vi[2] * m1 + Vi[4] * m2;
         const double d2 = Vi[3] * m0 + Vi[4] * m1 + Vi[5] * m2;
-        dp[3ll * p] = d0;
-        dp[3ll * p + 1] = d1;
-        dp[3ll * p + 2] = d2;
-        tpts[3ll * p] = pts[3ll * p] + d0;
-        tpts[3ll * p + 1] = pts[3ll * p + 1] + d1;
-        tpts[3ll * p + 2] = pts[3ll * p + 2] + d2;
-        const double v0 = V[6ll * p], v1 = V[6ll * p + 2], v2 = V[6ll * p + 5];
+        dp[3 * p] = d0;
+        dp[3 * p + 1] = d1;
+        dp[3 * p + 2] = d2;
+        tpts[3 * p] = pts[3 * p] + d0;
+        tpts[3 * p + 1] = pts[3 * p + 1] + d1;
+        tpts[3 * p + 2] = pts[3 * p + 2] + d2;
+        const double v0 = V[6 * p], v1 = V[6 * p + 2], v2 = V[6 * p + 5];
         den = d0 * (lambda * (v0 > 0.0 ? v0 : 1e-12) * d0 + b0) + d1 * (lambda * (v1 > 0.0 ? v1 : 1e-12) * d1 + b1) +
               d2 * (lambda * (v2 > 0.0 ? v2 : 1e-12) * d2 + b2);
     }
     const double t = block_sum<kTB>(den, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    if (threadIdx.x == 0) part[chunk] = t;
 }
 
-// Same, from the FP32 Jacobian records of the mixed form (FP64 arithmetic):
-// W_e^T dc = Jp^T (Jc dc).
-__global__ void __launch_bounds__(kTB) backsub_points_j32(
-    const int* __restrict__ pt_off, const int* __restrict__ s_cam, const float* __restrict__ J32,
-    const double* __restrict__ dc, const double* __restrict__ V, const double* __restrict__ Vinv,
-    const double* __restrict__ bp, const double* __restrict__ pts, double lambda, int P, double* __restrict__ dp,
-    double* __restrict__ tpts, double* __restrict__ part) {
-    __shared__ double red[kTB / 32];
-    double den = 0.0;
-    const int p = blockIdx.x * kTB + threadIdx.x;
-    if (p < P) {
-        double m0 = bp[3ll * p], m1 = bp[3ll * p + 1], m2 = bp[3ll * p + 2];
-        const double b0 = m0, b1 = m1, b2 = m2;
-        for (int s = pt_off[p]; s < pt_off[p + 1]; ++s) {
-            const float* J = J32 + 24ll * s;
-            const double* d = dc + 9ll * s_cam[s];
-            double y0 = 0.0, y1 = 0.0;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                y0 += static_cast<double>(J[i]) * d[i];
-                y1 += static_cast<double>(J[9 + i]) * d[i];
-            }
-            m0 -= static_cast<double>(J[18]) * y0 + static_cast<double>(J[21]) * y1;
-            m1 -= static_cast<double>(J[19]) * y0 + static_cast<double>(J[22]) * y1;
-            m2 -= static_cast<double>(J[20]) * y0 + static_cast<double>(J[23]) * y1;
-        }
-        const double* Vi = Vinv + 6ll * p;
-        const double d0 = Vi[0] * m0 + Vi[1] * m1 + Vi[3] * m2;
-        const double d1 = Vi[1] * m0 + Vi[2] * m1 + Vi[4] * m2;
-        const double d2 = Vi[3] * m0 + Vi[4] * m1 + Vi[5] * m2;
-        dp[3ll * p] = d0;
-        dp[3ll * p + 1] = d1;
-        dp[3ll * p + 2] = d2;
-        tpts[3ll * p] = pts[3ll * p] + d0;
-        tpts[3ll * p + 1] = pts[3ll * p + 1] + d1;
-        tpts[3ll * p + 2] = pts[3ll * p + 2] + d2;
-        const double v0 = V[6ll * p], v1 = V[6ll * p + 2], v2 = V[6ll * p + 5];
-        den = d0 * (lambda * (v0 > 0.0 ? v0 : 1e-12) * d0 + b0) + d1 * (lambda * (v1 > 0.0 ? v1 : 1e-12) * d1 + b1) +
-              d2 * (lambda * (v2 > 0.0 ? v2 : 1e-12) * d2 + b2);
-    }
-    const double t = block_sum<kTB>(den, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
+__global__ void to_f32_kernel(const double* __restrict__ a, int n, float* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = static_cast<float>(a[i]);
 }
 
 // Camera part of the denominator and the trial cameras (tcams = cams + dc).
@@ -200,7 +225,8 @@ __global__ void __launch_bounds__(256) denom_finalize(const double* __restrict__
 unsigned long long Solver::damp_invert_v(double lambda) {
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get() + 3, 0, sizeof(unsigned long long), stream_));
     const int grid = std::min(ceil_div(P_, kTB), 8 * device_sm_count());
-    damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), counters_.get() + 3);
+    damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), Vinv32_.get(),
+                                                    counters_.get() + 3);
     GBA_LAUNCH_CHECK();
     unsigned long long bad = 0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&bad, counters_.get() + 3, sizeof bad, cudaMemcpyDeviceToHost, stream_));
@@ -218,21 +244,27 @@ unsigned long long Solver::damp_invert_v(double lambda) {
 }
 
 double Solver::back_substitute(double lambda) {
-    const int ncam = ceil_div(9ll * C_, kTB), npt = ceil_div(P_, kTB);
+    const int ncam = ceil_div(9ll * C_, kTB);
     double* part = red_part_.get();
     camera_step_kernel<<<ncam, kTB, 0, stream_>>>(dc_.get(), U_.get(), bc_.get(), cams_.get(), lambda, C_,
                                                   tcams_.get(), part);
     GBA_LAUNCH_CHECK();
-    if (form_ == SolverForm::Plain)
-        backsub_points_w64<<<npt, kTB, 0, stream_>>>(pt_off_.get(), s_cam_.get(), W_.get(), dc_.get(), V_.get(),
-                                                     Vinv_.get(), bp_.get(), pts_.get(), lambda, P_, dp_.get(),
-                                                     tpts_.get(), part + ncam);
-    else
-        backsub_points_j32<<<npt, kTB, 0, stream_>>>(pt_off_.get(), s_cam_.get(), J32_.get(), dc_.get(), V_.get(),
-                                                     Vinv_.get(), bp_.get(), pts_.get(), lambda, P_, dp_.get(),
-                                                     tpts_.get(), part + ncam);
+    cudaEvent_t ev = prof_start();
+    if (form_ == SolverForm::Plain) {
+        backsub_chunk_kernel<false><<<n_pchunk_, kTB, 0, stream_>>>(
+            pchunk_.get(), pt_off_.get(), s_cam_.get(), W_.get(), nullptr, dc_.get(), nullptr, V_.get(), Vinv_.get(),
+            bp_.get(), pts_.get(), lambda, dp_.get(), tpts_.get(), part + ncam);
+    } else {
+        float* dc32 = pcg_p32_.get();  // free during back-substitution
+        to_f32_kernel<<<ceil_div(9ll * C_, 256), 256, 0, stream_>>>(dc_.get(), 9 * C_, dc32);
+        GBA_LAUNCH_CHECK();
+        backsub_chunk_kernel<true><<<n_pchunk_, kTB, 0, stream_>>>(
+            pchunk_.get(), pt_off_.get(), s_cam_.get(), nullptr, J32_.get(), dc_.get(), dc32, V_.get(), Vinv_.get(),
+            bp_.get(), pts_.get(), lambda, dp_.get(), tpts_.get(), part + ncam);
+    }
     GBA_LAUNCH_CHECK();
-    denom_finalize<<<1, 256, 0, stream_>>>(part, ncam, npt, scal_.get() + 2);
+    prof_stop("backsub", ev);
+    denom_finalize<<<1, 256, 0, stream_>>>(part, ncam, n_pchunk_, scal_.get() + 2);
     GBA_LAUNCH_CHECK();
     double denom = 0.0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&denom, scal_.get() + 2, sizeof denom, cudaMemcpyDeviceToHost, stream_));

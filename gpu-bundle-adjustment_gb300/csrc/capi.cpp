@@ -101,6 +101,9 @@ void fill_result(const gba::LMResult& r, gba_lm_result* out) {
     out->t_schur = r.t_schur;
     out->t_backsub = r.t_backsub;
     out->t_cost = r.t_cost;
+    out->learned_choice = r.learned_choice;
+    out->judge_iters_block_jacobi = r.judge_iters_block_jacobi;
+    out->judge_iters_learned = r.judge_iters_learned;
     out->trajectory_len = static_cast<int>(r.trajectory.size());
     const int n = std::min<int>(out->trajectory_len, std::max(0, out->trajectory_capacity));
     for (int i = 0; i < n; ++i) {

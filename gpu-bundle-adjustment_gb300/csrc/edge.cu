@@ -184,8 +184,9 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
     const int* __restrict__ s_pt, const double2* __restrict__ s_px, const double* __restrict__ cams,
-    const double* __restrict__ pts, const float2* __restrict__ r_cur, float* __restrict__ J32,
-    double* __restrict__ V, double* __restrict__ bp, unsigned long long* __restrict__ counters) {
+    const double* __restrict__ pts, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
+    float* __restrict__ J32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
+    unsigned long long* __restrict__ counters) {
     __shared__ float contrib[9][kPT];
     __shared__ unsigned long long redu[kPT / 32];
     const int chunk = blockIdx.x;
@@ -222,9 +223,13 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             r[1] = rf.y;
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
             float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
+            float4* outc = reinterpret_cast<float4*>(J32c + 20ll * cam_pos[s]);  // camera-major Jc copy
             if (fin) {
 #pragma unroll
                 for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) outc[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+                outc[4] = make_float4(J[16], J[17], 0.f, 0.f);
                 const float* Jp = J + 18;
                 v[0] = Jp[0] * Jp[0] + Jp[3] * Jp[3];
                 v[1] = Jp[1] * Jp[0] + Jp[4] * Jp[3];
@@ -238,6 +243,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
                 ++anom;
 #pragma unroll
                 for (int q = 0; q < 6; ++q) out[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) outc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
 #pragma unroll
@@ -338,11 +345,55 @@ __global__ void __launch_bounds__(256) ordered_sum(const double* __restrict__ pa
     if (threadIdx.x == 0) *out = t;
 }
 
+// Per-camera FP64 rotation matrix (Rodrigues, or I + [a]x on the first-order
+// branch, the same model as model::residual), translation and intrinsics:
+// 15 doubles per camera, so the cost kernel evaluates R X + t per observation
+// instead of a sin / cos / sqrt per observation on GB300's narrow FP64 pipe.
+constexpr int kCamPre = 16;
+__global__ void camera_precompute_kernel(const double* __restrict__ cams, int C, double* __restrict__ pre) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const double* a = cams + 9ll * c;
+    double* o = pre + static_cast<long long>(kCamPre) * c;
+    const double th2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    if (th2 > 1e-24) {
+        const double th = sqrt(th2);
+        const double w0 = a[0] / th, w1 = a[1] / th, w2 = a[2] / th;
+        double s, cth;
+        sincos(th, &s, &cth);
+        const double sh = sin(0.5 * th);
+        const double omc = 2.0 * sh * sh;
+        o[0] = cth + omc * w0 * w0;  o[1] = -s * w2 + omc * w0 * w1;  o[2] = s * w1 + omc * w0 * w2;
+        o[3] = s * w2 + omc * w1 * w0;  o[4] = cth + omc * w1 * w1;  o[5] = -s * w0 + omc * w1 * w2;
+        o[6] = -s * w1 + omc * w2 * w0;  o[7] = s * w0 + omc * w2 * w1;  o[8] = cth + omc * w2 * w2;
+    } else {
+        o[0] = 1.0;  o[1] = -a[2]; o[2] = a[1];
+        o[3] = a[2]; o[4] = 1.0;   o[5] = -a[0];
+        o[6] = -a[1]; o[7] = a[0]; o[8] = 1.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o[9 + i] = a[3 + i];
+    o[15] = 0.0;
+}
+
+__device__ __forceinline__ void residual_pre(const double* __restrict__ pc, const double* X, const double* obs,
+                                             double* r) {
+    const double P0 = pc[0] * X[0] + pc[1] * X[1] + pc[2] * X[2] + pc[9];
+    const double P1 = pc[3] * X[0] + pc[4] * X[1] + pc[5] * X[2] + pc[10];
+    const double P2 = pc[6] * X[0] + pc[7] * X[1] + pc[8] * X[2] + pc[11];
+    const double iz = 1.0 / P2;
+    const double u = -P0 * iz, v = -P1 * iz;
+    const double r2 = u * u + v * v;
+    const double d = 1.0 + r2 * (pc[13] + pc[14] * r2);
+    r[0] = pc[12] * d * u - obs[0];
+    r[1] = pc[12] * d * v - obs[1];
+}
+
 // FP64 SSE of all slots at (cams, pts), one CTA per point chunk. If r_out is
 // set, each slot's residual is also stored (FP32; NaN where not finite).
 __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                const int* __restrict__ s_cam, const int* __restrict__ s_pt,
-                                               const double2* __restrict__ s_px, const double* __restrict__ cams,
+                                               const double2* __restrict__ s_px, const double* __restrict__ pre,
                                                const double* __restrict__ pts, double* __restrict__ sse_part,
                                                unsigned long long* __restrict__ counters, float2* __restrict__ r_out) {
     __shared__ double red[kPT / 32];
@@ -353,15 +404,13 @@ __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, 
     unsigned long long anom = 0;
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int c = s_cam[s], p = s_pt[s];
-        double cam[9], X[3], obs[2], r[2];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) cam[k] = __ldg(cams + 9 * c + k);
+        double X[3], obs[2], r[2];
 #pragma unroll
         for (int k = 0; k < 3; ++k) X[k] = __ldg(pts + 3 * p + k);
         const double2 o = s_px[s];
         obs[0] = o.x;
         obs[1] = o.y;
-        model::residual(cam, X, obs, r);
+        residual_pre(pre + static_cast<long long>(kCamPre) * c, X, obs, r);
         const bool fin = isfinite(r[0]) && isfinite(r[1]);
         if (r_out) r_out[s] = fin ? make_float2(static_cast<float>(r[0]), static_cast<float>(r[1])) : make_float2(NAN, NAN);
         if (!fin) {
@@ -426,8 +475,10 @@ double Solver::accumulate() {
         // (the trial evaluation at these parameters). Its non-finite count goes
         // to a scratch counter: the FP32 pass counts this evaluation's anomalies.
         if (!resid_valid_) {
+            camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(cams_.get(), C_, cam_pre_.get());
+            GBA_LAUNCH_CHECK();
             cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                                     cams_.get(), pts_.get(), sse_part_.get(), counters_.get() + 2,
+                                                     cam_pre_.get(), pts_.get(), sse_part_.get(), counters_.get() + 2,
                                                      reinterpret_cast<float2*>(r_cur_.get()));
             GBA_LAUNCH_CHECK();
             ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
@@ -437,8 +488,8 @@ double Solver::accumulate() {
         const float2* rc = reinterpret_cast<const float2*>(r_cur_.get());
         cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
-                                                       spx, cams_.get(), pts_.get(), rc, J32_.get(), V_.get(),
-                                                       bp_.get(), counters_.get());
+                                                       spx, cams_.get(), pts_.get(), rc, cam_pos_.get(), J32_.get(),
+                                                       J32c_.get(), V_.get(), bp_.get(), counters_.get());
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);
         if (n_cchunk_ > 0) {
@@ -462,8 +513,10 @@ double Solver::accumulate() {
 double Solver::trial_cost() {
     const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
     cudaEvent_t ev = prof_start();
+    camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(tcams_.get(), C_, cam_pre_.get());
+    GBA_LAUNCH_CHECK();
     cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                             tcams_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
+                                             cam_pre_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
                                              reinterpret_cast<float2*>(r_trial_.get()));
     GBA_LAUNCH_CHECK();
     prof_stop("cost_f64", ev);

@@ -44,6 +44,7 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
         return r;
     };
 
+    s.begin_solve();
     double sse = phase(res.t_accumulate, [&] { return s.accumulate(); });
     res.initial_cost = sse / 2.0;
     res.trajectory.push_back(res.initial_cost);
@@ -144,6 +145,9 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
 
     res.final_cost = sse / 2.0;
     res.anomalies = s.anomalies();
+    res.learned_choice = s.learned_choice_;
+    res.judge_iters_block_jacobi = s.judge_iters_[0];
+    res.judge_iters_learned = s.judge_iters_[1];
     res.termination = converged ? "CONVERGENCE" : failed ? "FAILURE" : at_target ? "TARGET_COST" : "MAX_ITERATIONS";
     return res;
 }

@@ -52,12 +52,16 @@ __device__ __forceinline__ void load_j(const float* __restrict__ J32, long long 
     }
 }
 
+// Point pass of the implicit product. xt: the camera vector in the arithmetic
+// type (an FP32 copy inside PCG), Vinv_t: V'^-1 in the arithmetic type (6 per
+// point); u is written at the slot's camera-major position so that the camera
+// pass reads it contiguously.
 template <typename T>
 __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
-                                                       const float* __restrict__ J32,
-                                                       const double* __restrict__ Vinv, const double* __restrict__ bp,
-                                                       const double* __restrict__ x, double a, T* __restrict__ u,
+                                                       const int* __restrict__ cam_pos, const float* __restrict__ J32,
+                                                       const T* __restrict__ Vinv_t, const double* __restrict__ bp,
+                                                       const T* __restrict__ xt, double a, T* __restrict__ u_cm,
                                                        const double* __restrict__ done) {
     __shared__ T contrib[3][kPT];
     __shared__ T wsh[kPT][3];
@@ -72,18 +76,18 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         my_e = pt_off[my_p + 1];
     }
     T z0 = T(0), z1 = T(0), z2 = T(0);
-    if (x) {
+    if (xt) {
         for (int base = s0; base < s1; base += kPT) {
             const int s = base + threadIdx.x;
             T v0 = T(0), v1 = T(0), v2 = T(0);
             if (s < s1) {
                 T J[24];
                 load_j(J32, s, J);
-                const double* xc = x + 9ll * s_cam[s];
+                const T* xc = xt + 9ll * s_cam[s];
                 T t0 = T(0), t1 = T(0);
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
-                    const T xk = static_cast<T>(xc[k]);
+                    const T xk = xc[k];
                     t0 += J[k] * xk;
                     t1 += J[9 + k] * xk;
                 }
@@ -112,30 +116,32 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
             z1 += static_cast<T>(a * bp[3ll * my_p + 1]);
             z2 += static_cast<T>(a * bp[3ll * my_p + 2]);
         }
-        const double* Vi = Vinv + 6ll * my_p;
-        const T v00 = static_cast<T>(Vi[0]), v10 = static_cast<T>(Vi[1]), v11 = static_cast<T>(Vi[2]);
-        const T v20 = static_cast<T>(Vi[3]), v21 = static_cast<T>(Vi[4]), v22 = static_cast<T>(Vi[5]);
+        const T* Vi = Vinv_t + 6ll * my_p;
+        const T v00 = Vi[0], v10 = Vi[1], v11 = Vi[2], v20 = Vi[3], v21 = Vi[4], v22 = Vi[5];
         wsh[threadIdx.x][0] = v00 * z0 + v10 * z1 + v20 * z2;
         wsh[threadIdx.x][1] = v10 * z0 + v11 * z1 + v21 * z2;
         wsh[threadIdx.x][2] = v20 * z0 + v21 * z1 + v22 * z2;
     }
     __syncthreads();
-    // u_e = Jp_e w_p for every slot of the chunk
+    // u_e = Jp_e w_p for every slot of the chunk, stored camera-major
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int p = s_pt[s];
         const T w0 = wsh[p - p0][0], w1 = wsh[p - p0][1], w2 = wsh[p - p0][2];
-        const float* Jp = J32 + 24ll * s + 18;
-        u[2ll * s] = static_cast<T>(Jp[0]) * w0 + static_cast<T>(Jp[1]) * w1 + static_cast<T>(Jp[2]) * w2;
-        u[2ll * s + 1] = static_cast<T>(Jp[3]) * w0 + static_cast<T>(Jp[4]) * w1 + static_cast<T>(Jp[5]) * w2;
+        const float2* Jp2 = reinterpret_cast<const float2*>(J32 + 24ll * s + 18);
+        const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
+        const long long q = cam_pos[s];
+        u_cm[2 * q] = static_cast<T>(j01.x) * w0 + static_cast<T>(j01.y) * w1 + static_cast<T>(j23.x) * w2;
+        u_cm[2 * q + 1] = static_cast<T>(j23.y) * w0 + static_cast<T>(j45.x) * w1 + static_cast<T>(j45.y) * w2;
     }
 }
 
+// Camera pass: partial_c = sum over the chunk's camera-major positions of Jc^T u
+// (Jc from the camera-major copy J32c, 20 floats per position; both contiguous).
 template <typename T>
 __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__ cchunk_begin,
                                                         const int* __restrict__ cchunk_cam,
                                                         const int* __restrict__ cam_off,
-                                                        const int* __restrict__ cam_slots,
-                                                        const float* __restrict__ J32, const T* __restrict__ u,
+                                                        const float* __restrict__ J32c, const T* __restrict__ u_cm,
                                                         double* __restrict__ part, const double* __restrict__ done) {
     __shared__ double wpart[kCT / 32][9];
     if (done && *done != 0.0) return;
@@ -146,8 +152,7 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
 #pragma unroll
     for (int i = 0; i < 9; ++i) acc[i] = T(0);
     for (int i = b + threadIdx.x; i < e; i += kCT) {
-        const long long s = cam_slots[i];
-        const float4* q = reinterpret_cast<const float4*>(J32 + 24 * s);
+        const float4* q = reinterpret_cast<const float4*>(J32c + 20ll * i);
         float Jc[20];
 #pragma unroll
         for (int t = 0; t < 5; ++t) {
@@ -157,15 +162,17 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
             Jc[4 * t + 2] = v.z;
             Jc[4 * t + 3] = v.w;
         }
-        const T u0 = u[2 * s], u1 = u[2 * s + 1];
+        const T u0 = u_cm[2ll * i], u1 = u_cm[2ll * i + 1];
 #pragma unroll
         for (int t = 0; t < 9; ++t) acc[t] += static_cast<T>(Jc[t]) * u0 + static_cast<T>(Jc[9 + t]) * u1;
     }
+    // Warp sums in the arithmetic type (FP32 shuffles stay off GB300's narrow
+    // FP64 pipe); the four warp partials are added in FP64.
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
-        const double v = warp_sum(static_cast<double>(acc[t]));
-        if (lane == 0) wpart[warp][t] = v;
+        const T v = warp_sum(acc[t]);
+        if (lane == 0) wpart[warp][t] = static_cast<double>(v);
     }
     __syncthreads();
     if (threadIdx.x < 9) {
@@ -326,16 +333,21 @@ __global__ void __launch_bounds__(256) pcg_beta(const double* __restrict__ red_r
     }
 }
 
-__global__ void __launch_bounds__(kVT) pcg_p_update(double* __restrict__ p, const double* __restrict__ z, int n,
-                                                   const double* __restrict__ sc) {
+__global__ void __launch_bounds__(kVT) pcg_p_update(double* __restrict__ p, float* __restrict__ p32,
+                                                   const double* __restrict__ z, int n, const double* __restrict__ sc) {
     if (sc[S_DONE] != 0.0) return;
     const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < n) p[i] = z[i] + sc[S_BETA] * p[i];
+    if (i < n) {
+        const double v = z[i] + sc[S_BETA] * p[i];
+        p[i] = v;
+        p32[i] = static_cast<float>(v);
+    }
 }
 
 // x = 0, r = b, z = M b, p = z; partials b.b and r.z.
 __global__ void __launch_bounds__(kVT) pcg_init(double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
-                                               double* __restrict__ p, const double* __restrict__ b,
+                                               double* __restrict__ p, float* __restrict__ p32,
+                                               const double* __restrict__ b,
                                                const double* __restrict__ L, int C, double* __restrict__ red_rr,
                                                double* __restrict__ red_rz) {
     __shared__ double sh[kVT / 32];
@@ -355,6 +367,7 @@ __global__ void __launch_bounds__(kVT) pcg_init(double* __restrict__ x, double* 
         for (int k = 0; k < 9; ++k) {
             z[9ll * c + k] = zc[k];
             p[9ll * c + k] = zc[k];
+            p32[9ll * c + k] = static_cast<float>(zc[k]);
             rz += rc[k] * zc[k];
         }
     }
@@ -517,22 +530,25 @@ __global__ void __launch_bounds__(kVT) factor_blocks_kernel(const double* __rest
 
 }  // namespace
 
-// Implicit product y_parts for a given x (FP32 or FP64 arithmetic). x may be
-// null (then a must be 1: the rhs partials). Partials in cam_part_ (9 per chunk).
+// Implicit product partials for a given x (FP32 or FP64 arithmetic). x is in
+// the arithmetic type (FP32: the PCG direction copy; FP64: dc) or null (then
+// a = 1: the right-hand side). Partials in cam_part_ (9 per chunk).
 template <typename T>
-static void implicit_parts(Solver& s, const double* x, double a, const double* done) {
+static void implicit_parts(Solver& s, const T* x, double a, const double* done) {
     T* u = reinterpret_cast<T*>(s.u_.get());
     const bool f32 = sizeof(T) == 4;
+    const T* vinv = f32 ? reinterpret_cast<const T*>(s.Vinv32_.get()) : reinterpret_cast<const T*>(s.Vinv_.get());
     cudaEvent_t ev = s.prof_start();
     schur_point_pass<T><<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
-                                                           s.s_pt_.get(), s.J32_.get(), s.Vinv_.get(), s.bp_.get(), x, a, u, done);
+                                                           s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(), vinv,
+                                                           s.bp_.get(), x, a, u, done);
     GBA_LAUNCH_CHECK();
     s.prof_stop(f32 ? "schur_point_pass_f32" : "schur_point_pass_f64", ev);
     if (s.n_cchunk_ > 0) {
         ev = s.prof_start();
         schur_camera_pass<T><<<s.n_cchunk_, kCT, 0, s.stream_>>>(s.cchunk_begin_.get(), s.cchunk_cam_.get(),
-                                                                 s.cam_off_.get(), s.cam_slots_.get(), s.J32_.get(),
-                                                                 u, s.cam_part_.get(), done);
+                                                                 s.cam_off_.get(), s.J32c_.get(), u,
+                                                                 s.cam_part_.get(), done);
         GBA_LAUNCH_CHECK();
         s.prof_stop(f32 ? "schur_camera_pass_f32" : "schur_camera_pass_f64", ev);
     }
@@ -549,7 +565,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     const double* done = sc + S_DONE;
 
     // right-hand side, FP64 arithmetic
-    implicit_parts<double>(*this, nullptr, 1.0, nullptr);
+    implicit_parts<double>(*this, static_cast<const double*>(nullptr), 1.0, nullptr);
     rhs_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), bc_.get(), C_, rhs_.get(), red);
     GBA_LAUNCH_CHECK();
     sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
@@ -565,10 +581,9 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     sdiag_finalize<<<ncb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
                                              Sdiag_.get(), Pfac_.get());
     GBA_LAUNCH_CHECK();
-    if (learned) {
-        if (!model_) throw std::invalid_argument("learned form: no model loaded");
-        model_->correct_factors(*this, lambda);
-    }
+    if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
+    // Learned factors are used once they have won the judged solve (below).
+    if (learned && learned_choice_ == 1) model_->correct_factors(*this, lambda);
 
     double bnorm2 = 0.0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&bnorm2, sc + S_NORM, sizeof(double), cudaMemcpyDeviceToHost, stream_));
@@ -588,14 +603,15 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_). Returns the
     // iteration count; *ok = reached the inner tolerance without breakdown.
     auto inner_pcg = [&](bool* ok) -> long long {
-        pcg_init<<<ncb, kVT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), ref_r_.get(),
+        pcg_init<<<ncb, kVT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
+                                           ref_r_.get(),
                                            Pfac_.get(), C_, red, red2);
         GBA_LAUNCH_CHECK();
         pcg_init_finalize<<<1, 256, 0, stream_>>>(red, red2, ncb, opts.pcg_tol, sc);
         GBA_LAUNCH_CHECK();
         for (int it = 0; it < opts.pcg_max_iters; it += kCheck) {
             for (int j = 0; j < kCheck; ++j) {
-                implicit_parts<float>(*this, pcg_p_.get(), 0.0, done);
+                implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
                 pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
                                                          pcg_p_.get(), C_, pcg_q_.get(), red, sc);
                 GBA_LAUNCH_CHECK();
@@ -606,7 +622,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
                 GBA_LAUNCH_CHECK();
                 pcg_beta<<<1, 256, 0, stream_>>>(red, red2, ncb, opts.pcg_max_iters, sc);
                 GBA_LAUNCH_CHECK();
-                pcg_p_update<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_z_.get(), n, sc);
+                pcg_p_update<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_p32_.get(), pcg_z_.get(), n, sc);
                 GBA_LAUNCH_CHECK();
             }
             double flag = 0.0;
@@ -620,10 +636,42 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
         *ok = h[S_DONE] != 2.0 && h[S_RR] <= h[S_TOL2] * h[S_BB];
         return static_cast<long long>(h[S_ITERS]);
     };
-    bool use_learned = learned;
+    bool use_learned = learned && learned_choice_ == 1;
     for (int step = 0; step < opts.refine_max_steps && rnorm2 > tol2; ++step) {
         bool ok = false;
-        long long it_count = inner_pcg(&ok);
+        long long it_count = 0;
+        if (learned && learned_choice_ == 0) {
+            // Block-Jacobi judges the learned factors on the first inner solve of
+            // the LM solve: both preconditioners solve it, and the one that
+            // reaches the inner tolerance in fewer iterations serves for the rest
+            // of the solve. Both solves count in pcg_iterations.
+            bool ok_bj = false, ok_l = false;
+            const long long it_bj = inner_pcg(&ok_bj);
+            GBA_CUDA_CHECK(cudaMemcpyAsync(judge_x_.get(), pcg_x_.get(), n * sizeof(double),
+                                           cudaMemcpyDeviceToDevice, stream_));
+            model_->correct_factors(*this, lambda);
+            const long long it_l = inner_pcg(&ok_l);
+            judge_iters_[0] = it_bj;
+            judge_iters_[1] = it_l;
+            if (ok_l && (!ok_bj || it_l < it_bj)) {
+                learned_choice_ = 1;
+                use_learned = true;
+                st.pcg_iterations += it_bj;
+                it_count = it_l;
+                ok = ok_l;
+            } else {
+                learned_choice_ = 2;
+                GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
+                                               cudaMemcpyDeviceToDevice, stream_));
+                factor_blocks_kernel<<<ncb, kVT, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+                GBA_LAUNCH_CHECK();
+                st.pcg_iterations += it_l;
+                it_count = it_bj;
+                ok = ok_bj;
+            }
+        } else {
+            it_count = inner_pcg(&ok);
+        }
         if (use_learned && !ok) {
             // Block-Jacobi judges the learned factors: an inner solve that breaks
             // down or misses its tolerance is redone with the plain blocks, which
@@ -639,7 +687,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
         // dc += e; FP64 residual r = rhs - S64 dc
         axpy_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_x_.get(), n);
         GBA_LAUNCH_CHECK();
-        implicit_parts<double>(*this, dc_.get(), 0.0, nullptr);
+        implicit_parts<double>(*this, static_cast<const double*>(dc_.get()), 0.0, nullptr);
         residual_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
                                                     dc_.get(), rhs_.get(), C_, ref_r_.get(), red);
         GBA_LAUNCH_CHECK();

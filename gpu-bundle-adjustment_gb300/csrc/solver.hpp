@@ -149,6 +149,11 @@ public:
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
     DevBuf<float> J32_;
+    DevBuf<float> J32c_;    // mixed: Jc (18 + 2 pad) per slot in camera-major position (camera pass input)
+    DevBuf<float> Vinv32_;  // mixed: FP32 copy of V'^-1 (6 per point) for the FP32 matvec
+    DevBuf<float> pcg_p32_; // mixed: FP32 copy of the PCG direction for the FP32 matvec
+    DevBuf<int> cam_pos_;   // camera-major position of each slot (inverse of cam_slots_)
+    DevBuf<double> cam_pre_;  // per-camera rotation matrix, translation, intrinsics (16 per camera)
     DevBuf<float> r_cur_, r_trial_;  // mixed: FP64-evaluated residuals (FP32) at current / trial parameters
     bool resid_valid_ = false;       // r_cur_ and scal_[0] hold the current parameters' residuals / SSE
     DevBuf<double> sse_part_, cam_part_, scal_;  // scal_: [0] sse, [1] trial sse, [2] denom, [3..] scratch
@@ -161,10 +166,15 @@ public:
     DevBuf<int> info_;
     // mixed Schur
     DevBuf<double> Sdiag_, Pfac_;  // S diagonal blocks (81C), preconditioner factors (81C)
-    DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_;
+    DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_, judge_x_;
     DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or FP64)
     DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
     DevBuf<float> mlp_stats_;  // learned form: per-camera track statistics (3 per camera)
+    // Learned form, per solve: 0 = not judged yet, 1 = learned factors won the
+    // first inner solve, 2 = block-Jacobi won (used for the rest of the solve).
+    int learned_choice_ = 0;
+    long long judge_iters_[2] = {0, 0};  // inner PCG iterations of the judged solve: block-Jacobi, learned
+    void begin_solve() { learned_choice_ = 0; }
     bool harvest_ = false;     // plain form: keep the damped diagonal blocks S_cc in Sdiag_
 
     void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px);

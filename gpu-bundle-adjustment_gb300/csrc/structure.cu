@@ -77,6 +77,11 @@ __global__ void gather_obs_kernel(const int* __restrict__ order, const int* __re
     }
 }
 
+// pos[perm[i]] = i
+__global__ void inverse_perm_kernel(const int* __restrict__ perm, int n, int* __restrict__ pos) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[perm[i]] = i;
+}
+
 // offsets[k] = first position i with keys[i] >= k, for k = 0..nk (keys sorted).
 __global__ void csr_offsets_kernel(const int* __restrict__ keys, int n, int nk, int* __restrict__ off) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -176,6 +181,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     tcams_.alloc(9ull * C);
     tpts_.alloc(3ull * P);
     counters_.alloc(4);  // [0] anomalies, [1] non-SPD V blocks, [2] scratch, [3] per-call non-SPD
+    cam_pre_.alloc(16ull * C);
     scal_.alloc(8);
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get(), 0, 4 * sizeof(unsigned long long), stream_));
     set_params(cams, pts);
@@ -197,7 +203,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     dp_.alloc(3ull * P);
     sse_part_.alloc(std::max(n_pchunk_, 1));
     cam_part_.alloc(54ull * std::max(n_cchunk_, 1));
-    red_part_.alloc(ceil_div(P, 256) + 2 * ceil_div(9ll * C, 256) + 64);
+    red_part_.alloc(std::max(n_pchunk_, ceil_div(P, 256)) + 2 * ceil_div(9ll * C, 256) + 64);
     if (form_ == SolverForm::Plain) {
         W_.alloc(27ull * E);
         JcR_.alloc(20ull * E);
@@ -210,6 +216,10 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         build_pairs();
     } else {
         J32_.alloc(24ull * E);
+        J32c_.alloc(20ull * E);
+        judge_x_.alloc(9ull * C);
+        Vinv32_.alloc(6ull * P);
+        pcg_p32_.alloc(9ull * C);
         r_cur_.alloc(2ull * E);
         r_trial_.alloc(2ull * E);
         Sdiag_.alloc(81ull * C);
@@ -288,6 +298,9 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     GBA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tmp.get(), tb, s_cam_.get(), keys_sorted.get(), iota.get(),
                                                    cam_slots_.get(), E, 0, bits_for(C + 1), stream_));
     csr_offsets_kernel<<<grid_for(E), 256, 0, stream_>>>(keys_sorted.get(), E, C, cam_off_.get());
+    GBA_LAUNCH_CHECK();
+    cam_pos_.alloc(E);
+    inverse_perm_kernel<<<grid_for(E), 256, 0, stream_>>>(cam_slots_.get(), E, cam_pos_.get());
     GBA_LAUNCH_CHECK();
 
     // 3. work chunks, built on the host from the CSR offsets

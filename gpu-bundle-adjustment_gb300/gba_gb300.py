@@ -78,6 +78,9 @@ class LMResultC(C.Structure):
         ("trajectory_time_s", _dp),
         ("trajectory_capacity", C.c_int),
         ("trajectory_len", C.c_int),
+        ("learned_choice", C.c_int),
+        ("judge_iters_block_jacobi", C.c_longlong),
+        ("judge_iters_learned", C.c_longlong),
     ]
 
 
@@ -301,6 +304,8 @@ class LMResult:
     phases: dict
     trajectory: list = field(default_factory=list)
     trajectory_time_s: list = field(default_factory=list)
+    learned_choice: int = 0  # learned form: 1 learned, 2 block-Jacobi won the judged first inner solve
+    judge_iters: tuple = (0, 0)  # that solve's inner PCG iterations: (block-Jacobi, learned)
 
 
 def _result_struct(cap: int):
@@ -319,7 +324,8 @@ def _to_result(r, traj, ttime, cap) -> "LMResult":
         r.trials, r.pcg_iterations, r.refine_steps, r.time_to_target_s,
         dict(setup=r.t_setup, accumulate=r.t_accumulate, damp=r.t_damp, schur=r.t_schur, backsub=r.t_backsub,
              cost=r.t_cost),
-        traj[:n].tolist(), ttime[:n].tolist(),
+        traj[:n].tolist(), ttime[:n].tolist(), r.learned_choice,
+        (r.judge_iters_block_jacobi, r.judge_iters_learned),
     )
 
 

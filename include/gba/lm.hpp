@@ -63,6 +63,11 @@ struct LMResult {
     long long pcg_iterations = 0;          // mixed: total inner PCG iterations
     int refine_steps = 0;                  // mixed: total FP64 refinement steps
     double time_to_target_s = -1.0;        // first time cost <= LMOptions::target_cost, or -1
+    // Learned form: which preconditioner won the judged first inner solve
+    // (1 = learned, 2 = block-Jacobi, 0 = not judged) and its inner PCG
+    // iterations with block-Jacobi and with the learned factors.
+    int learned_choice = 0;
+    long long judge_iters_block_jacobi = 0, judge_iters_learned = 0;
     // Phase wall times (device-synchronised): setup, accumulate, damp+V^-1,
     // Schur solve (assembly+factor or PCG), back-substitution, trial cost.
     double t_setup = 0, t_accumulate = 0, t_damp = 0, t_schur = 0, t_backsub = 0, t_cost = 0;

@@ -75,6 +75,9 @@ typedef struct gba_lm_result {
     double* trajectory_time_s;       /* [host] out */
     int trajectory_capacity;
     int trajectory_len;
+    int learned_choice;              /* learned form: 1 learned, 2 block-Jacobi won the judged solve */
+    long long judge_iters_block_jacobi;
+    long long judge_iters_learned;
 } gba_lm_result;
 
 void gba_lm_options_default(gba_lm_options* opts);
