@@ -145,6 +145,10 @@ def run_ours(args):
     target = ref * TARGET_FACTOR if ref else 0.0
     form = args.form
     opts = dict(form=form, max_iterations=args.max_iterations, target_cost=target, stop_at_target=1 if ref else 0)
+    if args.pcg_tol is not None:
+        opts["pcg_tol"] = args.pcg_tol
+    if args.pcg_max_iters is not None:
+        opts["pcg_max_iters"] = args.pcg_max_iters
     if form == "learned":
         opts["model_path"] = str(MODEL)
 
@@ -240,6 +244,7 @@ def run_ours(args):
             "target_cost": target or None,
             "fp64_reference_cost": ref,
             "max_iterations": args.max_iterations,
+            "pcg_tol": opts.get("pcg_tol", "default"),
             "l2": "inputs larger than L2 (no flush)",
             "parallelism": f"replicas x{world}",
         },
@@ -341,6 +346,8 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--form", default="learned", choices=["plain", "mixed", "learned"])
     ap.add_argument("--max-iterations", type=int, default=50)
+    ap.add_argument("--pcg-tol", type=float, default=None, help="inner PCG relative tolerance (library default 1e-2)")
+    ap.add_argument("--pcg-max-iters", type=int, default=None)
     ap.add_argument("--reference-iterations", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -63,13 +63,14 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                                                        const T* __restrict__ Vinv_t, const double* __restrict__ bp,
                                                        const T* __restrict__ xt, double a, T* __restrict__ u_cm,
                                                        const double* __restrict__ done) {
-    __shared__ T contrib[3][kPT];
+    __shared__ T seg[kPT][3];  // warp-segment partial sums, at each segment's last slot
     __shared__ T wsh[kPT][3];
     if (done && *done != 0.0) return;
     const int chunk = blockIdx.x;
     const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
     const int s0 = pt_off[p0], s1 = pt_off[p1];
     const int my_p = p0 + threadIdx.x;
+    const int lane = threadIdx.x & 31;
     int my_b = 0, my_e = 0;
     if (my_p < p1) {
         my_b = pt_off[my_p];
@@ -80,7 +81,9 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         for (int base = s0; base < s1; base += kPT) {
             const int s = base + threadIdx.x;
             T v0 = T(0), v1 = T(0), v2 = T(0);
+            int key = -1;  // point of the slot (slots past the chunk end share key -1, value 0)
             if (s < s1) {
+                key = s_pt[s];
                 T J[24];
                 load_j(J32, s, J);
                 const T* xc = xt + 9ll * s_cam[s];
@@ -95,16 +98,34 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                 v1 = J[19] * t0 + J[22] * t1;
                 v2 = J[20] * t0 + J[23] * t1;
             }
-            contrib[0][threadIdx.x] = v0;
-            contrib[1][threadIdx.x] = v1;
-            contrib[2][threadIdx.x] = v2;
+            // inclusive segmented scan over the warp (slots of a point are contiguous)
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const T u0 = __shfl_up_sync(0xffffffffu, v0, d);
+                const T u1 = __shfl_up_sync(0xffffffffu, v1, d);
+                const T u2 = __shfl_up_sync(0xffffffffu, v2, d);
+                const int kd = __shfl_up_sync(0xffffffffu, key, d);
+                if (lane >= d && kd == key) {
+                    v0 += u0;
+                    v1 += u1;
+                    v2 += u2;
+                }
+            }
+            const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+            if (lane == 31 || knext != key) {
+                seg[threadIdx.x][0] = v0;
+                seg[threadIdx.x][1] = v1;
+                seg[threadIdx.x][2] = v2;
+            }
             __syncthreads();
+            // owner: add the point's warp-segment partials of this pass, warps in order
             if (my_p < p1) {
-                const int b = max(my_b, base), e = min(my_e, base + kPT);
-                for (int t = b; t < e; ++t) {
-                    z0 += contrib[0][t - base];
-                    z1 += contrib[1][t - base];
-                    z2 += contrib[2][t - base];
+                const int b = max(my_b, base) - base, e = min(my_e, base + kPT) - base;
+                for (int w = b >> 5; b < e && w <= (e - 1) >> 5; ++w) {
+                    const int t = min(e - 1, 32 * w + 31);
+                    z0 += seg[t][0];
+                    z1 += seg[t][1];
+                    z2 += seg[t][2];
                 }
             }
             __syncthreads();
