@@ -51,14 +51,29 @@ def _peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def reference_cost(workload: int, seed: int):
-    """FP64 reference final cost of a workload (committed fixture), or None."""
+def reference_entry(workload: int, seed: int):
+    """FP64 reference solve of a workload (committed fixture written by
+    tests/golden/make_workload_reference.py: the plain form on a GB300), or None."""
     f = GOLDEN / "workload_reference.json"
     if not f.exists():
         return None
-    data = json.loads(f.read_text())
-    e = data.get(f"{workload}:{seed}")
+    return json.loads(f.read_text()).get(f"{workload}:{seed}")
+
+
+def reference_cost(workload: int, seed: int):
+    e = reference_entry(workload, seed)
     return None if e is None else e["final_cost"]
+
+
+def plain_reference_summary(workload: int, seed: int):
+    """The plain FP64 form's own time to the same target, from its reference run."""
+    e = reference_entry(workload, seed)
+    if e is None:
+        return None
+    target = e["final_cost"] * TARGET_FACTOR
+    tt = next((t for c, t in zip(e["trajectory"], e["trajectory_time_s"]) if c <= target), None)
+    return {"time_to_target_s": tt, "solve_s": e["solve_seconds"], "iterations": e["iterations"],
+            "trials": e["trials"], "source": "tests/golden/workload_reference.json (plain form on GB300)"}
 
 
 class ClockSampler:
@@ -205,6 +220,13 @@ def run_ours(args):
             roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                         "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
                         "launches": n_launch, "avg_launch_us": per_launch_s * 1e6, "peak_source": peak_src}
+    breakdown = {}
+    for name in ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_f64", "schur_camera_pass_f64",
+                 "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "backsub",
+                 "mlp_forward", "schur_assemble", "dense_potrf"):
+        n_k, ms_k = solver.kernel_stats(name)
+        if n_k:
+            breakdown[name] = {"launches": n_k, "ms_per_step": ms_k / args.steps}
     solver.profile(False)
     final = timed[-1]
 
@@ -243,6 +265,7 @@ def run_ours(args):
             "form": form,
             "target_cost": target or None,
             "fp64_reference_cost": ref,
+            "plain_fp64_form": plain_reference_summary(args.workload, args.seed),
             "max_iterations": args.max_iterations,
             "pcg_tol": opts.get("pcg_tol", "default"),
             "l2": "inputs larger than L2 (no flush)",
@@ -258,6 +281,7 @@ def run_ours(args):
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roofline,
+        "kernel_breakdown": breakdown,
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline and world == 1:

@@ -6,9 +6,12 @@
 //   exit 1 = arguments / IO, 2 = solver initial cost differs from the reader's
 //   cost by more than 1e-9 max(1, |c|), 3 = device anomaly counter non-zero.
 // Additive flags: --synthetic=W (workload 1..5 instead of a file), --seed=S,
-// --form=plain|mixed|learned, --model=PATH, --target-cost=D. Additive JSON keys
-// after the reference's: form, trials, pcg_iterations, time_to_target_s,
-// trajectory.
+// --form=plain|mixed|learned, --model=PATH, --target-cost=D, and the loss flags
+// of the reference's Ceres benchmark (benchmarks/bench_ceres.cpp:10-11,117-131):
+// --loss=none|huber, --delta=D (default 1.0); with Huber the initial-cost gate
+// compares against sum rho(|r|^2) / 2 from the reader's own residual. Additive
+// JSON keys after the reference's: form, trials, pcg_iterations,
+// time_to_target_s, trajectory.
 
 #include <cuda_runtime.h>
 
@@ -36,12 +39,14 @@ struct Args {
     std::string form = "plain";
     std::string model;
     double target_cost = 0.0;
+    std::string loss = "none";
+    double delta = 1.0;
 };
 
 [[noreturn]] void usage_error(const std::string& msg) {
     std::fprintf(stderr, "%s\nusage: bench_bal <problem.txt[.bz2]> [--iterations=N] [--lambda=D] [--json=PATH] "
                          "[--verbose] [--synthetic=1..5 --seed=S] [--form=plain|mixed|learned] [--model=PATH] "
-                         "[--target-cost=D]\n",
+                         "[--target-cost=D] [--loss=none|huber] [--delta=D]\n",
                  msg.c_str());
     std::exit(1);
 }
@@ -64,6 +69,8 @@ Args parse(int argc, char** argv) {
             else if (const char* v = val("--form=")) a.form = v;
             else if (const char* v = val("--model=")) a.model = v;
             else if (const char* v = val("--target-cost=")) a.target_cost = std::stod(v);
+            else if (const char* v = val("--loss=")) a.loss = v;
+            else if (const char* v = val("--delta=")) a.delta = std::stod(v);
             else if (s.rfind("--", 0) != 0 && a.file.empty()) a.file = s;
             else usage_error("bad argument: " + s);
         } catch (const std::logic_error&) {
@@ -71,6 +78,8 @@ Args parse(int argc, char** argv) {
         }
     }
     if (a.file.empty() == (a.synthetic == 0)) usage_error("give exactly one of a problem file or --synthetic=W");
+    if (a.loss != "none" && a.loss != "huber") usage_error("unknown loss: " + a.loss);
+    if (a.loss == "huber" && !(a.delta > 0.0)) usage_error("--delta must be positive");
     return a;
 }
 
@@ -94,7 +103,18 @@ int main(int argc, char** argv) {
     }
     std::fprintf(stderr, "loaded %s: %d cameras, %d points, %d observations\n", name.c_str(), bal.num_cameras,
                  bal.num_points, bal.num_observations);
-    const double own_cost = gba::total_squared_error(bal) / 2.0;
+    double own_cost = gba::total_squared_error(bal) / 2.0;
+    if (args.loss == "huber") {
+        own_cost = 0.0;
+        const double d2 = args.delta * args.delta;
+        for (int i = 0; i < bal.num_observations; ++i) {
+            double r[2];
+            gba::snavely_residual(bal.camera(bal.obs_camera[i]), bal.point(bal.obs_point[i]), &bal.obs_pixel[2 * i],
+                                  r);
+            const double s = r[0] * r[0] + r[1] * r[1];
+            own_cost += 0.5 * (s <= d2 ? s : 2.0 * args.delta * std::sqrt(s) - d2);
+        }
+    }
 
     cudaDeviceProp prop{};
     int dev = 0;
@@ -107,6 +127,8 @@ int main(int argc, char** argv) {
     opts.verbose = args.verbose;
     opts.model_path = args.model;
     opts.target_cost = args.target_cost;
+    opts.loss = args.loss == "huber" ? gba::Loss::Huber : gba::Loss::None;
+    opts.huber_delta = args.delta;
     if (args.form == "plain") opts.form = gba::SolverForm::Plain;
     else if (args.form == "mixed") opts.form = gba::SolverForm::Mixed;
     else if (args.form == "learned") opts.form = gba::SolverForm::MixedLearned;
@@ -146,7 +168,7 @@ int main(int argc, char** argv) {
                       "{\n"
                       "  \"file\": \"%s\",\n"
                       "  \"solver\": \"gba-gb300-lm\",\n"
-                      "  \"loss\": \"none\",\n"
+                      "  \"loss\": \"%s\",\n"
                       "  \"num_cameras\": %d,\n"
                       "  \"num_points\": %d,\n"
                       "  \"num_observations\": %d,\n"
@@ -162,7 +184,7 @@ int main(int argc, char** argv) {
                       "  \"pcg_iterations\": %lld,\n"
                       "  \"time_to_target_s\": %.6f,\n"
                       "  \"trajectory\": ",
-                      name.c_str(), bal.num_cameras, bal.num_points, bal.num_observations, res.initial_cost,
+                      name.c_str(), args.loss.c_str(), bal.num_cameras, bal.num_points, bal.num_observations, res.initial_cost,
                       res.final_cost, res.iterations, res.total_time_s, per_iter, res.termination.c_str(), prop.name,
                       form_name.c_str(), res.trials, res.pcg_iterations, res.time_to_target_s);
         json = head + traj + "\n}";

@@ -78,6 +78,10 @@ gba::LMOptions to_options(const gba_lm_options* o) {
     r.model_path = o->model_path ? o->model_path : "";
     r.target_cost = o->target_cost;
     r.stop_at_target = o->stop_at_target != 0;
+    need(o->loss == GBA_LOSS_NONE || o->loss == GBA_LOSS_HUBER, "bad loss");
+    r.loss = static_cast<gba::Loss>(o->loss);
+    r.huber_delta = o->huber_delta;
+    need(r.loss == gba::Loss::None || r.huber_delta > 0.0, "huber_delta must be positive");
     return r;
 }
 
@@ -140,6 +144,8 @@ void gba_lm_options_default(gba_lm_options* o) {
     o->model_path = nullptr;
     o->target_cost = d.target_cost;
     o->stop_at_target = 0;
+    o->loss = GBA_LOSS_NONE;
+    o->huber_delta = d.huber_delta;
 }
 
 unsigned long long gba_launch_count(void) { return gba::launch_count(); }
@@ -244,6 +250,14 @@ int gba_solver_run(gba_solver* s, const gba_lm_options* opts, gba_lm_result* res
         gba::LMResult r = gba::run_lm(S(s), o, t0);
         r.total_time_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         fill_result(r, result);
+    });
+}
+
+int gba_solver_set_loss(gba_solver* s, int loss, double delta) {
+    return guarded([&] {
+        need(loss == GBA_LOSS_NONE || loss == GBA_LOSS_HUBER, "bad loss");
+        need(loss == GBA_LOSS_NONE || delta > 0.0, "huber_delta must be positive");
+        S(s).set_loss(static_cast<gba::Loss>(loss), delta);
     });
 }
 

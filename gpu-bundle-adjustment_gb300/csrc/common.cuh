@@ -77,6 +77,19 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
     return r;
 }
 
+// Huber loss of a squared residual norm s (delta <= 0: no loss): rho(s) and
+// the square root of its weight rho'(s) = min(1, delta / sqrt(s)), the factor
+// that scales an observation's residual and Jacobian rows.
+__device__ __forceinline__ double robust_rho(double s, double delta) {
+    return (delta > 0.0 && s > delta * delta) ? 2.0 * delta * sqrt(s) - delta * delta : s;
+}
+__device__ __forceinline__ double robust_sqrt_weight(double s, double delta) {
+    return (delta > 0.0 && s > delta * delta) ? sqrt(delta / sqrt(s)) : 1.0;
+}
+__device__ __forceinline__ float robust_sqrt_weight(float s, float delta) {
+    return (delta > 0.f && s > delta * delta) ? sqrtf(delta / sqrtf(s)) : 1.f;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

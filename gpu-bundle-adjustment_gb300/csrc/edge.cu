@@ -37,7 +37,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f64(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
     const int* __restrict__ s_pt, const double2* __restrict__ s_px, const double* __restrict__ cams,
     const double* __restrict__ pts, double* __restrict__ W, double* __restrict__ JcR, double* __restrict__ V,
-    double* __restrict__ bp, double* __restrict__ sse_part, unsigned long long* __restrict__ counters) {
+    double* __restrict__ bp, double* __restrict__ sse_part, unsigned long long* __restrict__ counters,
+    double delta) {
     __shared__ double contrib[9][kPT];
     __shared__ double red[kPT / 32];
     __shared__ unsigned long long redu[kPT / 32];
@@ -76,7 +77,17 @@ __global__ void __launch_bounds__(kPT) point_pass_f64(
             double* Ws = W + 27ll * s;
             double* Qs = JcR + 20ll * s;
             if (fin) {
-                sse += r[0] * r[0] + r[1] * r[1];
+                const double sq = r[0] * r[0] + r[1] * r[1];
+                sse += robust_rho(sq, delta);
+                if (delta > 0.0) {  // robust loss: rows scaled by sqrt(rho'(s))
+                    const double sw = robust_sqrt_weight(sq, delta);
+                    r[0] *= sw;
+                    r[1] *= sw;
+#pragma unroll
+                    for (int k = 0; k < 18; ++k) Jc[k] *= sw;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) Jp[k] *= sw;
+                }
 #pragma unroll
                 for (int i = 0; i < 9; ++i)
 #pragma unroll
@@ -186,7 +197,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int* __restrict__ s_pt, const double2* __restrict__ s_px, const double* __restrict__ cams,
     const double* __restrict__ pts, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
     float* __restrict__ J32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
-    unsigned long long* __restrict__ counters) {
+    unsigned long long* __restrict__ counters, float delta) {
     __shared__ float contrib[9][kPT];
     __shared__ unsigned long long redu[kPT / 32];
     const int chunk = blockIdx.x;
@@ -224,6 +235,13 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
             float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
             float4* outc = reinterpret_cast<float4*>(J32c + 20ll * cam_pos[s]);  // camera-major Jc copy
+            if (fin && delta > 0.f) {  // robust loss: rows scaled by sqrt(rho'(s)); J32 holds the scaled rows
+                const float sw = robust_sqrt_weight(r[0] * r[0] + r[1] * r[1], delta);
+                r[0] *= sw;
+                r[1] *= sw;
+#pragma unroll
+                for (int q = 0; q < 24; ++q) J[q] *= sw;
+            }
             if (fin) {
 #pragma unroll
                 for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
@@ -275,7 +293,7 @@ __global__ void __launch_bounds__(kCT) camera_pass_f32(
     const int* __restrict__ cchunk_begin, const int* __restrict__ cchunk_cam, const int* __restrict__ cam_off,
     const int* __restrict__ cam_slots, const int* __restrict__ s_pt, const double2* __restrict__ s_px,
     const double* __restrict__ cams, const double* __restrict__ pts, const float2* __restrict__ r_cur,
-    double* __restrict__ part) {
+    double* __restrict__ part, float delta) {
     const int k = blockIdx.x;
     const int b = cchunk_begin[k], c = cchunk_cam[k];
     const int e = min(b + kCamChunk, cam_off[c + 1]);
@@ -300,6 +318,13 @@ __global__ void __launch_bounds__(kCT) camera_pass_f32(
         r[1] = rf.y;
         const bool fin = all_finite(r, 2) && all_finite(Jc, 18) && all_finite(Jp, 6);
         if (!fin) continue;
+        if (delta > 0.f) {
+            const float sw = robust_sqrt_weight(r[0] * r[0] + r[1] * r[1], delta);
+            r[0] *= sw;
+            r[1] *= sw;
+#pragma unroll
+            for (int q = 0; q < 18; ++q) Jc[q] *= sw;
+        }
         int idx = 0;
 #pragma unroll
         for (int a = 0; a < 9; ++a)
@@ -395,7 +420,8 @@ __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, 
                                                const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                const double2* __restrict__ s_px, const double* __restrict__ pre,
                                                const double* __restrict__ pts, double* __restrict__ sse_part,
-                                               unsigned long long* __restrict__ counters, float2* __restrict__ r_out) {
+                                               unsigned long long* __restrict__ counters, float2* __restrict__ r_out,
+                                               double delta) {
     __shared__ double red[kPT / 32];
     __shared__ unsigned long long redu[kPT / 32];
     const int chunk = blockIdx.x;
@@ -417,7 +443,7 @@ __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, 
             ++anom;
             continue;
         }
-        sse += r[0] * r[0] + r[1] * r[1];
+        sse += robust_rho(r[0] * r[0] + r[1] * r[1], delta);
     }
     const double tot = block_sum<kPT>(sse, red);
     const unsigned long long na = block_sum_u64<kPT>(anom, redu);
@@ -456,7 +482,8 @@ double Solver::accumulate() {
         cudaEvent_t ev = prof_start();
         point_pass_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
                                                        spx, cams_.get(), pts_.get(), W_.get(), JcR_.get(),
-                                                       V_.get(), bp_.get(), sse_part_.get(), counters_.get());
+                                                       V_.get(), bp_.get(), sse_part_.get(), counters_.get(),
+                                                       huber_delta_);
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f64", ev);
         if (n_cchunk_ > 0) {
@@ -479,7 +506,7 @@ double Solver::accumulate() {
             GBA_LAUNCH_CHECK();
             cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
                                                      cam_pre_.get(), pts_.get(), sse_part_.get(), counters_.get() + 2,
-                                                     reinterpret_cast<float2*>(r_cur_.get()));
+                                                     reinterpret_cast<float2*>(r_cur_.get()), huber_delta_);
             GBA_LAUNCH_CHECK();
             ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
             GBA_LAUNCH_CHECK();
@@ -489,14 +516,16 @@ double Solver::accumulate() {
         cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
                                                        spx, cams_.get(), pts_.get(), rc, cam_pos_.get(), J32_.get(),
-                                                       J32c_.get(), V_.get(), bp_.get(), counters_.get());
+                                                       J32c_.get(), V_.get(), bp_.get(), counters_.get(),
+                                                       static_cast<float>(huber_delta_));
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);
         if (n_cchunk_ > 0) {
             ev = prof_start();
             camera_pass_f32<<<n_cchunk_, kCT, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(),
                                                             cam_off_.get(), cam_slots_.get(), s_pt_.get(), spx,
-                                                            cams_.get(), pts_.get(), rc, cam_part_.get());
+                                                            cams_.get(), pts_.get(), rc, cam_part_.get(),
+                                                            static_cast<float>(huber_delta_));
             GBA_LAUNCH_CHECK();
             prof_stop("camera_pass_f32", ev);
         }
@@ -517,7 +546,7 @@ double Solver::trial_cost() {
     GBA_LAUNCH_CHECK();
     cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
                                              cam_pre_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
-                                             reinterpret_cast<float2*>(r_trial_.get()));
+                                             reinterpret_cast<float2*>(r_trial_.get()), huber_delta_);
     GBA_LAUNCH_CHECK();
     prof_stop("cost_f64", ev);
     ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get() + 1);

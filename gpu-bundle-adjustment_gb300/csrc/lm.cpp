@@ -45,6 +45,7 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
     };
 
     s.begin_solve();
+    s.set_loss(opts.loss, opts.huber_delta);
     double sse = phase(res.t_accumulate, [&] { return s.accumulate(); });
     res.initial_cost = sse / 2.0;
     res.trajectory.push_back(res.initial_cost);

@@ -35,6 +35,7 @@ constexpr int kCT = 128;
 constexpr int kVT = 256;  // vector-kernel threads
 constexpr int kCamChunk = 1024;
 constexpr int kCheck = 8;
+constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to be decisive
 
 // device scalar slots (pcg_s_)
 enum { S_RZ = 0, S_ALPHA, S_BETA, S_RR, S_BB, S_DONE, S_ITERS, S_TOL2, S_NORM };
@@ -77,15 +78,24 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         my_e = pt_off[my_p + 1];
     }
     T z0 = T(0), z1 = T(0), z2 = T(0);
+    // Single-pass chunks (the usual case) keep the slot's Jp, point and
+    // camera-major position in registers for the u phase.
+    const bool single = (s1 - s0) <= kPT;
+    T jp[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    int key = -1;  // point of the slot (slots past the chunk end share key -1, value 0)
+    long long q = 0;
     if (xt) {
         for (int base = s0; base < s1; base += kPT) {
             const int s = base + threadIdx.x;
             T v0 = T(0), v1 = T(0), v2 = T(0);
-            int key = -1;  // point of the slot (slots past the chunk end share key -1, value 0)
+            key = -1;
             if (s < s1) {
                 key = s_pt[s];
+                q = cam_pos[s];
                 T J[24];
                 load_j(J32, s, J);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
                 const T* xc = xt + 9ll * s_cam[s];
                 T t0 = T(0), t1 = T(0);
 #pragma unroll
@@ -145,14 +155,22 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
     }
     __syncthreads();
     // u_e = Jp_e w_p for every slot of the chunk, stored camera-major
+    if (single && xt) {
+        if (s0 + static_cast<int>(threadIdx.x) < s1) {
+            const T w0 = wsh[key - p0][0], w1 = wsh[key - p0][1], w2 = wsh[key - p0][2];
+            u_cm[2 * q] = jp[0] * w0 + jp[1] * w1 + jp[2] * w2;
+            u_cm[2 * q + 1] = jp[3] * w0 + jp[4] * w1 + jp[5] * w2;
+        }
+        return;
+    }
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int p = s_pt[s];
         const T w0 = wsh[p - p0][0], w1 = wsh[p - p0][1], w2 = wsh[p - p0][2];
         const float2* Jp2 = reinterpret_cast<const float2*>(J32 + 24ll * s + 18);
         const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
-        const long long q = cam_pos[s];
-        u_cm[2 * q] = static_cast<T>(j01.x) * w0 + static_cast<T>(j01.y) * w1 + static_cast<T>(j23.x) * w2;
-        u_cm[2 * q + 1] = static_cast<T>(j23.y) * w0 + static_cast<T>(j45.x) * w1 + static_cast<T>(j45.y) * w2;
+        const long long qs = cam_pos[s];
+        u_cm[2 * qs] = static_cast<T>(j01.x) * w0 + static_cast<T>(j01.y) * w1 + static_cast<T>(j23.x) * w2;
+        u_cm[2 * qs + 1] = static_cast<T>(j23.y) * w0 + static_cast<T>(j45.x) * w1 + static_cast<T>(j45.y) * w2;
     }
 }
 
@@ -674,14 +692,17 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             const long long it_l = inner_pcg(&ok_l);
             judge_iters_[0] = it_bj;
             judge_iters_[1] = it_l;
-            if (ok_l && (!ok_bj || it_l < it_bj)) {
+            // Solves shorter than kJudgeMin iterations are too short to compare:
+            // keep block-Jacobi for now and judge again at the next inner solve.
+            const bool decisive = std::max(it_bj, it_l) >= kJudgeMin || !ok_bj || !ok_l;
+            if (decisive && ok_l && (!ok_bj || it_l < it_bj)) {
                 learned_choice_ = 1;
                 use_learned = true;
                 st.pcg_iterations += it_bj;
                 it_count = it_l;
                 ok = ok_l;
             } else {
-                learned_choice_ = 2;
+                learned_choice_ = decisive ? 2 : 0;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
                 factor_blocks_kernel<<<ncb, kVT, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());

@@ -175,6 +175,14 @@ public:
     int learned_choice_ = 0;
     long long judge_iters_[2] = {0, 0};  // inner PCG iterations of the judged solve: block-Jacobi, learned
     void begin_solve() { learned_choice_ = 0; }
+    // Robust loss of the cost and the normal equations (<= 0: none). Changing it
+    // invalidates the cached residuals / SSE of the current parameters.
+    double huber_delta_ = 0.0;
+    void set_loss(Loss loss, double delta) {
+        const double d = loss == Loss::Huber ? delta : 0.0;
+        if (d != huber_delta_) resid_valid_ = false;
+        huber_delta_ = d;
+    }
     bool harvest_ = false;     // plain form: keep the damped diagonal blocks S_cc in Sdiag_
 
     void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px);

@@ -21,6 +21,7 @@ LIB_PATH = PKG / "lib" / "libgba_gb300.so"
 
 GBA_OK = 0
 FORMS = {"plain": 0, "mixed": 1, "learned": 2}
+LOSSES = {"none": 0, "huber": 1}
 TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE", 3: "TARGET_COST"}
 BUF = {
     "U": 0, "V": 1, "bc": 2, "bp": 3, "W": 4, "Vinv": 5, "S": 6, "rhs": 7, "dc": 8, "dp": 9,
@@ -53,6 +54,8 @@ class LMOptions(C.Structure):
         ("model_path", C.c_char_p),
         ("target_cost", C.c_double),
         ("stop_at_target", C.c_int),
+        ("loss", C.c_int),
+        ("huber_delta", C.c_double),
     ]
 
 
@@ -129,6 +132,7 @@ _SIG = {
     "gba_solver_load_model": (C.c_int, [C.c_void_p, C.c_char_p]),
     "gba_solver_run": (C.c_int, [C.c_void_p, C.POINTER(LMOptions), C.POINTER(LMResultC)]),
     "gba_solver_reset_params": (C.c_int, [C.c_void_p]),
+    "gba_solver_set_loss": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "gba_solver_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "gba_solver_kernel_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "gba_solver_profile_reset": (C.c_int, [C.c_void_p]),
@@ -283,6 +287,8 @@ def default_options(**kw) -> LMOptions:
     for k, v in kw.items():
         if k == "form":
             v = FORMS[v] if isinstance(v, str) else v
+        if k == "loss":
+            v = LOSSES[v] if isinstance(v, str) else v
         if k == "model_path" and v is not None:
             v = str(v).encode()
         setattr(o, k, v)
@@ -457,6 +463,9 @@ class Solver:
 
     def reset_params(self) -> None:
         _check(lib.gba_solver_reset_params(self.h))
+
+    def set_loss(self, loss: str = "none", delta: float = 1.0) -> None:
+        _check(lib.gba_solver_set_loss(self.h, LOSSES[loss], delta))
 
     def profile(self, enable: bool = True) -> None:
         _check(lib.gba_solver_profile(self.h, int(enable)))

@@ -29,6 +29,13 @@ enum class SolverForm {
     MixedLearned = 2,
 };
 
+// Robust loss applied to each observation's squared residual s = |r|^2
+// (the reference GPU solver has none; its Ceres baseline offers Huber,
+// benchmarks/bench_ceres.cpp:120-142). Huber: rho(s) = s for s <= delta^2,
+// 2 delta sqrt(s) - delta^2 above; the normal equations use the weights
+// rho'(s) = min(1, delta / sqrt(s)).
+enum class Loss { None = 0, Huber = 1 };
+
 struct LMOptions {
     int max_iterations = 50;
     double initial_lambda = 1e-3;    // Marquardt diagonal damping
@@ -40,11 +47,13 @@ struct LMOptions {
     SolverForm form = SolverForm::Plain;
     double refine_tol = 1e-8;     // mixed: FP64 refinement stops at ||rhs - S dc|| <= tol ||rhs||
     int refine_max_steps = 8;     // mixed: FP64 refinement steps per trial
-    double pcg_tol = 1e-2;        // mixed: relative residual target of each inner FP32 PCG solve
+    double pcg_tol = 1e-4;        // mixed: relative residual target of each inner FP32 PCG solve
     int pcg_max_iters = 200;      // mixed: PCG iteration cap per inner solve
     std::string model_path;       // learned form: MLP weights file (gba_mlp binary)
     double target_cost = 0.0;     // if > 0: record the wall time at which cost first <= target
     bool stop_at_target = false;  // end the solve ("TARGET_COST") once cost <= target_cost
+    Loss loss = Loss::None;       // robust loss; cost = sum rho(|r|^2) / 2
+    double huber_delta = 1.0;     // Huber threshold (px)
 };
 
 struct LMResult {

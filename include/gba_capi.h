@@ -49,12 +49,16 @@ typedef struct gba_lm_options {
     int form;                 /* GBA_FORM_* (plain) */
     double refine_tol;        /* 1e-8 */
     int refine_max_steps;     /* 8 */
-    double pcg_tol;           /* 1e-2 */
+    double pcg_tol;           /* 1e-4 */
     int pcg_max_iters;        /* 200 */
     const char* model_path;   /* learned-form weights, or NULL */
     double target_cost;       /* 0 = off */
     int stop_at_target;       /* 0; 1 = end the solve once cost <= target_cost */
+    int loss;                 /* GBA_LOSS_NONE (0) or GBA_LOSS_HUBER (1) */
+    double huber_delta;       /* 1.0 */
 } gba_lm_options;
+
+enum { GBA_LOSS_NONE = 0, GBA_LOSS_HUBER = 1 };
 
 /* Mirrors gba::LMResult (reference include/gba/lm.hpp:21-29) plus additive
  * fields. trajectory / trajectory_time_s may be NULL; otherwise they hold
@@ -162,6 +166,10 @@ int gba_solver_accept(gba_solver* s);
 int gba_solver_counters(gba_solver* s, unsigned long long* out_anomalies, unsigned long long* out_nonspd);
 /* Loads the learned-preconditioner weights for the MixedLearned form. */
 int gba_solver_load_model(gba_solver* s, const char* path);
+/* Robust loss used by the stage functions from now on (GBA_LOSS_*; Huber
+ * threshold delta > 0). The Ceres baseline's --loss=huber (reference
+ * benchmarks/bench_ceres.cpp:120-142); the reference GPU solver has none. */
+int gba_solver_set_loss(gba_solver* s, int loss, double huber_delta);
 /* Runs the full LM loop on the solver's device-resident problem from its
  * current parameters (the stages above, in the reference's order; no host
  * copies of the problem). Same contract as gba_solve_bal; parameters stay on

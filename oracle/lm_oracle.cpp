@@ -126,6 +126,18 @@ void residual_jacobian(const double* cam, const double* X, const double* obs, do
     }
 }
 
+// Huber loss on the squared residual norm (Ceres HuberLoss, the loss option of
+// the reference's Ceres baseline, benchmarks/bench_ceres.cpp:120-142): rho(s) = s
+// for s <= delta^2, else 2 delta sqrt(s) - delta^2; rows weighted by
+// sqrt(rho'(s)) = sqrt(min(1, delta / sqrt(s))) (Ceres' corrector when rho'' <= 0).
+// delta <= 0: no loss.
+double huber_rho(double s, double delta) {
+    return (delta > 0.0 && s > delta * delta) ? 2.0 * delta * std::sqrt(s) - delta * delta : s;
+}
+double huber_sqrt_weight(double s, double delta) {
+    return (delta > 0.0 && s > delta * delta) ? std::sqrt(delta / std::sqrt(s)) : 1.0;
+}
+
 bool all_finite(const double* v, int n) {
     for (int i = 0; i < n; ++i)
         if (!std::isfinite(v[i])) return false;
@@ -156,6 +168,7 @@ struct Problem {
     const int* op;
     const double* px;
     std::vector<std::vector<int>> point_edges;  // src/lm.cu:380-381
+    double delta = 0.0;                         // Huber threshold, <= 0: no loss
 };
 
 // Normal equations, edge order (src/lm.cu:205-252 accumulation, 399-422).
@@ -178,7 +191,14 @@ void accumulate(const Problem& pr, const double* cams, const double* pts, double
             std::fill(We, We + 27, 0.0);
             continue;
         }
-        s += r[0] * r[0] + r[1] * r[1];
+        const double sq = r[0] * r[0] + r[1] * r[1];
+        s += huber_rho(sq, pr.delta);
+        if (pr.delta > 0.0) {
+            const double sw = huber_sqrt_weight(sq, pr.delta);
+            for (double& v : r) v *= sw;
+            for (double& v : Jc) v *= sw;
+            for (double& v : Jp) v *= sw;
+        }
         for (int i = 0; i < 9; ++i)
             for (int j = 0; j < 3; ++j) We[3 * i + j] = Jc[i] * Jp[j] + Jc[9 + i] * Jp[3 + j];
         double* Uc = U + 81ll * c;
@@ -210,7 +230,7 @@ double cost(const Problem& pr, const double* cams, const double* pts, unsigned l
             ++*anomalies;
             continue;
         }
-        s += r[0] * r[0] + r[1] * r[1];
+        s += huber_rho(r[0] * r[0] + r[1] * r[1], pr.delta);
     }
     return s;
 }
@@ -446,6 +466,19 @@ int oracle_residual(const double* cam, const double* pt, const double* obs, doub
 }
 
 // Normal equations in edge order. U 81C, V 9P (full), W 27E, bc 9C, bp 3P.
+// The _robust variants take the Huber threshold (<= 0: plain squared loss);
+// rows are scaled by the first-order corrector sqrt(rho'(s)) and the cost sums
+// rho(s) = s (s <= d^2) or 2 d sqrt(s) - d^2 per observation.
+int oracle_accumulate_robust(int C, int P, int E, const double* cams, const double* pts, const int* oc,
+                             const int* op, const double* px, double huber_delta, double* U, double* V, double* W,
+                             double* bc, double* bp, double* sse, unsigned long long* anomalies) {
+    Problem pr = make_problem(C, P, E, oc, op, px);
+    pr.delta = huber_delta;
+    *anomalies = 0;
+    accumulate(pr, cams, pts, U, V, W, bc, bp, sse, anomalies);
+    return 0;
+}
+
 int oracle_accumulate(int C, int P, int E, const double* cams, const double* pts, const int* oc, const int* op,
                       const double* px, double* U, double* V, double* W, double* bc, double* bp, double* sse,
                       unsigned long long* anomalies) {
@@ -458,6 +491,14 @@ int oracle_accumulate(int C, int P, int E, const double* cams, const double* pts
 double oracle_cost(int C, int P, int E, const double* cams, const double* pts, const int* oc, const int* op,
                    const double* px) {
     Problem pr = make_problem(C, P, E, oc, op, px);
+    unsigned long long a = 0;
+    return cost(pr, cams, pts, &a);
+}
+
+double oracle_cost_robust(int C, int P, int E, const double* cams, const double* pts, const int* oc, const int* op,
+                          const double* px, double huber_delta) {
+    Problem pr = make_problem(C, P, E, oc, op, px);
+    pr.delta = huber_delta;
     unsigned long long a = 0;
     return cost(pr, cams, pts, &a);
 }
@@ -503,12 +544,14 @@ int oracle_cholesky_solve(const double* L, int n, double* b) {
 // Full LM solve (src/lm.cu:371-724). cams/pts updated in place. termination:
 // 0 CONVERGENCE, 1 MAX_ITERATIONS, 2 FAILURE. trajectory: cost at start and
 // after every accepted iteration (up to traj_cap entries; *traj_len = count).
-int oracle_solve(int C, int P, int E, double* cams, double* pts, const int* oc, const int* op, const double* px,
-                 int max_iterations, double lambda0, double rel_tol, int max_trials, int threads, double* initial_cost,
-                 double* final_cost, int* iterations, int* termination, unsigned long long* anomalies_out,
-                 double* trajectory, int traj_cap, int* traj_len) {
+int oracle_solve_robust(int C, int P, int E, double* cams, double* pts, const int* oc, const int* op,
+                        const double* px, double huber_delta, int max_iterations, double lambda0, double rel_tol,
+                        int max_trials, int threads, double* initial_cost, double* final_cost, int* iterations,
+                        int* termination, unsigned long long* anomalies_out, double* trajectory, int traj_cap,
+                        int* traj_len) {
     if (threads <= 0) threads = default_threads();
     Problem pr = make_problem(C, P, E, oc, op, px);
+    pr.delta = huber_delta;
     State st;
     st.U.resize(81ll * C);
     st.V.resize(9ll * P);
@@ -581,6 +624,15 @@ int oracle_solve(int C, int P, int E, double* cams, double* pts, const int* oc, 
     *anomalies_out = anomalies;
     if (traj_len) *traj_len = tl;
     return 0;
+}
+
+int oracle_solve(int C, int P, int E, double* cams, double* pts, const int* oc, const int* op, const double* px,
+                 int max_iterations, double lambda0, double rel_tol, int max_trials, int threads, double* initial_cost,
+                 double* final_cost, int* iterations, int* termination, unsigned long long* anomalies_out,
+                 double* trajectory, int traj_cap, int* traj_len) {
+    return oracle_solve_robust(C, P, E, cams, pts, oc, op, px, 0.0, max_iterations, lambda0, rel_tol, max_trials,
+                               threads, initial_cost, final_cost, iterations, termination, anomalies_out, trajectory,
+                               traj_cap, traj_len);
 }
 
 }  // extern "C"

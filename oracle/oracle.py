@@ -33,12 +33,19 @@ _lib.oracle_accumulate.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip
                                    C.POINTER(C.c_ulonglong)]
 _lib.oracle_cost.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp]
 _lib.oracle_cost.restype = C.c_double
+_lib.oracle_accumulate_robust.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, _dp, _dp,
+                                          _dp, _dp, _dp, _dp, C.POINTER(C.c_ulonglong)]
+_lib.oracle_cost_robust.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double]
+_lib.oracle_cost_robust.restype = C.c_double
 _lib.oracle_schur_step.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_int, _dp,
                                    _dp, _dp, _dp, _dp]
 _lib.oracle_cholesky.argtypes = [_dp, C.c_int, C.c_int]
 _lib.oracle_cholesky_solve.argtypes = [_dp, C.c_int, _dp]
 _lib.oracle_solve.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_int, C.c_double, C.c_double,
                               C.c_int, C.c_int, _dp, _dp, _ip, _ip, C.POINTER(C.c_ulonglong), _dp, C.c_int, _ip]
+_lib.oracle_solve_robust.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_double, C.c_int,
+                                     C.c_double, C.c_double, C.c_int, C.c_int, _dp, _dp, _ip, _ip,
+                                     C.POINTER(C.c_ulonglong), _dp, C.c_int, _ip]
 
 TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE"}
 
@@ -61,24 +68,28 @@ def _args(prob):
     return (prob.num_cameras, prob.num_points, prob.num_observations)
 
 
-def accumulate(prob, cams=None, pts=None):
-    """Normal equations in observation order: dict U (C,9,9), V (P,3,3), W (E,9,3), bc, bp, sse, anomalies."""
+def accumulate(prob, cams=None, pts=None, huber_delta=0.0):
+    """Normal equations in observation order: dict U (C,9,9), V (P,3,3), W (E,9,3), bc, bp, sse, anomalies.
+
+    huber_delta > 0 applies the Huber loss (rows scaled by sqrt(rho'), sse = sum of rho)."""
     C_, P_, E_ = _args(prob)
     cams = prob.cameras if cams is None else cams
     pts = prob.points if pts is None else pts
     U, V, W = np.empty(81 * C_), np.empty(9 * P_), np.empty(27 * E_)
     bc, bp, sse, an = np.empty(9 * C_), np.empty(3 * P_), np.empty(1), C.c_ulonglong()
-    _lib.oracle_accumulate(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
-                           _d(prob.obs_pixel), _d(U), _d(V), _d(W), _d(bc), _d(bp), _d(sse), C.byref(an))
+    _lib.oracle_accumulate_robust(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
+                                  _d(prob.obs_pixel), float(huber_delta), _d(U), _d(V), _d(W), _d(bc), _d(bp),
+                                  _d(sse), C.byref(an))
     return dict(U=U.reshape(C_, 9, 9), V=V.reshape(P_, 3, 3), W=W.reshape(E_, 9, 3), bc=bc, bp=bp, sse=sse[0],
                 anomalies=an.value)
 
 
-def cost(prob, cams=None, pts=None) -> float:
+def cost(prob, cams=None, pts=None, huber_delta=0.0) -> float:
+    """Sum over observations of rho(|r|^2) (plain squared error when huber_delta <= 0)."""
     cams = prob.cameras if cams is None else cams
     pts = prob.points if pts is None else pts
-    return _lib.oracle_cost(*_args(prob), _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
-                            _d(prob.obs_pixel))
+    return _lib.oracle_cost_robust(*_args(prob), _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
+                                   _d(prob.obs_pixel), float(huber_delta))
 
 
 def schur_step(prob, lam, threads=0, want_S=False):
@@ -98,7 +109,8 @@ def cholesky(A_colmajor: np.ndarray, n: int, threads: int = 0) -> int:
     return _lib.oracle_cholesky(_d(A_colmajor), n, threads)
 
 
-def solve(prob, max_iterations=50, initial_lambda=1e-3, rel_decrease_tol=1e-6, max_inner_trials=16, threads=0):
+def solve(prob, max_iterations=50, initial_lambda=1e-3, rel_decrease_tol=1e-6, max_inner_trials=16, threads=0,
+          huber_delta=0.0):
     """Full LM solve on copies of the parameters; returns (result dict, cams, pts)."""
     C_, P_, E_ = _args(prob)
     cams, pts = prob.cameras.copy(), prob.points.copy()
@@ -106,9 +118,10 @@ def solve(prob, max_iterations=50, initial_lambda=1e-3, rel_decrease_tol=1e-6, m
     an, tl = C.c_ulonglong(), C.c_int()
     cap = max_iterations + 2
     traj = np.zeros(cap)
-    _lib.oracle_solve(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point), _d(prob.obs_pixel),
-                      max_iterations, initial_lambda, rel_decrease_tol, max_inner_trials, threads, C.byref(init),
-                      C.byref(fin), C.byref(it), C.byref(term), C.byref(an), _d(traj), cap, C.byref(tl))
+    _lib.oracle_solve_robust(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
+                             _d(prob.obs_pixel), float(huber_delta), max_iterations, initial_lambda,
+                             rel_decrease_tol, max_inner_trials, threads, C.byref(init), C.byref(fin), C.byref(it),
+                             C.byref(term), C.byref(an), _d(traj), cap, C.byref(tl))
     res = dict(initial_cost=init.value, final_cost=fin.value, iterations=it.value,
                termination=TERMINATION[term.value], anomalies=an.value, trajectory=traj[:min(tl.value, cap)].tolist())
     return res, cams, pts

@@ -91,3 +91,13 @@ def test_mixed_lm_launch_bounds(gba):
     assert res.initial_cost > 1.0
     assert res.anomalies == 0
     assert res.final_cost < 1e-4 * res.initial_cost
+
+
+def test_mixed_huber_reaches_oracle_cost_workload1(gba, oracle):
+    """Huber loss through the FP32 implicit-Schur path: final robust cost within 0.1% of the oracle's."""
+    prob = gba.synthetic(1)
+    ref, _, _ = oracle.solve(prob, max_iterations=15, huber_delta=1.0)
+    res = gba.solve(prob.copy(), max_iterations=15, form="mixed", loss="huber", huber_delta=1.0)
+    assert abs(res.initial_cost - ref["initial_cost"]) <= 1e-9 * ref["initial_cost"]
+    assert res.anomalies == 0
+    assert res.final_cost <= ref["final_cost"] * (1 + 1e-3)

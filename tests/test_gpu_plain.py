@@ -279,3 +279,33 @@ def test_optimum_start_fails_after_all_trials(gba):
     assert res.termination in ("FAILURE", "CONVERGENCE")
     if res.termination == "FAILURE":
         assert res.trials == 16 and res.iterations == 0
+
+
+def test_accumulate_huber_matches_oracle(gba, oracle, small):
+    """Huber loss (first-order corrector): rows scaled by sqrt(rho'), SSE = sum of rho."""
+    d = 2.0
+    with gba.Solver(small, "plain") as s:
+        s.set_loss("huber", d)
+        sse = s.accumulate()
+        dev = _oracle_layout(gba, s, small)
+    assert abs(sse - oracle.cost(small, huber_delta=d)) <= 1e-12 * sse
+    ref = oracle.accumulate(small, huber_delta=d)
+    assert abs(sse - ref["sse"]) <= 1e-12 * ref["sse"]
+    for k in ("U", "V", "W", "bc", "bp"):
+        assert rel_err(dev[k], ref[k]) < 1e-11, k
+
+
+def test_plain_huber_lm_trajectory_matches_oracle_workload1(gba, oracle):
+    """Workload 1 under the Huber loss (delta 1 px), 15 iterations: per-iteration cost 1e-9."""
+    prob = gba.synthetic(1)
+    ref, ref_cams, _ = oracle.solve(prob, max_iterations=15, huber_delta=1.0)
+    run = prob.copy()
+    res = gba.solve(run, max_iterations=15, loss="huber", huber_delta=1.0)
+    assert abs(res.initial_cost - oracle.cost(prob, huber_delta=1.0) / 2) <= 1e-9 * res.initial_cost
+    assert res.anomalies == 0
+    assert res.termination == ref["termination"]
+    assert res.iterations == ref["iterations"]
+    t_dev, t_ref = np.array(res.trajectory), np.array(ref["trajectory"])
+    assert t_dev.shape == t_ref.shape
+    assert np.max(np.abs(t_dev - t_ref) / t_ref) < 1e-9
+    assert rel_err(run.cameras, ref_cams) < 1e-6

@@ -245,3 +245,49 @@ def test_mlp_oracle_backward_vs_finite_differences():
         fd = (loss_at(flat + e) - loss_at(flat - e)) / 2e-5
         # the forward stores activations in FP32, so differences resolve ~1e-7
         assert abs(fd - grad[i]) < 1e-4 * max(1.0, abs(fd)) + 1e-6, (i, fd, grad[i])
+
+
+def test_oracle_huber_cost_matches_per_observation_rho(gba, oracle):
+    """Huber cost = sum rho(|r|^2), rho(s) = s for s <= d^2 else 2 d sqrt(s) - d^2; a huge d is the plain cost."""
+    prob = gba.synthetic_custom(4, 60, 2, 4, 1.5, seed=3)
+    d = 2.0
+    s = np.array([np.sum(oracle.residual(prob.cameras[9 * c:9 * c + 9], prob.points[3 * p:3 * p + 3],
+                                         prob.obs_pixel[2 * e:2 * e + 2]) ** 2)
+                  for e, (c, p) in enumerate(zip(prob.obs_camera, prob.obs_point))])
+    rho = np.where(s <= d * d, s, 2 * d * np.sqrt(s) - d * d)
+    assert abs(oracle.cost(prob, huber_delta=d) - rho.sum()) <= 1e-12 * rho.sum()
+    assert oracle.cost(prob, huber_delta=1e12) == oracle.cost(prob)
+    assert oracle.cost(prob, huber_delta=d) < oracle.cost(prob)
+
+
+@pytest.mark.parametrize("k", [0, 2, 4, 7, 8])
+def test_oracle_huber_gradient_vs_finite_differences(gba, oracle, k):
+    """With the first-order corrector, b = -grad(cost / 2) exactly (cameras; points likewise)."""
+    prob = gba.synthetic_custom(4, 60, 2, 4, 1.5, seed=3)
+    d = 2.0
+    ne = oracle.accumulate(prob, huber_delta=d)
+    for cam in range(prob.num_cameras):
+        i = 9 * cam + k
+        h = 1e-6 * max(1.0, abs(prob.cameras[i]))
+        cp, cm = prob.cameras.copy(), prob.cameras.copy()
+        cp[i] += h
+        cm[i] -= h
+        fd = 0.5 * (oracle.cost(prob, cp, None, d) - oracle.cost(prob, cm, None, d)) / (2 * h)
+        assert abs(fd + ne["bc"][i]) <= 1e-5 * max(1.0, abs(fd)), (cam, k, fd, ne["bc"][i])
+    for p in range(0, prob.num_points, 7):
+        i = 3 * p + k % 3
+        h = 1e-6 * max(1.0, abs(prob.points[i]))
+        pp, pm = prob.points.copy(), prob.points.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = 0.5 * (oracle.cost(prob, None, pp, d) - oracle.cost(prob, None, pm, d)) / (2 * h)
+        assert abs(fd + ne["bp"][i]) <= 1e-5 * max(1.0, abs(fd)), (p, fd, ne["bp"][i])
+
+
+def test_oracle_huber_lm_decreases_robust_cost(gba, oracle):
+    prob = gba.synthetic_custom(6, 400, 2, 6, 1.5, seed=4)
+    res, _, _ = oracle.solve(prob, max_iterations=20, threads=2, huber_delta=1.0)
+    assert res["anomalies"] == 0
+    traj = res["trajectory"]
+    assert all(b < a for a, b in zip(traj, traj[1:]))
+    assert abs(res["initial_cost"] - oracle.cost(prob, huber_delta=1.0) / 2) <= 1e-12 * res["initial_cost"]
