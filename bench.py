@@ -129,11 +129,12 @@ def _dist_env():
 def algorithmic_bytes(kernel: str, C: int, P: int, E: int) -> float:
     """Bytes one launch must move (each array once), per the kernel's definition."""
     if kernel == "schur_point_pass_f32":
-        # J32 (Jc, Jp) 96 B + s_cam 4 + s_pt 4 + u write 8 per slot; V^-1 48 + CSR 4 per point; x 72 per camera
-        return E * 112.0 + P * 52.0 + C * 72.0
+        # per slot: J32 (Jc, Jp) 96 B + s_cam 4 + s_pt 4 + cam_pos 4 + u write 8;
+        # per point: FP32 V'^-1 24 + CSR offset 4; per camera: x 36
+        return E * 116.0 + P * 28.0 + C * 36.0
     if kernel == "schur_camera_pass_f32":
-        # cam_slots 4 + Jc 72 (of the 80 B read) + u 8 per slot
-        return E * 84.0
+        # per slot: camera-major Jc 72 B + u 8 (both contiguous); chunk partials are negligible
+        return E * 80.0
     if kernel == "point_pass_f32":
         # s_cam, s_pt, s_px, r_cur (32 B) in, J32 96 B out per slot; point 24 B in, V/bp 72 B out per point
         return E * 128.0 + P * 96.0 + C * 72.0
@@ -164,6 +165,8 @@ def run_ours(args):
         opts["pcg_tol"] = args.pcg_tol
     if args.pcg_max_iters is not None:
         opts["pcg_max_iters"] = args.pcg_max_iters
+    if args.refine_tol is not None:
+        opts["refine_tol"] = args.refine_tol
     if form == "learned":
         opts["model_path"] = str(MODEL)
 
@@ -221,7 +224,7 @@ def run_ours(args):
                         "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
                         "launches": n_launch, "avg_launch_us": per_launch_s * 1e6, "peak_source": peak_src}
     breakdown = {}
-    for name in ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_f64", "schur_camera_pass_f64",
+    for name in ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
                  "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "backsub",
                  "mlp_forward", "schur_assemble", "dense_potrf"):
         n_k, ms_k = solver.kernel_stats(name)
@@ -268,6 +271,7 @@ def run_ours(args):
             "plain_fp64_form": plain_reference_summary(args.workload, args.seed),
             "max_iterations": args.max_iterations,
             "pcg_tol": opts.get("pcg_tol", "default"),
+            "refine_tol": opts.get("refine_tol", "default"),
             "l2": "inputs larger than L2 (no flush)",
             "parallelism": f"replicas x{world}",
         },
@@ -370,7 +374,9 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--form", default="learned", choices=["plain", "mixed", "learned"])
     ap.add_argument("--max-iterations", type=int, default=50)
-    ap.add_argument("--pcg-tol", type=float, default=None, help="inner PCG relative tolerance (library default 1e-2)")
+    ap.add_argument("--pcg-tol", type=float, default=None, help="inner PCG relative tolerance (library default 1e-4)")
+    ap.add_argument("--refine-tol", type=float, default=None,
+                    help="relative residual target of the refined Schur step (library default 1e-8)")
     ap.add_argument("--pcg-max-iters", type=int, default=None)
     ap.add_argument("--reference-iterations", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -17,9 +17,11 @@ namespace {
 constexpr int kTB = 256;
 
 // V' = V + lambda * max(diag V, 1e-12) on the diagonal; Vinv = V'^-1 (packed).
-// Vinv32 (may be null): FP32 copy for the mixed form's FP32 Schur matvec.
+// Vinv32 / Vinv32lo (may be null): FP32 copy for the mixed form's FP32 Schur
+// matvec and the FP32-rounded remainder, the pair being V'^-1 in float-float.
 __global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __restrict__ V, double lambda, int P,
                                                            double* __restrict__ Vinv, float* __restrict__ Vinv32,
+                                                           float* __restrict__ Vinv32lo,
                                                            unsigned long long* __restrict__ nonspd) {
     __shared__ unsigned long long redu[kTB / 32];
     unsigned long long bad = 0;
@@ -39,10 +41,19 @@ __global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __rest
 #pragma unroll
         for (int k = 0; k < 6; ++k) Vinv[6ll * p + k] = inv[k];
         if (Vinv32) {
+            float h[6], l[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                h[k] = __double2float_rn(inv[k]);
+                l[k] = __double2float_rn(inv[k] - static_cast<double>(h[k]));
+            }
             float2* o = reinterpret_cast<float2*>(Vinv32 + 6ll * p);
-            o[0] = make_float2(static_cast<float>(inv[0]), static_cast<float>(inv[1]));
-            o[1] = make_float2(static_cast<float>(inv[2]), static_cast<float>(inv[3]));
-            o[2] = make_float2(static_cast<float>(inv[4]), static_cast<float>(inv[5]));
+            float2* ol = reinterpret_cast<float2*>(Vinv32lo + 6ll * p);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                o[k] = make_float2(h[2 * k], h[2 * k + 1]);
+                ol[k] = make_float2(l[2 * k], l[2 * k + 1]);
+            }
         }
     }
     const unsigned long long nb = block_sum_u64<kTB>(bad, redu);
@@ -83,19 +94,16 @@ __global__ void batch_inverse3_kernel(const double* __restrict__ A, double* __re
     }
 }
 
-// Point back-substitution, one CTA per point chunk (slots sorted by point):
-//   dp_p = V'^-1_p (bp_p - sum_{e in p} W_e^T dc_{c(e)}),  tpts = pts + dp,
-// and the chunk's part of the gain denominator sum dp (lambda d dp + bp).
-// Plain form: W_e^T dc in FP64 from the W records. Mixed form: Jp^T (Jc dc)
-// in FP32 from the Jacobian records and an FP32 copy of dc, summed per point
-// in FP64 (FP64 V'^-1 and denominator).
-template <bool kMixed>
+// Plain-form point back-substitution, one CTA per point chunk (slots sorted by
+// point): dp_p = V'^-1_p (bp_p - sum_{e in p} W_e^T dc_{c(e)}), tpts = pts + dp,
+// and the chunk's part of the gain denominator sum dp (lambda d dp + bp), all
+// FP64 from the W records. (The mixed form runs the float-float point pass in
+// its back-substitution mode instead.)
 __global__ void __launch_bounds__(kTB) backsub_chunk_kernel(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
-    const double* __restrict__ W, const float* __restrict__ J32, const double* __restrict__ dc,
-    const float* __restrict__ dc32, const double* __restrict__ V, const double* __restrict__ Vinv,
-    const double* __restrict__ bp, const double* __restrict__ pts, double lambda, double* __restrict__ dp,
-    double* __restrict__ tpts, double* __restrict__ part) {
+    const double* __restrict__ W, const double* __restrict__ dc, const double* __restrict__ V,
+    const double* __restrict__ Vinv, const double* __restrict__ bp, const double* __restrict__ pts, double lambda,
+    double* __restrict__ dp, double* __restrict__ tpts, double* __restrict__ part) {
     __shared__ double contrib[3][kTB];
     __shared__ double red[kTB / 32];
     const int chunk = blockIdx.x;
@@ -112,38 +120,14 @@ __global__ void __launch_bounds__(kTB) backsub_chunk_kernel(
         const int s = base + threadIdx.x;
         double v0 = 0.0, v1 = 0.0, v2 = 0.0;
         if (s < s1) {
-            const int c = s_cam[s];
-            if (kMixed) {
-                const float4* q = reinterpret_cast<const float4*>(J32 + 24ll * s);
-                float J[24];
+            const double* We = W + 27ll * s;
+            const double* d = dc + 9ll * s_cam[s];
 #pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    const float4 t = q[k];
-                    J[4 * k] = t.x;
-                    J[4 * k + 1] = t.y;
-                    J[4 * k + 2] = t.z;
-                    J[4 * k + 3] = t.w;
-                }
-                const float* d = dc32 + 9ll * c;
-                float t0 = 0.f, t1 = 0.f;
-#pragma unroll
-                for (int k = 0; k < 9; ++k) {
-                    t0 += J[k] * d[k];
-                    t1 += J[9 + k] * d[k];
-                }
-                v0 = static_cast<double>(J[18] * t0 + J[21] * t1);
-                v1 = static_cast<double>(J[19] * t0 + J[22] * t1);
-                v2 = static_cast<double>(J[20] * t0 + J[23] * t1);
-            } else {
-                const double* We = W + 27ll * s;
-                const double* d = dc + 9ll * c;
-#pragma unroll
-                for (int i = 0; i < 9; ++i) {
-                    const double di = d[i];
-                    v0 += We[3 * i] * di;
-                    v1 += We[3 * i + 1] * di;
-                    v2 += We[3 * i + 2] * di;
-                }
+            for (int i = 0; i < 9; ++i) {
+                const double di = d[i];
+                v0 += We[3 * i] * di;
+                v1 += We[3 * i + 1] * di;
+                v2 += We[3 * i + 2] * di;
             }
         }
         contrib[0][threadIdx.x] = v0;
@@ -183,11 +167,6 @@ __global__ void __launch_bounds__(kTB) backsub_chunk_kernel(
     if (threadIdx.x == 0) part[chunk] = t;
 }
 
-__global__ void to_f32_kernel(const double* __restrict__ a, int n, float* __restrict__ b) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = static_cast<float>(a[i]);
-}
-
 // Camera part of the denominator and the trial cameras (tcams = cams + dc).
 __global__ void __launch_bounds__(kTB) camera_step_kernel(const double* __restrict__ dc, const double* __restrict__ U,
                                                          const double* __restrict__ bc,
@@ -225,7 +204,7 @@ __global__ void __launch_bounds__(256) denom_finalize(const double* __restrict__
 unsigned long long Solver::damp_invert_v(double lambda) {
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get() + 3, 0, sizeof(unsigned long long), stream_));
     const int grid = std::min(ceil_div(P_, kTB), 8 * device_sm_count());
-    damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), Vinv32_.get(),
+    damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), Vinv32_.get(), Vinv32lo_.get(),
                                                     counters_.get() + 3);
     GBA_LAUNCH_CHECK();
     unsigned long long bad = 0;
@@ -251,18 +230,13 @@ double Solver::back_substitute(double lambda) {
     GBA_LAUNCH_CHECK();
     cudaEvent_t ev = prof_start();
     if (form_ == SolverForm::Plain) {
-        backsub_chunk_kernel<false><<<n_pchunk_, kTB, 0, stream_>>>(
-            pchunk_.get(), pt_off_.get(), s_cam_.get(), W_.get(), nullptr, dc_.get(), nullptr, V_.get(), Vinv_.get(),
-            bp_.get(), pts_.get(), lambda, dp_.get(), tpts_.get(), part + ncam);
-    } else {
-        float* dc32 = pcg_p32_.get();  // free during back-substitution
-        to_f32_kernel<<<ceil_div(9ll * C_, 256), 256, 0, stream_>>>(dc_.get(), 9 * C_, dc32);
+        backsub_chunk_kernel<<<n_pchunk_, kTB, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), W_.get(),
+                                                             dc_.get(), V_.get(), Vinv_.get(), bp_.get(), pts_.get(),
+                                                             lambda, dp_.get(), tpts_.get(), part + ncam);
         GBA_LAUNCH_CHECK();
-        backsub_chunk_kernel<true><<<n_pchunk_, kTB, 0, stream_>>>(
-            pchunk_.get(), pt_off_.get(), s_cam_.get(), nullptr, J32_.get(), dc_.get(), dc32, V_.get(), Vinv_.get(),
-            bp_.get(), pts_.get(), lambda, dp_.get(), tpts_.get(), part + ncam);
+    } else {
+        mixed_back_substitute(*this, lambda, part + ncam);
     }
-    GBA_LAUNCH_CHECK();
     prof_stop("backsub", ev);
     denom_finalize<<<1, 256, 0, stream_>>>(part, ncam, n_pchunk_, scal_.get() + 2);
     GBA_LAUNCH_CHECK();

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             r[1] = rf.y;
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
             float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
-            float4* outc = reinterpret_cast<float4*>(J32c + 20ll * cam_pos[s]);  // camera-major Jc copy
+            float2* outc = reinterpret_cast<float2*>(J32c + 18ll * cam_pos[s]);  // camera-major Jc copy
             if (fin && delta > 0.f) {  // robust loss: rows scaled by sqrt(rho'(s)); J32 holds the scaled rows
                 const float sw = robust_sqrt_weight(r[0] * r[0] + r[1] * r[1], delta);
                 r[0] *= sw;
@@ -246,8 +246,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
 #pragma unroll
                 for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) outc[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
-                outc[4] = make_float4(J[16], J[17], 0.f, 0.f);
+                for (int q = 0; q < 9; ++q) outc[q] = make_float2(J[2 * q], J[2 * q + 1]);
                 const float* Jp = J + 18;
                 v[0] = Jp[0] * Jp[0] + Jp[3] * Jp[3];
                 v[1] = Jp[1] * Jp[0] + Jp[4] * Jp[3];
@@ -262,7 +261,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
 #pragma unroll
                 for (int q = 0; q < 6; ++q) out[q] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                for (int q = 0; q < 5; ++q) outc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int q = 0; q < 9; ++q) outc[q] = make_float2(0.f, 0.f);
             }
         }
 #pragma unroll

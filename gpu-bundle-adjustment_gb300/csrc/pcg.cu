@@ -24,6 +24,7 @@
 
 #include "blocks.cuh"
 #include "common.cuh"
+#include "ff.cuh"
 #include "mlp.hpp"
 #include "solver.hpp"
 
@@ -33,39 +34,155 @@ namespace {
 constexpr int kPT = 256;
 constexpr int kCT = 128;
 constexpr int kVT = 256;  // vector-kernel threads
+constexpr int kCB = 32;   // thread-per-camera kernels: one warp per block spreads C cameras over the SMs
 constexpr int kCamChunk = 1024;
 constexpr int kCheck = 8;
 constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to be decisive
 
-// device scalar slots (pcg_s_)
-enum { S_RZ = 0, S_ALPHA, S_BETA, S_RR, S_BB, S_DONE, S_ITERS, S_TOL2, S_NORM };
+constexpr int kUC = 32;        // cameras per block of the 9-threads-per-camera kernels
+constexpr int kUT = 9 * kUC;   // their block size
 
-template <typename T>
-__device__ __forceinline__ void load_j(const float* __restrict__ J32, long long s, T* J) {
+// Device scalar slots (pcg_s_). Within one PCG iteration each slot is written
+// by one kernel (block 0, thread 0) and read only by later kernels, except
+// S_DONE, whose value every block of the writing kernel derives itself:
+//   pcg_update         reads S_RZ;            writes S_RZPREV, S_ITERS (and S_DONE on breakdown)
+//   pcg_direction      reads S_RZPREV, S_ITERS; writes S_RZ, S_RR, S_BETA, S_DONE
+enum { S_RZ = 0, S_ALPHA, S_BETA, S_RR, S_BB, S_DONE, S_ITERS, S_TOL2, S_NORM, S_RZPREV };
+
+using ffa::ff;
+
+// Arithmetic of the implicit product: FP32 (PCG) or float-float (right-hand
+// side and refinement residual). The Jacobian records are FP32 either way and
+// enter every product exactly.
+template <typename T> __device__ __forceinline__ T zero();
+template <> __device__ __forceinline__ float zero<float>() { return 0.f; }
+template <> __device__ __forceinline__ ff zero<ff>() { return {0.f, 0.f}; }
+
+// FP32 forms; the float-float overloads (ffa::madd, add, norm, shfl_up) are
+// found by argument-dependent lookup.
+__device__ __forceinline__ void madd(float& acc, float a, float b) { acc = fmaf(a, b, acc); }
+__device__ __forceinline__ float add(float a, float b) { return a + b; }
+__device__ __forceinline__ float norm(float a) { return a; }
+__device__ __forceinline__ float shfl_up(float a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+__device__ __forceinline__ double as_double(float a) { return a; }
+__device__ __forceinline__ double as_double(ff a) { return ffa::to_double(a); }
+template <typename T> __device__ __forceinline__ T from_double(double d);
+template <> __device__ __forceinline__ float from_double<float>(double d) { return static_cast<float>(d); }
+template <> __device__ __forceinline__ ff from_double<ff>(double d) { return ffa::from_double(d); }
+__device__ __forceinline__ float warp_total(float v) { return warp_sum(v); }
+__device__ __forceinline__ ff warp_total(ff v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ffa::add(v, ffa::shfl_xor(v, o));
+    return v;
+}
+
+// V'^-1 of a point (6 packed): FP32 copy, or FP32 copy + low parts.
+__device__ __forceinline__ void load_vinv(const float* __restrict__ hi, const float* __restrict__, long long p,
+                                          float* v) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) v[k] = hi[6 * p + k];
+}
+__device__ __forceinline__ void load_vinv(const float* __restrict__ hi, const float* __restrict__ lo, long long p,
+                                          ff* v) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) v[k] = {hi[6 * p + k], lo[6 * p + k]};
+}
+
+// u_e: two values per slot (8 B in FP32, 16 B in float-float).
+__device__ __forceinline__ void store_u(float* u, long long q, float a, float b) {
+    reinterpret_cast<float2*>(u)[q] = make_float2(a, b);
+}
+__device__ __forceinline__ void store_u(ff* u, long long q, ff a, ff b) {
+    reinterpret_cast<float4*>(u)[q] = make_float4(a.hi, a.lo, b.hi, b.lo);
+}
+__device__ __forceinline__ void load_u(const float* u, long long q, float& a, float& b) {
+    const float2 v = reinterpret_cast<const float2*>(u)[q];
+    a = v.x;
+    b = v.y;
+}
+__device__ __forceinline__ void load_u(const ff* u, long long q, ff& a, ff& b) {
+    const float4 v = reinterpret_cast<const float4*>(u)[q];
+    a = {v.x, v.y};
+    b = {v.z, v.w};
+}
+
+__device__ __forceinline__ void load_j(const float* __restrict__ J32, long long s, float* J) {
     const float4* q = reinterpret_cast<const float4*>(J32 + 24 * s);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const float4 v = q[k];
-        J[4 * k] = static_cast<T>(v.x);
-        J[4 * k + 1] = static_cast<T>(v.y);
-        J[4 * k + 2] = static_cast<T>(v.z);
-        J[4 * k + 3] = static_cast<T>(v.w);
+        J[4 * k] = v.x;
+        J[4 * k + 1] = v.y;
+        J[4 * k + 2] = v.z;
+        J[4 * k + 3] = v.w;
     }
 }
 
-// Point pass of the implicit product. xt: the camera vector in the arithmetic
-// type (an FP32 copy inside PCG), Vinv_t: V'^-1 in the arithmetic type (6 per
-// point); u is written at the slot's camera-major position so that the camera
-// pass reads it contiguously.
+// w = V'^-1 z (3x3 packed symmetric)
 template <typename T>
+__device__ __forceinline__ void apply_vinv(const T* v, T z0, T z1, T z2, T& w0, T& w1, T& w2) {
+    z0 = norm(z0);
+    z1 = norm(z1);
+    z2 = norm(z2);
+    w0 = zero<T>();
+    w1 = zero<T>();
+    w2 = zero<T>();
+    madd(w0, v[0], z0);
+    madd(w0, v[1], z1);
+    madd(w0, v[3], z2);
+    madd(w1, v[1], z0);
+    madd(w1, v[2], z1);
+    madd(w1, v[4], z2);
+    madd(w2, v[3], z0);
+    madd(w2, v[4], z1);
+    madd(w2, v[5], z2);
+    w0 = norm(w0);
+    w1 = norm(w1);
+    w2 = norm(w2);
+}
+
+// u = Jp w (Jp row-major 2x3, FP32)
+template <typename T>
+__device__ __forceinline__ void jp_times(const float* jp, T w0, T w1, T w2, T& u0, T& u1) {
+    u0 = zero<T>();
+    u1 = zero<T>();
+    madd(u0, jp[0], w0);
+    madd(u0, jp[1], w1);
+    madd(u0, jp[2], w2);
+    madd(u1, jp[3], w0);
+    madd(u1, jp[4], w1);
+    madd(u1, jp[5], w2);
+}
+
+// Back-substitution outputs of the point pass (kBack): dp = V'^-1 (bp - W^T dc),
+// trial points, and per-chunk partials of the gain denominator's point terms.
+struct BacksubOut {
+    const double* V;
+    const double* pts;
+    double lambda;
+    double* dp;
+    double* tpts;
+    double* part;
+};
+
+// Point pass of the implicit product. xt: the camera vector in the arithmetic
+// type (an FP32 copy inside PCG, a float-float copy of dc in refinement), or
+// null for the right-hand side; z = sum_e Jp^T Jc x + a bp. V'^-1 from its FP32
+// copy (+ low parts for float-float). u is written at the slot's camera-major
+// position so that the camera pass reads it contiguously. With kBack (a = -1,
+// xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
+template <typename T, bool kBack = false>
 __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                        const int* __restrict__ cam_pos, const float* __restrict__ J32,
-                                                       const T* __restrict__ Vinv_t, const double* __restrict__ bp,
-                                                       const T* __restrict__ xt, double a, T* __restrict__ u_cm,
-                                                       const double* __restrict__ done) {
+                                                       const float* __restrict__ vinv_hi,
+                                                       const float* __restrict__ vinv_lo,
+                                                       const double* __restrict__ bp, const T* __restrict__ xt,
+                                                       double a, T* __restrict__ u_cm,
+                                                       const double* __restrict__ done, BacksubOut bk) {
     __shared__ T seg[kPT][3];  // warp-segment partial sums, at each segment's last slot
     __shared__ T wsh[kPT][3];
+    __shared__ double bsum[kPT / 32];
     if (done && *done != 0.0) return;
     const int chunk = blockIdx.x;
     const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
@@ -77,48 +194,53 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         my_b = pt_off[my_p];
         my_e = pt_off[my_p + 1];
     }
-    T z0 = T(0), z1 = T(0), z2 = T(0);
+    T z0 = zero<T>(), z1 = zero<T>(), z2 = zero<T>();
     // Single-pass chunks (the usual case) keep the slot's Jp, point and
     // camera-major position in registers for the u phase.
     const bool single = (s1 - s0) <= kPT;
-    T jp[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    float jp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int key = -1;  // point of the slot (slots past the chunk end share key -1, value 0)
     long long q = 0;
     if (xt) {
         for (int base = s0; base < s1; base += kPT) {
             const int s = base + threadIdx.x;
-            T v0 = T(0), v1 = T(0), v2 = T(0);
+            T v0 = zero<T>(), v1 = zero<T>(), v2 = zero<T>();
             key = -1;
             if (s < s1) {
                 key = s_pt[s];
                 q = cam_pos[s];
-                T J[24];
+                float J[24];
                 load_j(J32, s, J);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
                 const T* xc = xt + 9ll * s_cam[s];
-                T t0 = T(0), t1 = T(0);
+                T t0 = zero<T>(), t1 = zero<T>();
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
                     const T xk = xc[k];
-                    t0 += J[k] * xk;
-                    t1 += J[9 + k] * xk;
+                    madd(t0, J[k], xk);
+                    madd(t1, J[9 + k], xk);
                 }
-                v0 = J[18] * t0 + J[21] * t1;
-                v1 = J[19] * t0 + J[22] * t1;
-                v2 = J[20] * t0 + J[23] * t1;
+                t0 = norm(t0);
+                t1 = norm(t1);
+                madd(v0, J[18], t0);
+                madd(v0, J[21], t1);
+                madd(v1, J[19], t0);
+                madd(v1, J[22], t1);
+                madd(v2, J[20], t0);
+                madd(v2, J[23], t1);
             }
             // inclusive segmented scan over the warp (slots of a point are contiguous)
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                const T u0 = __shfl_up_sync(0xffffffffu, v0, d);
-                const T u1 = __shfl_up_sync(0xffffffffu, v1, d);
-                const T u2 = __shfl_up_sync(0xffffffffu, v2, d);
+                const T u0 = shfl_up(v0, d);
+                const T u1 = shfl_up(v1, d);
+                const T u2 = shfl_up(v2, d);
                 const int kd = __shfl_up_sync(0xffffffffu, key, d);
                 if (lane >= d && kd == key) {
-                    v0 += u0;
-                    v1 += u1;
-                    v2 += u2;
+                    v0 = add(v0, u0);
+                    v1 = add(v1, u1);
+                    v2 = add(v2, u2);
                 }
             }
             const int knext = __shfl_down_sync(0xffffffffu, key, 1);
@@ -133,49 +255,69 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                 const int b = max(my_b, base) - base, e = min(my_e, base + kPT) - base;
                 for (int w = b >> 5; b < e && w <= (e - 1) >> 5; ++w) {
                     const int t = min(e - 1, 32 * w + 31);
-                    z0 += seg[t][0];
-                    z1 += seg[t][1];
-                    z2 += seg[t][2];
+                    z0 = add(z0, seg[t][0]);
+                    z1 = add(z1, seg[t][1]);
+                    z2 = add(z2, seg[t][2]);
                 }
             }
             __syncthreads();
         }
     }
+    T w0 = zero<T>(), w1 = zero<T>(), w2 = zero<T>();
     if (my_p < p1) {
         if (a != 0.0) {
-            z0 += static_cast<T>(a * bp[3ll * my_p]);
-            z1 += static_cast<T>(a * bp[3ll * my_p + 1]);
-            z2 += static_cast<T>(a * bp[3ll * my_p + 2]);
+            z0 = add(z0, from_double<T>(a * bp[3ll * my_p]));
+            z1 = add(z1, from_double<T>(a * bp[3ll * my_p + 1]));
+            z2 = add(z2, from_double<T>(a * bp[3ll * my_p + 2]));
         }
-        const T* Vi = Vinv_t + 6ll * my_p;
-        const T v00 = Vi[0], v10 = Vi[1], v11 = Vi[2], v20 = Vi[3], v21 = Vi[4], v22 = Vi[5];
-        wsh[threadIdx.x][0] = v00 * z0 + v10 * z1 + v20 * z2;
-        wsh[threadIdx.x][1] = v10 * z0 + v11 * z1 + v21 * z2;
-        wsh[threadIdx.x][2] = v20 * z0 + v21 * z1 + v22 * z2;
+        T v[6];
+        load_vinv(vinv_hi, vinv_lo, my_p, v);
+        apply_vinv(v, z0, z1, z2, w0, w1, w2);
+        wsh[threadIdx.x][0] = w0;
+        wsh[threadIdx.x][1] = w1;
+        wsh[threadIdx.x][2] = w2;
+    }
+    if constexpr (kBack) {
+        double den = 0.0;
+        if (my_p < p1) {
+            const long long p = my_p;
+            const double d[3] = {-as_double(w0), -as_double(w1), -as_double(w2)};
+            const int diag[3] = {0, 2, 5};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                bk.dp[3 * p + k] = d[k];
+                bk.tpts[3 * p + k] = bk.pts[3 * p + k] + d[k];
+                const double vk = bk.V[6 * p + diag[k]];
+                den += d[k] * (bk.lambda * (vk > 0.0 ? vk : 1e-12) * d[k] + bp[3 * p + k]);
+            }
+        }
+        const double t = block_sum<kPT>(den, bsum);
+        if (threadIdx.x == 0) bk.part[chunk] = t;
+        return;
     }
     __syncthreads();
     // u_e = Jp_e w_p for every slot of the chunk, stored camera-major
     if (single && xt) {
         if (s0 + static_cast<int>(threadIdx.x) < s1) {
-            const T w0 = wsh[key - p0][0], w1 = wsh[key - p0][1], w2 = wsh[key - p0][2];
-            u_cm[2 * q] = jp[0] * w0 + jp[1] * w1 + jp[2] * w2;
-            u_cm[2 * q + 1] = jp[3] * w0 + jp[4] * w1 + jp[5] * w2;
+            T u0, u1;
+            jp_times(jp, wsh[key - p0][0], wsh[key - p0][1], wsh[key - p0][2], u0, u1);
+            store_u(u_cm, q, u0, u1);
         }
         return;
     }
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int p = s_pt[s];
-        const T w0 = wsh[p - p0][0], w1 = wsh[p - p0][1], w2 = wsh[p - p0][2];
         const float2* Jp2 = reinterpret_cast<const float2*>(J32 + 24ll * s + 18);
         const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
-        const long long qs = cam_pos[s];
-        u_cm[2 * qs] = static_cast<T>(j01.x) * w0 + static_cast<T>(j01.y) * w1 + static_cast<T>(j23.x) * w2;
-        u_cm[2 * qs + 1] = static_cast<T>(j23.y) * w0 + static_cast<T>(j45.x) * w1 + static_cast<T>(j45.y) * w2;
+        const float j[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
+        T u0, u1;
+        jp_times(j, wsh[p - p0][0], wsh[p - p0][1], wsh[p - p0][2], u0, u1);
+        store_u(u_cm, cam_pos[s], u0, u1);
     }
 }
 
 // Camera pass: partial_c = sum over the chunk's camera-major positions of Jc^T u
-// (Jc from the camera-major copy J32c, 20 floats per position; both contiguous).
+// (Jc from the camera-major copy J32c, 18 floats per position; both contiguous).
 template <typename T>
 __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__ cchunk_begin,
                                                         const int* __restrict__ cchunk_cam,
@@ -189,29 +331,31 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
     const int e = min(b + kCamChunk, cam_off[c + 1]);
     T acc[9];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) acc[i] = T(0);
+    for (int i = 0; i < 9; ++i) acc[i] = zero<T>();
     for (int i = b + threadIdx.x; i < e; i += kCT) {
-        const float4* q = reinterpret_cast<const float4*>(J32c + 20ll * i);
-        float Jc[20];
+        const float2* q = reinterpret_cast<const float2*>(J32c + 18ll * i);
+        float Jc[18];
 #pragma unroll
-        for (int t = 0; t < 5; ++t) {
-            const float4 v = q[t];
-            Jc[4 * t] = v.x;
-            Jc[4 * t + 1] = v.y;
-            Jc[4 * t + 2] = v.z;
-            Jc[4 * t + 3] = v.w;
+        for (int t = 0; t < 9; ++t) {
+            const float2 v = q[t];
+            Jc[2 * t] = v.x;
+            Jc[2 * t + 1] = v.y;
         }
-        const T u0 = u_cm[2ll * i], u1 = u_cm[2ll * i + 1];
+        T u0, u1;
+        load_u(u_cm, i, u0, u1);
 #pragma unroll
-        for (int t = 0; t < 9; ++t) acc[t] += static_cast<T>(Jc[t]) * u0 + static_cast<T>(Jc[9 + t]) * u1;
+        for (int t = 0; t < 9; ++t) {
+            madd(acc[t], Jc[t], u0);
+            madd(acc[t], Jc[9 + t], u1);
+        }
     }
     // Warp sums in the arithmetic type (FP32 shuffles stay off GB300's narrow
     // FP64 pipe); the four warp partials are added in FP64.
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
-        const T v = warp_sum(acc[t]);
-        if (lane == 0) wpart[warp][t] = static_cast<double>(v);
+        const T v = warp_total(acc[t]);
+        if (lane == 0) wpart[warp][t] = as_double(v);
     }
     __syncthreads();
     if (threadIdx.x < 9) {
@@ -298,120 +442,185 @@ __device__ __forceinline__ double ordered_block_sum(const double* __restrict__ r
     return block_sum<256>(s, sh);
 }
 
-__global__ void __launch_bounds__(256) pcg_alpha(const double* __restrict__ red, int n, double* __restrict__ sc) {
-    __shared__ double sh[8];
-    if (sc[S_DONE] != 0.0) return;
-    const double pq = ordered_block_sum(red, n, sh);
-    if (threadIdx.x == 0) {
-        if (!(pq > 0.0) || !isfinite(pq)) {
-            sc[S_DONE] = 2.0;  // breakdown: keep the current iterate
-        } else {
-            sc[S_ALPHA] = sc[S_RZ] / pq;
-        }
-    }
+// One read of a device flag per block, shared by all its threads: block 0 of
+// the same kernel may write the flag, and every thread of a block must take
+// the same branch before the block's barriers.
+__device__ __forceinline__ double block_flag(const double* flag, double* sh) {
+    if (threadIdx.x == 0) *sh = *flag;
+    __syncthreads();
+    const double v = *sh;
+    __syncthreads();
+    return v;
 }
 
-// z = M r with M = (L L^T)^-1 per camera (packed factor, 45 per camera).
-__device__ __forceinline__ void precond_apply(const double* __restrict__ L, const double* r, double* z) {
-    blk::chol9_solve(L, r, z);
+// Fixed-order sum of n partials, result in every thread of the block.
+template <int kThreads>
+__device__ __forceinline__ double ordered_sum_all(const double* __restrict__ red, int n, double* sh, double* out) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += kThreads) s += red[i];
+    s = block_sum<kThreads>(s, sh);
+    if (threadIdx.x == 0) *out = s;
+    __syncthreads();
+    return *out;
 }
 
-// Thread per camera: x += alpha p, r -= alpha q, z = M r; partials r.r, r.z.
-__global__ void __launch_bounds__(kVT) pcg_update(double* __restrict__ x, double* __restrict__ r,
-                                                 double* __restrict__ z, const double* __restrict__ p,
-                                                 const double* __restrict__ q, const double* __restrict__ L, int C,
-                                                 double* __restrict__ red_rr, double* __restrict__ red_rz,
-                                                 const double* __restrict__ sc) {
-    __shared__ double sh[kVT / 32];
-    if (sc[S_DONE] != 0.0) return;
-    const int c = blockIdx.x * kVT + threadIdx.x;
-    double rr = 0.0, rz = 0.0;
+// Explicit block-Jacobi inverse M_c = (L L^T)^-1 from the packed factor L
+// (45 per camera): thread (camera, j) forms column j of L^-1 by forward
+// substitution, then row a of M = L^-T L^-1. Once per inner solve; the PCG
+// update then applies M_c as a 9x9 product without divisions.
+__global__ void __launch_bounds__(kUT) precond_inverse_kernel(const double* __restrict__ L, int C,
+                                                             double* __restrict__ Minv) {
+    __shared__ double li[kUC][9][9];  // li[cl][i][j] = (L^-1)_ij
+    const int cl = threadIdx.x / 9, j = threadIdx.x % 9;
+    const int c = blockIdx.x * kUC + cl;
     if (c < C) {
-        const double alpha = sc[S_ALPHA];
-        double rc[9], zc[9];
+        const double* Lc = L + 45ll * c;
+        double y[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const long long i = 9ll * c + k;
-            x[i] += alpha * p[i];
-            rc[k] = r[i] - alpha * q[i];
-            r[i] = rc[k];
-            rr += rc[k] * rc[k];
-        }
-        precond_apply(L + 45ll * c, rc, zc);
+        for (int i = 0; i < 9; ++i) {
+            double t = (i == j) ? 1.0 : 0.0;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            z[9ll * c + k] = zc[k];
-            rz += rc[k] * zc[k];
+            for (int k = 0; k < i; ++k) t -= Lc[blk::tri(i, k)] * y[k];
+            y[i] = (i < j) ? 0.0 : t / Lc[blk::tri(i, i)];
+            li[cl][i][j] = y[i];
         }
     }
-    const double a = block_sum<kVT>(rr, sh);
-    const double b = block_sum<kVT>(rz, sh);
+    __syncthreads();
+    if (c < C) {
+        const int a = j;
+#pragma unroll
+        for (int b = 0; b < 9; ++b) {
+            double m = 0.0;
+            for (int k = max(a, b); k < 9; ++k) m += li[cl][k][a] * li[cl][k][b];
+            Minv[81ll * c + 9 * a + b] = m;
+        }
+    }
+}
+
+// z_i = (M_c r_c)_k for entry i = 9c + k; rs holds the block's r entries.
+__device__ __forceinline__ double apply_minv_row(const double* __restrict__ Minv, long long c, int k, const double* rs) {
+    const double* m = Minv + 81 * c + 9 * k;
+    double z = 0.0;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) z += m[j] * rs[j];
+    return z;
+}
+
+// alpha = rz / p.q (every block sums the p.q partials in the same order);
+// x += alpha p, r -= alpha q, z = M r; partials r.r and r.z. Nine threads per camera.
+__global__ void __launch_bounds__(kUT) pcg_update(double* __restrict__ x, double* __restrict__ r,
+                                                 double* __restrict__ z, const double* __restrict__ p,
+                                                 const double* __restrict__ q, const double* __restrict__ Minv, int C,
+                                                 const double* __restrict__ red_pq, int n_pq,
+                                                 double* __restrict__ red_rr, double* __restrict__ red_rz,
+                                                 double* __restrict__ sc) {
+    __shared__ double sh[kUT / 32];
+    __shared__ double rs[kUT];
+    __shared__ double bc;
+    if (block_flag(sc + S_DONE, &bc) != 0.0) return;
+    const double pq = ordered_sum_all<kUT>(red_pq, n_pq, sh, &bc);
+    const bool first = blockIdx.x == 0 && threadIdx.x == 0;
+    if (!(pq > 0.0) || !isfinite(pq)) {
+        if (first) sc[S_DONE] = 2.0;  // breakdown: keep the current iterate
+        return;
+    }
+    const double rz_old = sc[S_RZ];
+    const double alpha = rz_old / pq;
+    if (first) {
+        sc[S_ALPHA] = alpha;
+        sc[S_RZPREV] = rz_old;
+        sc[S_ITERS] += 1.0;
+    }
+    const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
+    const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
+    const long long i = 9 * c + k;
+    double ri = 0.0;
+    if (c < C) {
+        x[i] += alpha * p[i];
+        ri = r[i] - alpha * q[i];
+        r[i] = ri;
+    }
+    rs[threadIdx.x] = ri;
+    __syncthreads();
+    double rr = ri * ri, rz = 0.0;
+    if (c < C) {
+        const double zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+        z[i] = zi;
+        rz = ri * zi;
+    }
+    const double a = block_sum<kUT>(rr, sh);
+    const double b = block_sum<kUT>(rz, sh);
     if (threadIdx.x == 0) {
         red_rr[blockIdx.x] = a;
         red_rz[blockIdx.x] = b;
     }
 }
 
-__global__ void __launch_bounds__(256) pcg_beta(const double* __restrict__ red_rr, const double* __restrict__ red_rz,
-                                               int n, int max_iters, double* __restrict__ sc) {
-    __shared__ double sh[8];
-    if (sc[S_DONE] != 0.0) return;
-    const double rr = ordered_block_sum(red_rr, n, sh);
-    const double rz = ordered_block_sum(red_rz, n, sh);
-    if (threadIdx.x == 0) {
-        sc[S_ITERS] += 1.0;
+// Convergence test and beta = rz / rz_prev (every block sums the partials in
+// the same order), then p = z + beta p and its FP32 copy.
+__global__ void __launch_bounds__(kVT) pcg_direction(double* __restrict__ p, float* __restrict__ p32,
+                                                    const double* __restrict__ z, int n,
+                                                    const double* __restrict__ red_rr,
+                                                    const double* __restrict__ red_rz, int n_red, int max_iters,
+                                                    double* __restrict__ sc) {
+    __shared__ double sh[kVT / 32];
+    __shared__ double bc;
+    if (block_flag(sc + S_DONE, &bc) != 0.0) return;
+    const double rr = ordered_sum_all<kVT>(red_rr, n_red, sh, &bc);
+    const double rz = ordered_sum_all<kVT>(red_rz, n_red, sh, &bc);
+    double done = 0.0;
+    if (rr <= sc[S_TOL2] * sc[S_BB] || sc[S_ITERS] >= max_iters) {
+        done = 1.0;
+    } else if (!(rz > 0.0) || !isfinite(rz)) {
+        done = 2.0;
+    }
+    const double beta = rz / sc[S_RZPREV];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         sc[S_RR] = rr;
-        if (rr <= sc[S_TOL2] * sc[S_BB] || sc[S_ITERS] >= max_iters) {
-            sc[S_DONE] = 1.0;
-        } else if (!(rz > 0.0) || !isfinite(rz)) {
-            sc[S_DONE] = 2.0;
+        if (done != 0.0) {
+            sc[S_DONE] = done;
         } else {
-            sc[S_BETA] = rz / sc[S_RZ];
+            sc[S_BETA] = beta;
             sc[S_RZ] = rz;
         }
     }
-}
-
-__global__ void __launch_bounds__(kVT) pcg_p_update(double* __restrict__ p, float* __restrict__ p32,
-                                                   const double* __restrict__ z, int n, const double* __restrict__ sc) {
-    if (sc[S_DONE] != 0.0) return;
+    if (done != 0.0) return;
     const int i = blockIdx.x * kVT + threadIdx.x;
     if (i < n) {
-        const double v = z[i] + sc[S_BETA] * p[i];
+        const double v = z[i] + beta * p[i];
         p[i] = v;
         p32[i] = static_cast<float>(v);
     }
 }
 
-// x = 0, r = b, z = M b, p = z; partials b.b and r.z.
-__global__ void __launch_bounds__(kVT) pcg_init(double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
+// x = 0, r = b, z = M b, p = z; partials b.b and r.z. Nine threads per camera.
+__global__ void __launch_bounds__(kUT) pcg_init(double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
                                                double* __restrict__ p, float* __restrict__ p32,
-                                               const double* __restrict__ b,
-                                               const double* __restrict__ L, int C, double* __restrict__ red_rr,
-                                               double* __restrict__ red_rz) {
-    __shared__ double sh[kVT / 32];
-    const int c = blockIdx.x * kVT + threadIdx.x;
-    double rr = 0.0, rz = 0.0;
+                                               const double* __restrict__ b, const double* __restrict__ Minv, int C,
+                                               double* __restrict__ red_rr, double* __restrict__ red_rz) {
+    __shared__ double sh[kUT / 32];
+    __shared__ double rs[kUT];
+    const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
+    const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
+    const long long i = 9 * c + k;
+    double ri = 0.0;
     if (c < C) {
-        double rc[9], zc[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            rc[k] = b[9ll * c + k];
-            x[9ll * c + k] = 0.0;
-            r[9ll * c + k] = rc[k];
-            rr += rc[k] * rc[k];
-        }
-        precond_apply(L + 45ll * c, rc, zc);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            z[9ll * c + k] = zc[k];
-            p[9ll * c + k] = zc[k];
-            p32[9ll * c + k] = static_cast<float>(zc[k]);
-            rz += rc[k] * zc[k];
-        }
+        ri = b[i];
+        x[i] = 0.0;
+        r[i] = ri;
     }
-    const double a = block_sum<kVT>(rr, sh);
-    const double bb = block_sum<kVT>(rz, sh);
+    rs[threadIdx.x] = ri;
+    __syncthreads();
+    double rz = 0.0;
+    if (c < C) {
+        const double zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+        z[i] = zi;
+        p[i] = zi;
+        p32[i] = static_cast<float>(zi);
+        rz = ri * zi;
+    }
+    const double a = block_sum<kUT>(ri * ri, sh);
+    const double bb = block_sum<kUT>(rz, sh);
     if (threadIdx.x == 0) {
         red_rr[blockIdx.x] = a;
         red_rz[blockIdx.x] = bb;
@@ -442,9 +651,25 @@ __global__ void __launch_bounds__(256) sum_to_scalar(const double* __restrict__ 
     if (threadIdx.x == 0) sc[slot] = v;
 }
 
-__global__ void __launch_bounds__(kVT) axpy_kernel(double* __restrict__ y, const double* __restrict__ x, int n) {
+// Float-float split of y (hi, lo interleaved).
+__global__ void __launch_bounds__(kVT) split_kernel(const double* __restrict__ y, int n, float* __restrict__ yff) {
     const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < n) y[i] += x[i];
+    if (i < n) {
+        const ff f = ffa::from_double(y[i]);
+        reinterpret_cast<float2*>(yff)[i] = make_float2(f.hi, f.lo);
+    }
+}
+
+// y += x, and the float-float split of the new y (hi, lo interleaved).
+__global__ void __launch_bounds__(kVT) axpy_split_kernel(double* __restrict__ y, const double* __restrict__ x, int n,
+                                                        float* __restrict__ yff) {
+    const int i = blockIdx.x * kVT + threadIdx.x;
+    if (i < n) {
+        const double v = y[i] + x[i];
+        y[i] = v;
+        const ff f = ffa::from_double(v);
+        reinterpret_cast<float2*>(yff)[i] = make_float2(f.hi, f.lo);
+    }
 }
 
 // ---- block-Jacobi blocks S_cc = U_lambda,c - sum_{e in c} Jc^T (Jp V'^-1 Jp^T) Jc
@@ -452,7 +677,7 @@ __global__ void __launch_bounds__(kCT) sdiag_camera_pass(const int* __restrict__
                                                         const int* __restrict__ cchunk_cam,
                                                         const int* __restrict__ cam_off,
                                                         const int* __restrict__ cam_slots, const int* __restrict__ s_pt,
-                                                        const float* __restrict__ J32, const double* __restrict__ Vinv,
+                                                        const float* __restrict__ J32, const float* __restrict__ Vinv32,
                                                         double* __restrict__ part) {
     __shared__ double wpart[kCT / 32][45];
     const int k = blockIdx.x;
@@ -465,7 +690,7 @@ __global__ void __launch_bounds__(kCT) sdiag_camera_pass(const int* __restrict__
         const long long s = cam_slots[i];
         float J[24];
         load_j(J32, s, J);
-        const double* Vi = Vinv + 6ll * s_pt[s];
+        const float* Vi = Vinv32 + 6ll * s_pt[s];
         const float v00 = Vi[0], v10 = Vi[1], v11 = Vi[2], v20 = Vi[3], v21 = Vi[4], v22 = Vi[5];
         const float* Jp = J + 18;
         // M = Jp V^-1 (2x3), G = M Jp^T (2x2 symmetric)
@@ -499,8 +724,8 @@ __global__ void __launch_bounds__(kCT) sdiag_camera_pass(const int* __restrict__
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int t = 0; t < 45; ++t) {
-        const double v = warp_sum(static_cast<double>(acc[t]));
-        if (lane == 0) wpart[warp][t] = v;
+        const float v = warp_sum(acc[t]);
+        if (lane == 0) wpart[warp][t] = static_cast<double>(v);
     }
     __syncthreads();
     if (threadIdx.x < 45) {
@@ -529,11 +754,11 @@ __device__ void factor_block(const double* A, double* Lc) {
 }
 
 // Thread per camera: S_cc (full, FP64) and its packed Cholesky factor.
-__global__ void __launch_bounds__(kVT) sdiag_finalize(const int* __restrict__ cam_chunk_off,
+__global__ void __launch_bounds__(kCB) sdiag_finalize(const int* __restrict__ cam_chunk_off,
                                                      const double* __restrict__ part, const double* __restrict__ U,
                                                      double lambda, int C, double* __restrict__ Sdiag,
                                                      double* __restrict__ L) {
-    const int c = blockIdx.x * kVT + threadIdx.x;
+    const int c = blockIdx.x * kCB + threadIdx.x;
     if (c >= C) return;
     double A[81];
     const double* Uc = U + 81ll * c;
@@ -557,9 +782,9 @@ __global__ void __launch_bounds__(kVT) sdiag_finalize(const int* __restrict__ ca
 }
 
 // Block-Jacobi factors from stored diagonal blocks (the learned form's fallback).
-__global__ void __launch_bounds__(kVT) factor_blocks_kernel(const double* __restrict__ Sdiag, int C,
+__global__ void __launch_bounds__(kCB) factor_blocks_kernel(const double* __restrict__ Sdiag, int C,
                                                            double* __restrict__ L) {
-    const int c = blockIdx.x * kVT + threadIdx.x;
+    const int c = blockIdx.x * kCB + threadIdx.x;
     if (c >= C) return;
     double A[81];
 #pragma unroll
@@ -569,42 +794,56 @@ __global__ void __launch_bounds__(kVT) factor_blocks_kernel(const double* __rest
 
 }  // namespace
 
-// Implicit product partials for a given x (FP32 or FP64 arithmetic). x is in
-// the arithmetic type (FP32: the PCG direction copy; FP64: dc) or null (then
-// a = 1: the right-hand side). Partials in cam_part_ (9 per chunk).
+// Implicit product partials for a given x (FP32 or float-float arithmetic). x
+// is in the arithmetic type (FP32: the PCG direction copy; float-float: dc) or
+// null (then a = 1: the right-hand side). Partials in cam_part_ (9 per chunk).
 template <typename T>
 static void implicit_parts(Solver& s, const T* x, double a, const double* done) {
     T* u = reinterpret_cast<T*>(s.u_.get());
     const bool f32 = sizeof(T) == 4;
-    const T* vinv = f32 ? reinterpret_cast<const T*>(s.Vinv32_.get()) : reinterpret_cast<const T*>(s.Vinv_.get());
     cudaEvent_t ev = s.prof_start();
     schur_point_pass<T><<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
-                                                           s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(), vinv,
-                                                           s.bp_.get(), x, a, u, done);
+                                                           s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+                                                           s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
+                                                           u, done, BacksubOut{});
     GBA_LAUNCH_CHECK();
-    s.prof_stop(f32 ? "schur_point_pass_f32" : "schur_point_pass_f64", ev);
+    s.prof_stop(f32 ? "schur_point_pass_f32" : "schur_point_pass_ff", ev);
     if (s.n_cchunk_ > 0) {
         ev = s.prof_start();
         schur_camera_pass<T><<<s.n_cchunk_, kCT, 0, s.stream_>>>(s.cchunk_begin_.get(), s.cchunk_cam_.get(),
                                                                  s.cam_off_.get(), s.J32c_.get(), u,
                                                                  s.cam_part_.get(), done);
         GBA_LAUNCH_CHECK();
-        s.prof_stop(f32 ? "schur_camera_pass_f32" : "schur_camera_pass_f64", ev);
+        s.prof_stop(f32 ? "schur_camera_pass_f32" : "schur_camera_pass_ff", ev);
     }
+}
+
+// Mixed-form back-substitution: dc split to float-float, then the point pass
+// in back-substitution mode (dp, trial points, denominator partials per chunk).
+void mixed_back_substitute(Solver& s, double lambda, double* part) {
+    const int n = 9 * s.C_;
+    split_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, s.dcff_.get());
+    GBA_LAUNCH_CHECK();
+    schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
+        s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+        s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0, nullptr,
+        nullptr, BacksubOut{s.V_.get(), s.pts_.get(), lambda, s.dp_.get(), s.tpts_.get(), part});
+    GBA_LAUNCH_CHECK();
 }
 
 PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     PcgStats st;
     const int n = 9 * C_;
     const int nvb = ceil_div(n, kVT);   // vector blocks (element-wise kernels)
-    const int ncb = ceil_div(C_, kVT);  // camera blocks (per-camera kernels)
+    const int ncb = ceil_div(C_, kCB);  // camera blocks (thread-per-camera kernels)
+    const int nub = ceil_div(C_, kUC);  // camera blocks (nine-threads-per-camera kernels)
     double* red = red_part_.get();
     double* red2 = red_part_.get() + std::max(nvb, ncb) + 1;
     double* sc = pcg_s_.get();
     const double* done = sc + S_DONE;
 
-    // right-hand side, FP64 arithmetic
-    implicit_parts<double>(*this, static_cast<const double*>(nullptr), 1.0, nullptr);
+    // right-hand side, float-float arithmetic
+    implicit_parts<ff>(*this, static_cast<const ff*>(nullptr), 1.0, nullptr);
     rhs_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), bc_.get(), C_, rhs_.get(), red);
     GBA_LAUNCH_CHECK();
     sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
@@ -613,11 +852,11 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     // block-Jacobi blocks and factors (+ learned correction)
     if (n_cchunk_ > 0) {
         sdiag_camera_pass<<<n_cchunk_, kCT, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(), cam_off_.get(),
-                                                          cam_slots_.get(), s_pt_.get(), J32_.get(), Vinv_.get(),
+                                                          cam_slots_.get(), s_pt_.get(), J32_.get(), Vinv32_.get(),
                                                           cam_part_.get());
         GBA_LAUNCH_CHECK();
     }
-    sdiag_finalize<<<ncb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
+    sdiag_finalize<<<ncb, kCB, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
                                              Sdiag_.get(), Pfac_.get());
     GBA_LAUNCH_CHECK();
     if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
@@ -642,26 +881,26 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_). Returns the
     // iteration count; *ok = reached the inner tolerance without breakdown.
     auto inner_pcg = [&](bool* ok) -> long long {
-        pcg_init<<<ncb, kVT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
-                                           ref_r_.get(),
-                                           Pfac_.get(), C_, red, red2);
+        precond_inverse_kernel<<<nub, kUT, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
         GBA_LAUNCH_CHECK();
-        pcg_init_finalize<<<1, 256, 0, stream_>>>(red, red2, ncb, opts.pcg_tol, sc);
+        pcg_init<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
+                                           ref_r_.get(), Pinv_.get(), C_, red, red2);
         GBA_LAUNCH_CHECK();
+        pcg_init_finalize<<<1, 256, 0, stream_>>>(red, red2, nub, opts.pcg_tol, sc);
+        GBA_LAUNCH_CHECK();
+        // p.q partials (nvb) and r.r / r.z partials (nub) in disjoint ranges
+        double* red_pq = red2 + nub + 1;
         for (int it = 0; it < opts.pcg_max_iters; it += kCheck) {
             for (int j = 0; j < kCheck; ++j) {
                 implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
                 pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
-                                                         pcg_p_.get(), C_, pcg_q_.get(), red, sc);
+                                                         pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
                 GBA_LAUNCH_CHECK();
-                pcg_alpha<<<1, 256, 0, stream_>>>(red, nvb, sc);
+                pcg_update<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(),
+                                                     pcg_q_.get(), Pinv_.get(), C_, red_pq, nvb, red, red2, sc);
                 GBA_LAUNCH_CHECK();
-                pcg_update<<<ncb, kVT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(),
-                                                     pcg_q_.get(), Pfac_.get(), C_, red, red2, sc);
-                GBA_LAUNCH_CHECK();
-                pcg_beta<<<1, 256, 0, stream_>>>(red, red2, ncb, opts.pcg_max_iters, sc);
-                GBA_LAUNCH_CHECK();
-                pcg_p_update<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_p32_.get(), pcg_z_.get(), n, sc);
+                pcg_direction<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_p32_.get(), pcg_z_.get(), n, red, red2,
+                                                        nub, opts.pcg_max_iters, sc);
                 GBA_LAUNCH_CHECK();
             }
             double flag = 0.0;
@@ -705,7 +944,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
                 learned_choice_ = decisive ? 2 : 0;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
-                factor_blocks_kernel<<<ncb, kVT, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+                factor_blocks_kernel<<<ncb, kCB, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
                 GBA_LAUNCH_CHECK();
                 st.pcg_iterations += it_l;
                 it_count = it_bj;
@@ -718,7 +957,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             // Block-Jacobi judges the learned factors: an inner solve that breaks
             // down or misses its tolerance is redone with the plain blocks, which
             // then serve for the rest of this trial.
-            factor_blocks_kernel<<<ncb, kVT, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+            factor_blocks_kernel<<<ncb, kCB, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
             GBA_LAUNCH_CHECK();
             use_learned = false;
             ++st.fallbacks;
@@ -726,10 +965,10 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             it_count = inner_pcg(&ok);
         }
         const double iters = static_cast<double>(it_count);
-        // dc += e; FP64 residual r = rhs - S64 dc
-        axpy_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_x_.get(), n);
+        // dc += e; residual r = rhs - S dc in float-float products, FP64 sums
+        axpy_split_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_x_.get(), n, dcff_.get());
         GBA_LAUNCH_CHECK();
-        implicit_parts<double>(*this, static_cast<const double*>(dc_.get()), 0.0, nullptr);
+        implicit_parts<ff>(*this, reinterpret_cast<const ff*>(dcff_.get()), 0.0, nullptr);
         residual_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
                                                     dc_.get(), rhs_.get(), C_, ref_r_.get(), red);
         GBA_LAUNCH_CHECK();

@@ -149,8 +149,10 @@ public:
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
     DevBuf<float> J32_;
-    DevBuf<float> J32c_;    // mixed: Jc (18 + 2 pad) per slot in camera-major position (camera pass input)
+    DevBuf<float> J32c_;    // mixed: Jc (18 floats) per slot in camera-major position (camera pass input)
     DevBuf<float> Vinv32_;  // mixed: FP32 copy of V'^-1 (6 per point) for the FP32 matvec
+    DevBuf<float> Vinv32lo_;  // mixed: V'^-1 - Vinv32_ rounded to FP32 (float-float matvec)
+    DevBuf<float> dcff_;      // mixed: float-float copy of dc (hi, lo per entry) for the refinement residual
     DevBuf<float> pcg_p32_; // mixed: FP32 copy of the PCG direction for the FP32 matvec
     DevBuf<int> cam_pos_;   // camera-major position of each slot (inverse of cam_slots_)
     DevBuf<double> cam_pre_;  // per-camera rotation matrix, translation, intrinsics (16 per camera)
@@ -165,9 +167,10 @@ public:
     DevBuf<double> T_, S_, rhs_, dc_, dp_, red_part_;
     DevBuf<int> info_;
     // mixed Schur
-    DevBuf<double> Sdiag_, Pfac_;  // S diagonal blocks (81C), preconditioner factors (81C)
+    DevBuf<double> Sdiag_, Pfac_;  // S diagonal blocks (81C), preconditioner factors (packed, 45 per camera)
+    DevBuf<double> Pinv_;          // explicit preconditioner blocks M_c = (L L^T)^-1 (81C)
     DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_, judge_x_;
-    DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or FP64)
+    DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or float-float)
     DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
     DevBuf<float> mlp_stats_;  // learned form: per-camera track statistics (3 per camera)
     // Learned form, per solve: 0 = not judged yet, 1 = learned factors won the
@@ -196,6 +199,10 @@ void validate_problem(int C, int P, int E, const double* cams, const double* pts
                       const int* obs_pt, const double* obs_px);
 
 // Standalone kernels with raw device pointers (C-ABI entry points wrap these).
+// Mixed-form back-substitution (pcg.cu): dp, trial points and the point terms
+// of the gain denominator (one partial per point chunk in part).
+void mixed_back_substitute(Solver& s, double lambda, double* part);
+
 void launch_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n,
                                      cudaStream_t s);
 void launch_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, cudaStream_t s);

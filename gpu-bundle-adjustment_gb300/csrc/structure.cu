@@ -203,7 +203,9 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     dp_.alloc(3ull * P);
     sse_part_.alloc(std::max(n_pchunk_, 1));
     cam_part_.alloc(54ull * std::max(n_cchunk_, 1));
-    red_part_.alloc(std::max(n_pchunk_, ceil_div(P, 256)) + 2 * ceil_div(9ll * C, 256) + 64);
+    // block partials: the largest single reduction, or the PCG layout
+    // [r.r | r.z | p.q] = max(9C/256, C/32) + C/32 + 9C/256 (+ separators)
+    red_part_.alloc(std::max(n_pchunk_, ceil_div(P, 256)) + 2 * ceil_div(9ll * C, 256) + 2 * ceil_div(C, 32) + 64);
     if (form_ == SolverForm::Plain) {
         W_.alloc(27ull * E);
         JcR_.alloc(20ull * E);
@@ -216,14 +218,17 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         build_pairs();
     } else {
         J32_.alloc(24ull * E);
-        J32c_.alloc(20ull * E);
+        J32c_.alloc(18ull * E);
         judge_x_.alloc(9ull * C);
         Vinv32_.alloc(6ull * P);
+        Vinv32lo_.alloc(6ull * P);
+        dcff_.alloc(18ull * C);
         pcg_p32_.alloc(9ull * C);
         r_cur_.alloc(2ull * E);
         r_trial_.alloc(2ull * E);
         Sdiag_.alloc(81ull * C);
         Pfac_.alloc(81ull * C);
+        Pinv_.alloc(81ull * C);
         rhs_.alloc(9ull * C);
         pcg_x_.alloc(9ull * C);
         pcg_r_.alloc(9ull * C);

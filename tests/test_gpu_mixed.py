@@ -101,3 +101,64 @@ def test_mixed_huber_reaches_oracle_cost_workload1(gba, oracle):
     assert abs(res.initial_cost - ref["initial_cost"]) <= 1e-9 * ref["initial_cost"]
     assert res.anomalies == 0
     assert res.final_cost <= ref["final_cost"] * (1 + 1e-3)
+
+
+def _implicit_system(s, prob, lam):
+    """rhs and x -> S x of the mixed form's system, in numpy FP64 from the device's
+    own FP32 Jacobian records and FP64 U, V, bc, bp (the system the refinement solves)."""
+    C, P = prob.num_cameras, prob.num_points
+    J = s.download("J32").reshape(-1, 24).astype(np.float64)
+    order = s.download("order")
+    cam = prob.obs_camera[order]
+    pt = prob.obs_point[order]
+    Jc = J[:, :18].reshape(-1, 2, 9)
+    Jp = J[:, 18:].reshape(-1, 2, 3)
+    U = s.download("U").reshape(C, 9, 9)
+    Ud = np.diagonal(U, axis1=1, axis2=2)
+    Ul = U + lam * np.einsum("ci,ij->cij", np.where(Ud > 0, Ud, 1e-12), np.eye(9))
+    Vp = s.download("V").reshape(P, 6)
+    V = np.empty((P, 3, 3))
+    for k, (i, j) in enumerate([(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]):
+        V[:, i, j] = Vp[:, k]
+        V[:, j, i] = Vp[:, k]
+    for i in range(3):
+        d = V[:, i, i].copy()
+        V[:, i, i] += lam * np.where(d > 0, d, 1e-12)
+    Vinv = np.linalg.inv(V)
+    bc, bp = s.download("bc").reshape(C, 9), s.download("bp").reshape(P, 3)
+
+    def back(g):  # g (P,3) -> sum over slots of Jc^T Jp Vinv g, per camera
+        w = np.einsum("pij,pj->pi", Vinv, g)
+        u = np.einsum("sij,sj->si", Jp, w[pt])
+        out = np.zeros((C, 9))
+        np.add.at(out, cam, np.einsum("sri,sr->si", Jc, u))
+        return out
+
+    rhs = (bc - back(bp)).ravel()
+
+    def matvec(x):
+        x = x.reshape(C, 9)
+        t = np.einsum("sri,si->sr", Jc, x[cam])
+        g = np.zeros((P, 3))
+        np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
+        return (np.einsum("cij,cj->ci", Ul, x) - back(g)).ravel()
+
+    return rhs, matvec
+
+
+def test_float_float_refinement_residual_is_fp64_accurate(gba, small):
+    """The right-hand side and the refinement residual are computed in float-float
+    products with FP64 sums; checked here against numpy FP64 on the same system."""
+    lam = 1e-3
+    with gba.Solver(small, "mixed") as s:
+        s.accumulate()
+        assert s.damp_invert_v(lam) == 0
+        iters, steps, relres = s.schur_pcg(lam, refine_tol=1e-10, pcg_tol=1e-3, pcg_max_iters=500)
+        rhs_dev = s.download("rhs")[:9 * small.num_cameras]
+        dc = s.download("dc")
+        rhs, matvec = _implicit_system(s, small, lam)
+    assert rel_err(rhs_dev, rhs) < 1e-12
+    r = rhs - matvec(dc)
+    true_rel = np.linalg.norm(r) / np.linalg.norm(rhs)
+    assert relres <= 1e-10, relres
+    assert true_rel <= 2e-10, (true_rel, relres)
