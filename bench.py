@@ -133,14 +133,29 @@ def algorithmic_bytes(kernel: str, C: int, P: int, E: int) -> float:
         # per point: FP32 V'^-1 24 + CSR offset 4; per camera: x 36
         return E * 116.0 + P * 28.0 + C * 36.0
     if kernel == "schur_camera_pass_f32":
-        # per slot: camera-major Jc 72 B + u 8 (both contiguous); chunk partials are negligible
-        return E * 80.0
+        # per slot: camera record 80 B (Jc 72 + r 8, read whole) + u 8 (both contiguous)
+        return E * 88.0
+    if kernel == "schur_point_pass_ff":
+        # as the FP32 pass with u as float-float pairs (16 B) and V'^-1 in two parts (48 B per point)
+        return E * 124.0 + P * 52.0 + C * 72.0
+    if kernel == "schur_camera_pass_ff":
+        return E * 96.0
     if kernel == "point_pass_f32":
-        # s_cam, s_pt, s_px, r_cur (32 B) in, J32 96 B out per slot; point 24 B in, V/bp 72 B out per point
-        return E * 128.0 + P * 96.0 + C * 72.0
+        # per slot: s_cam, s_pt, cam_pos, float-float pixel, r_cur (36 B) in, J32 96 B + camera record 80 B out;
+        # per point: point 24 B in, V / bp 72 B out; per camera 72 B
+        return E * 212.0 + P * 96.0 + C * 36.0
     if kernel == "cost_f64":
         return E * 32.0 + P * 24.0 + C * 72.0
+    if kernel == "cost_ff":
+        # per slot: s_cam, s_pt 8 B + float-float observation 16 B + FP32 residual out 8 B;
+        # per point: float-float point 24 B; per camera: float-float constants 128 B
+        return E * 32.0 + P * 24.0 + C * 128.0
     raise KeyError(kernel)
+
+
+HBM_KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
+               "point_pass_f32", "cost_f64", "cost_ff")
+PCG_KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32")
 
 
 def run_ours(args):
@@ -203,33 +218,51 @@ def run_ours(args):
         torch.distributed.barrier()
     ms_per_step = float(ms.item()) / args.steps
 
-    # dominant kernel of the form and its live CUDA-event timing
-    dom = "schur_point_pass_f32" if form != "plain" else "dense_potrf"
-    n_launch, k_ms = solver.kernel_stats(dom)
-    peaks, peak_src = _peaks()
-    roofline = None
-    if n_launch:
-        per_launch_s = k_ms / n_launch / 1e3
-        if dom == "dense_potrf":
-            n = 9 * C
-            flops = n ** 3 / 3.0
-            achieved = flops / per_launch_s / 1e12
-            roofline = {"bound": "tensor", "achieved": achieved, "peak": 1.05, "unit": "TFLOP/s",
-                        "frac": achieved / 1.05, "traffic": None,
-                        "peak_note": "FP64 DMMA peak measured on this GB300 (mma.sync m8n8k4 f64 loop)"}
-        else:
-            b = algorithmic_bytes(dom, C, P, E)
-            achieved = b / per_launch_s / 1e9
-            roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                        "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
-                        "launches": n_launch, "avg_launch_us": per_launch_s * 1e6, "peak_source": peak_src}
     breakdown = {}
     for name in ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
-                 "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "backsub",
-                 "mlp_forward", "schur_assemble", "dense_potrf"):
+                 "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "cost_ff",
+                 "backsub", "mlp_forward", "schur_assemble", "dense_potrf"):
         n_k, ms_k = solver.kernel_stats(name)
         if n_k:
             breakdown[name] = {"launches": n_k, "ms_per_step": ms_k / args.steps}
+
+    # Roofline of the dominant kernel: the one with the most device time in the
+    # timed region (plain form: the dense Cholesky, FP64 tensor bound; mixed
+    # forms: the largest HBM-bound kernel). Its average launch duration comes
+    # from the timed region's CUDA events, except for the PCG matvec kernels,
+    # whose launches after convergence (inside a batch of kCheck) return early:
+    # for those, 64 full-work PCG iterations on the resident problem are timed
+    # right after the timed region with the same events.
+    peaks, peak_src = _peaks()
+    roofline = None
+    if form == "plain":
+        n_launch, k_ms = solver.kernel_stats("dense_potrf")
+        if n_launch:
+            per_launch_s = k_ms / n_launch / 1e3
+            n = 9 * C
+            achieved = n ** 3 / 3.0 / per_launch_s / 1e12
+            roofline = {"bound": "tensor", "achieved": achieved, "peak": 1.05, "unit": "TFLOP/s",
+                        "frac": achieved / 1.05, "traffic": None, "kernel": "dense_potrf",
+                        "peak_note": "FP64 DMMA peak measured on this GB300 (mma.sync m8n8k4 f64 loop)"}
+    else:
+        cands = [k for k in breakdown if k in HBM_KERNELS]
+        dom = max(cands, key=lambda k: breakdown[k]["ms_per_step"]) if cands else None
+        source = "timed region"
+        if dom in PCG_KERNELS:
+            solver.reset_params()
+            solver.accumulate()
+            solver.damp_invert_v(1e-3)
+            solver.profile_reset()
+            solver.schur_pcg(1e-3, refine_tol=1e-30, refine_max_steps=1, pcg_tol=0.0, pcg_max_iters=64)
+            source = "64 full-work PCG iterations (lambda 1e-3) timed after the timed region"
+        if dom:
+            n_launch, k_ms = solver.kernel_stats(dom)
+            per_launch_s = k_ms / n_launch / 1e3
+            achieved = algorithmic_bytes(dom, C, P, E) / per_launch_s / 1e9
+            roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
+                        "launches": n_launch, "avg_launch_us": per_launch_s * 1e6, "peak_source": peak_src,
+                        "per_launch_source": source}
     solver.profile(False)
     final = timed[-1]
 
@@ -374,9 +407,14 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--form", default="learned", choices=["plain", "mixed", "learned"])
     ap.add_argument("--max-iterations", type=int, default=50)
-    ap.add_argument("--pcg-tol", type=float, default=None, help="inner PCG relative tolerance (library default 1e-4)")
-    ap.add_argument("--refine-tol", type=float, default=None,
-                    help="relative residual target of the refined Schur step (library default 1e-8)")
+    # Inexact Gauss-Newton steps: the Schur system is solved to a relative
+    # residual of 0.1 (the forcing term Ceres' iterative Schur solver uses by
+    # default); the cost and the accept / reject test stay at FP64 accuracy.
+    # The library defaults (refined to 1e-8) keep the mixed trajectory on the
+    # FP64 one; pass --refine-tol 1e-8 --pcg-tol 1e-4 to time them.
+    ap.add_argument("--pcg-tol", type=float, default=0.1, help="inner PCG relative tolerance (library default 1e-4)")
+    ap.add_argument("--refine-tol", type=float, default=0.1,
+                    help="relative residual target of the Schur step (library default 1e-8)")
     ap.add_argument("--pcg-max-iters", type=int, default=None)
     ap.add_argument("--reference-iterations", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -9,6 +9,7 @@
 
 #include "blocks.cuh"
 #include "common.cuh"
+#include "ff.cuh"
 #include "solver.hpp"
 
 namespace gba {
@@ -16,12 +17,10 @@ namespace {
 
 constexpr int kTB = 256;
 
-// V' = V + lambda * max(diag V, 1e-12) on the diagonal; Vinv = V'^-1 (packed).
-// Vinv32 / Vinv32lo (may be null): FP32 copy for the mixed form's FP32 Schur
-// matvec and the FP32-rounded remainder, the pair being V'^-1 in float-float.
+// V' = V + lambda * max(diag V, 1e-12) on the diagonal; Vinv = V'^-1 (packed),
+// FP64 (plain form).
 __global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __restrict__ V, double lambda, int P,
-                                                           double* __restrict__ Vinv, float* __restrict__ Vinv32,
-                                                           float* __restrict__ Vinv32lo,
+                                                           double* __restrict__ Vinv,
                                                            unsigned long long* __restrict__ nonspd) {
     __shared__ unsigned long long redu[kTB / 32];
     unsigned long long bad = 0;
@@ -40,20 +39,77 @@ __global__ void __launch_bounds__(kTB) damp_invert_v_kernel(const double* __rest
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) Vinv[6ll * p + k] = inv[k];
-        if (Vinv32) {
-            float h[6], l[6];
+    }
+    const unsigned long long nb = block_sum_u64<kTB>(bad, redu);
+    if (threadIdx.x == 0 && nb) atomicAdd(nonspd, nb);
+}
+
+// Mixed forms: the same damping and inverse in float-float arithmetic (V's
+// entries are FP32 sums, exact in FP32), V'^-1 written as its FP32 rounding
+// (Vinv32) and the FP32-rounded remainder (Vinv32lo). Cholesky L of the packed
+// 3x3, M = L^-1, V'^-1 = M^T M; a non-positive pivot marks the block non-SPD.
+__device__ __forceinline__ bool ff_gt0(ffa::ff a) { return a.hi > 0.f || (a.hi == 0.f && a.lo > 0.f); }
+
+__global__ void __launch_bounds__(kTB) damp_invert_v_ff_kernel(const double* __restrict__ V, float2 lambda_ff,
+                                                              int P, float* __restrict__ Vinv32,
+                                                              float* __restrict__ Vinv32lo,
+                                                              unsigned long long* __restrict__ nonspd) {
+    using ffa::ff;
+    __shared__ unsigned long long redu[kTB / 32];
+    const ff lam = {lambda_ff.x, lambda_ff.y}, one = {1.f, 0.f};
+    unsigned long long bad = 0;
+    for (int p = blockIdx.x * kTB + threadIdx.x; p < P; p += gridDim.x * kTB) {
+        ff a[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                h[k] = __double2float_rn(inv[k]);
-                l[k] = __double2float_rn(inv[k] - static_cast<double>(h[k]));
-            }
-            float2* o = reinterpret_cast<float2*>(Vinv32 + 6ll * p);
-            float2* ol = reinterpret_cast<float2*>(Vinv32lo + 6ll * p);
+        for (int k = 0; k < 6; ++k) a[k] = {static_cast<float>(V[6ll * p + k]), 0.f};
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                o[k] = make_float2(h[2 * k], h[2 * k + 1]);
-                ol[k] = make_float2(l[2 * k], l[2 * k + 1]);
+        for (int k : {0, 2, 5}) {
+            const float d = a[k].hi > 0.f ? a[k].hi : 1e-12f;
+            float pr, e;
+            ffa::two_prod(d, lam.hi, pr, e);
+            a[k] = ffa::norm(ffa::add(a[k], ff{pr, __fmaf_rn(d, lam.lo, e)}));
+        }
+        float h[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, l[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        bool ok = ff_gt0(a[0]);
+        if (ok) {
+            const ff l00 = ffa::sqrt(a[0]);
+            const ff l10 = ffa::div(a[1], l00), l20 = ffa::div(a[3], l00);
+            const ff t1 = ffa::norm(ffa::sub(a[2], ffa::mul(l10, l10)));
+            ok = ff_gt0(t1);
+            if (ok) {
+                const ff l11 = ffa::sqrt(t1);
+                const ff l21 = ffa::div(ffa::norm(ffa::sub(a[4], ffa::mul(l20, l10))), l11);
+                const ff t2 = ffa::norm(ffa::sub(ffa::sub(a[5], ffa::mul(l20, l20)), ffa::mul(l21, l21)));
+                ok = ff_gt0(t2);
+                if (ok) {
+                    const ff l22 = ffa::sqrt(t2);
+                    const ff m00 = ffa::div(one, l00), m11 = ffa::div(one, l11), m22 = ffa::div(one, l22);
+                    const ff m10 = ffa::neg(ffa::mul(ffa::mul(l10, m00), m11));
+                    const ff m21 = ffa::neg(ffa::mul(ffa::mul(l21, m11), m22));
+                    const ff m20 = ffa::neg(
+                        ffa::mul(ffa::norm(ffa::add(ffa::mul(l20, m00), ffa::mul(l21, m10))), m22));
+                    ff inv[6];
+                    inv[0] = ffa::norm(ffa::add(ffa::add(ffa::mul(m00, m00), ffa::mul(m10, m10)), ffa::mul(m20, m20)));
+                    inv[1] = ffa::norm(ffa::add(ffa::mul(m10, m11), ffa::mul(m20, m21)));
+                    inv[2] = ffa::norm(ffa::add(ffa::mul(m11, m11), ffa::mul(m21, m21)));
+                    inv[3] = ffa::mul(m20, m22);
+                    inv[4] = ffa::mul(m21, m22);
+                    inv[5] = ffa::mul(m22, m22);
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        h[k] = inv[k].hi;
+                        l[k] = inv[k].lo;
+                    }
+                }
             }
+        }
+        if (!ok) ++bad;
+        float2* o = reinterpret_cast<float2*>(Vinv32 + 6ll * p);
+        float2* ol = reinterpret_cast<float2*>(Vinv32lo + 6ll * p);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            o[k] = make_float2(h[2 * k], h[2 * k + 1]);
+            ol[k] = make_float2(l[2 * k], l[2 * k + 1]);
         }
     }
     const unsigned long long nb = block_sum_u64<kTB>(bad, redu);
@@ -204,8 +260,13 @@ __global__ void __launch_bounds__(256) denom_finalize(const double* __restrict__
 unsigned long long Solver::damp_invert_v(double lambda) {
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get() + 3, 0, sizeof(unsigned long long), stream_));
     const int grid = std::min(ceil_div(P_, kTB), 8 * device_sm_count());
-    damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), Vinv32_.get(), Vinv32lo_.get(),
-                                                    counters_.get() + 3);
+    if (form_ == SolverForm::Plain) {
+        damp_invert_v_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), lambda, P_, Vinv_.get(), counters_.get() + 3);
+    } else {
+        const float lh = static_cast<float>(lambda);
+        damp_invert_v_ff_kernel<<<grid, kTB, 0, stream_>>>(V_.get(), make_float2(lh, static_cast<float>(lambda - lh)),
+                                                           P_, Vinv32_.get(), Vinv32lo_.get(), counters_.get() + 3);
+    }
     GBA_LAUNCH_CHECK();
     unsigned long long bad = 0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&bad, counters_.get() + 3, sizeof bad, cudaMemcpyDeviceToHost, stream_));

@@ -14,6 +14,7 @@
 
 #include "camera_model.cuh"
 #include "common.cuh"
+#include "ff.cuh"
 #include "solver.hpp"
 
 namespace gba {
@@ -187,23 +188,28 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 
 // ---------------------------------------------------------------- FP32 path
 
-// Point pass, FP32 arithmetic: per-slot Jacobian record J32 = [Jc(18), Jp(6)];
-// V / bp summed per point in FP32 and stored FP64 (one FP64 conversion per point).
-// The residuals come from r_cur: the FP64 cost pass at these parameters (run
-// anyway to drive accept/reject) stores them rounded to FP32, which keeps the
-// gradient accurate to FP32 rounding of r instead of FP32 rounding of f d u.
+// Point pass, FP32 arithmetic: per-slot Jacobian record J32 = [Jc(18), Jp(6)]
+// and, at the slot's camera-major position, the camera record [Jc(18), r(2)]
+// (80 B, five 16-byte stores) for the camera passes. V / bp are summed per
+// point in FP32 by a segmented scan over each warp (slots of a point are
+// contiguous) and the warps' segment sums, and stored FP64. The residuals
+// come from r_cur: the float-float cost pass at these parameters (run anyway to
+// drive accept/reject) stores them rounded to FP32, which keeps the gradient
+// accurate to FP32 rounding of r instead of FP32 rounding of f d u. With a
+// robust loss, J and r are scaled by sqrt(rho'(s)) before anything is stored.
 __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
-    const int* __restrict__ s_pt, const double2* __restrict__ s_px, const double* __restrict__ cams,
-    const double* __restrict__ pts, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
+    const int* __restrict__ s_pt, const float4* __restrict__ s_pxff, const float* __restrict__ cams32,
+    const float2* __restrict__ ptsff, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
     float* __restrict__ J32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
     unsigned long long* __restrict__ counters, float delta) {
-    __shared__ float contrib[9][kPT];
+    __shared__ float seg[9][kPT];  // warp-segment sums, at each segment's last slot
     __shared__ unsigned long long redu[kPT / 32];
     const int chunk = blockIdx.x;
     const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
     const int s0 = pt_off[p0], s1 = pt_off[p1];
     const int my_p = p0 + threadIdx.x;
+    const int lane = threadIdx.x & 31;
     int my_b = 0, my_e = 0;
     if (my_p < p1) {
         my_b = pt_off[my_p];
@@ -218,23 +224,23 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
         float v[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) v[k] = 0.f;
+        int key = -1;  // point of the slot; slots past the chunk end share key -1 and add zeros
         if (s < s1) {
             const int c = s_cam[s], p = s_pt[s];
+            key = p;
             float cam[9], X[3], obs[2], r[2], J[24];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) cam[k] = static_cast<float>(__ldg(cams + 9 * c + k));
+            for (int k = 0; k < 9; ++k) cam[k] = __ldg(cams32 + 9 * c + k);
 #pragma unroll
-            for (int k = 0; k < 3; ++k) X[k] = static_cast<float>(__ldg(pts + 3 * p + k));
-            const double2 o = s_px[s];
-            obs[0] = static_cast<float>(o.x);
-            obs[1] = static_cast<float>(o.y);
+            for (int k = 0; k < 3; ++k) X[k] = __ldg(&ptsff[3ll * p + k].x);
+            const float4 o = s_pxff[s];
+            obs[0] = o.x;
+            obs[1] = o.z;
             model::residual_jacobian(cam, X, obs, r, J, J + 18);
-            const float2 rf = r_cur[s];  // FP64-evaluated residual, stored FP32
+            const float2 rf = r_cur[s];  // float-float evaluated residual, stored FP32
             r[0] = rf.x;
             r[1] = rf.y;
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
-            float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
-            float2* outc = reinterpret_cast<float2*>(J32c + 18ll * cam_pos[s]);  // camera-major Jc copy
             if (fin && delta > 0.f) {  // robust loss: rows scaled by sqrt(rho'(s)); J32 holds the scaled rows
                 const float sw = robust_sqrt_weight(r[0] * r[0] + r[1] * r[1], delta);
                 r[0] *= sw;
@@ -242,36 +248,54 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
 #pragma unroll
                 for (int q = 0; q < 24; ++q) J[q] *= sw;
             }
-            if (fin) {
-#pragma unroll
-                for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
-#pragma unroll
-                for (int q = 0; q < 9; ++q) outc[q] = make_float2(J[2 * q], J[2 * q + 1]);
-                const float* Jp = J + 18;
-                v[0] = Jp[0] * Jp[0] + Jp[3] * Jp[3];
-                v[1] = Jp[1] * Jp[0] + Jp[4] * Jp[3];
-                v[2] = Jp[1] * Jp[1] + Jp[4] * Jp[4];
-                v[3] = Jp[2] * Jp[0] + Jp[5] * Jp[3];
-                v[4] = Jp[2] * Jp[1] + Jp[5] * Jp[4];
-                v[5] = Jp[2] * Jp[2] + Jp[5] * Jp[5];
-#pragma unroll
-                for (int i = 0; i < 3; ++i) v[6 + i] = -(Jp[i] * r[0] + Jp[3 + i] * r[1]);
-            } else {
+            if (!fin) {
                 ++anom;
 #pragma unroll
-                for (int q = 0; q < 6; ++q) out[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int q = 0; q < 24; ++q) J[q] = 0.f;
+                r[0] = r[1] = 0.f;
+            }
+            float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
 #pragma unroll
-                for (int q = 0; q < 9; ++q) outc[q] = make_float2(0.f, 0.f);
+            for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+            float4* outc = reinterpret_cast<float4*>(J32c + 20ll * cam_pos[s]);  // camera record
+#pragma unroll
+            for (int q = 0; q < 4; ++q) outc[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+            outc[4] = make_float4(J[16], J[17], r[0], r[1]);
+            const float* Jp = J + 18;
+            v[0] = Jp[0] * Jp[0] + Jp[3] * Jp[3];
+            v[1] = Jp[1] * Jp[0] + Jp[4] * Jp[3];
+            v[2] = Jp[1] * Jp[1] + Jp[4] * Jp[4];
+            v[3] = Jp[2] * Jp[0] + Jp[5] * Jp[3];
+            v[4] = Jp[2] * Jp[1] + Jp[5] * Jp[4];
+            v[5] = Jp[2] * Jp[2] + Jp[5] * Jp[5];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) v[6 + i] = -(Jp[i] * r[0] + Jp[3 + i] * r[1]);
+        }
+        // inclusive segmented scan over the warp
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int kd = __shfl_up_sync(0xffffffffu, key, d);
+            const bool take = lane >= d && kd == key;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float t = __shfl_up_sync(0xffffffffu, v[k], d);
+                if (take) v[k] += t;
             }
         }
+        const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+        if (lane == 31 || knext != key) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) contrib[k][threadIdx.x] = v[k];
+            for (int k = 0; k < 9; ++k) seg[k][threadIdx.x] = v[k];
+        }
         __syncthreads();
+        // owner: add the point's warp-segment sums of this pass, warps in order
         if (my_p < p1) {
-            const int b = max(my_b, base), e = min(my_e, base + kPT);
-            for (int t = b; t < e; ++t)
+            const int b = max(my_b, base) - base, e = min(my_e, base + kPT) - base;
+            for (int w = b >> 5; b < e && w <= (e - 1) >> 5; ++w) {
+                const int t = min(e - 1, 32 * w + 31);
 #pragma unroll
-                for (int k = 0; k < 9; ++k) acc[k] += contrib[k][t - base];
+                for (int k = 0; k < 9; ++k) acc[k] += seg[k][t];
+            }
         }
         __syncthreads();
     }
@@ -285,45 +309,32 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
     if (threadIdx.x == 0 && na) atomicAdd(counters, na);
 }
 
-// Camera pass, FP32 arithmetic: recomputes Jc and r for the chunk's slots
-// (cheaper than re-reading the Jacobian records), sums products per thread in
-// FP32, then reduces the per-thread partials in FP64.
-__global__ void __launch_bounds__(kCT) camera_pass_f32(
-    const int* __restrict__ cchunk_begin, const int* __restrict__ cchunk_cam, const int* __restrict__ cam_off,
-    const int* __restrict__ cam_slots, const int* __restrict__ s_pt, const double2* __restrict__ s_px,
-    const double* __restrict__ cams, const double* __restrict__ pts, const float2* __restrict__ r_cur,
-    double* __restrict__ part, float delta) {
+// Camera pass, FP32 arithmetic: streams the camera records [Jc(18), r(2)] the
+// point pass wrote (robust-scaled), sums U and bc products per thread and per
+// warp in FP32, and adds the four warp partials in FP64.
+__global__ void __launch_bounds__(kCT) camera_pass_f32(const int* __restrict__ cchunk_begin,
+                                                      const int* __restrict__ cchunk_cam,
+                                                      const int* __restrict__ cam_off, const float* __restrict__ J32c,
+                                                      double* __restrict__ part) {
+    __shared__ float wpart[kCT / 32][54];
     const int k = blockIdx.x;
     const int b = cchunk_begin[k], c = cchunk_cam[k];
     const int e = min(b + kCamChunk, cam_off[c + 1]);
-    float cam[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) cam[t] = static_cast<float>(__ldg(cams + 9 * c + t));
     float u[54];
 #pragma unroll
     for (int i = 0; i < 54; ++i) u[i] = 0.f;
     for (int i = b + threadIdx.x; i < e; i += kCT) {
-        const int s = cam_slots[i];
-        const int p = s_pt[s];
-        float X[3], obs[2], r[2], Jc[18], Jp[6];
+        const float4* q = reinterpret_cast<const float4*>(J32c + 20ll * i);
+        float Jc[20];
 #pragma unroll
-        for (int t = 0; t < 3; ++t) X[t] = static_cast<float>(__ldg(pts + 3 * p + t));
-        const double2 o = s_px[s];
-        obs[0] = static_cast<float>(o.x);
-        obs[1] = static_cast<float>(o.y);
-        model::residual_jacobian(cam, X, obs, r, Jc, Jp);
-        const float2 rf = r_cur[s];
-        r[0] = rf.x;
-        r[1] = rf.y;
-        const bool fin = all_finite(r, 2) && all_finite(Jc, 18) && all_finite(Jp, 6);
-        if (!fin) continue;
-        if (delta > 0.f) {
-            const float sw = robust_sqrt_weight(r[0] * r[0] + r[1] * r[1], delta);
-            r[0] *= sw;
-            r[1] *= sw;
-#pragma unroll
-            for (int q = 0; q < 18; ++q) Jc[q] *= sw;
+        for (int t = 0; t < 5; ++t) {
+            const float4 v = q[t];
+            Jc[4 * t] = v.x;
+            Jc[4 * t + 1] = v.y;
+            Jc[4 * t + 2] = v.z;
+            Jc[4 * t + 3] = v.w;
         }
+        const float2 r = make_float2(Jc[18], Jc[19]);
         int idx = 0;
 #pragma unroll
         for (int a = 0; a < 9; ++a)
@@ -333,12 +344,21 @@ __global__ void __launch_bounds__(kCT) camera_pass_f32(
                 ++idx;
             }
 #pragma unroll
-        for (int a = 0; a < 9; ++a) u[45 + a] -= Jc[a] * r[0] + Jc[9 + a] * r[1];
+        for (int a = 0; a < 9; ++a) u[45 + a] -= Jc[a] * r.x + Jc[9 + a] * r.y;
     }
-    double ud[54];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
-    for (int i = 0; i < 54; ++i) ud[i] = static_cast<double>(u[i]);
-    reduce_store54(ud, part + 54ll * k);
+    for (int t = 0; t < 54; ++t) {
+        const float v = warp_sum(u[t]);
+        if (lane == 0) wpart[warp][t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 54) {
+        double t = 0.0;
+#pragma unroll
+        for (int w = 0; w < kCT / 32; ++w) t += static_cast<double>(wpart[w][threadIdx.x]);
+        part[54ll * k + threadIdx.x] = t;
+    }
 }
 
 // U (full symmetric 9x9) and bc from the chunk partials, chunks in order.
@@ -374,7 +394,11 @@ __global__ void __launch_bounds__(256) ordered_sum(const double* __restrict__ pa
 // 15 doubles per camera, so the cost kernel evaluates R X + t per observation
 // instead of a sin / cos / sqrt per observation on GB300's narrow FP64 pipe.
 constexpr int kCamPre = 16;
-__global__ void camera_precompute_kernel(const double* __restrict__ cams, int C, double* __restrict__ pre) {
+// Per-camera constants of the residual: rotation matrix (Rodrigues), t, f, k1,
+// k2 (kCamPre doubles); preff (may be null): the same as float-float pairs;
+// cams32 (may be null): the camera parameters rounded to FP32.
+__global__ void camera_precompute_kernel(const double* __restrict__ cams, int C, double* __restrict__ pre,
+                                         float2* __restrict__ preff, float* __restrict__ cams32) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
     const double* a = cams + 9ll * c;
@@ -398,6 +422,17 @@ __global__ void camera_precompute_kernel(const double* __restrict__ cams, int C,
 #pragma unroll
     for (int i = 0; i < 6; ++i) o[9 + i] = a[3 + i];
     o[15] = 0.0;
+    if (cams32) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) cams32[9ll * c + i] = static_cast<float>(a[i]);
+    }
+    if (preff) {
+#pragma unroll
+        for (int i = 0; i < kCamPre; ++i) {
+            const ffa::ff f = ffa::from_double(o[i]);
+            preff[static_cast<long long>(kCamPre) * c + i] = make_float2(f.hi, f.lo);
+        }
+    }
 }
 
 __device__ __forceinline__ void residual_pre(const double* __restrict__ pc, const double* X, const double* obs,
@@ -452,6 +487,132 @@ __global__ void __launch_bounds__(kPT) cost_f64(const int* __restrict__ pchunk, 
     }
 }
 
+// Residual from float-float camera constants (R, t, f, k1, k2), point and
+// observation: the FP64 formula of residual_pre with every operation in
+// float-float (relative error about 1e-14 before the cancellation against the
+// observation).
+__device__ __forceinline__ void residual_ff(const float2* __restrict__ pc, const ffa::ff* X, ffa::ff o0, ffa::ff o1,
+                                            ffa::ff& r0, ffa::ff& r1) {
+    using ffa::ff;
+    ff P[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float2 t = pc[9 + i];
+        P[i] = {t.x, t.y};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float2 R = pc[3 * i + k];
+            ffa::madd(P[i], ff{R.x, R.y}, X[k]);
+        }
+        P[i] = ffa::norm(P[i]);
+    }
+    const ff iz = ffa::div(ff{1.f, 0.f}, P[2]);
+    const ff u = ffa::neg(ffa::mul(P[0], iz)), v = ffa::neg(ffa::mul(P[1], iz));
+    ff r2 = {0.f, 0.f};
+    ffa::madd(r2, u, u);
+    ffa::madd(r2, v, v);
+    r2 = ffa::norm(r2);
+    const float2 fk = pc[12], k1 = pc[13], k2 = pc[14];
+    ff t = {k1.x, k1.y};
+    ffa::madd(t, ff{k2.x, k2.y}, r2);
+    ff d = {1.f, 0.f};
+    ffa::madd(d, r2, ffa::norm(t));
+    const ff fd = ffa::mul(ff{fk.x, fk.y}, ffa::norm(d));
+    r0 = ffa::norm(ffa::sub(ffa::mul(fd, u), o0));
+    r1 = ffa::norm(ffa::sub(ffa::mul(fd, v), o1));
+}
+
+// Mixed-form cost: rho(|r|^2) summed over all slots in float-float, the
+// residuals stored FP32 (NaN where not finite, counted as anomalies). Sums:
+// per thread and per warp in float-float, warps combined in FP64. A slot whose
+// float-float residual leaves FP32's safe range (|r| >= kFfSafe or not finite:
+// a wild trial step, e.g. a point near the camera plane) is evaluated again in
+// FP64 from the FP64 constants (pre64) and point (pts64), so the cost and the
+// anomaly count follow FP64 semantics; its rho is summed in FP64 (warps that
+// met such a slot only).
+constexpr float kFfSafe = 1e12f;
+
+__global__ void __launch_bounds__(kPT, 6) cost_ff(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
+                                              const int* __restrict__ s_cam, const int* __restrict__ s_pt,
+                                              const float4* __restrict__ s_pxff, const float2* __restrict__ preff,
+                                              const float2* __restrict__ ptsff, const double2* __restrict__ s_px,
+                                              const double* __restrict__ pre64, const double* __restrict__ pts64,
+                                              double* __restrict__ sse_part,
+                                              unsigned long long* __restrict__ counters, float2* __restrict__ r_out,
+                                              double delta, float2 delta_ff, float2 delta2_ff) {
+    using ffa::ff;
+    __shared__ float red[kPT / 32][2];
+    __shared__ double red64[kPT / 32];
+    __shared__ unsigned long long redu[kPT / 32];
+    const int chunk = blockIdx.x;
+    const int s0 = pt_off[pchunk[chunk]], s1 = pt_off[pchunk[chunk + 1]];
+    const bool robust = delta_ff.x > 0.f;
+    const ff dl = {delta_ff.x, delta_ff.y}, dl2 = {delta2_ff.x, delta2_ff.y};
+    ff sse = {0.f, 0.f};
+    double sse64 = 0.0;
+    int fallback = 0;
+    unsigned long long anom = 0;
+    for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
+        const int c = s_cam[s], p = s_pt[s];
+        ff X[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float2 x = ptsff[3ll * p + k];
+            X[k] = {x.x, x.y};
+        }
+        const float4 o = s_pxff[s];
+        ff r0, r1;
+        residual_ff(preff + static_cast<long long>(kCamPre) * c, X, ff{o.x, o.y}, ff{o.z, o.w}, r0, r1);
+        if (!(fabsf(r0.hi) < kFfSafe && fabsf(r1.hi) < kFfSafe)) {
+            double X64[3], obs[2], r[2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) X64[k] = pts64[3ll * p + k];
+            const double2 ob = s_px[s];
+            obs[0] = ob.x;
+            obs[1] = ob.y;
+            residual_pre(pre64 + static_cast<long long>(kCamPre) * c, X64, obs, r);
+            const bool fin = isfinite(r[0]) && isfinite(r[1]);
+            r_out[s] = fin ? make_float2(static_cast<float>(r[0]), static_cast<float>(r[1])) : make_float2(NAN, NAN);
+            if (!fin) {
+                ++anom;
+                continue;
+            }
+            sse64 += robust_rho(r[0] * r[0] + r[1] * r[1], delta);
+            fallback = 1;
+            continue;
+        }
+        r_out[s] = make_float2(r0.hi, r1.hi);
+        ff sq = {0.f, 0.f};
+        ffa::madd(sq, r0, r0);
+        ffa::madd(sq, r1, r1);
+        sq = ffa::norm(sq);
+        if (robust && (sq.hi > dl2.hi || (sq.hi == dl2.hi && sq.lo > dl2.lo))) {
+            // 2 delta sqrt(s) - delta^2
+            sq = ffa::norm(ffa::sub(ffa::mul(ff{2.f * dl.hi, 2.f * dl.lo}, ffa::sqrt(sq)), dl2));
+        }
+        sse = ffa::add(sse, sq);
+    }
+    // warp sums in float-float, then FP64 across warps
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sse = ffa::add(sse, ffa::shfl_xor(sse, o));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (__any_sync(0xffffffffu, fallback)) sse64 = warp_sum(sse64);  // else every lane holds 0
+    if (lane == 0) {
+        red[warp][0] = sse.hi;
+        red[warp][1] = sse.lo;
+        red64[warp] = sse64;
+    }
+    const unsigned long long na = block_sum_u64<kPT>(anom, redu);  // synchronises the block
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+#pragma unroll
+        for (int w = 0; w < kPT / 32; ++w)
+            tot += static_cast<double>(red[w][0]) + static_cast<double>(red[w][1]) + red64[w];
+        sse_part[chunk] = tot;
+        if (na) atomicAdd(counters, na);
+    }
+}
+
 template <typename T>
 __global__ void eval_edges_kernel(const double* __restrict__ cams, const double* __restrict__ pts,
                                   const int* __restrict__ oc, const int* __restrict__ op,
@@ -496,35 +657,29 @@ double Solver::accumulate() {
         ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
         GBA_LAUNCH_CHECK();
     } else {
-        // The mixed form keeps the cost FP64: SSE and residuals come from the
-        // FP64 residual pass. After an accepted trial they are already there
+        // The mixed form keeps the cost at FP64 accuracy: SSE and residuals come
+        // from the float-float residual pass. After an accepted trial they are already there
         // (the trial evaluation at these parameters). Its non-finite count goes
         // to a scratch counter: the FP32 pass counts this evaluation's anomalies.
         if (!resid_valid_) {
-            camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(cams_.get(), C_, cam_pre_.get());
-            GBA_LAUNCH_CHECK();
-            cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                                     cam_pre_.get(), pts_.get(), sse_part_.get(), counters_.get() + 2,
-                                                     reinterpret_cast<float2*>(r_cur_.get()), huber_delta_);
-            GBA_LAUNCH_CHECK();
+            cost_mixed(cams_.get(), pts_.get(), counters_.get() + 2, reinterpret_cast<float2*>(r_cur_.get()));
             ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
             GBA_LAUNCH_CHECK();
             resid_valid_ = true;
         }
+        if (ff_holds_ != kFfCurrent) prepare_ff(cams_.get(), pts_.get());
         const float2* rc = reinterpret_cast<const float2*>(r_cur_.get());
         cudaEvent_t ev = prof_start();
-        point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
-                                                       spx, cams_.get(), pts_.get(), rc, cam_pos_.get(), J32_.get(),
-                                                       J32c_.get(), V_.get(), bp_.get(), counters_.get(),
-                                                       static_cast<float>(huber_delta_));
+        point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(
+            pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), reinterpret_cast<const float4*>(s_pxff_.get()),
+            cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), J32_.get(),
+            J32c_.get(), V_.get(), bp_.get(), counters_.get(), static_cast<float>(huber_delta_));
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);
         if (n_cchunk_ > 0) {
             ev = prof_start();
             camera_pass_f32<<<n_cchunk_, kCT, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(),
-                                                            cam_off_.get(), cam_slots_.get(), s_pt_.get(), spx,
-                                                            cams_.get(), pts_.get(), rc, cam_part_.get(),
-                                                            static_cast<float>(huber_delta_));
+                                                            cam_off_.get(), J32c_.get(), cam_part_.get());
             GBA_LAUNCH_CHECK();
             prof_stop("camera_pass_f32", ev);
         }
@@ -538,16 +693,55 @@ double Solver::accumulate() {
     return sse;
 }
 
-double Solver::trial_cost() {
-    const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
+// Mixed-form cost at (cams, pts): camera constants and points split to
+// float-float, then the float-float residual pass (SSE partials per chunk in
+// sse_part_, residuals in r_out).
+void Solver::cost_mixed(const double* cams, const double* pts, unsigned long long* anomalies, float2* r_out) {
     cudaEvent_t ev = prof_start();
-    camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(tcams_.get(), C_, cam_pre_.get());
+    prepare_ff(cams, pts);
+    // Huber threshold and its square as float-float pairs (host-split: no
+    // per-thread FP64 conversions)
+    const double d2 = huber_delta_ * huber_delta_;
+    const float dh = static_cast<float>(huber_delta_), d2h = static_cast<float>(d2);
+    const float2 dl = huber_delta_ > 0.0 ? make_float2(dh, static_cast<float>(huber_delta_ - dh)) : make_float2(0.f, 0.f);
+    const float2 dl2 = make_float2(d2h, static_cast<float>(d2 - d2h));
+    cost_ff<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
+                                            reinterpret_cast<const float4*>(s_pxff_.get()),
+                                            reinterpret_cast<const float2*>(cam_pre_ff_.get()),
+                                            reinterpret_cast<const float2*>(pts_ff_.get()),
+                                            reinterpret_cast<const double2*>(s_px_.get()), cam_pre_.get(), pts,
+                                            sse_part_.get(), anomalies, r_out, huber_delta_, dl, dl2);
     GBA_LAUNCH_CHECK();
-    cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                             cam_pre_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
-                                             reinterpret_cast<float2*>(r_trial_.get()), huber_delta_);
+    prof_stop("cost_ff", ev);
+}
+
+// Float-float camera constants, FP32 cameras and float-float points of
+// (cams, pts), for the cost pass and the FP32 Jacobian pass.
+void Solver::prepare_ff(const double* cams, const double* pts) {
+    camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(
+        cams, C_, cam_pre_.get(), reinterpret_cast<float2*>(cam_pre_ff_.get()), cams32_.get());
     GBA_LAUNCH_CHECK();
-    prof_stop("cost_f64", ev);
+    launch_split_ff(pts, 3ll * P_, pts_ff_.get(), stream_);
+    ff_holds_ = (cams == cams_.get() && pts == pts_.get()) ? kFfCurrent
+                : (cams == tcams_.get() && pts == tpts_.get()) ? kFfTrial
+                                                                : kFfNone;
+}
+
+double Solver::trial_cost() {
+    if (form_ == SolverForm::Plain) {
+        const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
+        cudaEvent_t ev = prof_start();
+        camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(tcams_.get(), C_, cam_pre_.get(), nullptr,
+                                                                         nullptr);
+        GBA_LAUNCH_CHECK();
+        cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
+                                                 cam_pre_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
+                                                 nullptr, huber_delta_);
+        GBA_LAUNCH_CHECK();
+        prof_stop("cost_f64", ev);
+    } else {
+        cost_mixed(tcams_.get(), tpts_.get(), counters_.get(), reinterpret_cast<float2*>(r_trial_.get()));
+    }
     ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get() + 1);
     GBA_LAUNCH_CHECK();
     double sse = 0.0;

@@ -66,6 +66,35 @@ __device__ __forceinline__ void madd(ff& acc, ff a, ff b) {
     acc.lo = __fadd_rn(acc.lo, __fadd_rn(r, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e))));
 }
 
+__device__ __forceinline__ ff neg(ff a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ ff sub(ff a, ff b) { return add(a, neg(b)); }
+
+// a * b, renormalised
+__device__ __forceinline__ ff mul(ff a, ff b) {
+    float p, e;
+    two_prod(a.hi, b.hi, p, e);
+    return norm({p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e))});
+}
+
+// a / b (b normalised, non-zero): Dekker's division, one correction of the
+// FP32 quotient q1 by the exactly computed remainder a - q1 b.
+__device__ __forceinline__ ff div(ff a, ff b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    float p, e;
+    two_prod(q1, b.hi, p, e);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), __fmaf_rn(-q1, b.lo, a.lo));
+    return norm({q1, __fdiv_rn(r, b.hi)});
+}
+
+// sqrt(a) for a > 0 (normalised): the FP32 root y corrected by (a - y^2) / 2y.
+__device__ __forceinline__ ff sqrt(ff a) {
+    const float y = __fsqrt_rn(a.hi);
+    float p, e;
+    two_prod(y, y, p, e);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
+    return norm({y, __fdiv_rn(r, __fmul_rn(2.f, y))});
+}
+
 // Nearest float-float to an FP64 value (exact for |d| in FP32's normal range
 // and 48 significant bits).
 __device__ __forceinline__ ff from_double(double d) {

@@ -38,6 +38,8 @@ constexpr int kCB = 32;   // thread-per-camera kernels: one warp per block sprea
 constexpr int kCamChunk = 1024;
 constexpr int kCheck = 8;
 constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to be decisive
+constexpr int kJudgeAttempts = 2;    // indecisive judgements before block-Jacobi is kept for the solve
+constexpr double kLooseTol = 1e-3;   // refinement targets at or above this run the fast (FP32) path
 
 constexpr int kUC = 32;        // cameras per block of the 9-threads-per-camera kernels
 constexpr int kUT = 9 * kUC;   // their block size
@@ -69,6 +71,8 @@ __device__ __forceinline__ double as_double(ff a) { return ffa::to_double(a); }
 template <typename T> __device__ __forceinline__ T from_double(double d);
 template <> __device__ __forceinline__ float from_double<float>(double d) { return static_cast<float>(d); }
 template <> __device__ __forceinline__ ff from_double<ff>(double d) { return ffa::from_double(d); }
+__device__ __forceinline__ ff to_ff(float x) { return {x, 0.f}; }
+__device__ __forceinline__ ff to_ff(ff x) { return x; }
 __device__ __forceinline__ float warp_total(float v) { return warp_sum(v); }
 __device__ __forceinline__ ff warp_total(ff v) {
 #pragma unroll
@@ -159,7 +163,7 @@ __device__ __forceinline__ void jp_times(const float* jp, T w0, T w1, T w2, T& u
 struct BacksubOut {
     const double* V;
     const double* pts;
-    double lambda;
+    float2 lambda;  // float-float
     double* dp;
     double* tpts;
     double* part;
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                                                        const double* __restrict__ done, BacksubOut bk) {
     __shared__ T seg[kPT][3];  // warp-segment partial sums, at each segment's last slot
     __shared__ T wsh[kPT][3];
-    __shared__ double bsum[kPT / 32];
+    __shared__ float bsum[kPT / 32][2];
     if (done && *done != 0.0) return;
     const int chunk = blockIdx.x;
     const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
@@ -278,21 +282,39 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         wsh[threadIdx.x][2] = w2;
     }
     if constexpr (kBack) {
-        double den = 0.0;
+        // dp (FP64 out), trial points (FP64 sum), and the gain denominator's
+        // point terms dp_k (lambda max(V_kk, 1e-12) dp_k + bp_k) in float-float;
+        // V and bp hold FP32 sums here, exact in FP32.
+        ff den = {0.f, 0.f};
         if (my_p < p1) {
             const long long p = my_p;
-            const double d[3] = {-as_double(w0), -as_double(w1), -as_double(w2)};
+            const ff lam = {bk.lambda.x, bk.lambda.y};
+            const ff d[3] = {ffa::neg(to_ff(w0)), ffa::neg(to_ff(w1)), ffa::neg(to_ff(w2))};
             const int diag[3] = {0, 2, 5};
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                bk.dp[3 * p + k] = d[k];
-                bk.tpts[3 * p + k] = bk.pts[3 * p + k] + d[k];
-                const double vk = bk.V[6 * p + diag[k]];
-                den += d[k] * (bk.lambda * (vk > 0.0 ? vk : 1e-12) * d[k] + bp[3 * p + k]);
+                const double dk = ffa::to_double(d[k]);
+                bk.dp[3 * p + k] = dk;
+                bk.tpts[3 * p + k] = bk.pts[3 * p + k] + dk;
+                const float vk = static_cast<float>(bk.V[6 * p + diag[k]]);
+                ff t = {static_cast<float>(bp[3 * p + k]), 0.f};
+                ffa::madd(t, ffa::mul(lam, ff{vk > 0.f ? vk : 1e-12f, 0.f}), d[k]);
+                ffa::madd(den, ffa::norm(t), d[k]);
             }
         }
-        const double t = block_sum<kPT>(den, bsum);
-        if (threadIdx.x == 0) bk.part[chunk] = t;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) den = ffa::add(den, ffa::shfl_xor(den, o));
+        if (lane == 0) {
+            bsum[threadIdx.x >> 5][0] = den.hi;
+            bsum[threadIdx.x >> 5][1] = den.lo;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+#pragma unroll
+            for (int w = 0; w < kPT / 32; ++w) t += static_cast<double>(bsum[w][0]) + static_cast<double>(bsum[w][1]);
+            bk.part[chunk] = t;
+        }
         return;
     }
     __syncthreads();
@@ -317,7 +339,7 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
 }
 
 // Camera pass: partial_c = sum over the chunk's camera-major positions of Jc^T u
-// (Jc from the camera-major copy J32c, 18 floats per position; both contiguous).
+// (Jc from the camera records J32c = [Jc(18), r(2)] per position; both contiguous).
 template <typename T>
 __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__ cchunk_begin,
                                                         const int* __restrict__ cchunk_cam,
@@ -333,13 +355,15 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
 #pragma unroll
     for (int i = 0; i < 9; ++i) acc[i] = zero<T>();
     for (int i = b + threadIdx.x; i < e; i += kCT) {
-        const float2* q = reinterpret_cast<const float2*>(J32c + 18ll * i);
-        float Jc[18];
+        const float4* q = reinterpret_cast<const float4*>(J32c + 20ll * i);
+        float Jc[20];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const float2 v = q[t];
-            Jc[2 * t] = v.x;
-            Jc[2 * t + 1] = v.y;
+        for (int t = 0; t < 5; ++t) {
+            const float4 v = q[t];
+            Jc[4 * t] = v.x;
+            Jc[4 * t + 1] = v.y;
+            Jc[4 * t + 2] = v.z;
+            Jc[4 * t + 3] = v.w;
         }
         T u0, u1;
         load_u(u_cm, i, u0, u1);
@@ -651,9 +675,15 @@ __global__ void __launch_bounds__(256) sum_to_scalar(const double* __restrict__ 
     if (threadIdx.x == 0) sc[slot] = v;
 }
 
-// Float-float split of y (hi, lo interleaved).
-__global__ void __launch_bounds__(kVT) split_kernel(const double* __restrict__ y, int n, float* __restrict__ yff) {
+__global__ void __launch_bounds__(kVT) to_f32_kernel(const double* __restrict__ y, int n, float* __restrict__ y32) {
     const int i = blockIdx.x * kVT + threadIdx.x;
+    if (i < n) y32[i] = static_cast<float>(y[i]);
+}
+
+// Float-float split of y (hi, lo interleaved).
+__global__ void __launch_bounds__(kVT) split_kernel(const double* __restrict__ y, long long n,
+                                                   float* __restrict__ yff) {
+    const long long i = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x;
     if (i < n) {
         const ff f = ffa::from_double(y[i]);
         reinterpret_cast<float2*>(yff)[i] = make_float2(f.hi, f.lo);
@@ -818,16 +848,35 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     }
 }
 
-// Mixed-form back-substitution: dc split to float-float, then the point pass
-// in back-substitution mode (dp, trial points, denominator partials per chunk).
+void launch_split_ff(const double* x, long long n, float* out, cudaStream_t s) {
+    if (n <= 0) return;
+    split_kernel<<<ceil_div(n, kVT), kVT, 0, s>>>(x, n, out);
+    GBA_LAUNCH_CHECK();
+}
+
+// Mixed-form back-substitution: the point pass in back-substitution mode (dp,
+// trial points, denominator partials per chunk), in the arithmetic of the last
+// Schur solve: FP32 after a loose solve, float-float otherwise.
 void mixed_back_substitute(Solver& s, double lambda, double* part) {
     const int n = 9 * s.C_;
-    split_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, s.dcff_.get());
-    GBA_LAUNCH_CHECK();
-    schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-        s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
-        s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0, nullptr,
-        nullptr, BacksubOut{s.V_.get(), s.pts_.get(), lambda, s.dp_.get(), s.tpts_.get(), part});
+    const BacksubOut bk{s.V_.get(), s.pts_.get(),
+                        make_float2(static_cast<float>(lambda), static_cast<float>(lambda - static_cast<float>(lambda))),
+                        s.dp_.get(), s.tpts_.get(), part};
+    if (s.fast_solve_) {
+        float* dc32 = s.pcg_p32_.get();  // free after the Schur solve
+        to_f32_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, dc32);
+        GBA_LAUNCH_CHECK();
+        schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
+            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+            s.Vinv32_.get(), nullptr, s.bp_.get(), dc32, -1.0, nullptr, nullptr, bk);
+    } else {
+        split_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, s.dcff_.get());
+        GBA_LAUNCH_CHECK();
+        schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
+            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
+            nullptr, nullptr, bk);
+    }
     GBA_LAUNCH_CHECK();
 }
 
@@ -842,8 +891,17 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     double* sc = pcg_s_.get();
     const double* done = sc + S_DONE;
 
-    // right-hand side, float-float arithmetic
-    implicit_parts<ff>(*this, static_cast<const ff*>(nullptr), 1.0, nullptr);
+    // Loose targets (refine_tol >= kLooseTol) are far above the FP32 operator's
+    // rounding (~1e-6 relative): the right-hand side and back-substitution run
+    // in FP32 and a converged inner solve is its own residual check. Tighter
+    // targets use float-float products for both and an explicit residual.
+    const bool fast = opts.refine_tol >= kLooseTol;
+    fast_solve_ = fast;
+    if (fast) {
+        implicit_parts<float>(*this, static_cast<const float*>(nullptr), 1.0, nullptr);
+    } else {
+        implicit_parts<ff>(*this, static_cast<const ff*>(nullptr), 1.0, nullptr);
+    }
     rhs_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), bc_.get(), C_, rhs_.get(), red);
     GBA_LAUNCH_CHECK();
     sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
@@ -879,7 +937,9 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     double rnorm2 = bnorm2;
     const double tol2 = opts.refine_tol * opts.refine_tol * bnorm2;
     // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_). Returns the
-    // iteration count; *ok = reached the inner tolerance without breakdown.
+    // iteration count; *ok = reached the inner tolerance without breakdown;
+    // inner_rel2 = its final ||r||^2 / ||b||^2.
+    double inner_rel2 = 0.0;
     auto inner_pcg = [&](bool* ok) -> long long {
         precond_inverse_kernel<<<nub, kUT, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
         GBA_LAUNCH_CHECK();
@@ -912,6 +972,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
         GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
         sync();
         *ok = h[S_DONE] != 2.0 && h[S_RR] <= h[S_TOL2] * h[S_BB];
+        inner_rel2 = h[S_BB] > 0.0 ? h[S_RR] / h[S_BB] : 0.0;
         return static_cast<long long>(h[S_ITERS]);
     };
     bool use_learned = learned && learned_choice_ == 1;
@@ -925,6 +986,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             // of the solve. Both solves count in pcg_iterations.
             bool ok_bj = false, ok_l = false;
             const long long it_bj = inner_pcg(&ok_bj);
+            const double rel2_bj = inner_rel2;
             GBA_CUDA_CHECK(cudaMemcpyAsync(judge_x_.get(), pcg_x_.get(), n * sizeof(double),
                                            cudaMemcpyDeviceToDevice, stream_));
             model_->correct_factors(*this, lambda);
@@ -933,6 +995,10 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             judge_iters_[1] = it_l;
             // Solves shorter than kJudgeMin iterations are too short to compare:
             // keep block-Jacobi for now and judge again at the next inner solve.
+            // After kJudgeAttempts indecisive judgements (loose inner
+            // tolerances end every solve in a few iterations) block-Jacobi is
+            // kept: judging costs a second solve each time.
+            ++judge_attempts_;
             const bool decisive = std::max(it_bj, it_l) >= kJudgeMin || !ok_bj || !ok_l;
             if (decisive && ok_l && (!ok_bj || it_l < it_bj)) {
                 learned_choice_ = 1;
@@ -941,7 +1007,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
                 it_count = it_l;
                 ok = ok_l;
             } else {
-                learned_choice_ = decisive ? 2 : 0;
+                learned_choice_ = (decisive || judge_attempts_ >= kJudgeAttempts) ? 2 : 0;
+                inner_rel2 = rel2_bj;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
                 factor_blocks_kernel<<<ncb, kCB, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
@@ -965,6 +1032,15 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             it_count = inner_pcg(&ok);
         }
         const double iters = static_cast<double>(it_count);
+        if (fast && step == 0 && ok && inner_rel2 <= tol2 / bnorm2) {
+            // dc = e, with the inner solve's residual as the check
+            GBA_CUDA_CHECK(cudaMemcpyAsync(dc_.get(), pcg_x_.get(), n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                           stream_));
+            rnorm2 = inner_rel2 * bnorm2;
+            st.pcg_iterations += static_cast<long long>(iters);
+            ++st.refine_steps;
+            break;
+        }
         // dc += e; residual r = rhs - S dc in float-float products, FP64 sums
         axpy_split_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_x_.get(), n, dcff_.get());
         GBA_LAUNCH_CHECK();

@@ -98,9 +98,17 @@ public:
     // dp = V'^-1 (bp - sum_e W_e^T dc), the gain denominator, and the trial
     // parameters (current + step). Returns the denominator (SSE units).
     double back_substitute(double lambda);
-    // SSE at the trial parameters (FP64); adds non-finite residuals to the
-    // anomaly counter.
+    // SSE at the trial parameters (FP64; float-float in the mixed forms); adds
+    // non-finite residuals to the anomaly counter.
     double trial_cost();
+    // Mixed forms: float-float cost pass at (cams, pts); SSE partials per point
+    // chunk in sse_part_, FP32 residuals in r_out, non-finite count to anomalies.
+    void cost_mixed(const double* cams, const double* pts, unsigned long long* anomalies, float2* r_out);
+    // Mixed forms: float-float camera constants and points plus FP32 cameras of
+    // (cams, pts) into cam_pre_ff_, pts_ff_, cams32_; ff_holds_ says whose.
+    void prepare_ff(const double* cams, const double* pts);
+    enum FfHolds { kFfNone, kFfCurrent, kFfTrial };
+    FfHolds ff_holds_ = kFfNone;
     // Trial parameters become current.
     void accept();
 
@@ -149,13 +157,17 @@ public:
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
     DevBuf<float> J32_;
-    DevBuf<float> J32c_;    // mixed: Jc (18 floats) per slot in camera-major position (camera pass input)
+    DevBuf<float> J32c_;    // mixed: camera record [Jc(18), r(2)] per slot in camera-major position
     DevBuf<float> Vinv32_;  // mixed: FP32 copy of V'^-1 (6 per point) for the FP32 matvec
     DevBuf<float> Vinv32lo_;  // mixed: V'^-1 - Vinv32_ rounded to FP32 (float-float matvec)
     DevBuf<float> dcff_;      // mixed: float-float copy of dc (hi, lo per entry) for the refinement residual
     DevBuf<float> pcg_p32_; // mixed: FP32 copy of the PCG direction for the FP32 matvec
     DevBuf<int> cam_pos_;   // camera-major position of each slot (inverse of cam_slots_)
     DevBuf<double> cam_pre_;  // per-camera rotation matrix, translation, intrinsics (16 per camera)
+    DevBuf<float> cam_pre_ff_;  // mixed: the same as float-float pairs (32 floats per camera)
+    DevBuf<float> pts_ff_;      // mixed: float-float copy of the points being costed (6 floats per point)
+    DevBuf<float> s_pxff_;      // mixed: observations in slot order as float-float pairs (4 floats per slot)
+    DevBuf<float> cams32_;      // mixed: cameras rounded to FP32 (9 per camera), for the FP32 Jacobians
     DevBuf<float> r_cur_, r_trial_;  // mixed: FP64-evaluated residuals (FP32) at current / trial parameters
     bool resid_valid_ = false;       // r_cur_ and scal_[0] hold the current parameters' residuals / SSE
     DevBuf<double> sse_part_, cam_part_, scal_;  // scal_: [0] sse, [1] trial sse, [2] denom, [3..] scratch
@@ -177,7 +189,12 @@ public:
     // first inner solve, 2 = block-Jacobi won (used for the rest of the solve).
     int learned_choice_ = 0;
     long long judge_iters_[2] = {0, 0};  // inner PCG iterations of the judged solve: block-Jacobi, learned
-    void begin_solve() { learned_choice_ = 0; }
+    int judge_attempts_ = 0;             // judgements made in this solve
+    bool fast_solve_ = false;            // the last Schur solve ran the loose-target FP32 path
+    void begin_solve() {
+        learned_choice_ = 0;
+        judge_attempts_ = 0;
+    }
     // Robust loss of the cost and the normal equations (<= 0: none). Changing it
     // invalidates the cached residuals / SSE of the current parameters.
     double huber_delta_ = 0.0;
@@ -199,6 +216,9 @@ void validate_problem(int C, int P, int E, const double* cams, const double* pts
                       const int* obs_pt, const double* obs_px);
 
 // Standalone kernels with raw device pointers (C-ABI entry points wrap these).
+// Float-float split of n FP64 values into (hi, lo) float pairs (pcg.cu).
+void launch_split_ff(const double* x, long long n, float* out, cudaStream_t s);
+
 // Mixed-form back-substitution (pcg.cu): dp, trial points and the point terms
 // of the gain denominator (one partial per point chunk in part).
 void mixed_back_substitute(Solver& s, double lambda, double* part);

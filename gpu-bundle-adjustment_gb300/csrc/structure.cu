@@ -198,7 +198,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     bc_.alloc(9ull * C);
     V_.alloc(6ull * P);
     bp_.alloc(3ull * P);
-    Vinv_.alloc(6ull * P);
+    if (form_ == SolverForm::Plain) Vinv_.alloc(6ull * P);  // the mixed forms hold V'^-1 as float-float parts
     dc_.alloc(9ull * C);
     dp_.alloc(3ull * P);
     sse_part_.alloc(std::max(n_pchunk_, 1));
@@ -218,9 +218,12 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         build_pairs();
     } else {
         J32_.alloc(24ull * E);
-        J32c_.alloc(18ull * E);
+        J32c_.alloc(20ull * E);
         judge_x_.alloc(9ull * C);
         Vinv32_.alloc(6ull * P);
+        cam_pre_ff_.alloc(32ull * C);
+        pts_ff_.alloc(6ull * P);
+        cams32_.alloc(9ull * C);
         Vinv32lo_.alloc(6ull * P);
         dcff_.alloc(18ull * C);
         pcg_p32_.alloc(9ull * C);
@@ -246,6 +249,7 @@ void Solver::sync() const { GBA_CUDA_CHECK(cudaStreamSynchronize(stream_)); }
 
 void Solver::set_params(const double* cams, const double* pts) {
     resid_valid_ = false;
+    ff_holds_ = kFfNone;
     GBA_CUDA_CHECK(cudaMemcpyAsync(cams_.get(), cams, 9ull * C_ * sizeof(double), cudaMemcpyHostToDevice,
                                    stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(pts_.get(), pts, 3ull * P_ * sizeof(double), cudaMemcpyHostToDevice,
@@ -297,6 +301,10 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     GBA_LAUNCH_CHECK();
     csr_offsets_kernel<<<grid_for(E), 256, 0, stream_>>>(s_pt_.get(), E, P, pt_off_.get());
     GBA_LAUNCH_CHECK();
+    if (form_ != SolverForm::Plain) {
+        s_pxff_.alloc(4ull * E);
+        launch_split_ff(s_px_.get(), 2ll * E, s_pxff_.get(), stream_);
+    }
 
     // 2. camera-major view of the slots (stable: slot order within a camera)
     tb = tmp.size();
@@ -447,6 +455,7 @@ unsigned long long Solver::nonspd_total() const {
 void Solver::accept() {
     cams_.swap(tcams_);
     pts_.swap(tpts_);
+    ff_holds_ = ff_holds_ == kFfTrial ? kFfCurrent : kFfNone;
     if (form_ != SolverForm::Plain) {
         // the trial evaluation is the current one now: residuals and SSE
         r_cur_.swap(r_trial_);
@@ -489,6 +498,7 @@ namespace gba {
 
 void Solver::reset_params() {
     resid_valid_ = false;
+    ff_holds_ = kFfNone;
     GBA_CUDA_CHECK(cudaMemcpyAsync(cams_.get(), cams0_.get(), 9ull * C_ * sizeof(double), cudaMemcpyDeviceToDevice,
                                    stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(pts_.get(), pts0_.get(), 3ull * P_ * sizeof(double), cudaMemcpyDeviceToDevice,

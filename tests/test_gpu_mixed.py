@@ -1,5 +1,6 @@
 """GPU: the mixed-precision form (FP32 Jacobians with FP64 accumulation,
-implicit FP32 Schur matvecs in block-Jacobi PCG, FP64 iterative refinement).
+implicit FP32 Schur matvecs in block-Jacobi PCG, iterative refinement with a
+float-float residual, float-float cost).
 
 Gates: normal equations within FP32 rounding of the FP64 oracle; the refined
 Schur step satisfies the FP64 residual target 1e-8 and agrees with the exact
@@ -30,7 +31,9 @@ def test_mixed_normal_equations_within_fp32(gba, oracle, small):
         J = s.download("J32").reshape(-1, 24)
         order = s.download("order")
     ref = oracle.accumulate(small)
-    assert abs(sse - ref["sse"]) <= 1e-12 * ref["sse"]  # cost stays FP64
+    # the cost is float-float (~48-bit significands); the residual cancels
+    # ~500 px predictions against the observations, so 1e-11 bounds it
+    assert abs(sse - ref["sse"]) <= 1e-11 * ref["sse"]
     assert rel_err(U, ref["U"]) < 2e-5
     assert rel_err(bc, ref["bc"]) < 2e-5
     assert rel_err(Vp[:, 0], ref["V"][:, 0, 0]) < 2e-5
@@ -127,6 +130,12 @@ def _implicit_system(s, prob, lam):
     Vinv = np.linalg.inv(V)
     bc, bp = s.download("bc").reshape(C, 9), s.download("bp").reshape(P, 3)
 
+    def point_step(dc):  # dp = V'^-1 (bp - sum_e W_e^T dc)
+        t = np.einsum("sri,si->sr", Jc, dc.reshape(C, 9)[cam])
+        g = np.zeros((P, 3))
+        np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
+        return np.einsum("pij,pj->pi", Vinv, bp - g).ravel()
+
     def back(g):  # g (P,3) -> sum over slots of Jc^T Jp Vinv g, per camera
         w = np.einsum("pij,pj->pi", Vinv, g)
         u = np.einsum("sij,sj->si", Jp, w[pt])
@@ -143,7 +152,38 @@ def _implicit_system(s, prob, lam):
         np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
         return (np.einsum("cij,cj->ci", Ul, x) - back(g)).ravel()
 
+    matvec.point_step = point_step
     return rhs, matvec
+
+
+def test_loose_target_fast_path(gba, small):
+    """refine_tol >= 1e-3: FP32 right-hand side, the converged inner solve as its
+    own check, FP32 back-substitution. The true residual of the step meets the
+    target (up to FP32 rounding) and dp follows from dc."""
+    lam = 1e-3
+    with gba.Solver(small, "mixed") as s:
+        s.accumulate()
+        assert s.damp_invert_v(lam) == 0
+        iters, steps, relres = s.schur_pcg(lam, refine_tol=0.1, pcg_tol=0.1, pcg_max_iters=500)
+        dc = s.download("dc")
+        s.back_substitute(lam)
+        dp = s.download("dp")
+        rhs, matvec = _implicit_system(s, small, lam)
+    assert steps == 1 and 1 <= iters and relres <= 0.1
+    true_rel = np.linalg.norm(rhs - matvec(dc)) / np.linalg.norm(rhs)
+    assert true_rel <= 0.1 + 1e-4, (true_rel, relres)
+    assert abs(true_rel - relres) <= 1e-4
+    assert rel_err(dp, matvec.point_step(dc)) < 1e-4  # FP32 products, bp - W^T dc cancels
+
+
+def test_mixed_lm_loose_target_reaches_oracle_cost_workload1(gba, oracle):
+    """Inexact steps (forcing 0.1): the LM solve still reaches the FP64 oracle's
+    final cost within 0.1%."""
+    prob = gba.synthetic(1)
+    ref, _, _ = oracle.solve(prob, max_iterations=20)
+    res = gba.solve(prob.copy(), max_iterations=20, form="mixed", refine_tol=0.1, pcg_tol=0.1)
+    assert res.anomalies == 0
+    assert res.final_cost <= ref["final_cost"] * (1 + 1e-3)
 
 
 def test_float_float_refinement_residual_is_fp64_accurate(gba, small):
@@ -162,3 +202,45 @@ def test_float_float_refinement_residual_is_fp64_accurate(gba, small):
     true_rel = np.linalg.norm(r) / np.linalg.norm(rhs)
     assert relres <= 1e-10, relres
     assert true_rel <= 2e-10, (true_rel, relres)
+
+
+@pytest.mark.parametrize("delta", [0.0, 2.0])
+def test_float_float_cost_matches_oracle(gba, oracle, small, delta):
+    """Trial cost of the mixed form (float-float residual pass) against the FP64
+    oracle at perturbed parameters, plain and Huber."""
+    rng = np.random.default_rng(5)
+    cams = small.cameras + rng.normal(0, 1e-3, small.cameras.shape)
+    pts = small.points + rng.normal(0, 1e-2, small.points.shape)
+    with gba.Solver(small, "mixed") as s:
+        if delta > 0:
+            s.set_loss("huber", delta)
+        s.set_params(cams, pts)
+        sse = s.accumulate()
+    ref = oracle.cost(small, cams, pts, huber_delta=delta)
+    assert abs(sse - ref) <= 1e-11 * ref
+
+
+def _rodrigues(w):
+    th = np.linalg.norm(w)
+    k = w / th
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) * np.cos(th) + np.sin(th) * K + (1 - np.cos(th)) * np.outer(k, k)
+
+
+def test_float_float_cost_falls_back_to_fp64_out_of_range(gba, oracle, small):
+    """A point 1e-6 from a camera's plane: its residual (~1e28 px) leaves FP32's
+    range in float-float; that slot is re-evaluated in FP64, so the cost stays
+    finite and equal to the FP64 oracle's (no anomaly)."""
+    cams, pts = small.cameras.copy(), small.points.copy()
+    e = 0
+    c, p = small.obs_camera[e], small.obs_point[e]
+    R = _rodrigues(cams[9 * c:9 * c + 3])
+    target = np.array([0.3, 0.2, -1e-6])
+    pts[3 * p:3 * p + 3] = R.T @ (target - cams[9 * c + 3:9 * c + 6])
+    ref = oracle.cost(small, cams, pts)
+    assert np.isfinite(ref) and ref > 1e40
+    with gba.Solver(small, "mixed") as s:
+        s.set_params(cams, pts)
+        sse = s.accumulate()
+    assert np.isfinite(sse)
+    assert abs(sse - ref) <= 1e-6 * ref
