@@ -193,8 +193,8 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 // (80 B, five 16-byte stores) for the camera passes. V / bp are summed per
 // point in FP32 by a segmented scan over each warp (slots of a point are
 // contiguous) and the warps' segment sums, and stored FP64. The residuals
-// come from r_cur: the float-float cost pass at these parameters (run anyway to
-// drive accept/reject) stores them rounded to FP32, which keeps the gradient
+// come from r_cur (camera-major): the float-float cost pass at these parameters
+// (run anyway to drive accept/reject) stores them rounded to FP32, which keeps the gradient
 // accurate to FP32 rounding of r instead of FP32 rounding of f d u. With a
 // robust loss, J and r are scaled by sqrt(rho'(s)) before anything is stored.
 __global__ void __launch_bounds__(kPT) point_pass_f32(
@@ -237,7 +237,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             obs[0] = o.x;
             obs[1] = o.z;
             model::residual_jacobian(cam, X, obs, r, J, J + 18);
-            const float2 rf = r_cur[s];  // float-float evaluated residual, stored FP32
+            const long long q = cam_pos[s];
+            const float2 rf = r_cur[q];  // float-float evaluated residual, stored FP32 (camera-major)
             r[0] = rf.x;
             r[1] = rf.y;
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
 #pragma unroll
             for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
-            float4* outc = reinterpret_cast<float4*>(J32c + 20ll * cam_pos[s]);  // camera record
+            float4* outc = reinterpret_cast<float4*>(J32c + 20ll * q);  // camera record
 #pragma unroll
             for (int q = 0; q < 4; ++q) outc[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
             outc[4] = make_float4(J[16], J[17], r[0], r[1]);
@@ -522,57 +523,67 @@ __device__ __forceinline__ void residual_ff(const float2* __restrict__ pc, const
     r1 = ffa::norm(ffa::sub(ffa::mul(fd, v), o1));
 }
 
-// Mixed-form cost: rho(|r|^2) summed over all slots in float-float, the
-// residuals stored FP32 (NaN where not finite, counted as anomalies). Sums:
-// per thread and per warp in float-float, warps combined in FP64. A slot whose
-// float-float residual leaves FP32's safe range (|r| >= kFfSafe or not finite:
-// a wild trial step, e.g. a point near the camera plane) is evaluated again in
-// FP64 from the FP64 constants (pre64) and point (pts64), so the cost and the
-// anomaly count follow FP64 semantics; its rho is summed in FP64 (warps that
-// met such a slot only).
+// Mixed-form cost, camera-major: one CTA per camera chunk holds the camera's
+// float-float constants in shared memory and streams the chunk's positions
+// (camera-major point index and float-float observation), gathering only the
+// point. rho(|r|^2) is summed in float-float per thread and per warp, warps
+// combined in FP64; the residuals are stored FP32 at the camera-major position
+// (NaN where not finite, counted as anomalies). A position whose float-float
+// residual leaves FP32's safe range (|r| >= kFfSafe or not finite: a wild trial
+// step, e.g. a point near the camera plane) is evaluated again in FP64 from
+// the FP64 constants (pre64), point (pts64) and observation, so the cost and
+// the anomaly count follow FP64 semantics; its rho is summed in FP64 (warps
+// that met such a position only).
 constexpr float kFfSafe = 1e12f;
+constexpr int kCostT = 256;
 
-__global__ void __launch_bounds__(kPT, 6) cost_ff(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
-                                              const int* __restrict__ s_cam, const int* __restrict__ s_pt,
-                                              const float4* __restrict__ s_pxff, const float2* __restrict__ preff,
-                                              const float2* __restrict__ ptsff, const double2* __restrict__ s_px,
-                                              const double* __restrict__ pre64, const double* __restrict__ pts64,
-                                              double* __restrict__ sse_part,
-                                              unsigned long long* __restrict__ counters, float2* __restrict__ r_out,
-                                              double delta, float2 delta_ff, float2 delta2_ff) {
+__global__ void __launch_bounds__(kCostT, 4) cost_ff(const int* __restrict__ cchunk_begin,
+                                                 const int* __restrict__ cchunk_cam, const int* __restrict__ cam_off,
+                                                 const int* __restrict__ cm_pt, const float4* __restrict__ cm_pxff,
+                                                 const float2* __restrict__ preff, const float2* __restrict__ ptsff,
+                                                 const int* __restrict__ cam_slots, const double2* __restrict__ s_px,
+                                                 const double* __restrict__ pre64, const double* __restrict__ pts64,
+                                                 double* __restrict__ sse_part,
+                                                 unsigned long long* __restrict__ counters,
+                                                 float2* __restrict__ r_out, double delta, float2 delta_ff,
+                                                 float2 delta2_ff) {
     using ffa::ff;
-    __shared__ float red[kPT / 32][2];
-    __shared__ double red64[kPT / 32];
-    __shared__ unsigned long long redu[kPT / 32];
-    const int chunk = blockIdx.x;
-    const int s0 = pt_off[pchunk[chunk]], s1 = pt_off[pchunk[chunk + 1]];
+    __shared__ float2 pc[kCamPre];
+    __shared__ float red[kCostT / 32][2];
+    __shared__ double red64[kCostT / 32];
+    __shared__ unsigned long long redu[kCostT / 32];
+    const int k = blockIdx.x;
+    const int b = cchunk_begin[k], c = cchunk_cam[k];
+    const int e = min(b + kCamChunk, cam_off[c + 1]);
+    if (threadIdx.x < kCamPre) pc[threadIdx.x] = preff[static_cast<long long>(kCamPre) * c + threadIdx.x];
+    __syncthreads();
     const bool robust = delta_ff.x > 0.f;
     const ff dl = {delta_ff.x, delta_ff.y}, dl2 = {delta2_ff.x, delta2_ff.y};
     ff sse = {0.f, 0.f};
     double sse64 = 0.0;
     int fallback = 0;
     unsigned long long anom = 0;
-    for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
-        const int c = s_cam[s], p = s_pt[s];
+    for (int i = b + threadIdx.x; i < e; i += kCostT) {
+        const int p = cm_pt[i];
         ff X[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float2 x = ptsff[3ll * p + k];
-            X[k] = {x.x, x.y};
+        for (int q = 0; q < 3; ++q) {
+            const float2 x = ptsff[3ll * p + q];
+            X[q] = {x.x, x.y};
         }
-        const float4 o = s_pxff[s];
+        const float4 o = cm_pxff[i];
         ff r0, r1;
-        residual_ff(preff + static_cast<long long>(kCamPre) * c, X, ff{o.x, o.y}, ff{o.z, o.w}, r0, r1);
+        residual_ff(pc, X, ff{o.x, o.y}, ff{o.z, o.w}, r0, r1);
         if (!(fabsf(r0.hi) < kFfSafe && fabsf(r1.hi) < kFfSafe)) {
             double X64[3], obs[2], r[2];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) X64[k] = pts64[3ll * p + k];
-            const double2 ob = s_px[s];
+            for (int q = 0; q < 3; ++q) X64[q] = pts64[3ll * p + q];
+            const double2 ob = s_px[cam_slots[i]];
             obs[0] = ob.x;
             obs[1] = ob.y;
             residual_pre(pre64 + static_cast<long long>(kCamPre) * c, X64, obs, r);
             const bool fin = isfinite(r[0]) && isfinite(r[1]);
-            r_out[s] = fin ? make_float2(static_cast<float>(r[0]), static_cast<float>(r[1])) : make_float2(NAN, NAN);
+            r_out[i] = fin ? make_float2(static_cast<float>(r[0]), static_cast<float>(r[1])) : make_float2(NAN, NAN);
             if (!fin) {
                 ++anom;
                 continue;
@@ -581,7 +592,7 @@ __global__ void __launch_bounds__(kPT, 6) cost_ff(const int* __restrict__ pchunk
             fallback = 1;
             continue;
         }
-        r_out[s] = make_float2(r0.hi, r1.hi);
+        r_out[i] = make_float2(r0.hi, r1.hi);
         ff sq = {0.f, 0.f};
         ffa::madd(sq, r0, r0);
         ffa::madd(sq, r1, r1);
@@ -602,13 +613,13 @@ __global__ void __launch_bounds__(kPT, 6) cost_ff(const int* __restrict__ pchunk
         red[warp][1] = sse.lo;
         red64[warp] = sse64;
     }
-    const unsigned long long na = block_sum_u64<kPT>(anom, redu);  // synchronises the block
+    const unsigned long long na = block_sum_u64<kCostT>(anom, redu);  // synchronises the block
     if (threadIdx.x == 0) {
         double tot = 0.0;
 #pragma unroll
-        for (int w = 0; w < kPT / 32; ++w)
+        for (int w = 0; w < kCostT / 32; ++w)
             tot += static_cast<double>(red[w][0]) + static_cast<double>(red[w][1]) + red64[w];
-        sse_part[chunk] = tot;
+        sse_part[k] = tot;
         if (na) atomicAdd(counters, na);
     }
 }
@@ -663,7 +674,7 @@ double Solver::accumulate() {
         // to a scratch counter: the FP32 pass counts this evaluation's anomalies.
         if (!resid_valid_) {
             cost_mixed(cams_.get(), pts_.get(), counters_.get() + 2, reinterpret_cast<float2*>(r_cur_.get()));
-            ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
+            ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_cchunk_, scal_.get());
             GBA_LAUNCH_CHECK();
             resid_valid_ = true;
         }
@@ -705,12 +716,14 @@ void Solver::cost_mixed(const double* cams, const double* pts, unsigned long lon
     const float dh = static_cast<float>(huber_delta_), d2h = static_cast<float>(d2);
     const float2 dl = huber_delta_ > 0.0 ? make_float2(dh, static_cast<float>(huber_delta_ - dh)) : make_float2(0.f, 0.f);
     const float2 dl2 = make_float2(d2h, static_cast<float>(d2 - d2h));
-    cost_ff<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(),
-                                            reinterpret_cast<const float4*>(s_pxff_.get()),
-                                            reinterpret_cast<const float2*>(cam_pre_ff_.get()),
-                                            reinterpret_cast<const float2*>(pts_ff_.get()),
-                                            reinterpret_cast<const double2*>(s_px_.get()), cam_pre_.get(), pts,
-                                            sse_part_.get(), anomalies, r_out, huber_delta_, dl, dl2);
+    if (n_cchunk_ > 0) {
+        cost_ff<<<n_cchunk_, kCostT, 0, stream_>>>(
+            cchunk_begin_.get(), cchunk_cam_.get(), cam_off_.get(), cm_pt_.get(),
+            reinterpret_cast<const float4*>(cm_pxff_.get()), reinterpret_cast<const float2*>(cam_pre_ff_.get()),
+            reinterpret_cast<const float2*>(pts_ff_.get()), cam_slots_.get(),
+            reinterpret_cast<const double2*>(s_px_.get()), cam_pre_.get(), pts, sse_part_.get(), anomalies, r_out,
+            huber_delta_, dl, dl2);
+    }
     GBA_LAUNCH_CHECK();
     prof_stop("cost_ff", ev);
 }
@@ -742,7 +755,8 @@ double Solver::trial_cost() {
     } else {
         cost_mixed(tcams_.get(), tpts_.get(), counters_.get(), reinterpret_cast<float2*>(r_trial_.get()));
     }
-    ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get() + 1);
+    ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), form_ == SolverForm::Plain ? n_pchunk_ : n_cchunk_,
+                                        scal_.get() + 1);
     GBA_LAUNCH_CHECK();
     double sse = 0.0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&sse, scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, stream_));

@@ -36,7 +36,8 @@ constexpr int kCT = 128;
 constexpr int kVT = 256;  // vector-kernel threads
 constexpr int kCB = 32;   // thread-per-camera kernels: one warp per block spreads C cameras over the SMs
 constexpr int kCamChunk = 1024;
-constexpr int kCheck = 8;
+constexpr int kCheck = 8;       // PCG iterations launched between host checks of the convergence flag
+constexpr int kCheckFirst = 2;  // ... for the first check (loose solves end in one or two)
 constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to be decisive
 constexpr int kJudgeAttempts = 2;    // indecisive judgements before block-Jacobi is kept for the solve
 constexpr double kLooseTol = 1e-3;   // refinement targets at or above this run the fast (FP32) path
@@ -183,9 +184,11 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                                                        const float* __restrict__ vinv_lo,
                                                        const double* __restrict__ bp, const T* __restrict__ xt,
                                                        double a, T* __restrict__ u_cm,
-                                                       const double* __restrict__ done, BacksubOut bk) {
+                                                       const double* __restrict__ done, BacksubOut bk,
+                                                       float4* __restrict__ g_cm) {
     __shared__ T seg[kPT][3];  // warp-segment partial sums, at each segment's last slot
     __shared__ T wsh[kPT][3];
+    __shared__ float vsh[kPT][6];  // FP32 V'^-1 of the chunk's points (g_cm only)
     __shared__ float bsum[kPT / 32][2];
     if (done && *done != 0.0) return;
     const int chunk = blockIdx.x;
@@ -280,6 +283,10 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         wsh[threadIdx.x][0] = w0;
         wsh[threadIdx.x][1] = w1;
         wsh[threadIdx.x][2] = w2;
+        if (g_cm) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) vsh[threadIdx.x][k] = vinv_hi[6ll * my_p + k];
+        }
     }
     if constexpr (kBack) {
         // dp (FP64 out), trial points (FP64 sum), and the gain denominator's
@@ -334,19 +341,45 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         const float j[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
         T u0, u1;
         jp_times(j, wsh[p - p0][0], wsh[p - p0][1], wsh[p - p0][2], u0, u1);
-        store_u(u_cm, cam_pos[s], u0, u1);
+        const long long q = cam_pos[s];
+        store_u(u_cm, q, u0, u1);
+        if (g_cm) {
+            // G = Jp V'^-1 Jp^T (2x2, FP32) for the block-Jacobi diagonal blocks
+            const float* vi = vsh[p - p0];
+            float m[6];
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const float a0 = j[3 * r], a1 = j[3 * r + 1], a2 = j[3 * r + 2];
+                m[3 * r] = a0 * vi[0] + a1 * vi[1] + a2 * vi[3];
+                m[3 * r + 1] = a0 * vi[1] + a1 * vi[2] + a2 * vi[4];
+                m[3 * r + 2] = a0 * vi[3] + a1 * vi[4] + a2 * vi[5];
+            }
+            g_cm[q] = make_float4(m[0] * j[0] + m[1] * j[1] + m[2] * j[2], m[0] * j[3] + m[1] * j[4] + m[2] * j[5],
+                                  m[3] * j[3] + m[4] * j[4] + m[5] * j[5], 0.f);
+        }
     }
 }
 
 // Camera pass: partial_c = sum over the chunk's camera-major positions of Jc^T u
 // (Jc from the camera records J32c = [Jc(18), r(2)] per position; both contiguous).
-template <typename T>
+// Partials at part[kStride * chunk]. kDiag (the right-hand side pass): also the
+// chunk's part of sum Jc^T G Jc (lower triangle, 45, FP32 sums) from the slots'
+// G = Jp V'^-1 Jp^T, at part[54 chunk + 9 ..], for the block-Jacobi blocks.
+template <typename T, bool kDiag = false>
 __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__ cchunk_begin,
                                                         const int* __restrict__ cchunk_cam,
                                                         const int* __restrict__ cam_off,
                                                         const float* __restrict__ J32c, const T* __restrict__ u_cm,
-                                                        double* __restrict__ part, const double* __restrict__ done) {
+                                                        double* __restrict__ part, const double* __restrict__ done,
+                                                        const float4* __restrict__ g_cm) {
+    constexpr int kStride = kDiag ? 54 : 9;
     __shared__ double wpart[kCT / 32][9];
+    __shared__ float dpart[kDiag ? kCT / 32 : 1][kDiag ? 45 : 1];
+    float dacc[kDiag ? 45 : 1];
+    if constexpr (kDiag) {
+#pragma unroll
+        for (int i = 0; i < 45; ++i) dacc[i] = 0.f;
+    }
     if (done && *done != 0.0) return;
     const int k = blockIdx.x;
     const int b = cchunk_begin[k], c = cchunk_cam[k];
@@ -372,6 +405,23 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
             madd(acc[t], Jc[t], u0);
             madd(acc[t], Jc[9 + t], u1);
         }
+        if constexpr (kDiag) {
+            const float4 g = g_cm[i];
+            float H0[9], H1[9];  // G Jc
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+                H0[t] = g.x * Jc[t] + g.y * Jc[9 + t];
+                H1[t] = g.y * Jc[t] + g.z * Jc[9 + t];
+            }
+            int idx = 0;
+#pragma unroll
+            for (int a = 0; a < 9; ++a)
+#pragma unroll
+                for (int bb = 0; bb <= a; ++bb) {
+                    dacc[idx] += Jc[a] * H0[bb] + Jc[9 + a] * H1[bb];
+                    ++idx;
+                }
+        }
     }
     // Warp sums in the arithmetic type (FP32 shuffles stay off GB300's narrow
     // FP64 pipe); the four warp partials are added in FP64.
@@ -381,12 +431,28 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
         const T v = warp_total(acc[t]);
         if (lane == 0) wpart[warp][t] = as_double(v);
     }
+    if constexpr (kDiag) {
+#pragma unroll
+        for (int t = 0; t < 45; ++t) {
+            const float v = warp_sum(dacc[t]);
+            if (lane == 0) dpart[warp][t] = v;
+        }
+    }
     __syncthreads();
     if (threadIdx.x < 9) {
         double v = 0.0;
 #pragma unroll
         for (int w = 0; w < kCT / 32; ++w) v += wpart[w][threadIdx.x];
-        part[9ll * k + threadIdx.x] = v;
+        part[static_cast<long long>(kStride) * k + threadIdx.x] = v;
+    }
+    if constexpr (kDiag) {
+        if (threadIdx.x >= 32 && threadIdx.x < 32 + 45) {
+            const int t = threadIdx.x - 32;
+            double v = 0.0;
+#pragma unroll
+            for (int w = 0; w < kCT / 32; ++w) v += static_cast<double>(dpart[w][t]);
+            part[54ll * k + 9 + t] = v;
+        }
     }
 }
 
@@ -400,9 +466,9 @@ __device__ __forceinline__ double damped_u_row_dot(const double* __restrict__ Uc
 }
 
 __device__ __forceinline__ double chunk_sum(const int* __restrict__ cam_chunk_off, const double* __restrict__ part,
-                                            int c, int k) {
+                                            int c, int k, int stride = 9) {
     double s = 0.0;
-    for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[9ll * q + k];
+    for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[static_cast<long long>(stride) * q + k];
     return s;
 }
 
@@ -414,7 +480,7 @@ __global__ void __launch_bounds__(kVT) rhs_finalize(const int* __restrict__ cam_
     const int i = blockIdx.x * kVT + threadIdx.x;
     double v = 0.0;
     if (i < 9 * C) {
-        v = bc[i] - chunk_sum(cam_chunk_off, part, i / 9, i % 9);
+        v = bc[i] - chunk_sum(cam_chunk_off, part, i / 9, i % 9, 54);  // the right-hand side pass writes 54 per chunk
         rhs[i] = v;
     }
     const double t = block_sum<kVT>(v * v, sh);
@@ -703,68 +769,7 @@ __global__ void __launch_bounds__(kVT) axpy_split_kernel(double* __restrict__ y,
 }
 
 // ---- block-Jacobi blocks S_cc = U_lambda,c - sum_{e in c} Jc^T (Jp V'^-1 Jp^T) Jc
-__global__ void __launch_bounds__(kCT) sdiag_camera_pass(const int* __restrict__ cchunk_begin,
-                                                        const int* __restrict__ cchunk_cam,
-                                                        const int* __restrict__ cam_off,
-                                                        const int* __restrict__ cam_slots, const int* __restrict__ s_pt,
-                                                        const float* __restrict__ J32, const float* __restrict__ Vinv32,
-                                                        double* __restrict__ part) {
-    __shared__ double wpart[kCT / 32][45];
-    const int k = blockIdx.x;
-    const int b = cchunk_begin[k], c = cchunk_cam[k];
-    const int e = min(b + kCamChunk, cam_off[c + 1]);
-    float acc[45];
-#pragma unroll
-    for (int i = 0; i < 45; ++i) acc[i] = 0.f;
-    for (int i = b + threadIdx.x; i < e; i += kCT) {
-        const long long s = cam_slots[i];
-        float J[24];
-        load_j(J32, s, J);
-        const float* Vi = Vinv32 + 6ll * s_pt[s];
-        const float v00 = Vi[0], v10 = Vi[1], v11 = Vi[2], v20 = Vi[3], v21 = Vi[4], v22 = Vi[5];
-        const float* Jp = J + 18;
-        // M = Jp V^-1 (2x3), G = M Jp^T (2x2 symmetric)
-        float M[6];
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const float a0 = Jp[3 * r], a1 = Jp[3 * r + 1], a2 = Jp[3 * r + 2];
-            M[3 * r] = a0 * v00 + a1 * v10 + a2 * v20;
-            M[3 * r + 1] = a0 * v10 + a1 * v11 + a2 * v21;
-            M[3 * r + 2] = a0 * v20 + a1 * v21 + a2 * v22;
-        }
-        const float g00 = M[0] * Jp[0] + M[1] * Jp[1] + M[2] * Jp[2];
-        const float g01 = M[0] * Jp[3] + M[1] * Jp[4] + M[2] * Jp[5];
-        const float g11 = M[3] * Jp[3] + M[4] * Jp[4] + M[5] * Jp[5];
-        // H = G Jc (2x9)
-        float H0[9], H1[9];
-#pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            H0[t] = g00 * J[t] + g01 * J[9 + t];
-            H1[t] = g01 * J[t] + g11 * J[9 + t];
-        }
-        int idx = 0;
-#pragma unroll
-        for (int a = 0; a < 9; ++a)
-#pragma unroll
-            for (int bb = 0; bb <= a; ++bb) {
-                acc[idx] += J[a] * H0[bb] + J[9 + a] * H1[bb];
-                ++idx;
-            }
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-#pragma unroll
-    for (int t = 0; t < 45; ++t) {
-        const float v = warp_sum(acc[t]);
-        if (lane == 0) wpart[warp][t] = static_cast<double>(v);
-    }
-    __syncthreads();
-    if (threadIdx.x < 45) {
-        double v = 0.0;
-#pragma unroll
-        for (int w = 0; w < kCT / 32; ++w) v += wpart[w][threadIdx.x];
-        part[54ll * k + threadIdx.x] = v;
-    }
-}
+// (the sums come from the right-hand side camera pass)
 
 // Packed Cholesky factor of a full 9x9 block; a block that is not SPD in FP64
 // (round-off with tiny damping) falls back to the square root of its diagonal.
@@ -800,7 +805,7 @@ __global__ void __launch_bounds__(kCB) sdiag_finalize(const int* __restrict__ ca
     for (int a = 0; a < 9; ++a)
         for (int b = 0; b <= a; ++b) {
             double s = 0.0;
-            for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[54ll * q + idx];
+            for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[54ll * q + 9 + idx];
             A[9 * a + b] -= s;
             if (a != b) A[9 * b + a] = A[9 * a + b];
             ++idx;
@@ -831,20 +836,28 @@ template <typename T>
 static void implicit_parts(Solver& s, const T* x, double a, const double* done) {
     T* u = reinterpret_cast<T*>(s.u_.get());
     const bool f32 = sizeof(T) == 4;
+    const bool rhs = x == nullptr;  // right-hand side: also the block-Jacobi diagonal-block partials
+    float4* g = rhs ? reinterpret_cast<float4*>(s.g_cm_.get()) : nullptr;
     cudaEvent_t ev = s.prof_start();
     schur_point_pass<T><<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
                                                            s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
                                                            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
-                                                           u, done, BacksubOut{});
+                                                           u, done, BacksubOut{}, g);
     GBA_LAUNCH_CHECK();
-    s.prof_stop(f32 ? "schur_point_pass_f32" : "schur_point_pass_ff", ev);
+    s.prof_stop(rhs ? "schur_rhs_point_pass" : f32 ? "schur_point_pass_f32" : "schur_point_pass_ff", ev);
     if (s.n_cchunk_ > 0) {
         ev = s.prof_start();
-        schur_camera_pass<T><<<s.n_cchunk_, kCT, 0, s.stream_>>>(s.cchunk_begin_.get(), s.cchunk_cam_.get(),
-                                                                 s.cam_off_.get(), s.J32c_.get(), u,
-                                                                 s.cam_part_.get(), done);
+        if (rhs) {
+            schur_camera_pass<T, true><<<s.n_cchunk_, kCT, 0, s.stream_>>>(
+                s.cchunk_begin_.get(), s.cchunk_cam_.get(), s.cam_off_.get(), s.J32c_.get(), u, s.cam_part_.get(),
+                done, g);
+        } else {
+            schur_camera_pass<T><<<s.n_cchunk_, kCT, 0, s.stream_>>>(s.cchunk_begin_.get(), s.cchunk_cam_.get(),
+                                                                     s.cam_off_.get(), s.J32c_.get(), u,
+                                                                     s.cam_part_.get(), done, nullptr);
+        }
         GBA_LAUNCH_CHECK();
-        s.prof_stop(f32 ? "schur_camera_pass_f32" : "schur_camera_pass_ff", ev);
+        s.prof_stop(rhs ? "schur_rhs_camera_pass" : f32 ? "schur_camera_pass_f32" : "schur_camera_pass_ff", ev);
     }
 }
 
@@ -868,14 +881,14 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
         GBA_LAUNCH_CHECK();
         schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
             s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
-            s.Vinv32_.get(), nullptr, s.bp_.get(), dc32, -1.0, nullptr, nullptr, bk);
+            s.Vinv32_.get(), nullptr, s.bp_.get(), dc32, -1.0, nullptr, nullptr, bk, nullptr);
     } else {
         split_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, s.dcff_.get());
         GBA_LAUNCH_CHECK();
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
             s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
-            nullptr, nullptr, bk);
+            nullptr, nullptr, bk, nullptr);
     }
     GBA_LAUNCH_CHECK();
 }
@@ -907,13 +920,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
     sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
     GBA_LAUNCH_CHECK();
 
-    // block-Jacobi blocks and factors (+ learned correction)
-    if (n_cchunk_ > 0) {
-        sdiag_camera_pass<<<n_cchunk_, kCT, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(), cam_off_.get(),
-                                                          cam_slots_.get(), s_pt_.get(), J32_.get(), Vinv32_.get(),
-                                                          cam_part_.get());
-        GBA_LAUNCH_CHECK();
-    }
+    // block-Jacobi blocks (partials from the right-hand side pass) and factors
+    // (+ learned correction)
     sdiag_finalize<<<ncb, kCB, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
                                              Sdiag_.get(), Pfac_.get());
     GBA_LAUNCH_CHECK();
@@ -950,8 +958,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
         GBA_LAUNCH_CHECK();
         // p.q partials (nvb) and r.r / r.z partials (nub) in disjoint ranges
         double* red_pq = red2 + nub + 1;
-        for (int it = 0; it < opts.pcg_max_iters; it += kCheck) {
-            for (int j = 0; j < kCheck; ++j) {
+        for (int it = 0, batch = kCheckFirst; it < opts.pcg_max_iters; it += batch, batch = kCheck) {
+            for (int j = 0; j < batch; ++j) {
                 implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
                 pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
                                                          pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);

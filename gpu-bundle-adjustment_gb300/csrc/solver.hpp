@@ -167,8 +167,10 @@ public:
     DevBuf<float> cam_pre_ff_;  // mixed: the same as float-float pairs (32 floats per camera)
     DevBuf<float> pts_ff_;      // mixed: float-float copy of the points being costed (6 floats per point)
     DevBuf<float> s_pxff_;      // mixed: observations in slot order as float-float pairs (4 floats per slot)
+    DevBuf<float> cm_pxff_;     // mixed: the same at camera-major positions
+    DevBuf<int> cm_pt_;         // mixed: point of each camera-major position
     DevBuf<float> cams32_;      // mixed: cameras rounded to FP32 (9 per camera), for the FP32 Jacobians
-    DevBuf<float> r_cur_, r_trial_;  // mixed: FP64-evaluated residuals (FP32) at current / trial parameters
+    DevBuf<float> r_cur_, r_trial_;  // mixed: float-float evaluated residuals (FP32, camera-major) at current / trial parameters
     bool resid_valid_ = false;       // r_cur_ and scal_[0] hold the current parameters' residuals / SSE
     DevBuf<double> sse_part_, cam_part_, scal_;  // scal_: [0] sse, [1] trial sse, [2] denom, [3..] scratch
     DevBuf<unsigned long long> counters_;        // [0] anomalies, [1] non-SPD V blocks
@@ -183,6 +185,7 @@ public:
     DevBuf<double> Pinv_;          // explicit preconditioner blocks M_c = (L L^T)^-1 (81C)
     DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_, judge_x_;
     DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or float-float)
+    DevBuf<float> g_cm_;     // per-slot G_e = Jp V'^-1 Jp^T (00, 01, 11, pad) at camera-major positions
     DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
     DevBuf<float> mlp_stats_;  // learned form: per-camera track statistics (3 per camera)
     // Learned form, per solve: 0 = not judged yet, 1 = learned factors won the

@@ -82,6 +82,18 @@ __global__ void inverse_perm_kernel(const int* __restrict__ perm, int n, int* __
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[perm[i]] = i;
 }
 
+// Camera-major copies of per-slot data: point index and float-float observation
+// of camera-major position i (slot cam_slots[i]).
+__global__ void gather_cm_kernel(const int* __restrict__ cam_slots, const int* __restrict__ s_pt,
+                                 const float4* __restrict__ s_pxff, int n, int* __restrict__ cm_pt,
+                                 float4* __restrict__ cm_pxff) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int s = cam_slots[i];
+        cm_pt[i] = s_pt[s];
+        cm_pxff[i] = s_pxff[s];
+    }
+}
+
 // offsets[k] = first position i with keys[i] >= k, for k = 0..nk (keys sorted).
 __global__ void csr_offsets_kernel(const int* __restrict__ keys, int n, int nk, int* __restrict__ off) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -201,7 +213,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     if (form_ == SolverForm::Plain) Vinv_.alloc(6ull * P);  // the mixed forms hold V'^-1 as float-float parts
     dc_.alloc(9ull * C);
     dp_.alloc(3ull * P);
-    sse_part_.alloc(std::max(n_pchunk_, 1));
+    sse_part_.alloc(std::max({n_pchunk_, n_cchunk_, 1}));
     cam_part_.alloc(54ull * std::max(n_cchunk_, 1));
     // block partials: the largest single reduction, or the PCG layout
     // [r.r | r.z | p.q] = max(9C/256, C/32) + C/32 + 9C/256 (+ separators)
@@ -240,6 +252,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         pcg_q_.alloc(9ull * C);
         ref_r_.alloc(9ull * C);
         u_.alloc(2ull * E);
+        g_cm_.alloc(4ull * E);
         pcg_s_.alloc(16);
     }
     sync();
@@ -315,6 +328,14 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     cam_pos_.alloc(E);
     inverse_perm_kernel<<<grid_for(E), 256, 0, stream_>>>(cam_slots_.get(), E, cam_pos_.get());
     GBA_LAUNCH_CHECK();
+    if (form_ != SolverForm::Plain) {
+        cm_pt_.alloc(E);
+        cm_pxff_.alloc(4ull * E);
+        gather_cm_kernel<<<grid_for(E), 256, 0, stream_>>>(cam_slots_.get(), s_pt_.get(),
+                                                           reinterpret_cast<const float4*>(s_pxff_.get()), E,
+                                                           cm_pt_.get(), reinterpret_cast<float4*>(cm_pxff_.get()));
+        GBA_LAUNCH_CHECK();
+    }
 
     // 3. work chunks, built on the host from the CSR offsets
     std::vector<int> h_pt_off(P + 1), h_cam_off(C + 1);
