@@ -6,7 +6,8 @@
 //   exit 1 = arguments / IO, 2 = solver initial cost differs from the reader's
 //   cost by more than 1e-9 max(1, |c|), 3 = device anomaly counter non-zero.
 // Additive flags: --synthetic=W (workload 1..5 instead of a file), --seed=S,
-// --form=plain|mixed|learned, --model=PATH, --target-cost=D, and the loss flags
+// --form=plain|mixed|learned, --model=PATH, --target-cost=D, --refine-tol=D and
+// --pcg-tol=D (mixed forms' Schur solve targets), and the loss flags
 // of the reference's Ceres benchmark (benchmarks/bench_ceres.cpp:10-11,117-131):
 // --loss=none|huber, --delta=D (default 1.0); with Huber the initial-cost gate
 // compares against sum rho(|r|^2) / 2 from the reader's own residual. Additive
@@ -41,12 +42,13 @@ struct Args {
     double target_cost = 0.0;
     std::string loss = "none";
     double delta = 1.0;
+    double refine_tol = -1.0, pcg_tol = -1.0;  // < 0: library defaults
 };
 
 [[noreturn]] void usage_error(const std::string& msg) {
     std::fprintf(stderr, "%s\nusage: bench_bal <problem.txt[.bz2]> [--iterations=N] [--lambda=D] [--json=PATH] "
                          "[--verbose] [--synthetic=1..5 --seed=S] [--form=plain|mixed|learned] [--model=PATH] "
-                         "[--target-cost=D] [--loss=none|huber] [--delta=D]\n",
+                         "[--target-cost=D] [--loss=none|huber] [--delta=D] [--refine-tol=D] [--pcg-tol=D]\n",
                  msg.c_str());
     std::exit(1);
 }
@@ -71,6 +73,8 @@ Args parse(int argc, char** argv) {
             else if (const char* v = val("--target-cost=")) a.target_cost = std::stod(v);
             else if (const char* v = val("--loss=")) a.loss = v;
             else if (const char* v = val("--delta=")) a.delta = std::stod(v);
+            else if (const char* v = val("--refine-tol=")) a.refine_tol = std::stod(v);
+            else if (const char* v = val("--pcg-tol=")) a.pcg_tol = std::stod(v);
             else if (s.rfind("--", 0) != 0 && a.file.empty()) a.file = s;
             else usage_error("bad argument: " + s);
         } catch (const std::logic_error&) {
@@ -129,6 +133,8 @@ int main(int argc, char** argv) {
     opts.target_cost = args.target_cost;
     opts.loss = args.loss == "huber" ? gba::Loss::Huber : gba::Loss::None;
     opts.huber_delta = args.delta;
+    if (args.refine_tol > 0.0) opts.refine_tol = args.refine_tol;
+    if (args.pcg_tol > 0.0) opts.pcg_tol = args.pcg_tol;
     if (args.form == "plain") opts.form = gba::SolverForm::Plain;
     else if (args.form == "mixed") opts.form = gba::SolverForm::Mixed;
     else if (args.form == "learned") opts.form = gba::SolverForm::MixedLearned;

@@ -150,6 +150,10 @@ void gba_lm_options_default(gba_lm_options* o) {
 
 unsigned long long gba_launch_count(void) { return gba::launch_count(); }
 
+int gba_release_cached_memory(void) {
+    return guarded([&] { gba::release_cached_memory(); });
+}
+
 int gba_solver_set_harvest(gba_solver* s, int enable) {
     return guarded([&] {
         need(S(s).form() == gba::SolverForm::Plain, "harvest needs the plain form");
@@ -519,7 +523,7 @@ int gba_solver_load_model(gba_solver* s, const char* path) {
 int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out) {
     return guarded([&] {
         need(out != nullptr, "null argument");
-        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_TRIAL_PTS, "bad buffer id");
+        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_JP32, "bad buffer id");
         size_t bytes = 0;
         S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &bytes);
         *out = bytes;
@@ -529,7 +533,7 @@ int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out) {
 int gba_solver_download(gba_solver* s, int buffer, void* dst, size_t bytes) {
     return guarded([&] {
         need(dst != nullptr, "null destination");
-        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_TRIAL_PTS, "bad buffer id");
+        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_JP32, "bad buffer id");
         size_t have = 0;
         const void* src = S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &have);
         need(src != nullptr, "buffer not held by this solver form");
@@ -542,7 +546,7 @@ int gba_solver_download(gba_solver* s, int buffer, void* dst, size_t bytes) {
 int gba_solver_device_ptr(gba_solver* s, int buffer, void** out) {
     return guarded([&] {
         need(out != nullptr, "null argument");
-        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_TRIAL_PTS, "bad buffer id");
+        need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_JP32, "bad buffer id");
         size_t have = 0;
         *out = const_cast<void*>(S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &have));
     });

@@ -188,8 +188,8 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 
 // ---------------------------------------------------------------- FP32 path
 
-// Point pass, FP32 arithmetic: per-slot Jacobian record J32 = [Jc(18), Jp(6)]
-// and, at the slot's camera-major position, the camera record [Jc(18), r(2)]
+// Point pass, FP32 arithmetic: per-slot Jacobian rows Jc32 (18) and Jp32 (6),
+// in slot order, and, at the slot's camera-major position, the camera record [Jc(18), r(2)]
 // (80 B, five 16-byte stores) for the camera passes. V / bp are summed per
 // point in FP32 by a segmented scan over each warp (slots of a point are
 // contiguous) and the warps' segment sums, and stored FP64. The residuals
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
     const int* __restrict__ s_pt, const float4* __restrict__ s_pxff, const float* __restrict__ cams32,
     const float2* __restrict__ ptsff, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
-    float* __restrict__ J32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
+    float* __restrict__ Jc32, float* __restrict__ Jp32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
     unsigned long long* __restrict__ counters, float delta) {
     __shared__ float seg[9][kPT];  // warp-segment sums, at each segment's last slot
     __shared__ unsigned long long redu[kPT / 32];
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             r[0] = rf.x;
             r[1] = rf.y;
             const bool fin = all_finite(r, 2) && all_finite(J, 24);
-            if (fin && delta > 0.f) {  // robust loss: rows scaled by sqrt(rho'(s)); J32 holds the scaled rows
+            if (fin && delta > 0.f) {  // robust loss: rows scaled by sqrt(rho'(s)); the records hold the scaled rows
                 const float sw = robust_sqrt_weight(r[0] * r[0] + r[1] * r[1], delta);
                 r[0] *= sw;
                 r[1] *= sw;
@@ -255,9 +255,12 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
                 for (int q = 0; q < 24; ++q) J[q] = 0.f;
                 r[0] = r[1] = 0.f;
             }
-            float4* out = reinterpret_cast<float4*>(J32 + 24ll * s);
+            float2* oc = reinterpret_cast<float2*>(Jc32 + 18ll * s);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) out[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+            for (int k = 0; k < 9; ++k) oc[k] = make_float2(J[2 * k], J[2 * k + 1]);
+            float2* op = reinterpret_cast<float2*>(Jp32 + 6ll * s);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) op[k] = make_float2(J[18 + 2 * k], J[19 + 2 * k]);
             float4* outc = reinterpret_cast<float4*>(J32c + 20ll * q);  // camera record
 #pragma unroll
             for (int q = 0; q < 4; ++q) outc[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
@@ -683,7 +686,7 @@ double Solver::accumulate() {
         cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(
             pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), reinterpret_cast<const float4*>(s_pxff_.get()),
-            cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), J32_.get(),
+            cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), Jc32_.get(), Jp32_.get(),
             J32c_.get(), V_.get(), bp_.get(), counters_.get(), static_cast<float>(huber_delta_));
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);

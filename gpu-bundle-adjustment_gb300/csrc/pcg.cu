@@ -3,7 +3,7 @@
 //   S x   = U_lambda x - sum_p W_p V'_p^-1 W_p^T x,   W_e = Jc_e^T Jp_e
 //   rhs   = bc - sum_p W_p V'_p^-1 bp_p
 //
-// computed implicitly from the per-slot FP32 Jacobian records (J32 = Jc, Jp):
+// computed implicitly from the per-slot FP32 Jacobian rows (Jc32, Jp32, slot order):
 //   point pass   (slots sorted by point)  w_p = V'^-1 (a bp_p + sum_e Jp_e^T (Jc_e x_c)),
 //                                         u_e = Jp_e w_p          (2 values per slot)
 //   camera pass  (camera-major chunks)    partial_c = sum_e Jc_e^T u_e
@@ -72,6 +72,8 @@ __device__ __forceinline__ double as_double(ff a) { return ffa::to_double(a); }
 template <typename T> __device__ __forceinline__ T from_double(double d);
 template <> __device__ __forceinline__ float from_double<float>(double d) { return static_cast<float>(d); }
 template <> __device__ __forceinline__ ff from_double<ff>(double d) { return ffa::from_double(d); }
+__device__ __forceinline__ float hi_of(float x) { return x; }
+__device__ __forceinline__ float hi_of(ff x) { return x.hi; }
 __device__ __forceinline__ ff to_ff(float x) { return {x, 0.f}; }
 __device__ __forceinline__ ff to_ff(ff x) { return x; }
 __device__ __forceinline__ float warp_total(float v) { return warp_sum(v); }
@@ -111,15 +113,22 @@ __device__ __forceinline__ void load_u(const ff* u, long long q, ff& a, ff& b) {
     b = {v.z, v.w};
 }
 
-__device__ __forceinline__ void load_j(const float* __restrict__ J32, long long s, float* J) {
-    const float4* q = reinterpret_cast<const float4*>(J32 + 24 * s);
+// J = [Jc(18), Jp(6)] of slot s
+__device__ __forceinline__ void load_j(const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long s,
+                                       float* J) {
+    const float2* qc = reinterpret_cast<const float2*>(Jc32 + 18 * s);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const float4 v = q[k];
-        J[4 * k] = v.x;
-        J[4 * k + 1] = v.y;
-        J[4 * k + 2] = v.z;
-        J[4 * k + 3] = v.w;
+    for (int k = 0; k < 9; ++k) {
+        const float2 v = qc[k];
+        J[2 * k] = v.x;
+        J[2 * k + 1] = v.y;
+    }
+    const float2* qp = reinterpret_cast<const float2*>(Jp32 + 6 * s);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 v = qp[k];
+        J[18 + 2 * k] = v.x;
+        J[19 + 2 * k] = v.y;
     }
 }
 
@@ -179,7 +188,8 @@ struct BacksubOut {
 template <typename T, bool kBack = false>
 __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
-                                                       const int* __restrict__ cam_pos, const float* __restrict__ J32,
+                                                       const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
+                                                       const float* __restrict__ Jp32,
                                                        const float* __restrict__ vinv_hi,
                                                        const float* __restrict__ vinv_lo,
                                                        const double* __restrict__ bp, const T* __restrict__ xt,
@@ -202,6 +212,9 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
         my_e = pt_off[my_p + 1];
     }
     T z0 = zero<T>(), z1 = zero<T>(), z2 = zero<T>();
+    // owners fetch V'^-1 first: its latency overlaps the slot loads and the scan
+    T vinv[6];
+    if (my_p < p1) load_vinv(vinv_hi, vinv_lo, my_p, vinv);
     // Single-pass chunks (the usual case) keep the slot's Jp, point and
     // camera-major position in registers for the u phase.
     const bool single = (s1 - s0) <= kPT;
@@ -217,7 +230,7 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                 key = s_pt[s];
                 q = cam_pos[s];
                 float J[24];
-                load_j(J32, s, J);
+                load_j(Jc32, Jp32, s, J);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
                 const T* xc = xt + 9ll * s_cam[s];
@@ -277,15 +290,13 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
             z1 = add(z1, from_double<T>(a * bp[3ll * my_p + 1]));
             z2 = add(z2, from_double<T>(a * bp[3ll * my_p + 2]));
         }
-        T v[6];
-        load_vinv(vinv_hi, vinv_lo, my_p, v);
-        apply_vinv(v, z0, z1, z2, w0, w1, w2);
+        apply_vinv(vinv, z0, z1, z2, w0, w1, w2);
         wsh[threadIdx.x][0] = w0;
         wsh[threadIdx.x][1] = w1;
         wsh[threadIdx.x][2] = w2;
         if (g_cm) {
 #pragma unroll
-            for (int k = 0; k < 6; ++k) vsh[threadIdx.x][k] = vinv_hi[6ll * my_p + k];
+            for (int k = 0; k < 6; ++k) vsh[threadIdx.x][k] = hi_of(vinv[k]);
         }
     }
     if constexpr (kBack) {
@@ -336,7 +347,7 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
     }
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int p = s_pt[s];
-        const float2* Jp2 = reinterpret_cast<const float2*>(J32 + 24ll * s + 18);
+        const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
         const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
         const float j[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
         T u0, u1;
@@ -840,7 +851,7 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     float4* g = rhs ? reinterpret_cast<float4*>(s.g_cm_.get()) : nullptr;
     cudaEvent_t ev = s.prof_start();
     schur_point_pass<T><<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
-                                                           s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+                                                           s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
                                                            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
                                                            u, done, BacksubOut{}, g);
     GBA_LAUNCH_CHECK();
@@ -880,13 +891,13 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
         to_f32_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, dc32);
         GBA_LAUNCH_CHECK();
         schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), nullptr, s.bp_.get(), dc32, -1.0, nullptr, nullptr, bk, nullptr);
     } else {
         split_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, s.dcff_.get());
         GBA_LAUNCH_CHECK();
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.J32_.get(),
+            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
             nullptr, nullptr, bk, nullptr);
     }

@@ -11,7 +11,7 @@
 //   work chunks    point chunks (whole points, <= 256 slots) for the point pass;
 //                  camera chunks (<= kCamChunk slots of one camera) for the camera pass
 //   normal eqs     U[81C] (full symmetric 9x9), bc[9C], V[6P] (packed lower 3x3),
-//                  bp[3P], W[27 E] (FP64, slot order) or J32[28 E] (FP32: Jc, Jp, r)
+//                  bp[3P], W[27 E] (FP64, slot order) or Jc32[18 E], Jp32[6 E] (FP32, slot order)
 //   Schur (plain)  pair list sorted by camera-pair block, dense S (n_pad x n_pad,
 //                  column-major, lower triangle), rhs, dc, dp
 //   Schur (mixed)  PCG vectors (9C) and block-Jacobi factors (81C)
@@ -35,21 +35,61 @@ public:
     ~DevBuf() { release(); }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
-    DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+    DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_), s_(o.s_), async_(o.async_) { o.p_ = nullptr; o.n_ = 0; }
     DevBuf& operator=(DevBuf&& o) noexcept {
-        if (this != &o) { release(); p_ = o.p_; n_ = o.n_; o.p_ = nullptr; o.n_ = 0; }
+        if (this != &o) {
+            release();
+            p_ = o.p_;
+            n_ = o.n_;
+            s_ = o.s_;
+            async_ = o.async_;
+            o.p_ = nullptr;
+            o.n_ = 0;
+        }
         return *this;
     }
-    void alloc(size_t n);   // defined in structure.cu (throws CudaError)
+    // Inside a StreamAllocScope: stream-ordered allocation on the scope's
+    // stream from the device's memory pool; otherwise cudaMalloc. Defined in
+    // structure.cu (throws CudaError).
+    void alloc(size_t n);
     void release();
     T* get() const { return p_; }
     size_t size() const { return n_; }
-    void swap(DevBuf& o) { std::swap(p_, o.p_); std::swap(n_, o.n_); }
+    void swap(DevBuf& o) {
+        std::swap(p_, o.p_);
+        std::swap(n_, o.n_);
+        std::swap(s_, o.s_);
+        std::swap(async_, o.async_);
+    }
 
 private:
     T* p_ = nullptr;
     size_t n_ = 0;
+    cudaStream_t s_ = nullptr;  // stream of a stream-ordered allocation (freed on it)
+    bool async_ = false;
 };
+
+// While alive, DevBuf allocations on this thread are stream-ordered on stream s
+// (cudaMallocAsync / cudaFreeAsync from the device's default memory pool),
+// and the pool keeps up to kPoolKeepBytes of freed memory for the next solve
+// instead of returning it to the driver: repeated solves then allocate and
+// free their working set without driver calls. The stream must outlive the
+// buffers allocated under the scope.
+class StreamAllocScope {
+public:
+    static constexpr unsigned long long kPoolKeepBytes = 32ull << 30;
+    explicit StreamAllocScope(cudaStream_t s);
+    ~StreamAllocScope();
+    StreamAllocScope(const StreamAllocScope&) = delete;
+    StreamAllocScope& operator=(const StreamAllocScope&) = delete;
+
+private:
+    cudaStream_t prev_s_;
+    bool prev_on_;
+};
+
+// Returns the memory the current device's pool keeps between solves to the driver.
+void release_cached_memory();
 
 struct PcgStats {
     int refine_steps = 0;
@@ -120,8 +160,8 @@ public:
     LearnedPreconditioner* model() { return model_; }
 
     // Raw views for the C-ABI download/inspection entry points.
-    enum Buf { kU, kV, kBc, kBp, kW, kVinv, kS, kRhs, kDc, kDp, kOrder, kJ32, kSdiag, kCams, kPts,
-               kTrialCams, kTrialPts };
+    enum Buf { kU, kV, kBc, kBp, kW, kVinv, kS, kRhs, kDc, kDp, kOrder, kJc32, kSdiag, kCams, kPts,
+               kTrialCams, kTrialPts, kJp32 };
     const void* buffer(Buf b, size_t* bytes) const;
 
     // Optional per-kernel device timing (CUDA events on the solver stream
@@ -156,7 +196,7 @@ public:
     DevBuf<int> pchunk_, cchunk_begin_, cchunk_cam_, cam_chunk_off_;
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
-    DevBuf<float> J32_;
+    DevBuf<float> Jc32_, Jp32_;  // mixed: FP32 Jacobian rows per slot, slot order (18 and 6 floats)
     DevBuf<float> J32c_;    // mixed: camera record [Jc(18), r(2)] per slot in camera-major position
     DevBuf<float> Vinv32_;  // mixed: FP32 copy of V'^-1 (6 per point) for the FP32 matvec
     DevBuf<float> Vinv32lo_;  // mixed: V'^-1 - Vinv32_ rounded to FP32 (float-float matvec)

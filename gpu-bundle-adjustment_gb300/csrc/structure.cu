@@ -21,16 +21,59 @@
 
 namespace gba {
 
+namespace {
+thread_local cudaStream_t t_alloc_stream = nullptr;
+thread_local bool t_alloc_async = false;
+
+cudaMemPool_t device_pool() {
+    int dev = 0;
+    GBA_CUDA_CHECK(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    GBA_CUDA_CHECK(cudaDeviceGetDefaultMemPool(&pool, dev));
+    return pool;
+}
+}  // namespace
+
+StreamAllocScope::StreamAllocScope(cudaStream_t s) : prev_s_(t_alloc_stream), prev_on_(t_alloc_async) {
+    unsigned long long keep = kPoolKeepBytes;  // the attribute is a 64-bit unsigned value
+    GBA_CUDA_CHECK(cudaMemPoolSetAttribute(device_pool(), cudaMemPoolAttrReleaseThreshold, &keep));
+    t_alloc_stream = s;
+    t_alloc_async = true;
+}
+
+StreamAllocScope::~StreamAllocScope() {
+    t_alloc_stream = prev_s_;
+    t_alloc_async = prev_on_;
+}
+
+void release_cached_memory() {
+    GBA_CUDA_CHECK(cudaDeviceSynchronize());
+    GBA_CUDA_CHECK(cudaMemPoolTrimTo(device_pool(), 0));
+}
+
 template <typename T>
 void DevBuf<T>::alloc(size_t n) {
     release();
     if (n == 0) return;
-    GBA_CUDA_CHECK(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)));
+    if (t_alloc_async) {
+        GBA_CUDA_CHECK(cudaMallocAsync(reinterpret_cast<void**>(&p_), n * sizeof(T), t_alloc_stream));
+        s_ = t_alloc_stream;
+        async_ = true;
+    } else {
+        GBA_CUDA_CHECK(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)));
+        async_ = false;
+    }
     n_ = n;
 }
 template <typename T>
 void DevBuf<T>::release() {
-    if (p_) cudaFree(p_);
+    if (p_) {
+        if (async_) {
+            cudaFreeAsync(p_, s_);
+        } else {
+            cudaFree(p_);
+        }
+    }
     p_ = nullptr;
     n_ = 0;
 }
@@ -80,6 +123,16 @@ __global__ void gather_obs_kernel(const int* __restrict__ order, const int* __re
 // pos[perm[i]] = i
 __global__ void inverse_perm_kernel(const int* __restrict__ perm, int n, int* __restrict__ pos) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[perm[i]] = i;
+}
+
+// Count of observations whose camera or point index is out of range.
+__global__ void check_indices_kernel(const int* __restrict__ oc, const int* __restrict__ op, int n, int C, int P,
+                                     unsigned long long* __restrict__ bad) {
+    unsigned long long cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        cnt += (oc[i] < 0 || oc[i] >= C || op[i] < 0 || op[i] >= P) ? 1ull : 0ull;
+    cnt = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(cnt));
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(bad, cnt);
 }
 
 // Camera-major copies of per-slot data: point index and float-float observation
@@ -173,13 +226,12 @@ int grid_for(long long n, int threads = 256) {
 
 }  // namespace
 
+// Host-side checks (sizes, pointers); the observation indices are checked on
+// the device when the solver is built (build_structure).
 void validate_problem(int C, int P, int E, const double* cams, const double* pts, const int* obs_cam,
                       const int* obs_pt, const double* obs_px) {
     if (C <= 0 || P <= 0 || E <= 0) throw std::invalid_argument("empty BAL problem");
     if (!cams || !pts || !obs_cam || !obs_pt || !obs_px) throw std::invalid_argument("null problem array");
-    for (int e = 0; e < E; ++e)
-        if (obs_cam[e] < 0 || obs_cam[e] >= C || obs_pt[e] < 0 || obs_pt[e] >= P)
-            throw std::invalid_argument("observation index out of range");
     if (static_cast<long long>(C) * 9 > INT_MAX / 2) throw std::invalid_argument("too many cameras");
 }
 
@@ -187,6 +239,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
                const int* obs_pt, const double* obs_px, SolverForm form, cudaStream_t stream)
     : C_(C), P_(P), E_(E), form_(form), stream_(stream) {
     validate_problem(C, P, E, cams, pts, obs_cam, obs_pt, obs_px);
+    StreamAllocScope alloc_scope(stream_);
 
     cams_.alloc(9ull * C);
     pts_.alloc(3ull * P);
@@ -229,7 +282,8 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         info_.alloc(1);
         build_pairs();
     } else {
-        J32_.alloc(24ull * E);
+        Jc32_.alloc(18ull * E);
+        Jp32_.alloc(6ull * E);
         J32c_.alloc(20ull * E);
         judge_x_.alloc(9ull * C);
         Vinv32_.alloc(6ull * P);
@@ -295,6 +349,19 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     pt_off_.alloc(P + 1ull);
     cam_off_.alloc(C + 1ull);
     cam_slots_.alloc(E);
+
+    // 0. observation indices in range, checked on the device before any kernel
+    //    indexes with them
+    {
+        DevBuf<unsigned long long> bad(1);
+        GBA_CUDA_CHECK(cudaMemsetAsync(bad.get(), 0, sizeof(unsigned long long), stream_));
+        check_indices_kernel<<<grid_for(E), 256, 0, stream_>>>(d_oc.get(), d_op.get(), E, C, P, bad.get());
+        GBA_LAUNCH_CHECK();
+        unsigned long long h_bad = 0;
+        GBA_CUDA_CHECK(cudaMemcpyAsync(&h_bad, bad.get(), sizeof h_bad, cudaMemcpyDeviceToHost, stream_));
+        sync();
+        if (h_bad) throw std::invalid_argument("observation index out of range");
+    }
 
     iota_kernel<<<grid_for(E), 256, 0, stream_>>>(iota.get(), E);
     GBA_LAUNCH_CHECK();
@@ -502,7 +569,8 @@ const void* Solver::buffer(Buf b, size_t* bytes) const {
         case kDc: return ret(dc_);
         case kDp: return ret(dp_);
         case kOrder: return ret(order_);
-        case kJ32: return ret(J32_);
+        case kJc32: return ret(Jc32_);
+        case kJp32: return ret(Jp32_);
         case kSdiag: return ret(Sdiag_);
         case kCams: return ret(cams_);
         case kPts: return ret(pts_);

@@ -25,9 +25,9 @@ LOSSES = {"none": 0, "huber": 1}
 TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE", 3: "TARGET_COST"}
 BUF = {
     "U": 0, "V": 1, "bc": 2, "bp": 3, "W": 4, "Vinv": 5, "S": 6, "rhs": 7, "dc": 8, "dp": 9,
-    "order": 10, "J32": 11, "Sdiag": 12, "cams": 13, "pts": 14, "trial_cams": 15, "trial_pts": 16,
+    "order": 10, "Jc32": 11, "Sdiag": 12, "cams": 13, "pts": 14, "trial_cams": 15, "trial_pts": 16, "Jp32": 17,
 }
-_BUF_DTYPE = {"order": np.int32, "J32": np.float32}
+_BUF_DTYPE = {"order": np.int32, "Jc32": np.float32, "Jp32": np.float32}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -137,6 +137,7 @@ _SIG = {
     "gba_solver_kernel_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "gba_solver_profile_reset": (C.c_int, [C.c_void_p]),
     "gba_launch_count": (C.c_ulonglong, []),
+    "gba_release_cached_memory": (C.c_int, []),
     "gba_solver_set_harvest": (C.c_int, [C.c_void_p, C.c_int]),
     "gba_solver_features": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
     "gba_mlp_num_params": (C.c_longlong, []),
@@ -333,6 +334,11 @@ def _to_result(r, traj, ttime, cap) -> "LMResult":
         traj[:n].tolist(), ttime[:n].tolist(), r.learned_choice,
         (r.judge_iters_block_jacobi, r.judge_iters_learned),
     )
+
+
+def release_cached_memory() -> None:
+    """Return the device memory the solvers' pool keeps between solves to the driver."""
+    _check(lib.gba_release_cached_memory())
 
 
 def launch_count() -> int:

@@ -179,15 +179,24 @@ int gba_solver_run(gba_solver* s, const gba_lm_options* opts, gba_lm_result* res
 int gba_solver_reset_params(gba_solver* s);
 /* Per-kernel device timing with CUDA events on the solver stream: enable /
  * disable, query (launches and total milliseconds of a named kernel since the
- * last reset), reset. Names: point_pass_f64, camera_pass_f64, point_pass_f32,
- * camera_pass_f32, cost_f64, schur_point_pass_f32, schur_camera_pass_f32,
- * schur_point_pass_f64, schur_camera_pass_f64, schur_assemble, dense_potrf. */
+ * last reset), reset. Names: point_pass_f64, camera_pass_f64, cost_f64,
+ * schur_assemble, dense_potrf, backsub (plain form); point_pass_f32,
+ * camera_pass_f32, cost_ff, schur_rhs_point_pass, schur_rhs_camera_pass,
+ * schur_point_pass_f32, schur_camera_pass_f32, schur_point_pass_ff,
+ * schur_camera_pass_ff, backsub, mlp_forward (mixed forms). */
 int gba_solver_profile(gba_solver* s, int enable);
 int gba_solver_kernel_stats(gba_solver* s, const char* name, long long* out_launches, double* out_total_ms);
 int gba_solver_profile_reset(gba_solver* s);
 
 /* Number of kernels this library has launched in the process so far. */
 unsigned long long gba_launch_count(void);
+
+/* Solvers allocate their device working set stream-ordered from the current
+ * device's default memory pool, which keeps up to 32 GiB of freed memory for
+ * the next solve (repeated solves then make no driver allocation calls). This
+ * synchronises the device and returns that cached memory to the driver. No
+ * reference counterpart (the reference allocates with cudaMalloc per call). */
+int gba_release_cached_memory(void);
 
 /* ------------------------------------------------------------ learned preconditioner
  * No reference counterpart (the reference has no iterative solver). The MLP
@@ -235,12 +244,13 @@ enum {
     GBA_BUF_DC = 8,       /* double[9 C] */
     GBA_BUF_DP = 9,       /* double[3 P] */
     GBA_BUF_ORDER = 10,   /* int[E]  original observation index of each slot */
-    GBA_BUF_J32 = 11,     /* float[24 E] Jc(18), Jp(6) per slot (mixed form) */
+    GBA_BUF_JC32 = 11,    /* float[18 E] Jc (2x9 row-major) per slot (mixed forms) */
     GBA_BUF_SDIAG = 12,   /* double[81 C] S diagonal blocks (mixed form) */
     GBA_BUF_CAMS = 13,    /* double[9 C] current cameras */
     GBA_BUF_PTS = 14,     /* double[3 P] current points */
     GBA_BUF_TRIAL_CAMS = 15,
-    GBA_BUF_TRIAL_PTS = 16
+    GBA_BUF_TRIAL_PTS = 16,
+    GBA_BUF_JP32 = 17     /* float[6 E]  Jp (2x3 row-major) per slot (mixed forms) */
 };
 /* Size in bytes of a solver buffer (0 if the form does not hold it). */
 int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out_bytes);

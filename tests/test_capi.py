@@ -68,17 +68,6 @@ def test_launch_bounds_generator_is_noise_free(gba):
     assert gba.total_squared_error(prob) > 1.0
 
 
-def test_solver_create_rejects_bad_indices(gba):
-    prob = gba.synthetic_custom(3, 10, 2, 3, 1.5, seed=1)
-    bad = prob.copy()
-    bad.obs_point[0] = 10
-    with pytest.raises(gba.GbaError) as ei:
-        gba.Solver(bad)
-    assert ei.value.status == 1
-    with pytest.raises(gba.GbaError):
-        gba.solve(bad)
-
-
 def test_options_defaults_mirror_reference(gba):
     o = gba.default_options()
     assert (o.max_iterations, o.initial_lambda, o.rel_decrease_tol, o.max_inner_trials, o.verbose) == (

@@ -28,7 +28,7 @@ def test_mixed_normal_equations_within_fp32(gba, oracle, small):
         bc = s.download("bc")
         Vp = s.download("V").reshape(-1, 6)
         bp = s.download("bp")
-        J = s.download("J32").reshape(-1, 24)
+        J = np.hstack([s.download("Jc32").reshape(-1, 18), s.download("Jp32").reshape(-1, 6)])
         order = s.download("order")
     ref = oracle.accumulate(small)
     # the cost is float-float (~48-bit significands); the residual cancels
@@ -110,7 +110,7 @@ def _implicit_system(s, prob, lam):
     """rhs and x -> S x of the mixed form's system, in numpy FP64 from the device's
     own FP32 Jacobian records and FP64 U, V, bc, bp (the system the refinement solves)."""
     C, P = prob.num_cameras, prob.num_points
-    J = s.download("J32").reshape(-1, 24).astype(np.float64)
+    J = np.hstack([s.download("Jc32").reshape(-1, 18), s.download("Jp32").reshape(-1, 6)]).astype(np.float64)
     order = s.download("order")
     cam = prob.obs_camera[order]
     pt = prob.obs_point[order]

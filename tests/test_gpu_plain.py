@@ -309,3 +309,20 @@ def test_plain_huber_lm_trajectory_matches_oracle_workload1(gba, oracle):
     assert t_dev.shape == t_ref.shape
     assert np.max(np.abs(t_dev - t_ref) / t_ref) < 1e-9
     assert rel_err(run.cameras, ref_cams) < 1e-6
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_solver_create_rejects_bad_indices(gba, form):
+    """Observation indices are range-checked on the device before any kernel
+    indexes with them; a bad one is an invalid-argument status (1)."""
+    prob = gba.synthetic_custom(3, 10, 2, 3, 1.5, seed=1)
+    for field, value in (("obs_point", 10), ("obs_point", -1), ("obs_camera", 3)):
+        bad = prob.copy()
+        getattr(bad, field)[0] = value
+        with pytest.raises(gba.GbaError) as ei:
+            gba.Solver(bad, form)
+        assert ei.value.status == 1
+        with pytest.raises(gba.GbaError) as ei:
+            gba.solve(bad, form=form)
+        assert ei.value.status == 1
+    gba.Solver(prob, form).close()  # the device is still usable
