@@ -178,5 +178,80 @@ GBA_HD void residual_jacobian(const T* cam, const T* X, const T* obs, T* r, T* J
     }
 }
 
+// Residual + Jacobian from per-camera constants precomputed once per camera
+// (in FP64, stored in T): pre = [R (9, row-major), J_l (9), t (3), f, k1, k2,
+// first_order (0 / 1)]. On the first-order branch R = I + [a]x (so R X is the
+// branch's X + a x X), J_l = I, and the branch's dRX/da = -[X]x and dX_c/dX = I
+// are applied here; otherwise the same formulas as residual_jacobian.
+template <typename T>
+GBA_HD void residual_jacobian_pre(const T* pre, const T* X, const T* obs, T* r, T* Jc, T* Jp) {
+    const T* R = pre;
+    const T* Jl = pre + 9;
+    const bool first_order = pre[24] != T(0);
+    T RX[3];
+    for (int i = 0; i < 3; ++i) RX[i] = R[3 * i] * X[0] + R[3 * i + 1] * X[1] + R[3 * i + 2] * X[2];
+    const T P0 = RX[0] + pre[18], P1 = RX[1] + pre[19], P2 = RX[2] + pre[20];
+    const T iz = T(1) / P2;
+    const T u = -P0 * iz, v = -P1 * iz;
+    const T r2 = u * u + v * v;
+    const T f = pre[21], k1 = pre[22], k2 = pre[23];
+    const T d = T(1) + r2 * (k1 + k2 * r2);
+    const T L = k1 + T(2) * k2 * r2;
+    r[0] = f * d * u - obs[0];
+    r[1] = f * d * v - obs[1];
+    const T D00 = f * (d + T(2) * L * u * u);
+    const T D01 = f * (T(2) * L * u * v);
+    const T D11 = f * (d + T(2) * L * v * v);
+    const T m02 = -u * iz, m12 = -v * iz;
+    T DM[6];
+    DM[0] = -D00 * iz;  DM[1] = -D01 * iz;  DM[2] = D00 * m02 + D01 * m12;
+    DM[3] = -D01 * iz;  DM[4] = -D11 * iz;  DM[5] = D01 * m02 + D11 * m12;
+    const T y0 = first_order ? X[0] : RX[0];
+    const T y1 = first_order ? X[1] : RX[1];
+    const T y2 = first_order ? X[2] : RX[2];
+    for (int row = 0; row < 2; ++row) {
+        const T g0 = DM[row * 3 + 0], g1 = DM[row * 3 + 1], g2 = DM[row * 3 + 2];
+        const T b0 = -g1 * y2 + g2 * y1, b1 = g0 * y2 - g2 * y0, b2 = -g0 * y1 + g1 * y0;
+        for (int j = 0; j < 3; ++j) Jc[row * 9 + j] = b0 * Jl[j] + b1 * Jl[3 + j] + b2 * Jl[6 + j];
+        for (int j = 0; j < 3; ++j) Jc[row * 9 + 3 + j] = DM[row * 3 + j];
+        const T p = row == 0 ? u : v;
+        Jc[row * 9 + 6] = d * p;
+        Jc[row * 9 + 7] = f * r2 * p;
+        Jc[row * 9 + 8] = f * r2 * r2 * p;
+        for (int j = 0; j < 3; ++j)
+            Jp[row * 3 + j] = first_order ? DM[row * 3 + j]
+                                          : g0 * R[j] + g1 * R[3 + j] + g2 * R[6 + j];
+    }
+}
+
+// The per-camera constants of residual_jacobian_pre, in FP64 (28 slots; the
+// last three are padding).
+GBA_HD void camera_constants(const double* a, double* o) {
+    const double th2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    if (th2 > 1e-24) {
+        const double th = sqrt(th2);
+        const double inv = 1.0 / th;
+        const double w0 = a[0] * inv, w1 = a[1] * inv, w2 = a[2] * inv;
+        const double s = sin(th), c = cos(th), sh = sin(0.5 * th);
+        const double omc = 2.0 * sh * sh;
+        o[0] = c + omc * w0 * w0;  o[1] = -s * w2 + omc * w0 * w1;  o[2] = s * w1 + omc * w0 * w2;
+        o[3] = s * w2 + omc * w1 * w0;  o[4] = c + omc * w1 * w1;  o[5] = -s * w0 + omc * w1 * w2;
+        o[6] = -s * w1 + omc * w2 * w0;  o[7] = s * w0 + omc * w2 * w1;  o[8] = c + omc * w2 * w2;
+        const double p = s * inv, q = omc * inv, g = 1.0 - p;
+        o[9] = p + g * w0 * w0;  o[10] = -q * w2 + g * w0 * w1;  o[11] = q * w1 + g * w0 * w2;
+        o[12] = q * w2 + g * w1 * w0;  o[13] = p + g * w1 * w1;  o[14] = -q * w0 + g * w1 * w2;
+        o[15] = -q * w1 + g * w2 * w0;  o[16] = q * w0 + g * w2 * w1;  o[17] = p + g * w2 * w2;
+        o[24] = 0.0;
+    } else {
+        o[0] = 1.0;   o[1] = -a[2]; o[2] = a[1];
+        o[3] = a[2];  o[4] = 1.0;   o[5] = -a[0];
+        o[6] = -a[1]; o[7] = a[0];  o[8] = 1.0;
+        for (int i = 0; i < 9; ++i) o[9 + i] = (i % 4 == 0) ? 1.0 : 0.0;
+        o[24] = 1.0;
+    }
+    for (int i = 0; i < 6; ++i) o[18 + i] = a[3 + i];
+    o[25] = o[26] = o[27] = 0.0;
+}
+
 }  // namespace model
 }  // namespace gba

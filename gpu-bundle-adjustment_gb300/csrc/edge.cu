@@ -23,6 +23,7 @@ namespace {
 constexpr int kPT = 256;       // point-pass threads (= max slots per chunk)
 constexpr int kCT = 128;       // camera-pass threads
 constexpr int kCamChunk = 1024;
+constexpr int kCamRec = 28;    // floats per camera record of the FP32 Jacobian pass
 
 template <typename T>
 __device__ __forceinline__ bool all_finite(const T* v, int n) {
@@ -228,15 +229,22 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
         if (s < s1) {
             const int c = s_cam[s], p = s_pt[s];
             key = p;
-            float cam[9], X[3], obs[2], r[2], J[24];
+            float cam[kCamRec], X[3], obs[2], r[2], J[24];
+            const float4* c4 = reinterpret_cast<const float4*>(cams32 + static_cast<long long>(kCamRec) * c);
 #pragma unroll
-            for (int k = 0; k < 9; ++k) cam[k] = __ldg(cams32 + 9 * c + k);
+            for (int k = 0; k < kCamRec / 4; ++k) {
+                const float4 t = __ldg(c4 + k);
+                cam[4 * k] = t.x;
+                cam[4 * k + 1] = t.y;
+                cam[4 * k + 2] = t.z;
+                cam[4 * k + 3] = t.w;
+            }
 #pragma unroll
             for (int k = 0; k < 3; ++k) X[k] = __ldg(&ptsff[3ll * p + k].x);
             const float4 o = s_pxff[s];
             obs[0] = o.x;
             obs[1] = o.z;
-            model::residual_jacobian(cam, X, obs, r, J, J + 18);
+            model::residual_jacobian_pre(cam, X, obs, r, J, J + 18);
             const long long q = cam_pos[s];
             const float2 rf = r_cur[q];  // float-float evaluated residual, stored FP32 (camera-major)
             r[0] = rf.x;
@@ -400,7 +408,9 @@ __global__ void __launch_bounds__(256) ordered_sum(const double* __restrict__ pa
 constexpr int kCamPre = 16;
 // Per-camera constants of the residual: rotation matrix (Rodrigues), t, f, k1,
 // k2 (kCamPre doubles); preff (may be null): the same as float-float pairs;
-// cams32 (may be null): the camera parameters rounded to FP32.
+// cams32 (may be null): the FP32 Jacobian pass's per-camera record
+// (model::camera_constants, 28 floats: R, J_l, t, f, k1, k2, branch flag),
+// computed in FP64 and rounded.
 __global__ void camera_precompute_kernel(const double* __restrict__ cams, int C, double* __restrict__ pre,
                                          float2* __restrict__ preff, float* __restrict__ cams32) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -427,8 +437,13 @@ __global__ void camera_precompute_kernel(const double* __restrict__ cams, int C,
     for (int i = 0; i < 6; ++i) o[9 + i] = a[3 + i];
     o[15] = 0.0;
     if (cams32) {
+        double k[kCamRec];
+        model::camera_constants(a, k);
+        float4* o4 = reinterpret_cast<float4*>(cams32 + static_cast<long long>(kCamRec) * c);
 #pragma unroll
-        for (int i = 0; i < 9; ++i) cams32[9ll * c + i] = static_cast<float>(a[i]);
+        for (int i = 0; i < kCamRec / 4; ++i)
+            o4[i] = make_float4(static_cast<float>(k[4 * i]), static_cast<float>(k[4 * i + 1]),
+                                static_cast<float>(k[4 * i + 2]), static_cast<float>(k[4 * i + 3]));
     }
     if (preff) {
 #pragma unroll

@@ -209,7 +209,7 @@ public:
     DevBuf<float> s_pxff_;      // mixed: observations in slot order as float-float pairs (4 floats per slot)
     DevBuf<float> cm_pxff_;     // mixed: the same at camera-major positions
     DevBuf<int> cm_pt_;         // mixed: point of each camera-major position
-    DevBuf<float> cams32_;      // mixed: cameras rounded to FP32 (9 per camera), for the FP32 Jacobians
+    DevBuf<float> cams32_;      // mixed: per-camera R, J_l, t, f, k1, k2, branch flag (28 floats) for the FP32 Jacobians
     DevBuf<float> r_cur_, r_trial_;  // mixed: float-float evaluated residuals (FP32, camera-major) at current / trial parameters
     bool resid_valid_ = false;       // r_cur_ and scal_[0] hold the current parameters' residuals / SSE
     DevBuf<double> sse_part_, cam_part_, scal_;  // scal_: [0] sse, [1] trial sse, [2] denom, [3..] scratch

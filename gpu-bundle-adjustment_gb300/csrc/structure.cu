@@ -289,7 +289,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         Vinv32_.alloc(6ull * P);
         cam_pre_ff_.alloc(32ull * C);
         pts_ff_.alloc(6ull * P);
-        cams32_.alloc(9ull * C);
+        cams32_.alloc(28ull * C);
         Vinv32lo_.alloc(6ull * P);
         dcff_.alloc(18ull * C);
         pcg_p32_.alloc(9ull * C);

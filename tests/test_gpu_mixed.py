@@ -244,3 +244,21 @@ def test_float_float_cost_falls_back_to_fp64_out_of_range(gba, oracle, small):
         sse = s.accumulate()
     assert np.isfinite(sse)
     assert abs(sse - ref) <= 1e-6 * ref
+
+
+def test_mixed_normal_equations_first_order_rotation_branch(gba, oracle):
+    """A camera with a zero rotation vector takes the first-order branch
+    (R X = X + a x X, dRX/da = -[X]x): the per-camera precomputed records of the
+    FP32 Jacobian pass reproduce it (U, bc, V, bp within FP32 rounding)."""
+    prob = gba.synthetic_custom(5, 600, 2, 5, 1.4, seed=41)
+    prob.cameras[9 * 2:9 * 2 + 3] = 0.0
+    prob.cameras[9 * 3:9 * 3 + 3] = [1e-13, -2e-13, 0.0]
+    with gba.Solver(prob, "mixed") as s:
+        s.accumulate()
+        U = s.download("U").reshape(-1, 9, 9)
+        bc = s.download("bc")
+        bp = s.download("bp")
+    ref = oracle.accumulate(prob)
+    assert rel_err(U, ref["U"]) < 2e-5
+    assert rel_err(bc, ref["bc"]) < 2e-5
+    assert rel_err(bp, ref["bp"]) < 2e-5
