@@ -141,9 +141,9 @@ def algorithmic_bytes(kernel: str, C: int, P: int, E: int) -> float:
     if kernel == "schur_camera_pass_ff":
         return E * 96.0
     if kernel == "point_pass_f32":
-        # per slot: s_cam, s_pt, cam_pos, float-float pixel, r_cur (36 B) in, Jc32 + Jp32 96 B + camera record 80 B out;
-        # per point: point 24 B in, V / bp 72 B out; per camera 72 B
-        return E * 212.0 + P * 96.0 + C * 36.0
+        # per slot: s_cam, s_pt, cam_pos, r_cur (20 B) in, Jc32 + Jp32 96 B + camera record 80 B out;
+        # per point: point 24 B in, V / bp 72 B out; per camera: record 112 B
+        return E * 196.0 + P * 96.0 + C * 112.0
     if kernel == "cost_f64":
         return E * 32.0 + P * 24.0 + C * 72.0
     if kernel == "cost_ff":

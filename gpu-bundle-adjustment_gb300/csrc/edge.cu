@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 // robust loss, J and r are scaled by sqrt(rho'(s)) before anything is stored.
 __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
-    const int* __restrict__ s_pt, const float4* __restrict__ s_pxff, const float* __restrict__ cams32,
+    const int* __restrict__ s_pt, const float* __restrict__ cams32,
     const float2* __restrict__ ptsff, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
     float* __restrict__ Jc32, float* __restrict__ Jp32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
     unsigned long long* __restrict__ counters, float delta) {
@@ -241,9 +241,9 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             }
 #pragma unroll
             for (int k = 0; k < 3; ++k) X[k] = __ldg(&ptsff[3ll * p + k].x);
-            const float4 o = s_pxff[s];
-            obs[0] = o.x;
-            obs[1] = o.z;
+            // The Jacobian does not depend on the observation, and the residual
+            // comes from the cost pass: the model's own residual is not used.
+            obs[0] = obs[1] = 0.f;
             model::residual_jacobian_pre(cam, X, obs, r, J, J + 18);
             const long long q = cam_pos[s];
             const float2 rf = r_cur[q];  // float-float evaluated residual, stored FP32 (camera-major)
@@ -700,8 +700,7 @@ double Solver::accumulate() {
         const float2* rc = reinterpret_cast<const float2*>(r_cur_.get());
         cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(
-            pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), reinterpret_cast<const float4*>(s_pxff_.get()),
-            cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), Jc32_.get(), Jp32_.get(),
+            pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), Jc32_.get(), Jp32_.get(),
             J32c_.get(), V_.get(), bp_.get(), counters_.get(), static_cast<float>(huber_delta_));
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);

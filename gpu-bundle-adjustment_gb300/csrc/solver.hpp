@@ -206,8 +206,7 @@ public:
     DevBuf<double> cam_pre_;  // per-camera rotation matrix, translation, intrinsics (16 per camera)
     DevBuf<float> cam_pre_ff_;  // mixed: the same as float-float pairs (32 floats per camera)
     DevBuf<float> pts_ff_;      // mixed: float-float copy of the points being costed (6 floats per point)
-    DevBuf<float> s_pxff_;      // mixed: observations in slot order as float-float pairs (4 floats per slot)
-    DevBuf<float> cm_pxff_;     // mixed: the same at camera-major positions
+    DevBuf<float> cm_pxff_;     // mixed: observations as float-float pairs (4 floats) at camera-major positions
     DevBuf<int> cm_pt_;         // mixed: point of each camera-major position
     DevBuf<float> cams32_;      // mixed: per-camera R, J_l, t, f, k1, k2, branch flag (28 floats) for the FP32 Jacobians
     DevBuf<float> r_cur_, r_trial_;  // mixed: float-float evaluated residuals (FP32, camera-major) at current / trial parameters

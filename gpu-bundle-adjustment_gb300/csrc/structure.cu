@@ -135,15 +135,18 @@ __global__ void check_indices_kernel(const int* __restrict__ oc, const int* __re
     if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(bad, cnt);
 }
 
-// Camera-major copies of per-slot data: point index and float-float observation
-// of camera-major position i (slot cam_slots[i]).
+// Camera-major copies of per-slot data: point index and observation (as
+// float-float pairs) of camera-major position i (slot cam_slots[i]).
 __global__ void gather_cm_kernel(const int* __restrict__ cam_slots, const int* __restrict__ s_pt,
-                                 const float4* __restrict__ s_pxff, int n, int* __restrict__ cm_pt,
+                                 const double2* __restrict__ s_px, int n, int* __restrict__ cm_pt,
                                  float4* __restrict__ cm_pxff) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int s = cam_slots[i];
         cm_pt[i] = s_pt[s];
-        cm_pxff[i] = s_pxff[s];
+        const double2 o = s_px[s];
+        const float hx = __double2float_rn(o.x), hy = __double2float_rn(o.y);
+        cm_pxff[i] = make_float4(hx, __double2float_rn(o.x - static_cast<double>(hx)), hy,
+                                 __double2float_rn(o.y - static_cast<double>(hy)));
     }
 }
 
@@ -381,10 +384,6 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     GBA_LAUNCH_CHECK();
     csr_offsets_kernel<<<grid_for(E), 256, 0, stream_>>>(s_pt_.get(), E, P, pt_off_.get());
     GBA_LAUNCH_CHECK();
-    if (form_ != SolverForm::Plain) {
-        s_pxff_.alloc(4ull * E);
-        launch_split_ff(s_px_.get(), 2ll * E, s_pxff_.get(), stream_);
-    }
 
     // 2. camera-major view of the slots (stable: slot order within a camera)
     tb = tmp.size();
@@ -399,7 +398,7 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
         cm_pt_.alloc(E);
         cm_pxff_.alloc(4ull * E);
         gather_cm_kernel<<<grid_for(E), 256, 0, stream_>>>(cam_slots_.get(), s_pt_.get(),
-                                                           reinterpret_cast<const float4*>(s_pxff_.get()), E,
+                                                           reinterpret_cast<const double2*>(s_px_.get()), E,
                                                            cm_pt_.get(), reinterpret_cast<float4*>(cm_pxff_.get()));
         GBA_LAUNCH_CHECK();
     }
