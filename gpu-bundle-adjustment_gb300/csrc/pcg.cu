@@ -18,7 +18,7 @@
 // products, FP64 sums, FP64 Cholesky); the learned form replaces their
 // factors by the MLP-corrected ones (mlp.cu). PCG vectors and dot products are
 // FP64 with deterministic reductions; all PCG control scalars live on the
-// device and the host polls a convergence flag every kCheck iterations.
+// device and the host polls a convergence flag after batches of iterations.
 //
 // No reference counterpart: the reference solves S densely on the host.
 
@@ -36,8 +36,7 @@ constexpr int kCT = 128;
 constexpr int kVT = 256;  // vector-kernel threads
 constexpr int kCB = 32;   // thread-per-camera kernels: one warp per block spreads C cameras over the SMs
 constexpr int kCamChunk = 1024;
-constexpr int kCheck = 8;       // PCG iterations launched between host checks of the convergence flag
-constexpr int kCheckFirst = 2;  // ... for the first check (loose solves end in one or two)
+constexpr int kCheck = 8;       // most PCG iterations launched between host checks of the convergence flag
 constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to be decisive
 constexpr int kJudgeAttempts = 2;    // indecisive judgements before block-Jacobi is kept for the solve
 constexpr double kLooseTol = 1e-3;   // refinement targets at or above this run the fast (FP32) path
@@ -969,7 +968,17 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
         GBA_LAUNCH_CHECK();
         // p.q partials (nvb) and r.r / r.z partials (nub) in disjoint ranges
         double* red_pq = red2 + nub + 1;
-        for (int it = 0, batch = kCheckFirst; it < opts.pcg_max_iters; it += batch, batch = kCheck) {
+        // Launch batches sized from the previous inner solve's iteration count
+        // (then 1, 2, 4, 8, 8, ...): a launch after convergence returns at once
+        // but still dispatches its whole grid (tens of microseconds for the
+        // point pass), so overshooting costs more than one extra check.
+        int batch = std::max(1, std::min(prev_inner_ - 1, std::min(kCheck, opts.pcg_max_iters)));
+        double h[9];
+        if (opts.pcg_max_iters <= 0) {  // no iteration: the state pcg_init_finalize left
+            GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
+            sync();
+        }
+        for (int it = 0, next = 1; it < opts.pcg_max_iters; it += batch, batch = std::min(next, kCheck), next *= 2) {
             for (int j = 0; j < batch; ++j) {
                 implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
                 pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
@@ -982,16 +991,13 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
                                                         nub, opts.pcg_max_iters, sc);
                 GBA_LAUNCH_CHECK();
             }
-            double flag = 0.0;
-            GBA_CUDA_CHECK(cudaMemcpyAsync(&flag, done, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+            GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
             sync();
-            if (flag != 0.0) break;
+            if (h[S_DONE] != 0.0) break;
         }
-        double h[9];
-        GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
-        sync();
         *ok = h[S_DONE] != 2.0 && h[S_RR] <= h[S_TOL2] * h[S_BB];
         inner_rel2 = h[S_BB] > 0.0 ? h[S_RR] / h[S_BB] : 0.0;
+        prev_inner_ = static_cast<int>(h[S_ITERS]);
         return static_cast<long long>(h[S_ITERS]);
     };
     bool use_learned = learned && learned_choice_ == 1;

@@ -233,9 +233,11 @@ public:
     long long judge_iters_[2] = {0, 0};  // inner PCG iterations of the judged solve: block-Jacobi, learned
     int judge_attempts_ = 0;             // judgements made in this solve
     bool fast_solve_ = false;            // the last Schur solve ran the loose-target FP32 path
+    int prev_inner_ = 0;                 // iterations of the last inner PCG solve (launch-batch predictor)
     void begin_solve() {
         learned_choice_ = 0;
         judge_attempts_ = 0;
+        prev_inner_ = 0;
     }
     // Robust loss of the cost and the normal equations (<= 0: none). Changing it
     // invalidates the cached residuals / SSE of the current parameters.
