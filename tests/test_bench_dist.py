@@ -1,0 +1,60 @@
+"""Multi-process plumbing of bench.py on CPU (gloo, world size 2): the
+max-over-ranks timing and the reference arm's rank-0-only run. The solve path
+itself runs as independent replicas (no collective on the data path)."""
+import importlib.util
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _load_bench():
+    spec = importlib.util.spec_from_file_location("bench_under_test", ROOT / "bench.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        bench = _load_bench()
+        out[rank] = bench.max_over_ranks(1.5 + rank, world, device="cpu")
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_world2():
+    torch = pytest.importorskip("torch")
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    manager = mp.Manager()
+    out = manager.dict()
+    mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
+    assert dict(out) == {0: 2.5, 1: 2.5}
+
+
+def test_single_rank_max_is_identity():
+    bench = _load_bench()
+    assert bench.max_over_ranks(3.25, 1) == 3.25
+
+
+def test_reference_arm_only_on_rank0(monkeypatch, capsys):
+    bench = _load_bench()
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    args = bench.argparse.Namespace(workload=1, seed=None, reference_iterations=1, warmup=0, steps=1)
+    assert bench.run_reference(args) is None
+    assert capsys.readouterr().out == ""
