@@ -258,6 +258,25 @@ __global__ void __launch_bounds__(256) denom_finalize(const double* __restrict__
 }  // namespace
 
 unsigned long long Solver::damp_invert_v(double lambda) {
+    damp_launch(lambda);
+    unsigned long long bad = 0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&bad, counters_.get() + 3, sizeof bad, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    if (bad) add_nonspd(bad);
+    return bad;
+}
+
+// keep the cumulative non-SPD count (reference counters[1])
+void Solver::add_nonspd(unsigned long long n) {
+    unsigned long long h[2];
+    GBA_CUDA_CHECK(cudaMemcpyAsync(h, counters_.get(), sizeof h, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    h[1] += n;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(counters_.get(), h, sizeof h, cudaMemcpyHostToDevice, stream_));
+    sync();
+}
+
+void Solver::damp_launch(double lambda) {
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get() + 3, 0, sizeof(unsigned long long), stream_));
     const int grid = std::min(ceil_div(P_, kTB), 8 * device_sm_count());
     if (form_ == SolverForm::Plain) {
@@ -268,22 +287,18 @@ unsigned long long Solver::damp_invert_v(double lambda) {
                                                            P_, Vinv32_.get(), Vinv32lo_.get(), counters_.get() + 3);
     }
     GBA_LAUNCH_CHECK();
-    unsigned long long bad = 0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&bad, counters_.get() + 3, sizeof bad, cudaMemcpyDeviceToHost, stream_));
-    sync();
-    if (bad) {
-        // keep the cumulative non-SPD count (reference counters[1])
-        unsigned long long h[2];
-        GBA_CUDA_CHECK(cudaMemcpyAsync(h, counters_.get(), sizeof h, cudaMemcpyDeviceToHost, stream_));
-        sync();
-        h[1] += bad;
-        GBA_CUDA_CHECK(cudaMemcpyAsync(counters_.get(), h, sizeof h, cudaMemcpyHostToDevice, stream_));
-        sync();
-    }
-    return bad;
 }
 
 double Solver::back_substitute(double lambda) {
+    backsub_launch(lambda);
+    double denom = 0.0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&denom, scal_.get() + 2, sizeof denom, cudaMemcpyDeviceToHost, stream_));
+    sync();
+    return denom;
+}
+
+// dp, trial parameters and the gain denominator into scal_[2], without a host read.
+void Solver::backsub_launch(double lambda) {
     const int ncam = ceil_div(9ll * C_, kTB);
     double* part = red_part_.get();
     camera_step_kernel<<<ncam, kTB, 0, stream_>>>(dc_.get(), U_.get(), bc_.get(), cams_.get(), lambda, C_,
@@ -301,10 +316,6 @@ double Solver::back_substitute(double lambda) {
     prof_stop("backsub", ev);
     denom_finalize<<<1, 256, 0, stream_>>>(part, ncam, n_pchunk_, scal_.get() + 2);
     GBA_LAUNCH_CHECK();
-    double denom = 0.0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&denom, scal_.get() + 2, sizeof denom, cudaMemcpyDeviceToHost, stream_));
-    sync();
-    return denom;
 }
 
 void launch_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n, cudaStream_t s) {

@@ -392,6 +392,10 @@ __global__ void camera_finalize(const int* __restrict__ cam_chunk_off, const dou
     }
 }
 
+__global__ void add_counter_kernel(unsigned long long* __restrict__ dst, const unsigned long long* __restrict__ src) {
+    *dst += *src;
+}
+
 // Sum of n partials in a fixed order (single CTA) -> *out.
 __global__ void __launch_bounds__(256) ordered_sum(const double* __restrict__ part, int n, double* __restrict__ out) {
     __shared__ double red[8];
@@ -758,6 +762,32 @@ void Solver::prepare_ff(const double* cams, const double* pts) {
 }
 
 double Solver::trial_cost() {
+    trial_cost_launch(counters_.get());
+    double sse = 0.0;
+    GBA_CUDA_CHECK(cudaMemcpyAsync(&sse, scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    sync();
+    return sse;
+}
+
+void Solver::read_trial(double* denom, double* sse, unsigned long long* cost_anomalies) {
+    GBA_CUDA_CHECK(cudaMemcpyAsync(denom, scal_.get() + 2, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(sse, scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cost_anomalies, counters_.get() + 2, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, stream_));
+    sync();
+}
+
+void Solver::zero_cost_scratch() {
+    GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get() + 2, 0, sizeof(unsigned long long), stream_));
+}
+
+void Solver::commit_cost_anomalies() {
+    add_counter_kernel<<<1, 1, 0, stream_>>>(counters_.get(), counters_.get() + 2);
+    GBA_LAUNCH_CHECK();
+}
+
+// Trial SSE into scal_[1] (non-finite residual count added to *anomalies), without a host read.
+void Solver::trial_cost_launch(unsigned long long* anomalies) {
     if (form_ == SolverForm::Plain) {
         const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
         cudaEvent_t ev = prof_start();
@@ -765,20 +795,16 @@ double Solver::trial_cost() {
                                                                          nullptr);
         GBA_LAUNCH_CHECK();
         cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,
-                                                 cam_pre_.get(), tpts_.get(), sse_part_.get(), counters_.get(),
+                                                 cam_pre_.get(), tpts_.get(), sse_part_.get(), anomalies,
                                                  nullptr, huber_delta_);
         GBA_LAUNCH_CHECK();
         prof_stop("cost_f64", ev);
     } else {
-        cost_mixed(tcams_.get(), tpts_.get(), counters_.get(), reinterpret_cast<float2*>(r_trial_.get()));
+        cost_mixed(tcams_.get(), tpts_.get(), anomalies, reinterpret_cast<float2*>(r_trial_.get()));
     }
     ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), form_ == SolverForm::Plain ? n_pchunk_ : n_cchunk_,
                                         scal_.get() + 1);
     GBA_LAUNCH_CHECK();
-    double sse = 0.0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&sse, scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    sync();
-    return sse;
 }
 
 void launch_eval_edges_f64(const double* cams, const double* pts, const int* oc, const int* op, const double* px,

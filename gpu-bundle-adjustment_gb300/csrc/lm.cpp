@@ -63,6 +63,71 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
         bool accepted = false;
         for (int trial = 0; trial < opts.max_inner_trials; ++trial) {
             ++res.trials;
+            if (!plain) {
+                // Mixed forms: the same trial with three host reads (non-SPD
+                // count with the right-hand side norm; the PCG checks; the
+                // denominator, trial SSE and its non-finite count together).
+                phase(res.t_damp, [&] { s.damp_launch(lambda); return 0; });
+                unsigned long long bad = 0;
+                const PcgStats st = phase(res.t_schur, [&] { return s.schur_pcg(lambda, opts, learned, &bad); });
+                if (bad) {
+                    s.add_nonspd(bad);
+                    if (opts.verbose)
+                        std::fprintf(stderr, "  iter %d trial: lambda %.3g non-SPD point blocks %llu: reject\n",
+                                     res.iterations, lambda, bad);
+                    lambda *= nu;
+                    nu *= 2.0;
+                    continue;
+                }
+                res.pcg_iterations += st.pcg_iterations;
+                res.refine_steps += st.refine_steps;
+                if (!std::isfinite(st.rel_residual)) {
+                    lambda *= nu;
+                    nu *= 2.0;
+                    continue;
+                }
+                double denom = 0.0, trial_sse = 0.0;
+                unsigned long long cost_anom = 0;
+                phase(res.t_backsub, [&] { s.backsub_launch(lambda); return 0; });
+                phase(res.t_cost, [&] {
+                    s.zero_cost_scratch();
+                    s.trial_cost_launch(s.counters_.get() + 2);
+                    s.read_trial(&denom, &trial_sse, &cost_anom);
+                    return 0;
+                });
+                if (!(denom > 0.0)) {  // rejected before its cost counts (the cost pass ran speculatively)
+                    if (opts.verbose)
+                        std::fprintf(stderr, "  iter %d trial: lambda %.3g denominator %.3g: reject\n",
+                                     res.iterations, lambda, denom);
+                    lambda *= nu;
+                    nu *= 2.0;
+                    continue;
+                }
+                if (cost_anom) {
+                    s.commit_cost_anomalies();
+                    anomalies += cost_anom;
+                }
+                if (cost_anom || !std::isfinite(trial_sse)) {
+                    lambda *= nu;
+                    nu *= 2.0;
+                    continue;
+                }
+                const double rho = (sse - trial_sse) / (0.5 * denom);
+                if (opts.verbose)
+                    std::fprintf(stderr, "  iter %d trial: lambda %.3g cost %.9g rho %.3g %s\n", res.iterations,
+                                 lambda, trial_sse / 2.0, rho, rho > 0.0 ? "accept" : "reject");
+                if (rho > 0.0 && trial_sse < sse) {
+                    s.accept();
+                    rel_decrease = (sse - trial_sse) / std::max(sse, 1.0);
+                    sse = trial_sse;
+                    lambda *= std::max(1.0 / 3.0, 1.0 - std::pow(2.0 * rho - 1.0, 3.0));
+                    accepted = true;
+                    break;
+                }
+                lambda *= nu;
+                nu *= 2.0;
+                continue;
+            }
             const unsigned long long before = anomalies;
             const unsigned long long bad = phase(res.t_damp, [&] { return s.damp_invert_v(lambda); });
             if (bad) {

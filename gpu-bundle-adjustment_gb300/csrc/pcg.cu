@@ -781,60 +781,87 @@ __global__ void __launch_bounds__(kVT) axpy_split_kernel(double* __restrict__ y,
 // ---- block-Jacobi blocks S_cc = U_lambda,c - sum_{e in c} Jc^T (Jp V'^-1 Jp^T) Jc
 // (the sums come from the right-hand side camera pass)
 
-// Packed Cholesky factor of a full 9x9 block; a block that is not SPD in FP64
-// (round-off with tiny damping) falls back to the square root of its diagonal.
-__device__ void factor_block(const double* A, double* Lc) {
-    double f[45];
-    if (!blk::chol9_factor(A, f)) {
-#pragma unroll
-        for (int i = 0; i < 45; ++i) f[i] = 0.0;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) {
-            const double d = A[10 * i];
-            f[blk::tri(i, i)] = sqrt(d > 1e-300 ? d : 1e-300);
-        }
+// Block-Jacobi factor of one camera block, one CTA of kSD threads per camera
+// (A: the full 9x9 block in shared memory): right-looking FP64 Cholesky with
+// one thread per entry of the lower triangle, nine steps of (pivot square
+// root, column scale, trailing update). FP64, because even Jacobi-scaled the
+// camera blocks' condition numbers make an FP32 factor a visibly weaker
+// preconditioner; parallel, because a one-thread FP64 factorisation is bound
+// by the FP64 pipe's latency. A block that is not SPD in FP64 (round-off with
+// tiny damping) falls back to the square root of its diagonal.
+constexpr int kSD = 64;
+
+__device__ __forceinline__ void bj_factor_cta(const double* A, double* __restrict__ Lc) {
+    __shared__ double m[45];
+    __shared__ int fail;
+    const int t = threadIdx.x;
+    int ti = 0, tj = 0;
+    if (t < 45) {
+        while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+        tj = t - ti * (ti + 1) / 2;
+        m[t] = A[9 * ti + tj];
     }
-#pragma unroll
-    for (int i = 0; i < 45; ++i) Lc[i] = f[i];
+    if (t == 0) fail = 0;
+    __syncthreads();
+    for (int k = 0; k < 9; ++k) {
+        if (t == blk::tri(k, k)) {
+            const double d = m[t];
+            if (d > 0.0) {
+                m[t] = sqrt(d);
+            } else {
+                fail = 1;
+            }
+        }
+        __syncthreads();
+        if (fail) break;
+        if (t < 45 && tj == k && ti > k) m[t] /= m[blk::tri(k, k)];
+        __syncthreads();
+        if (t < 45 && tj > k) m[t] -= m[blk::tri(ti, k)] * m[blk::tri(tj, k)];
+        __syncthreads();
+    }
+    if (t < 45) {
+        double v = m[t];
+        if (fail) {
+            const double d = A[10 * ti];
+            v = ti == tj ? sqrt(d > 1e-300 ? d : 1e-300) : 0.0;
+        }
+        Lc[t] = v;
+    }
 }
 
-// Thread per camera: S_cc (full, FP64) and its packed Cholesky factor.
-__global__ void __launch_bounds__(kCB) sdiag_finalize(const int* __restrict__ cam_chunk_off,
+// One CTA per camera: S_cc = U_lambda,c - (chunk sums from the right-hand side
+// pass), stored full FP64, and its block-Jacobi factor.
+__global__ void __launch_bounds__(kSD) sdiag_finalize(const int* __restrict__ cam_chunk_off,
                                                      const double* __restrict__ part, const double* __restrict__ U,
                                                      double lambda, int C, double* __restrict__ Sdiag,
                                                      double* __restrict__ L) {
-    const int c = blockIdx.x * kCB + threadIdx.x;
-    if (c >= C) return;
-    double A[81];
+    __shared__ double A[81];
+    const int c = blockIdx.x, t = threadIdx.x;
     const double* Uc = U + 81ll * c;
-#pragma unroll
-    for (int i = 0; i < 81; ++i) A[i] = Uc[i];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[10 * i] += lambda * (Uc[10 * i] > 0.0 ? Uc[10 * i] : 1e-12);
-    int idx = 0;
-    for (int a = 0; a < 9; ++a)
-        for (int b = 0; b <= a; ++b) {
-            double s = 0.0;
-            for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[54ll * q + 9 + idx];
-            A[9 * a + b] -= s;
-            if (a != b) A[9 * b + a] = A[9 * a + b];
-            ++idx;
-        }
-    double* Sd = Sdiag + 81ll * c;
-#pragma unroll
-    for (int i = 0; i < 81; ++i) Sd[i] = A[i];
-    factor_block(A, L + 45ll * c);
+    if (t < 45) {
+        int a = 0;
+        while ((a + 1) * (a + 2) / 2 <= t) ++a;
+        const int b = t - a * (a + 1) / 2;
+        double s = 0.0;
+        for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[54ll * q + 9 + t];
+        double v = Uc[9 * a + b] - s;
+        if (a == b) v += lambda * (Uc[10 * a] > 0.0 ? Uc[10 * a] : 1e-12);
+        A[9 * a + b] = v;
+        A[9 * b + a] = v;
+    }
+    __syncthreads();
+    for (int i = t; i < 81; i += kSD) Sdiag[81ll * c + i] = A[i];
+    bj_factor_cta(A, L + 45ll * c);
 }
 
 // Block-Jacobi factors from stored diagonal blocks (the learned form's fallback).
-__global__ void __launch_bounds__(kCB) factor_blocks_kernel(const double* __restrict__ Sdiag, int C,
+__global__ void __launch_bounds__(kSD) factor_blocks_kernel(const double* __restrict__ Sdiag, int C,
                                                            double* __restrict__ L) {
-    const int c = blockIdx.x * kCB + threadIdx.x;
-    if (c >= C) return;
-    double A[81];
-#pragma unroll
-    for (int i = 0; i < 81; ++i) A[i] = Sdiag[81ll * c + i];
-    factor_block(A, L + 45ll * c);
+    __shared__ double A[81];
+    const int c = blockIdx.x;
+    for (int i = threadIdx.x; i < 81; i += kSD) A[i] = Sdiag[81ll * c + i];
+    __syncthreads();
+    bj_factor_cta(A, L + 45ll * c);
 }
 
 }  // namespace
@@ -904,6 +931,10 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
 }
 
 PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
+    return schur_pcg(lambda, opts, learned, nullptr);
+}
+
+PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, unsigned long long* nonspd_out) {
     PcgStats st;
     const int n = 9 * C_;
     const int nvb = ceil_div(n, kVT);   // vector blocks (element-wise kernels)
@@ -932,7 +963,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
 
     // block-Jacobi blocks (partials from the right-hand side pass) and factors
     // (+ learned correction)
-    sdiag_finalize<<<ncb, kCB, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
+    sdiag_finalize<<<C_, kSD, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
                                              Sdiag_.get(), Pfac_.get());
     GBA_LAUNCH_CHECK();
     if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
@@ -941,9 +972,16 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
 
     double bnorm2 = 0.0;
     GBA_CUDA_CHECK(cudaMemcpyAsync(&bnorm2, sc + S_NORM, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    if (nonspd_out)
+        GBA_CUDA_CHECK(cudaMemcpyAsync(nonspd_out, counters_.get() + 3, sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream_));
     GBA_CUDA_CHECK(cudaMemsetAsync(dc_.get(), 0, n * sizeof(double), stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(ref_r_.get(), rhs_.get(), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
     sync();
+    if (nonspd_out && *nonspd_out) {  // a non-SPD damped point block: the trial is rejected
+        st.rel_residual = NAN;
+        return st;
+    }
     if (!std::isfinite(bnorm2)) {
         st.rel_residual = NAN;
         return st;
@@ -1036,7 +1074,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
                 inner_rel2 = rel2_bj;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
-                factor_blocks_kernel<<<ncb, kCB, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+                factor_blocks_kernel<<<C_, kSD, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
                 GBA_LAUNCH_CHECK();
                 st.pcg_iterations += it_l;
                 it_count = it_bj;
@@ -1049,7 +1087,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {
             // Block-Jacobi judges the learned factors: an inner solve that breaks
             // down or misses its tolerance is redone with the plain blocks, which
             // then serve for the rest of this trial.
-            factor_blocks_kernel<<<ncb, kCB, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+            factor_blocks_kernel<<<C_, kSD, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
             GBA_LAUNCH_CHECK();
             use_learned = false;
             ++st.fallbacks;

@@ -135,6 +135,20 @@ public:
     int schur_dense(double lambda);
     // Mixed form: solve S dc = rhs by FP32 PCG inside FP64 iterative refinement.
     PcgStats schur_pcg(double lambda, const LMOptions& opts, bool learned);
+    // The LM driver's fused trial (mixed forms): the stages above, launched
+    // without their own host reads. damp_launch leaves the non-SPD count on the
+    // device; schur_pcg with nonspd_out reads it together with the right-hand
+    // side norm (and stops there if it is non-zero); backsub_launch and
+    // trial_cost_launch (non-finite count to counters_[2]) are followed by one
+    // read_trial() of the denominator, the SSE and that count.
+    void damp_launch(double lambda);
+    PcgStats schur_pcg(double lambda, const LMOptions& opts, bool learned, unsigned long long* nonspd_out);
+    void backsub_launch(double lambda);
+    void trial_cost_launch(unsigned long long* anomalies);
+    void read_trial(double* denom, double* sse, unsigned long long* cost_anomalies);
+    void add_nonspd(unsigned long long n);     // adds to the cumulative non-SPD count
+    void commit_cost_anomalies();              // counters_[0] += counters_[2] (device side)
+    void zero_cost_scratch();                  // counters_[2] = 0 (device side)
     // dp = V'^-1 (bp - sum_e W_e^T dc), the gain denominator, and the trial
     // parameters (current + step). Returns the denominator (SSE units).
     double back_substitute(double lambda);
