@@ -166,6 +166,11 @@ def algorithmic_bytes(kernel: str, C: int, P: int, E: int) -> float:
     raise KeyError(kernel)
 
 
+# DRAM bytes (read + write) per launch from one ncu capture on workload 5
+# (profiles/mixed_kernels_workload5_ncu.md), for the roofline's traffic field.
+NCU_TRAFFIC_W5 = {"point_pass_f32": 245.0e6 + 1612.1e6, "schur_point_pass_f32": 992.1e6 + 66.6e6,
+                  "schur_camera_pass_f32": 774.5e6 + 3.7e6, "cost_ff": 241.2e6 + 60.5e6}
+
 HBM_KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
                "point_pass_f32", "cost_f64", "cost_ff")
 PCG_KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32")
@@ -275,8 +280,11 @@ def run_ours(args):
                 n_launch = min(n_launch, 64)
             per_launch_s = k_ms / n_launch / 1e3
             achieved = algorithmic_bytes(dom, C, P, E) / per_launch_s / 1e9
+            traffic = NCU_TRAFFIC_W5.get(dom) if args.workload == 5 and args.seed in (None, 5) else None
             roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                        "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": dom,
+                        "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                        "traffic_source": "profiles/mixed_kernels_workload5_ncu.md" if traffic else None,
+                        "algorithmic_bytes": algorithmic_bytes(dom, C, P, E), "kernel": dom,
                         "launches": n_launch, "avg_launch_us": per_launch_s * 1e6, "peak_source": peak_src,
                         "per_launch_source": source}
     solver.profile(False)
