@@ -262,3 +262,44 @@ def test_mixed_normal_equations_first_order_rotation_branch(gba, oracle):
     assert rel_err(U, ref["U"]) < 2e-5
     assert rel_err(bc, ref["bc"]) < 2e-5
     assert rel_err(bp, ref["bp"]) < 2e-5
+
+
+@pytest.fixture(scope="module")
+def long_tracks(gba):
+    """Every point observed ~300 times: point chunks with more slots than one
+    CTA pass (256), the multi-pass paths of the point kernels."""
+    return gba.synthetic_custom(320, 40, 290, 310, 1.2, seed=3)
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_long_tracks_normal_equations(gba, oracle, long_tracks, form):
+    with gba.Solver(long_tracks, form) as s:
+        sse = s.accumulate()
+        V = s.download("V").reshape(-1, 6)
+        bp = s.download("bp")
+        bc = s.download("bc")
+    ref = oracle.accumulate(long_tracks)
+    tol = 1e-11 if form == "plain" else 2e-5
+    assert abs(sse - ref["sse"]) <= 1e-11 * ref["sse"]
+    assert rel_err(V[:, 0], ref["V"][:, 0, 0]) < tol
+    assert rel_err(bp, ref["bp"]) < tol
+    assert rel_err(bc, ref["bc"]) < tol
+
+
+def test_long_tracks_refined_step(gba, oracle, long_tracks):
+    """Schur step through the multi-pass point kernels: refined to 1e-10 and
+    agreeing with the exact (numpy FP64) system of the FP32 Jacobians."""
+    lam = 1e-3
+    with gba.Solver(long_tracks, "mixed") as s:
+        s.accumulate()
+        assert s.damp_invert_v(lam) == 0
+        _, _, relres = s.schur_pcg(lam, refine_tol=1e-10, pcg_tol=1e-3, pcg_max_iters=500)
+        rhs_dev = s.download("rhs")[:9 * long_tracks.num_cameras]
+        dc = s.download("dc")
+        s.back_substitute(lam)
+        dp = s.download("dp")
+        rhs, matvec = _implicit_system(s, long_tracks, lam)
+    assert rel_err(rhs_dev, rhs) < 1e-12
+    assert relres <= 1e-10
+    assert np.linalg.norm(rhs - matvec(dc)) / np.linalg.norm(rhs) <= 2e-10
+    assert rel_err(dp, matvec.point_step(dc)) < 1e-9

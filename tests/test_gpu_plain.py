@@ -326,3 +326,22 @@ def test_solver_create_rejects_bad_indices(gba, form):
             gba.solve(bad, form=form)
         assert ei.value.status == 1
     gba.Solver(prob, form).close()  # the device is still usable
+
+
+def test_long_tracks_plain_schur_step_matches_oracle(gba, oracle):
+    """Points observed ~300 times (point chunks longer than one CTA pass,
+    ~45,000 edge pairs per point in the S assembly): FP64 step vs the oracle."""
+    prob = gba.synthetic_custom(320, 40, 290, 310, 1.2, seed=3)
+    lam = 1e-3
+    ref = oracle.schur_step(prob, lam, threads=4)
+    assert ref["status"] == 0
+    with gba.Solver(prob, "plain") as s:
+        s.accumulate()
+        assert s.damp_invert_v(lam) == 0
+        assert s.schur_dense(lam) == 0
+        dc = s.download("dc")
+        denom = s.back_substitute(lam)
+        dp = s.download("dp")
+    assert rel_err(dc, ref["dc"]) < 1e-9
+    assert rel_err(dp, ref["dp"]) < 1e-9
+    assert abs(denom - ref["denom"]) <= 1e-9 * abs(ref["denom"])
