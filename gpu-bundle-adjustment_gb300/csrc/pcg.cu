@@ -8,17 +8,21 @@
 //                                         u_e = Jp_e w_p          (2 values per slot)
 //   camera pass  (camera-major chunks)    partial_c = sum_e Jc_e^T u_e
 //   finalize                              y = U_lambda x - sum partials   (or rhs = bc - ...)
-// templated on the arithmetic type: FP32 inside PCG, FP64 for the right-hand
-// side and the iterative-refinement residual. Chunk partials are summed in
-// FP64 in a fixed order, so every product is deterministic.
+// templated on the arithmetic type: FP32 inside PCG, float-float (ff.cuh) for
+// the right-hand side and the refinement residual when the Schur target is
+// tight. Chunk partials are summed in FP64 in a fixed order, so every product
+// is deterministic. The right-hand side pass also produces the block-Jacobi
+// diagonal-block sums (G = Jp V'^-1 Jp^T per slot, summed by the camera pass).
 //
-// Solve: FP64 iterative refinement (dc += e, r = rhs - S64 dc, until
-// ||r|| <= refine_tol ||rhs||) around inner block-Jacobi PCG solves on the FP32
-// operator. The block-Jacobi blocks are the 9x9 diagonal blocks S_cc (FP32
-// products, FP64 sums, FP64 Cholesky); the learned form replaces their
-// factors by the MLP-corrected ones (mlp.cu). PCG vectors and dot products are
-// FP64 with deterministic reductions; all PCG control scalars live on the
-// device and the host polls a convergence flag after batches of iterations.
+// Solve: iterative refinement (dc += e, r = rhs - S dc with float-float
+// products, until ||r|| <= refine_tol ||rhs||) around inner block-Jacobi PCG
+// solves on the FP32 operator; with refine_tol >= kLooseTol the right-hand side
+// is FP32 and a converged inner solve is its own check. The block-Jacobi blocks
+// are the 9x9 diagonal blocks S_cc (FP32 products, FP64 sums, FP64 Cholesky,
+// explicit inverses); the learned form replaces their factors by the
+// MLP-corrected ones (mlp.cu). PCG vectors and dot products are FP64 with
+// deterministic reductions; all PCG control scalars live on the device and the
+// host polls a convergence flag after batches of iterations.
 //
 // No reference counterpart: the reference solves S densely on the host.
 
