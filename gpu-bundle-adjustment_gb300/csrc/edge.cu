@@ -1,14 +1,18 @@
-// Normal-equation accumulation (edge kernels) and the FP64 trial-cost kernel.
+// Normal-equation accumulation (edge kernels) and the trial-cost kernels.
 //
 // Replaces the reference edge_kernel / cost_kernel (src/lm.cu:205-281), which
 // accumulate U, V, bc, bp and the SSE with global FP64 atomics in file order.
 // Here every sum is atomic-free and deterministic:
 //   point pass   one CTA per point chunk (whole points, <= 256 slots, slots
-//                sorted by point): residual + Jacobian per slot, per-edge W (or the
-//                FP32 Jacobian record), and V / bp as in-CTA ordered sums.
+//                sorted by point): Jacobian per slot, per-edge W (plain form) or
+//                the FP32 Jacobian rows and camera records (mixed forms), and
+//                V / bp as in-CTA ordered sums.
 //   camera pass  one CTA per camera chunk (<= 1024 slots of one camera, from the
 //                camera-major view): U / bc partial sums per chunk, then a
 //                finalize kernel adds the chunk partials of each camera in order.
+//   cost         FP64 per slot (plain form); float-float per camera-major
+//                position with the camera's constants in shared memory (mixed
+//                forms), FP64 for positions outside FP32's range.
 // Non-finite edges contribute nothing, bump counters[0] and get W = 0
 // (reference semantics src/lm.cu:219-225; the reference leaves W stale).
 
