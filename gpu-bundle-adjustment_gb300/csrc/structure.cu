@@ -135,6 +135,62 @@ __global__ void check_indices_kernel(const int* __restrict__ oc, const int* __re
     if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(bad, cnt);
 }
 
+// Greedy point chunk from point p: points p .. q-1 with q the largest index in
+// [p + 1, min(P, p + kPointChunk)] whose slots fit in kPointChunk (p + 1 when
+// point p alone has more). next[P] = P.
+__global__ void chunk_next_kernel(const int* __restrict__ pt_off, int P, int* __restrict__ next) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= P; p += gridDim.x * blockDim.x) {
+        if (p == P) {
+            next[p] = P;
+            continue;
+        }
+        const int base = pt_off[p];
+        int lo = p + 1, hi = min(P, p + kPointChunk);  // lo always qualifies as the answer's floor
+        while (lo < hi) {
+            const int mid = lo + (hi - lo + 1) / 2;
+            if (pt_off[mid] - base <= kPointChunk) {
+                lo = mid;
+            } else {
+                hi = mid - 1;
+            }
+        }
+        next[p] = lo;
+    }
+}
+
+// One binary-lifting level: out[p] = in[in[p]].
+__global__ void lift_kernel(const int* __restrict__ in, int P, int* __restrict__ out) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= P; p += gridDim.x * blockDim.x) out[p] = in[in[p]];
+}
+
+// Number of greedy chunks: lifted walk from point 0 while short of P.
+__global__ void chunk_count_kernel(const int* __restrict__ jump, int levels, int P, int* __restrict__ n) {
+    int cur = 0, cnt = 0;
+    for (int k = levels - 1; k >= 0; --k) {
+        const int nx = jump[static_cast<size_t>(k) * (P + 1ull) + cur];
+        if (nx < P) {
+            cur = nx;
+            cnt += 1 << k;
+        }
+    }
+    *n = cnt + 1;
+}
+
+// starts[i] = next^i(0) for i < n, starts[n] = P.
+__global__ void chunk_starts_kernel(const int* __restrict__ jump, int levels, int P, int n,
+                                    int* __restrict__ starts) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+        if (i == n) {
+            starts[i] = P;
+            continue;
+        }
+        int cur = 0;
+        for (int k = 0; k < levels; ++k)
+            if ((i >> k) & 1) cur = jump[static_cast<size_t>(k) * (P + 1ull) + cur];
+        starts[i] = cur;
+    }
+}
+
 // Camera-major copies of per-slot data: point index and observation (as
 // float-float pairs) of camera-major position i (slot cam_slots[i]).
 __global__ void gather_cm_kernel(const int* __restrict__ cam_slots, const int* __restrict__ s_pt,
@@ -403,30 +459,38 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
         GBA_LAUNCH_CHECK();
     }
 
-    // 3. work chunks, built on the host from the CSR offsets
-    std::vector<int> h_pt_off(P + 1), h_cam_off(C + 1);
-    GBA_CUDA_CHECK(cudaMemcpyAsync(h_pt_off.data(), pt_off_.get(), (P + 1) * sizeof(int),
-                                   cudaMemcpyDeviceToHost, stream_));
+    // 3. work chunks. Point chunks: the greedy packing (whole points, at most
+    //    kPointChunk slots and points per chunk; a longer point alone) computed
+    //    on the device by binary lifting: next[p] = end of the greedy chunk
+    //    that starts at p (binary search on the CSR offsets), J_{k+1} =
+    //    J_k(J_k), the chunk count from one lifted walk from point 0, and
+    //    chunk i's start = next^i(0). Camera chunks are built on the host.
+    int levels = 1;
+    while ((1ll << levels) <= P) ++levels;
+    {
+        DevBuf<int> jump(static_cast<size_t>(levels) * (P + 1ull));
+        chunk_next_kernel<<<grid_for(P + 1ll), 256, 0, stream_>>>(pt_off_.get(), P, jump.get());
+        GBA_LAUNCH_CHECK();
+        for (int k = 0; k + 1 < levels; ++k) {
+            lift_kernel<<<grid_for(P + 1ll), 256, 0, stream_>>>(jump.get() + static_cast<size_t>(k) * (P + 1ull), P,
+                                                               jump.get() + static_cast<size_t>(k + 1) * (P + 1ull));
+            GBA_LAUNCH_CHECK();
+        }
+        DevBuf<int> d_n(1);
+        chunk_count_kernel<<<1, 1, 0, stream_>>>(jump.get(), levels, P, d_n.get());
+        GBA_LAUNCH_CHECK();
+        int n = 0;
+        GBA_CUDA_CHECK(cudaMemcpyAsync(&n, d_n.get(), sizeof n, cudaMemcpyDeviceToHost, stream_));
+        sync();
+        n_pchunk_ = n;
+        pchunk_.alloc(n + 1ull);
+        chunk_starts_kernel<<<grid_for(n + 1ll), 256, 0, stream_>>>(jump.get(), levels, P, n, pchunk_.get());
+        GBA_LAUNCH_CHECK();
+    }
+    std::vector<int> h_cam_off(C + 1);
     GBA_CUDA_CHECK(cudaMemcpyAsync(h_cam_off.data(), cam_off_.get(), (C + 1) * sizeof(int),
                                    cudaMemcpyDeviceToHost, stream_));
     sync();
-
-    std::vector<int> pchunk;
-    pchunk.reserve(E / 64 + 16);
-    pchunk.push_back(0);
-    int edges = 0, pts_in = 0;
-    for (int p = 0; p < P; ++p) {
-        const int k = h_pt_off[p + 1] - h_pt_off[p];
-        if (pts_in > 0 && (edges + k > kPointChunk || pts_in >= kPointChunk)) {
-            pchunk.push_back(p);
-            edges = 0;
-            pts_in = 0;
-        }
-        edges += k;
-        ++pts_in;
-    }
-    pchunk.push_back(P);
-    n_pchunk_ = static_cast<int>(pchunk.size()) - 1;
 
     std::vector<int> cbeg, ccam, cam_chunk_off(C + 1);
     for (int c = 0; c < C; ++c) {
@@ -439,12 +503,9 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     cam_chunk_off[C] = static_cast<int>(cbeg.size());
     n_cchunk_ = static_cast<int>(cbeg.size());
 
-    pchunk_.alloc(pchunk.size());
     cchunk_begin_.alloc(std::max<size_t>(cbeg.size(), 1));
     cchunk_cam_.alloc(std::max<size_t>(ccam.size(), 1));
     cam_chunk_off_.alloc(C + 1ull);
-    GBA_CUDA_CHECK(cudaMemcpyAsync(pchunk_.get(), pchunk.data(), pchunk.size() * sizeof(int),
-                                   cudaMemcpyHostToDevice, stream_));
     if (!cbeg.empty()) {
         GBA_CUDA_CHECK(cudaMemcpyAsync(cchunk_begin_.get(), cbeg.data(), cbeg.size() * sizeof(int),
                                        cudaMemcpyHostToDevice, stream_));
