@@ -396,10 +396,29 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     const int E = E_, P = P_, C = C_;
     DevBuf<int> d_oc(E), d_op(E), keys_sorted(E), iota(E);
     DevBuf<double> d_px(2ull * E);
+    // The pixels (16 B per observation, the bulk of the problem) cross on a
+    // side stream while the index check and the sort by point run; the main
+    // stream waits for them only before the gather that reads them.
+    struct SideCopy {
+        cudaStream_t s = nullptr;
+        cudaEvent_t ready = nullptr, done = nullptr;
+        ~SideCopy() {  // runs before d_px is freed (declared after it): its copy must have landed
+            if (s) cudaStreamSynchronize(s);
+            if (done) cudaEventDestroy(done);
+            if (ready) cudaEventDestroy(ready);
+            if (s) cudaStreamDestroy(s);
+        }
+    } side;
+    GBA_CUDA_CHECK(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+    GBA_CUDA_CHECK(cudaEventCreateWithFlags(&side.ready, cudaEventDisableTiming));
+    GBA_CUDA_CHECK(cudaEventCreateWithFlags(&side.done, cudaEventDisableTiming));
+    GBA_CUDA_CHECK(cudaEventRecord(side.ready, stream_));  // after d_px's stream-ordered allocation
+    GBA_CUDA_CHECK(cudaStreamWaitEvent(side.s, side.ready, 0));
+    GBA_CUDA_CHECK(
+        cudaMemcpyAsync(d_px.get(), obs_px, 2ull * E * sizeof(double), cudaMemcpyHostToDevice, side.s));
+    GBA_CUDA_CHECK(cudaEventRecord(side.done, side.s));
     GBA_CUDA_CHECK(cudaMemcpyAsync(d_oc.get(), obs_cam, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(d_op.get(), obs_pt, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
-    GBA_CUDA_CHECK(
-        cudaMemcpyAsync(d_px.get(), obs_px, 2ull * E * sizeof(double), cudaMemcpyHostToDevice, stream_));
 
     order_.alloc(E);
     s_cam_.alloc(E);
@@ -435,6 +454,7 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     size_t tb = tmp.size();
     GBA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tmp.get(), tb, d_op.get(), s_pt_.get(), iota.get(),
                                                    order_.get(), E, 0, bits_for(P + 1), stream_));
+    GBA_CUDA_CHECK(cudaStreamWaitEvent(stream_, side.done, 0));
     gather_obs_kernel<<<grid_for(E), 256, 0, stream_>>>(order_.get(), d_oc.get(), d_px.get(), E, s_cam_.get(),
                                                         reinterpret_cast<double2*>(s_px_.get()));
     GBA_LAUNCH_CHECK();
