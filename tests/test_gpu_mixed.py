@@ -303,3 +303,20 @@ def test_long_tracks_refined_step(gba, oracle, long_tracks):
     assert relres <= 1e-10
     assert np.linalg.norm(rhs - matvec(dc)) / np.linalg.norm(rhs) <= 2e-10
     assert rel_err(dp, matvec.point_step(dc)) < 1e-9
+
+
+def test_repeated_solves_bit_identical_and_cache_release(gba):
+    """Solves allocate from the device memory pool: repeated solves (reusing
+    cached memory) and a solve after the cache is released give bit-identical
+    results (every reduction is ordered)."""
+    prob = gba.synthetic_custom(9, 1500, 2, 7, 1.4, seed=31)
+    runs = []
+    for i in range(3):
+        if i == 2:
+            gba.release_cached_memory()
+        run = prob.copy()
+        r = gba.solve(run, max_iterations=6, form="mixed", refine_tol=0.1, pcg_tol=0.1)
+        runs.append((r.trajectory, run.cameras.copy(), run.points.copy()))
+    for traj, cams, pts in runs[1:]:
+        assert traj == runs[0][0]
+        assert np.array_equal(cams, runs[0][1]) and np.array_equal(pts, runs[0][2])
