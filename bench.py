@@ -25,6 +25,8 @@ per solve (see cpu_sample()).
 from __future__ import annotations
 
 import argparse
+import atexit
+import datetime
 import json
 import os
 import statistics
@@ -77,47 +79,85 @@ def plain_reference_summary(workload: int, seed: int):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """SM clocks and throttle reasons during the timed region, from ONE
+    long-lived `nvidia-smi -lms` process. It is started before the warm-up
+    steps: each nvidia-smi start-up initialises NVML, which can stall this
+    process's CUDA calls for tens of milliseconds, so no start-up may fall
+    inside the timed region. Samples carry nvidia-smi's own timestamp (the
+    pipe may be block-buffered); the summary keeps those inside the timed
+    window, plus the nearest sample on either side when the window holds
+    fewer than two."""
 
-    QUERY = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    QUERY = ("timestamp,clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 100
 
     def __init__(self):
-        self.samples = []
-        self._stop = threading.Event()
+        self.samples = []  # (datetime, [sm, max, 4 reasons])
+        self.window = None
+        self._p = None
         self._t = None
+        self._t0 = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
-                                      f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits"],
-                                     capture_output=True, text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.splitlines()[0].split(",")])
-            except (OSError, subprocess.SubprocessError):
-                return
-            self._stop.wait(0.2)
-
-    def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
+    def start(self):
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", dev, f"--query-gpu={self.QUERY}",
+                                        "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            return self
+        atexit.register(self.stop)
+        self._t = threading.Thread(target=self._read, daemon=True)
         self._t.start()
         return self
 
-    def __exit__(self, *exc):
-        self._stop.set()
-        if self._t:
-            self._t.join(timeout=10)
+    def _read(self):
+        for line in self._p.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                continue
+            self.samples.append((ts, f[1:7]))
+
+    def begin(self):
+        self._t0 = datetime.datetime.now()
+
+    def end(self):
+        self.window = (self._t0, datetime.datetime.now())
+
+    def stop(self):
+        if self._p is not None and self._p.poll() is None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._p.kill()
+                self._p.wait()
+        if self._t is not None:
+            self._t.join(timeout=5)
 
     def summary(self):
-        if not self.samples:
+        if not self.samples or self.window is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        t0, t1 = self.window
+        picked = [f for ts, f in self.samples if t0 <= ts <= t1]
+        n_in = len(picked)
+        if n_in < 2:
+            before = [(ts, f) for ts, f in self.samples if ts < t0]
+            after = [(ts, f) for ts, f in self.samples if ts > t1]
+            picked += [max(before, key=lambda x: x[0])[1]] if before else []
+            picked += [min(after, key=lambda x: x[0])[1]] if after else []
+        sm = [float(s[0]) for s in picked if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in picked if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        reasons = sorted({names[i] for s in picked for i in range(4) if s[2 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons}
+                "reasons": reasons, "samples_in_window": n_in, "samples_used": len(picked)}
 
 
 def _dist_env():
@@ -188,6 +228,7 @@ def run_ours(args):
     if world > 1 and not torch.distributed.is_initialized():
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", dev))
 
+    clocks = ClockSampler().start()  # long before the timed region (see ClockSampler)
     prob = gba.synthetic(args.workload, args.seed)
     C, P, E = prob.num_cameras, prob.num_points, prob.num_observations
     ref = reference_cost(args.workload, args.seed)
@@ -221,13 +262,18 @@ def run_ours(args):
     l0 = gba.launch_count()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     timed = []
-    with ClockSampler() as clocks:
-        start.record(stream)
-        for _ in range(args.steps):
-            solver.reset_params()
-            timed.append(solver.run(**opts))
-        end.record(stream)
-        torch.cuda.synchronize()
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks.begin()
+    start.record(stream)
+    for k in range(args.steps):
+        solver.reset_params()
+        timed.append(solver.run(**opts))
+        marks[k].record(stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    clocks.end()
+    clocks.stop()
+    step_ms = [(marks[k - 1] if k else start).elapsed_time(marks[k]) for k in range(args.steps)]
     launches = gba.launch_count() - l0
     ms_total = start.elapsed_time(end)
     ms_per_step = max_over_ranks(ms_total, world) / args.steps
@@ -317,6 +363,7 @@ def run_ours(args):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": ms_per_step,
+        "step_ms": [round(x, 3) for x in step_ms],
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,

@@ -58,3 +58,28 @@ def test_reference_arm_only_on_rank0(monkeypatch, capsys):
     args = bench.argparse.Namespace(workload=1, seed=None, reference_iterations=1, warmup=0, steps=1)
     assert bench.run_reference(args) is None
     assert capsys.readouterr().out == ""
+
+
+def test_clock_summary_keeps_the_timed_window():
+    """The clock summary uses the samples inside the timed window; with fewer
+    than two there, it adds the nearest sample on either side."""
+    import datetime as dt
+
+    bench = _load_bench()
+    t = dt.datetime(2026, 1, 1, 12, 0, 0)
+    ms = lambda k: t + dt.timedelta(milliseconds=k)
+    row = lambda mhz, cap="Not Active": [str(mhz), "2070", "Not Active", "Not Active", "Not Active", cap]
+
+    s = bench.ClockSampler()
+    s.samples = [(ms(0), row(900)), (ms(100), row(2070)), (ms(200), row(2060, "Active")), (ms(300), row(800))]
+    s.window = (ms(50), ms(250))
+    out = s.summary()
+    assert out["samples_in_window"] == 2 and out["samples_used"] == 2
+    assert out["sm_mhz"] == 2065 and out["sm_max_mhz"] == 2070 and out["reasons"] == ["sw_power_cap"]
+
+    s.window = (ms(120), ms(180))  # no sample inside: bracket with the neighbours
+    out = s.summary()
+    assert out["samples_in_window"] == 0 and out["samples_used"] == 2 and out["sm_mhz"] == 2065
+
+    s.window = None
+    assert s.summary()["reasons"] == ["unsampled"]
