@@ -45,6 +45,7 @@ constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to 
 constexpr int kJudgeAttempts = 2;    // indecisive judgements before block-Jacobi is kept for the solve
 constexpr double kLooseTol = 1e-3;   // refinement targets at or above this run the fast (FP32) path
 
+constexpr int kX32 = 12;       // floats per camera of the FP32 camera-vector copies (9 used; 48 B, float4 loads)
 constexpr int kUC = 32;        // cameras per block of the 9-threads-per-camera kernels
 constexpr int kUT = 9 * kUC;   // their block size
 
@@ -114,6 +115,21 @@ __device__ __forceinline__ void load_u(const ff* u, long long q, ff& a, ff& b) {
     const float4 v = reinterpret_cast<const float4*>(u)[q];
     a = {v.x, v.y};
     b = {v.z, v.w};
+}
+
+// The nine entries of a camera's x: FP32 copies are padded to kX32 floats per
+// camera and read as two float4 and a float (a third of the gather requests of
+// nine scalar loads); float-float copies are dense (9 per camera).
+__device__ __forceinline__ void load_x(const float* __restrict__ x, int c, float* xv) {
+    const float* xc = x + static_cast<long long>(kX32) * c;
+    const float4 a = reinterpret_cast<const float4*>(xc)[0], b = reinterpret_cast<const float4*>(xc)[1];
+    xv[0] = a.x; xv[1] = a.y; xv[2] = a.z; xv[3] = a.w;
+    xv[4] = b.x; xv[5] = b.y; xv[6] = b.z; xv[7] = b.w;
+    xv[8] = xc[8];
+}
+__device__ __forceinline__ void load_x(const ff* __restrict__ x, int c, ff* xv) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) xv[k] = x[9ll * c + k];
 }
 
 // J = [Jc(18), Jp(6)] of slot s
@@ -189,7 +205,7 @@ struct BacksubOut {
 // position so that the camera pass reads it contiguously. With kBack (a = -1,
 // xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
 template <typename T, bool kBack = false>
-__global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
+__global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                        const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
                                                        const float* __restrict__ Jp32,
@@ -236,13 +252,13 @@ __global__ void __launch_bounds__(kPT) schur_point_pass(const int* __restrict__ 
                 load_j(Jc32, Jp32, s, J);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
-                const T* xc = xt + 9ll * s_cam[s];
+                T xv[9];
+                load_x(xt, s_cam[s], xv);
                 T t0 = zero<T>(), t1 = zero<T>();
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
-                    const T xk = xc[k];
-                    madd(t0, J[k], xk);
-                    madd(t1, J[9 + k], xk);
+                    madd(t0, J[k], xv[k]);
+                    madd(t1, J[9 + k], xv[k]);
                 }
                 t0 = norm(t0);
                 t1 = norm(t1);
@@ -693,7 +709,8 @@ __global__ void __launch_bounds__(kVT) pcg_direction(double* __restrict__ p, flo
     if (i < n) {
         const double v = z[i] + beta * p[i];
         p[i] = v;
-        p32[i] = static_cast<float>(v);
+        const int c = i / 9;
+        p32[kX32 * c + (i - 9 * c)] = static_cast<float>(v);
     }
 }
 
@@ -720,7 +737,7 @@ __global__ void __launch_bounds__(kUT) pcg_init(double* __restrict__ x, double* 
         const double zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
         z[i] = zi;
         p[i] = zi;
-        p32[i] = static_cast<float>(zi);
+        p32[kX32 * c + k] = static_cast<float>(zi);
         rz = ri * zi;
     }
     const double a = block_sum<kUT>(ri * ri, sh);
@@ -755,9 +772,13 @@ __global__ void __launch_bounds__(256) sum_to_scalar(const double* __restrict__ 
     if (threadIdx.x == 0) sc[slot] = v;
 }
 
+// FP32 copy of a camera vector (9 per camera) in the padded layout (kX32 per camera).
 __global__ void __launch_bounds__(kVT) to_f32_kernel(const double* __restrict__ y, int n, float* __restrict__ y32) {
     const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < n) y32[i] = static_cast<float>(y[i]);
+    if (i < n) {
+        const int c = i / 9;
+        y32[kX32 * c + (i - 9 * c)] = static_cast<float>(y[i]);
+    }
 }
 
 // Float-float split of y (hi, lo interleaved).

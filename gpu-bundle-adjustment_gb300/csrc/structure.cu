@@ -351,7 +351,8 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         cams32_.alloc(28ull * C);
         Vinv32lo_.alloc(6ull * P);
         dcff_.alloc(18ull * C);
-        pcg_p32_.alloc(9ull * C);
+        pcg_p32_.alloc(12ull * C);  // padded FP32 camera vector (12 floats per camera; pads zeroed)
+        if (C > 0) GBA_CUDA_CHECK(cudaMemsetAsync(pcg_p32_.get(), 0, 12ull * C * sizeof(float), stream_));
         r_cur_.alloc(2ull * E);
         r_trial_.alloc(2ull * E);
         Sdiag_.alloc(81ull * C);
