@@ -223,11 +223,14 @@ __global__ void __launch_bounds__(kTB) backsub_chunk_kernel(
     if (threadIdx.x == 0) part[chunk] = t;
 }
 
-// Camera part of the denominator and the trial cameras (tcams = cams + dc).
+// Camera part of the denominator and the trial cameras (tcams = cams + dc);
+// for the mixed back-substitution also dc's FP32 copy in the padded layout
+// (dc32, kX32 per camera) or its float-float split (dcff), when given.
 __global__ void __launch_bounds__(kTB) camera_step_kernel(const double* __restrict__ dc, const double* __restrict__ U,
                                                          const double* __restrict__ bc,
                                                          const double* __restrict__ cams, double lambda, int C,
-                                                         double* __restrict__ tcams, double* __restrict__ part) {
+                                                         double* __restrict__ tcams, double* __restrict__ part,
+                                                         float* __restrict__ dc32, float2* __restrict__ dcff) {
     __shared__ double red[kTB / 32];
     double den = 0.0;
     const int i = blockIdx.x * kTB + threadIdx.x;
@@ -237,6 +240,11 @@ __global__ void __launch_bounds__(kTB) camera_step_kernel(const double* __restri
         const double d = dc[i];
         den = d * (lambda * (dg > 0.0 ? dg : 1e-12) * d + bc[i]);
         tcams[i] = cams[i] + d;
+        if (dc32) dc32[kX32 * c + k] = static_cast<float>(d);
+        if (dcff) {
+            const ffa::ff f = ffa::from_double(d);
+            dcff[i] = make_float2(f.hi, f.lo);
+        }
     }
     const double t = block_sum<kTB>(den, red);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
@@ -301,8 +309,11 @@ double Solver::back_substitute(double lambda) {
 void Solver::backsub_launch(double lambda) {
     const int ncam = ceil_div(9ll * C_, kTB);
     double* part = red_part_.get();
+    const bool mixed = form_ != SolverForm::Plain;
     camera_step_kernel<<<ncam, kTB, 0, stream_>>>(dc_.get(), U_.get(), bc_.get(), cams_.get(), lambda, C_,
-                                                  tcams_.get(), part);
+                                                  tcams_.get(), part, mixed && fast_solve_ ? pcg_p32_.get() : nullptr,
+                                                  mixed && !fast_solve_ ? reinterpret_cast<float2*>(dcff_.get())
+                                                                        : nullptr);
     GBA_LAUNCH_CHECK();
     cudaEvent_t ev = prof_start();
     if (form_ == SolverForm::Plain) {
@@ -310,6 +321,7 @@ void Solver::backsub_launch(double lambda) {
                                                              dc_.get(), V_.get(), Vinv_.get(), bp_.get(), pts_.get(),
                                                              lambda, dp_.get(), tpts_.get(), part + ncam);
         GBA_LAUNCH_CHECK();
+        pts_ff_trial_ = false;
     } else {
         mixed_back_substitute(*this, lambda, part + ncam);
     }

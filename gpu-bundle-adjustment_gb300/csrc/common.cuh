@@ -10,6 +10,10 @@
 
 namespace gba {
 
+// Floats per camera of the FP32 camera-vector copies read by the point-side
+// passes: 9 used, padded to 48 B so that a gather is two float4 and a float.
+constexpr int kX32 = 12;
+
 // Thrown by the host driver on CUDA failure (the C-ABI layer converts it to a
 // status code; nothing throws across the ABI).
 struct CudaError : std::runtime_error {

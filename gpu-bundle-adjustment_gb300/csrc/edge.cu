@@ -785,7 +785,8 @@ void Solver::prepare_ff(const double* cams, const double* pts) {
     camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(
         cams, C_, cam_pre_.get(), reinterpret_cast<float2*>(cam_pre_ff_.get()), cams32_.get());
     GBA_LAUNCH_CHECK();
-    launch_split_ff(pts, 3ll * P_, pts_ff_.get(), stream_);
+    if (!(pts == tpts_.get() && pts_ff_trial_)) launch_split_ff(pts, 3ll * P_, pts_ff_.get(), stream_);
+    pts_ff_trial_ = pts == tpts_.get();
     ff_holds_ = (cams == cams_.get() && pts == pts_.get()) ? kFfCurrent
                 : (cams == tcams_.get() && pts == tpts_.get()) ? kFfTrial
                                                                 : kFfNone;

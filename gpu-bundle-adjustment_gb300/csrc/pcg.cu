@@ -45,7 +45,6 @@ constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to 
 constexpr int kJudgeAttempts = 2;    // indecisive judgements before block-Jacobi is kept for the solve
 constexpr double kLooseTol = 1e-3;   // refinement targets at or above this run the fast (FP32) path
 
-constexpr int kX32 = 12;       // floats per camera of the FP32 camera-vector copies (9 used; 48 B, float4 loads)
 constexpr int kUC = 32;        // cameras per block of the 9-threads-per-camera kernels
 constexpr int kUT = 9 * kUC;   // their block size
 
@@ -195,6 +194,7 @@ struct BacksubOut {
     float2 lambda;  // float-float
     double* dp;
     double* tpts;
+    float2* tpts_ff;  // float-float split of the trial points (for the trial cost)
     double* part;
 };
 
@@ -332,7 +332,10 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
             for (int k = 0; k < 3; ++k) {
                 const double dk = ffa::to_double(d[k]);
                 bk.dp[3 * p + k] = dk;
-                bk.tpts[3 * p + k] = bk.pts[3 * p + k] + dk;
+                const double tp = bk.pts[3 * p + k] + dk;
+                bk.tpts[3 * p + k] = tp;
+                const ff tf = ffa::from_double(tp);
+                bk.tpts_ff[3 * p + k] = make_float2(tf.hi, tf.lo);
                 const float vk = static_cast<float>(bk.V[6 * p + diag[k]]);
                 ff t = {static_cast<float>(bp[3 * p + k]), 0.f};
                 ffa::madd(t, ffa::mul(lam, ff{vk > 0.f ? vk : 1e-12f, 0.f}), d[k]);
@@ -772,15 +775,6 @@ __global__ void __launch_bounds__(256) sum_to_scalar(const double* __restrict__ 
     if (threadIdx.x == 0) sc[slot] = v;
 }
 
-// FP32 copy of a camera vector (9 per camera) in the padded layout (kX32 per camera).
-__global__ void __launch_bounds__(kVT) to_f32_kernel(const double* __restrict__ y, int n, float* __restrict__ y32) {
-    const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < n) {
-        const int c = i / 9;
-        y32[kX32 * c + (i - 9 * c)] = static_cast<float>(y[i]);
-    }
-}
-
 // Float-float split of y (hi, lo interleaved).
 __global__ void __launch_bounds__(kVT) split_kernel(const double* __restrict__ y, long long n,
                                                    float* __restrict__ yff) {
@@ -930,29 +924,27 @@ void launch_split_ff(const double* x, long long n, float* out, cudaStream_t s) {
 }
 
 // Mixed-form back-substitution: the point pass in back-substitution mode (dp,
-// trial points, denominator partials per chunk), in the arithmetic of the last
-// Schur solve: FP32 after a loose solve, float-float otherwise.
+// trial points and their float-float split, denominator partials per chunk),
+// in the arithmetic of the last Schur solve: FP32 after a loose solve,
+// float-float otherwise. The camera step kernel has written dc in that
+// arithmetic (pcg_p32_ padded FP32, or dcff_).
 void mixed_back_substitute(Solver& s, double lambda, double* part) {
-    const int n = 9 * s.C_;
     const BacksubOut bk{s.V_.get(), s.pts_.get(),
                         make_float2(static_cast<float>(lambda), static_cast<float>(lambda - static_cast<float>(lambda))),
-                        s.dp_.get(), s.tpts_.get(), part};
+                        s.dp_.get(), s.tpts_.get(), reinterpret_cast<float2*>(s.pts_ff_.get()), part};
     if (s.fast_solve_) {
-        float* dc32 = s.pcg_p32_.get();  // free after the Schur solve
-        to_f32_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, dc32);
-        GBA_LAUNCH_CHECK();
         schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
             s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
-            s.Vinv32_.get(), nullptr, s.bp_.get(), dc32, -1.0, nullptr, nullptr, bk, nullptr);
+            s.Vinv32_.get(), nullptr, s.bp_.get(), s.pcg_p32_.get(), -1.0, nullptr, nullptr, bk, nullptr);
     } else {
-        split_kernel<<<ceil_div(n, kVT), kVT, 0, s.stream_>>>(s.dc_.get(), n, s.dcff_.get());
-        GBA_LAUNCH_CHECK();
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
             s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
             nullptr, nullptr, bk, nullptr);
     }
     GBA_LAUNCH_CHECK();
+    s.ff_holds_ = Solver::kFfNone;  // pts_ff_ holds the trial points now
+    s.pts_ff_trial_ = true;
 }
 
 PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned) {

@@ -163,6 +163,9 @@ public:
     void prepare_ff(const double* cams, const double* pts);
     enum FfHolds { kFfNone, kFfCurrent, kFfTrial };
     FfHolds ff_holds_ = kFfNone;
+    // pts_ff_ holds the split of tpts_, written by the mixed back-substitution
+    // (the trial cost then skips the point split).
+    bool pts_ff_trial_ = false;
     // Trial parameters become current.
     void accept();
 

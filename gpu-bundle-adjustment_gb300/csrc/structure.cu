@@ -625,6 +625,7 @@ void Solver::accept() {
     cams_.swap(tcams_);
     pts_.swap(tpts_);
     ff_holds_ = ff_holds_ == kFfTrial ? kFfCurrent : kFfNone;
+    pts_ff_trial_ = false;
     if (form_ != SolverForm::Plain) {
         // the trial evaluation is the current one now: residuals and SSE
         r_cur_.swap(r_trial_);
