@@ -591,35 +591,6 @@ __device__ __forceinline__ double ordered_sum_all(const double* __restrict__ red
 // (45 per camera): thread (camera, j) forms column j of L^-1 by forward
 // substitution, then row a of M = L^-T L^-1. Once per inner solve; the PCG
 // update then applies M_c as a 9x9 product without divisions.
-__global__ void __launch_bounds__(kUT) precond_inverse_kernel(const double* __restrict__ L, int C,
-                                                             double* __restrict__ Minv) {
-    __shared__ double li[kUC][9][9];  // li[cl][i][j] = (L^-1)_ij
-    const int cl = threadIdx.x / 9, j = threadIdx.x % 9;
-    const int c = blockIdx.x * kUC + cl;
-    if (c < C) {
-        const double* Lc = L + 45ll * c;
-        double y[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) {
-            double t = (i == j) ? 1.0 : 0.0;
-#pragma unroll
-            for (int k = 0; k < i; ++k) t -= Lc[blk::tri(i, k)] * y[k];
-            y[i] = (i < j) ? 0.0 : t / Lc[blk::tri(i, i)];
-            li[cl][i][j] = y[i];
-        }
-    }
-    __syncthreads();
-    if (c < C) {
-        const int a = j;
-#pragma unroll
-        for (int b = 0; b < 9; ++b) {
-            double m = 0.0;
-            for (int k = max(a, b); k < 9; ++k) m += li[cl][k][a] * li[cl][k][b];
-            Minv[81ll * c + 9 * a + b] = m;
-        }
-    }
-}
-
 // z_i = (M_c r_c)_k for entry i = 9c + k; rs holds the block's r entries.
 __device__ __forceinline__ double apply_minv_row(const double* __restrict__ Minv, long long c, int k, const double* rs) {
     const double* m = Minv + 81 * c + 9 * k;
@@ -800,87 +771,138 @@ __global__ void __launch_bounds__(kVT) axpy_split_kernel(double* __restrict__ y,
 // ---- block-Jacobi blocks S_cc = U_lambda,c - sum_{e in c} Jc^T (Jp V'^-1 Jp^T) Jc
 // (the sums come from the right-hand side camera pass)
 
-// Block-Jacobi factor of one camera block, one CTA of kSD threads per camera
-// (A: the full 9x9 block in shared memory): right-looking FP64 Cholesky with
-// one thread per entry of the lower triangle, nine steps of (pivot square
-// root, column scale, trailing update). FP64, because even Jacobi-scaled the
-// camera blocks' condition numbers make an FP32 factor a visibly weaker
-// preconditioner; parallel, because a one-thread FP64 factorisation is bound
-// by the FP64 pipe's latency. A block that is not SPD in FP64 (round-off with
-// tiny damping) falls back to the square root of its diagonal.
-constexpr int kSD = 64;
+// Block-Jacobi factor of one camera block: right-looking FP64 Cholesky of the
+// 9x9 block. FP64, because even Jacobi-scaled the camera blocks' condition
+// numbers make an FP32 factor a visibly weaker preconditioner. A block that is
+// not SPD in FP64 (round-off with tiny damping) falls back to the square root
+// of its diagonal.
+//
+// One camera per lane: the 45 packed entries live in registers (fully
+// unrolled, constant indices), so every FP64 instruction serves 32 cameras.
+// GB300's FP64 pipe takes the same time for a warp instruction whatever its
+// active lanes: a CTA per camera (one thread per entry, 1-8 active lanes per
+// step) took 80 us per launch on 5,000 cameras, this 37 us. The pivot
+// reciprocal scales the column.
+constexpr int kSL = 32;  // threads (= cameras) per block of the per-lane kernels
 
-__device__ __forceinline__ void bj_factor_cta(const double* A, double* __restrict__ Lc) {
-    __shared__ double m[45];
-    __shared__ int fail;
-    const int t = threadIdx.x;
-    int ti = 0, tj = 0;
-    if (t < 45) {
-        while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-        tj = t - ti * (ti + 1) / 2;
-        m[t] = A[9 * ti + tj];
-    }
-    if (t == 0) fail = 0;
-    __syncthreads();
+__device__ __forceinline__ void chol9_lane(double (&a)[45]) {
+    double d0[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) d0[i] = a[blk::tri(i, i)];
+    bool ok = true;
+#pragma unroll
     for (int k = 0; k < 9; ++k) {
-        if (t == blk::tri(k, k)) {
-            const double d = m[t];
-            if (d > 0.0) {
-                m[t] = sqrt(d);
-            } else {
-                fail = 1;
-            }
-        }
-        __syncthreads();
-        if (fail) break;
-        if (t < 45 && tj == k && ti > k) m[t] /= m[blk::tri(k, k)];
-        __syncthreads();
-        if (t < 45 && tj > k) m[t] -= m[blk::tri(ti, k)] * m[blk::tri(tj, k)];
-        __syncthreads();
+        const double d = a[blk::tri(k, k)];
+        ok = ok && d > 0.0;
+        const double l = sqrt(d > 0.0 ? d : 1.0);
+        a[blk::tri(k, k)] = l;
+        const double r = 1.0 / l;
+#pragma unroll
+        for (int i = k + 1; i < 9; ++i) a[blk::tri(i, k)] *= r;
+#pragma unroll
+        for (int j = k + 1; j < 9; ++j)
+#pragma unroll
+            for (int i = j; i < 9; ++i) a[blk::tri(i, j)] -= a[blk::tri(i, k)] * a[blk::tri(j, k)];
     }
-    if (t < 45) {
-        double v = m[t];
-        if (fail) {
-            const double d = A[10 * ti];
-            v = ti == tj ? sqrt(d > 1e-300 ? d : 1e-300) : 0.0;
-        }
-        Lc[t] = v;
+    if (!ok) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+#pragma unroll
+            for (int j = 0; j <= i; ++j)
+                a[blk::tri(i, j)] = i == j ? sqrt(d0[i] > 1e-300 ? d0[i] : 1e-300) : 0.0;
     }
 }
 
-// One CTA per camera: S_cc = U_lambda,c - (chunk sums from the right-hand side
-// pass), stored full FP64, and its block-Jacobi factor.
-__global__ void __launch_bounds__(kSD) sdiag_finalize(const int* __restrict__ cam_chunk_off,
-                                                     const double* __restrict__ part, const double* __restrict__ U,
-                                                     double lambda, int C, double* __restrict__ Sdiag,
-                                                     double* __restrict__ L) {
-    __shared__ double A[81];
-    const int c = blockIdx.x, t = threadIdx.x;
+// One camera per lane: S_cc = U_lambda,c - (chunk sums from the right-hand
+// side pass, in chunk order), stored full FP64, and its block-Jacobi factor.
+__global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict__ cam_chunk_off,
+                                                          const double* __restrict__ part,
+                                                          const double* __restrict__ U, double lambda, int C,
+                                                          double* __restrict__ Sdiag, double* __restrict__ L) {
+    const int c = blockIdx.x * kSL + threadIdx.x;
+    if (c >= C) return;
     const double* Uc = U + 81ll * c;
-    if (t < 45) {
-        int a = 0;
-        while ((a + 1) * (a + 2) / 2 <= t) ++a;
-        const int b = t - a * (a + 1) / 2;
-        double s = 0.0;
-        for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) s += part[54ll * q + 9 + t];
-        double v = Uc[9 * a + b] - s;
-        if (a == b) v += lambda * (Uc[10 * a] > 0.0 ? Uc[10 * a] : 1e-12);
-        A[9 * a + b] = v;
-        A[9 * b + a] = v;
+    double a[45];
+#pragma unroll
+    for (int t = 0; t < 45; ++t) a[t] = 0.0;
+    const int q1 = cam_chunk_off[c + 1];
+    for (int q = cam_chunk_off[c]; q < q1; ++q) {
+        const double* pq = part + 54ll * q + 9;
+#pragma unroll
+        for (int t = 0; t < 45; ++t) a[t] += pq[t];
     }
-    __syncthreads();
-    for (int i = t; i < 81; i += kSD) Sdiag[81ll * c + i] = A[i];
-    bj_factor_cta(A, L + 45ll * c);
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+            double v = Uc[9 * i + j] - a[blk::tri(i, j)];
+            if (i == j) v += lambda * (Uc[10 * i] > 0.0 ? Uc[10 * i] : 1e-12);
+            a[blk::tri(i, j)] = v;
+        }
+    double* Sc = Sdiag + 81ll * c;
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+#pragma unroll
+        for (int j = 0; j < 9; ++j) Sc[9 * i + j] = a[i >= j ? blk::tri(i, j) : blk::tri(j, i)];
+    chol9_lane(a);
+    double* Lc = L + 45ll * c;
+#pragma unroll
+    for (int t = 0; t < 45; ++t) Lc[t] = a[t];
 }
 
-// Block-Jacobi factors from stored diagonal blocks (the learned form's fallback).
-__global__ void __launch_bounds__(kSD) factor_blocks_kernel(const double* __restrict__ Sdiag, int C,
-                                                           double* __restrict__ L) {
-    __shared__ double A[81];
-    const int c = blockIdx.x;
-    for (int i = threadIdx.x; i < 81; i += kSD) A[i] = Sdiag[81ll * c + i];
-    __syncthreads();
-    bj_factor_cta(A, L + 45ll * c);
+// Block-Jacobi factors from stored diagonal blocks, one camera per lane.
+__global__ void __launch_bounds__(kSL) factor_blocks_lane(const double* __restrict__ Sdiag, int C,
+                                                         double* __restrict__ L) {
+    const int c = blockIdx.x * kSL + threadIdx.x;
+    if (c >= C) return;
+    const double* Sc = Sdiag + 81ll * c;
+    double a[45];
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) a[blk::tri(i, j)] = Sc[9 * i + j];
+    chol9_lane(a);
+    double* Lc = L + 45ll * c;
+#pragma unroll
+    for (int t = 0; t < 45; ++t) Lc[t] = a[t];
+}
+
+// Explicit block inverse M_c = (L L^T)^-1 = X^T X with X = L^-1, one camera per
+// lane. X overwrites L column by column (column j of X needs L_ij only for its
+// own entry X_ij, and L's later columns); sums run in increasing k as in the
+// nine-threads-per-camera kernel.
+__global__ void __launch_bounds__(kSL) precond_inverse_lane(const double* __restrict__ L, int C,
+                                                           double* __restrict__ Minv) {
+    const int c = blockIdx.x * kSL + threadIdx.x;
+    if (c >= C) return;
+    const double* Lc = L + 45ll * c;
+    double x[45], rd[9];
+#pragma unroll
+    for (int t = 0; t < 45; ++t) x[t] = Lc[t];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) rd[i] = 1.0 / x[blk::tri(i, i)];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        x[blk::tri(j, j)] = rd[j];
+#pragma unroll
+        for (int i = j + 1; i < 9; ++i) {
+            double t = -(x[blk::tri(i, j)] * x[blk::tri(j, j)]);
+#pragma unroll
+            for (int k = j + 1; k < i; ++k) t -= x[blk::tri(i, k)] * x[blk::tri(k, j)];
+            x[blk::tri(i, j)] = t * rd[i];
+        }
+    }
+    double* M = Minv + 81ll * c;
+#pragma unroll
+    for (int a = 0; a < 9; ++a)
+#pragma unroll
+        for (int b = 0; b <= a; ++b) {
+            double m = 0.0;
+#pragma unroll
+            for (int k = a; k < 9; ++k) m += x[blk::tri(k, a)] * x[blk::tri(k, b)];
+            M[9 * a + b] = m;
+            M[9 * b + a] = m;
+        }
 }
 
 }  // namespace
@@ -980,9 +1002,11 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
 
     // block-Jacobi blocks (partials from the right-hand side pass) and factors
     // (+ learned correction)
-    sdiag_finalize<<<C_, kSD, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda, C_,
-                                             Sdiag_.get(), Pfac_.get());
+    cudaEvent_t bj_ev = prof_start();
+    sdiag_finalize_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
+                                                               C_, Sdiag_.get(), Pfac_.get());
     GBA_LAUNCH_CHECK();
+    prof_stop("bj_blocks", bj_ev);
     if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
     // Learned factors are used once they have won the judged solve (below).
     if (learned && learned_choice_ == 1) model_->correct_factors(*this, lambda);
@@ -1014,8 +1038,10 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     // inner_rel2 = its final ||r||^2 / ||b||^2.
     double inner_rel2 = 0.0;
     auto inner_pcg = [&](bool* ok) -> long long {
-        precond_inverse_kernel<<<nub, kUT, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
+        cudaEvent_t inv_ev = prof_start();
+        precond_inverse_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
         GBA_LAUNCH_CHECK();
+        prof_stop("bj_inverse", inv_ev);
         pcg_init<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
                                            ref_r_.get(), Pinv_.get(), C_, red, red2);
         GBA_LAUNCH_CHECK();
@@ -1091,7 +1117,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                 inner_rel2 = rel2_bj;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
-                factor_blocks_kernel<<<C_, kSD, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+                factor_blocks_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
                 GBA_LAUNCH_CHECK();
                 st.pcg_iterations += it_l;
                 it_count = it_bj;
@@ -1104,7 +1130,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             // Block-Jacobi judges the learned factors: an inner solve that breaks
             // down or misses its tolerance is redone with the plain blocks, which
             // then serve for the rest of this trial.
-            factor_blocks_kernel<<<C_, kSD, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
+            factor_blocks_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
             GBA_LAUNCH_CHECK();
             use_learned = false;
             ++st.fallbacks;
