@@ -251,15 +251,13 @@ __global__ void __launch_bounds__(kTB) camera_step_kernel(const double* __restri
 }
 
 // denom = (camera partials in order) + (point partials in order).
-__global__ void __launch_bounds__(256) denom_finalize(const double* __restrict__ part, int ncam, int npt,
-                                                     double* __restrict__ out) {
-    __shared__ double red[8];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < ncam; i += 256) s += part[i];
-    const double a = block_sum<256>(s, red);
-    s = 0.0;
-    for (int i = threadIdx.x; i < npt; i += 256) s += part[ncam + i];
-    const double b = block_sum<256>(s, red);
+constexpr int kSumT = 1024;
+
+__global__ void __launch_bounds__(kSumT) denom_finalize(const double* __restrict__ part, int ncam, int npt,
+                                                       double* __restrict__ out) {
+    __shared__ double red[kSumT / 32];
+    const double a = wide_block_sum<kSumT>(part, ncam, red);
+    const double b = wide_block_sum<kSumT>(part + ncam, npt, red);
     if (threadIdx.x == 0) *out = a + b;
 }
 
@@ -326,7 +324,7 @@ void Solver::backsub_launch(double lambda) {
         mixed_back_substitute(*this, lambda, part + ncam);
     }
     prof_stop("backsub", ev);
-    denom_finalize<<<1, 256, 0, stream_>>>(part, ncam, n_pchunk_, scal_.get() + 2);
+    denom_finalize<<<1, kSumT, 0, stream_>>>(part, ncam, n_pchunk_, scal_.get() + 2);
     GBA_LAUNCH_CHECK();
 }
 

@@ -64,6 +64,26 @@ __device__ __forceinline__ double block_sum(double v, double* shared) {
     return r;
 }
 
+// Deterministic sum of part[0, n) by one block of kThreads threads (result in
+// thread 0): four interleaved accumulators per thread keep four independent
+// loads in flight instead of one dependent load per add; they are combined in
+// a fixed order, then summed over the block.
+template <int kThreads>
+__device__ __forceinline__ double wide_block_sum(const double* __restrict__ part, int n, double* shared) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = threadIdx.x;
+    for (; i + 3 * kThreads < n; i += 4 * kThreads) {
+        s0 += part[i];
+        s1 += part[i + kThreads];
+        s2 += part[i + 2 * kThreads];
+        s3 += part[i + 3 * kThreads];
+    }
+    if (i < n) s0 += part[i];
+    if (i + kThreads < n) s1 += part[i + kThreads];
+    if (i + 2 * kThreads < n) s2 += part[i + 2 * kThreads];
+    return block_sum<kThreads>((s0 + s1) + (s2 + s3), shared);
+}
+
 template <int kThreads>
 __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v,
                                                             unsigned long long* shared) {

@@ -427,11 +427,11 @@ __global__ void add_counter_kernel(unsigned long long* __restrict__ dst, const u
 }
 
 // Sum of n partials in a fixed order (single CTA) -> *out.
-__global__ void __launch_bounds__(256) ordered_sum(const double* __restrict__ part, int n, double* __restrict__ out) {
-    __shared__ double red[8];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += 256) s += part[i];
-    const double t = block_sum<256>(s, red);
+constexpr int kSumT = 1024;  // threads of the single-block partial sums
+
+__global__ void __launch_bounds__(kSumT) ordered_sum(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double red[kSumT / 32];
+    const double t = wide_block_sum<kSumT>(part, n, red);
     if (threadIdx.x == 0) *out = t;
 }
 
@@ -717,7 +717,7 @@ double Solver::accumulate() {
             GBA_LAUNCH_CHECK();
             prof_stop("camera_pass_f64", ev);
         }
-        ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
+        ordered_sum<<<1, kSumT, 0, stream_>>>(sse_part_.get(), n_pchunk_, scal_.get());
         GBA_LAUNCH_CHECK();
     } else {
         // The mixed form keeps the cost at FP64 accuracy: SSE and residuals come
@@ -726,7 +726,7 @@ double Solver::accumulate() {
         // to a scratch counter: the FP32 pass counts this evaluation's anomalies.
         if (!resid_valid_) {
             cost_mixed(cams_.get(), pts_.get(), counters_.get() + 2, reinterpret_cast<float2*>(r_cur_.get()));
-            ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), n_cchunk_, scal_.get());
+            ordered_sum<<<1, kSumT, 0, stream_>>>(sse_part_.get(), n_cchunk_, scal_.get());
             GBA_LAUNCH_CHECK();
             resid_valid_ = true;
         }
@@ -833,7 +833,7 @@ void Solver::trial_cost_launch(unsigned long long* anomalies) {
     } else {
         cost_mixed(tcams_.get(), tpts_.get(), anomalies, reinterpret_cast<float2*>(r_trial_.get()));
     }
-    ordered_sum<<<1, 256, 0, stream_>>>(sse_part_.get(), form_ == SolverForm::Plain ? n_pchunk_ : n_cchunk_,
+    ordered_sum<<<1, kSumT, 0, stream_>>>(sse_part_.get(), form_ == SolverForm::Plain ? n_pchunk_ : n_cchunk_,
                                         scal_.get() + 1);
     GBA_LAUNCH_CHECK();
 }

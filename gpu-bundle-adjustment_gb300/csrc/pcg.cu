@@ -186,6 +186,21 @@ __device__ __forceinline__ void jp_times(const float* jp, T w0, T w1, T w2, T& u
     madd(u1, jp[5], w2);
 }
 
+// G = Jp V'^-1 Jp^T (2x2 symmetric, FP32: g00, g01, g11) of one slot, for the
+// block-Jacobi diagonal blocks; vi: the point's FP32 V'^-1 (packed lower).
+__device__ __forceinline__ float4 jp_vinv_jpt(const float* j, const float* vi) {
+    float m[6];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const float a0 = j[3 * r], a1 = j[3 * r + 1], a2 = j[3 * r + 2];
+        m[3 * r] = a0 * vi[0] + a1 * vi[1] + a2 * vi[3];
+        m[3 * r + 1] = a0 * vi[1] + a1 * vi[2] + a2 * vi[4];
+        m[3 * r + 2] = a0 * vi[3] + a1 * vi[4] + a2 * vi[5];
+    }
+    return make_float4(m[0] * j[0] + m[1] * j[1] + m[2] * j[2], m[0] * j[3] + m[1] * j[4] + m[2] * j[5],
+                       m[3] * j[3] + m[4] * j[4] + m[5] * j[5], 0.f);
+}
+
 // Back-substitution outputs of the point pass (kBack): dp = V'^-1 (bp - W^T dc),
 // trial points, and per-chunk partials of the gain denominator's point terms.
 struct BacksubOut {
@@ -204,7 +219,8 @@ struct BacksubOut {
 // copy (+ low parts for float-float). u is written at the slot's camera-major
 // position so that the camera pass reads it contiguously. With kBack (a = -1,
 // xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
-template <typename T, bool kBack = false>
+// kRhs: the right-hand side instantiation (xt = null, a = 1, also G).
+template <typename T, bool kBack = false, bool kRhs = false>
 __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                        const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
@@ -240,7 +256,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
     float jp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int key = -1;  // point of the slot (slots past the chunk end share key -1, value 0)
     long long q = 0;
-    if (xt) {
+    if (!kRhs && xt) {
         for (int base = s0; base < s1; base += kPT) {
             const int s = base + threadIdx.x;
             T v0 = zero<T>(), v1 = zero<T>(), v2 = zero<T>();
@@ -302,6 +318,24 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
             __syncthreads();
         }
     }
+    if (kRhs && single) {
+        // right-hand side: the slot's point, Jp and camera-major position are
+        // loaded before the barrier, so their latency overlaps the owners' bp
+        // and V'^-1 loads
+        const int s = s0 + threadIdx.x;
+        if (s < s1) {
+            key = s_pt[s];
+            q = cam_pos[s];
+            const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
+            const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
+            jp[0] = j01.x;
+            jp[1] = j01.y;
+            jp[2] = j23.x;
+            jp[3] = j23.y;
+            jp[4] = j45.x;
+            jp[5] = j45.y;
+        }
+    }
     T w0 = zero<T>(), w1 = zero<T>(), w2 = zero<T>();
     if (my_p < p1) {
         if (a != 0.0) {
@@ -359,11 +393,12 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
     }
     __syncthreads();
     // u_e = Jp_e w_p for every slot of the chunk, stored camera-major
-    if (single && xt) {
+    if (single) {
         if (s0 + static_cast<int>(threadIdx.x) < s1) {
             T u0, u1;
             jp_times(jp, wsh[key - p0][0], wsh[key - p0][1], wsh[key - p0][2], u0, u1);
             store_u(u_cm, q, u0, u1);
+            if (g_cm) g_cm[q] = jp_vinv_jpt(jp, vsh[key - p0]);
         }
         return;
     }
@@ -376,20 +411,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
         jp_times(j, wsh[p - p0][0], wsh[p - p0][1], wsh[p - p0][2], u0, u1);
         const long long q = cam_pos[s];
         store_u(u_cm, q, u0, u1);
-        if (g_cm) {
-            // G = Jp V'^-1 Jp^T (2x2, FP32) for the block-Jacobi diagonal blocks
-            const float* vi = vsh[p - p0];
-            float m[6];
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const float a0 = j[3 * r], a1 = j[3 * r + 1], a2 = j[3 * r + 2];
-                m[3 * r] = a0 * vi[0] + a1 * vi[1] + a2 * vi[3];
-                m[3 * r + 1] = a0 * vi[1] + a1 * vi[2] + a2 * vi[4];
-                m[3 * r + 2] = a0 * vi[3] + a1 * vi[4] + a2 * vi[5];
-            }
-            g_cm[q] = make_float4(m[0] * j[0] + m[1] * j[1] + m[2] * j[2], m[0] * j[3] + m[1] * j[4] + m[2] * j[5],
-                                  m[3] * j[3] + m[4] * j[4] + m[5] * j[5], 0.f);
-        }
+        if (g_cm) g_cm[q] = jp_vinv_jpt(j, vsh[p - p0]);
     }
 }
 
@@ -917,7 +939,7 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     const bool rhs = x == nullptr;  // right-hand side: also the block-Jacobi diagonal-block partials
     float4* g = rhs ? reinterpret_cast<float4*>(s.g_cm_.get()) : nullptr;
     cudaEvent_t ev = s.prof_start();
-    schur_point_pass<T><<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
+    (rhs ? schur_point_pass<T, false, true> : schur_point_pass<T, false, false>)<<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
                                                            s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
                                                            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
                                                            u, done, BacksubOut{}, g);
