@@ -835,12 +835,57 @@ __device__ __forceinline__ void chol9_lane(double (&a)[45]) {
     }
 }
 
+// Explicit block inverse M_c = (L L^T)^-1 = X^T X with X = L^-1, from the
+// factor in registers (one camera per lane). X overwrites L column by column
+// (column j of X needs L_ij only for its own entry X_ij, and L's later
+// columns); sums run in increasing k.
+__device__ __forceinline__ void inverse_from_factor_lane(double (&x)[45], double* __restrict__ M) {
+    double rd[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) rd[i] = 1.0 / x[blk::tri(i, i)];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        x[blk::tri(j, j)] = rd[j];
+#pragma unroll
+        for (int i = j + 1; i < 9; ++i) {
+            double t = -(x[blk::tri(i, j)] * x[blk::tri(j, j)]);
+#pragma unroll
+            for (int k = j + 1; k < i; ++k) t -= x[blk::tri(i, k)] * x[blk::tri(k, j)];
+            x[blk::tri(i, j)] = t * rd[i];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 9; ++a)
+#pragma unroll
+        for (int b = 0; b <= a; ++b) {
+            double m = 0.0;
+#pragma unroll
+            for (int k = a; k < 9; ++k) m += x[blk::tri(k, a)] * x[blk::tri(k, b)];
+            M[9 * a + b] = m;
+            M[9 * b + a] = m;
+        }
+}
+
+__global__ void __launch_bounds__(kSL) precond_inverse_lane(const double* __restrict__ L, int C,
+                                                           double* __restrict__ Minv) {
+    const int c = blockIdx.x * kSL + threadIdx.x;
+    if (c >= C) return;
+    const double* Lc = L + 45ll * c;
+    double x[45];
+#pragma unroll
+    for (int t = 0; t < 45; ++t) x[t] = Lc[t];
+    inverse_from_factor_lane(x, Minv + 81ll * c);
+}
+
 // One camera per lane: S_cc = U_lambda,c - (chunk sums from the right-hand
-// side pass, in chunk order), stored full FP64, and its block-Jacobi factor.
+// side pass, in chunk order), stored full FP64, its block-Jacobi factor and,
+// when Minv is given (no learned correction of the factor follows), the
+// explicit inverse as well.
 __global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict__ cam_chunk_off,
                                                           const double* __restrict__ part,
                                                           const double* __restrict__ U, double lambda, int C,
-                                                          double* __restrict__ Sdiag, double* __restrict__ L) {
+                                                          double* __restrict__ Sdiag, double* __restrict__ L,
+                                                          double* __restrict__ Minv) {
     const int c = blockIdx.x * kSL + threadIdx.x;
     if (c >= C) return;
     const double* Uc = U + 81ll * c;
@@ -870,6 +915,7 @@ __global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict
     double* Lc = L + 45ll * c;
 #pragma unroll
     for (int t = 0; t < 45; ++t) Lc[t] = a[t];
+    if (Minv) inverse_from_factor_lane(a, Minv + 81ll * c);
 }
 
 // Block-Jacobi factors from stored diagonal blocks, one camera per lane.
@@ -887,44 +933,6 @@ __global__ void __launch_bounds__(kSL) factor_blocks_lane(const double* __restri
     double* Lc = L + 45ll * c;
 #pragma unroll
     for (int t = 0; t < 45; ++t) Lc[t] = a[t];
-}
-
-// Explicit block inverse M_c = (L L^T)^-1 = X^T X with X = L^-1, one camera per
-// lane. X overwrites L column by column (column j of X needs L_ij only for its
-// own entry X_ij, and L's later columns); sums run in increasing k as in the
-// nine-threads-per-camera kernel.
-__global__ void __launch_bounds__(kSL) precond_inverse_lane(const double* __restrict__ L, int C,
-                                                           double* __restrict__ Minv) {
-    const int c = blockIdx.x * kSL + threadIdx.x;
-    if (c >= C) return;
-    const double* Lc = L + 45ll * c;
-    double x[45], rd[9];
-#pragma unroll
-    for (int t = 0; t < 45; ++t) x[t] = Lc[t];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) rd[i] = 1.0 / x[blk::tri(i, i)];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        x[blk::tri(j, j)] = rd[j];
-#pragma unroll
-        for (int i = j + 1; i < 9; ++i) {
-            double t = -(x[blk::tri(i, j)] * x[blk::tri(j, j)]);
-#pragma unroll
-            for (int k = j + 1; k < i; ++k) t -= x[blk::tri(i, k)] * x[blk::tri(k, j)];
-            x[blk::tri(i, j)] = t * rd[i];
-        }
-    }
-    double* M = Minv + 81ll * c;
-#pragma unroll
-    for (int a = 0; a < 9; ++a)
-#pragma unroll
-        for (int b = 0; b <= a; ++b) {
-            double m = 0.0;
-#pragma unroll
-            for (int k = a; k < 9; ++k) m += x[blk::tri(k, a)] * x[blk::tri(k, b)];
-            M[9 * a + b] = m;
-            M[9 * b + a] = m;
-        }
 }
 
 }  // namespace
@@ -1024,9 +1032,13 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
 
     // block-Jacobi blocks (partials from the right-hand side pass) and factors
     // (+ learned correction)
+    // Pinv_ is current for Pfac_ (set by the fused inverse or the inverse kernel,
+    // cleared whenever the factors change).
+    bool pinv_valid = !(learned && learned_choice_ != 2);
     cudaEvent_t bj_ev = prof_start();
     sdiag_finalize_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
-                                                               C_, Sdiag_.get(), Pfac_.get());
+                                                               C_, Sdiag_.get(), Pfac_.get(),
+                                                               pinv_valid ? Pinv_.get() : nullptr);
     GBA_LAUNCH_CHECK();
     prof_stop("bj_blocks", bj_ev);
     if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
@@ -1060,10 +1072,13 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     // inner_rel2 = its final ||r||^2 / ||b||^2.
     double inner_rel2 = 0.0;
     auto inner_pcg = [&](bool* ok) -> long long {
-        cudaEvent_t inv_ev = prof_start();
-        precond_inverse_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
-        GBA_LAUNCH_CHECK();
-        prof_stop("bj_inverse", inv_ev);
+        if (!pinv_valid) {
+            cudaEvent_t inv_ev = prof_start();
+            precond_inverse_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
+            GBA_LAUNCH_CHECK();
+            prof_stop("bj_inverse", inv_ev);
+            pinv_valid = true;
+        }
         pcg_init<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
                                            ref_r_.get(), Pinv_.get(), C_, red, red2);
         GBA_LAUNCH_CHECK();
@@ -1118,6 +1133,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             GBA_CUDA_CHECK(cudaMemcpyAsync(judge_x_.get(), pcg_x_.get(), n * sizeof(double),
                                            cudaMemcpyDeviceToDevice, stream_));
             model_->correct_factors(*this, lambda);
+            pinv_valid = false;
             const long long it_l = inner_pcg(&ok_l);
             judge_iters_[0] = it_bj;
             judge_iters_[1] = it_l;
@@ -1141,6 +1157,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                                                cudaMemcpyDeviceToDevice, stream_));
                 factor_blocks_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
                 GBA_LAUNCH_CHECK();
+                pinv_valid = false;
                 st.pcg_iterations += it_l;
                 it_count = it_bj;
                 ok = ok_bj;
@@ -1154,6 +1171,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             // then serve for the rest of this trial.
             factor_blocks_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
             GBA_LAUNCH_CHECK();
+            pinv_valid = false;
             use_learned = false;
             ++st.fallbacks;
             st.pcg_iterations += it_count;
