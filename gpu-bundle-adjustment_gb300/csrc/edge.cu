@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kCT) camera_pass_f64(const int* __restrict__ c
 constexpr int kStg = 28;  // floats per slot in the store-staging buffer: Jc(18), r(2), Jp(6), q, pad
 
 __global__ void __launch_bounds__(kPT) point_pass_f32(
-    const int* __restrict__ pchunk, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
+    const int4* __restrict__ prange, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
     const int* __restrict__ s_pt, const float* __restrict__ cams32,
     const float2* __restrict__ ptsff, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
     float* __restrict__ Jc32, float* __restrict__ Jp32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
@@ -215,8 +215,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
     __shared__ unsigned long long redu[kPT / 32];
     __shared__ __align__(16) float stg[kPT * kStg];  // this pass's rows, per slot (kStg floats)
     const int chunk = blockIdx.x;
-    const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
-    const int s0 = pt_off[p0], s1 = pt_off[p1];
+    const int4 rg = prange[chunk];
+    const int p0 = rg.x, p1 = rg.y, s0 = rg.z, s1 = rg.w;
     const int my_p = p0 + threadIdx.x;
     const int lane = threadIdx.x & 31;
     int my_b = 0, my_e = 0;
@@ -734,7 +734,7 @@ double Solver::accumulate() {
         const float2* rc = reinterpret_cast<const float2*>(r_cur_.get());
         cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(
-            pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), Jc32_.get(), Jp32_.get(),
+            reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(), s_cam_.get(), s_pt_.get(), cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), Jc32_.get(), Jp32_.get(),
             J32c_.get(), V_.get(), bp_.get(), counters_.get(), static_cast<float>(huber_delta_));
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);

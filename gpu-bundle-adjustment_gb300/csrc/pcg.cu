@@ -221,7 +221,7 @@ struct BacksubOut {
 // xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
 // kRhs: the right-hand side instantiation (xt = null, a = 1, also G).
 template <typename T, bool kBack = false, bool kRhs = false>
-__global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int* __restrict__ pchunk, const int* __restrict__ pt_off,
+__global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int4* __restrict__ prange, const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                        const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
                                                        const float* __restrict__ Jp32,
@@ -237,8 +237,16 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
     __shared__ float bsum[kPT / 32][2];
     if (done && *done != 0.0) return;
     const int chunk = blockIdx.x;
-    const int p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
-    const int s0 = pt_off[p0], s1 = pt_off[p1];
+    // the chunk's points and slots: one 16-byte load from the range table (a
+    // null table: the chunk starts and the CSR offsets)
+    int p0, p1, s0, s1;
+    if (prange) {
+        const int4 rg = prange[chunk];
+        p0 = rg.x, p1 = rg.y, s0 = rg.z, s1 = rg.w;
+    } else {
+        p0 = pchunk[chunk], p1 = pchunk[chunk + 1];
+        s0 = pt_off[p0], s1 = pt_off[p1];
+    }
     const int my_p = p0 + threadIdx.x;
     const int lane = threadIdx.x & 31;
     int my_b = 0, my_e = 0;
@@ -947,7 +955,7 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     const bool rhs = x == nullptr;  // right-hand side: also the block-Jacobi diagonal-block partials
     float4* g = rhs ? reinterpret_cast<float4*>(s.g_cm_.get()) : nullptr;
     cudaEvent_t ev = s.prof_start();
-    (rhs ? schur_point_pass<T, false, true> : schur_point_pass<T, false, false>)<<<s.n_pchunk_, kPT, 0, s.stream_>>>(s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
+    (rhs ? schur_point_pass<T, false, true> : schur_point_pass<T, false, false>)<<<s.n_pchunk_, kPT, 0, s.stream_>>>(reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
                                                            s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
                                                            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
                                                            u, done, BacksubOut{}, g);
@@ -986,11 +994,11 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
                         s.dp_.get(), s.tpts_.get(), reinterpret_cast<float2*>(s.pts_ff_.get()), part};
     if (s.fast_solve_) {
         schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
+            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), nullptr, s.bp_.get(), s.pcg_p32_.get(), -1.0, nullptr, nullptr, bk, nullptr);
     } else {
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
+            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
             nullptr, nullptr, bk, nullptr);
     }

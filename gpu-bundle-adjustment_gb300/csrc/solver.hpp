@@ -211,6 +211,7 @@ public:
     DevBuf<double> s_px_;
     int n_pchunk_ = 0, n_cchunk_ = 0;
     DevBuf<int> pchunk_, cchunk_begin_, cchunk_cam_, cam_chunk_off_;
+    DevBuf<int> pchunk4_;  // per point chunk, int4 {first point, end point, first slot, end slot}
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
     DevBuf<float> Jc32_, Jp32_;  // mixed: FP32 Jacobian rows per slot, slot order (18 and 6 floats)

@@ -191,6 +191,16 @@ __global__ void chunk_starts_kernel(const int* __restrict__ jump, int levels, in
     }
 }
 
+// Per point chunk {p0, p1, s0, s1}: the point-side passes read their ranges
+// with one 16-byte load instead of two dependent loads (chunk table, CSR).
+__global__ void chunk_ranges_kernel(const int* __restrict__ pchunk, const int* __restrict__ pt_off, int n,
+                                    int4* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p0 = pchunk[i], p1 = pchunk[i + 1];
+        out[i] = make_int4(p0, p1, pt_off[p0], pt_off[p1]);
+    }
+}
+
 // Camera-major copies of per-slot data: point index and observation (as
 // float-float pairs) of camera-major position i (slot cam_slots[i]).
 __global__ void gather_cm_kernel(const int* __restrict__ cam_slots, const int* __restrict__ s_pt,
@@ -507,6 +517,12 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
         pchunk_.alloc(n + 1ull);
         chunk_starts_kernel<<<grid_for(n + 1ll), 256, 0, stream_>>>(jump.get(), levels, P, n, pchunk_.get());
         GBA_LAUNCH_CHECK();
+        pchunk4_.alloc(4ull * std::max(n, 1));
+        if (n > 0) {
+            chunk_ranges_kernel<<<grid_for(n), 256, 0, stream_>>>(pchunk_.get(), pt_off_.get(), n,
+                                                                 reinterpret_cast<int4*>(pchunk4_.get()));
+            GBA_LAUNCH_CHECK();
+        }
     }
     std::vector<int> h_cam_off(C + 1);
     GBA_CUDA_CHECK(cudaMemcpyAsync(h_cam_off.data(), cam_off_.get(), (C + 1) * sizeof(int),
