@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
     __shared__ T wsh[kPT][3];
     __shared__ float vsh[kPT][6];  // FP32 V'^-1 of the chunk's points (g_cm only)
     __shared__ float bsum[kPT / 32][2];
+    __shared__ double bout[kBack ? 9 * kPT : 1];  // back-substitution outputs of the chunk's points
     if (done && *done != 0.0) return;
     const int chunk = blockIdx.x;
     // the chunk's points and slots: one 16-byte load from the range table (a
@@ -373,11 +374,11 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const double dk = ffa::to_double(d[k]);
-                bk.dp[3 * p + k] = dk;
                 const double tp = bk.pts[3 * p + k] + dk;
-                bk.tpts[3 * p + k] = tp;
                 const ff tf = ffa::from_double(tp);
-                bk.tpts_ff[3 * p + k] = make_float2(tf.hi, tf.lo);
+                bout[3 * threadIdx.x + k] = dk;
+                bout[3 * kPT + 3 * threadIdx.x + k] = tp;
+                reinterpret_cast<float2*>(bout + 6 * kPT)[3 * threadIdx.x + k] = make_float2(tf.hi, tf.lo);
                 const float vk = static_cast<float>(bk.V[6 * p + diag[k]]);
                 ff t = {static_cast<float>(bp[3 * p + k]), 0.f};
                 ffa::madd(t, ffa::mul(lam, ff{vk > 0.f ? vk : 1e-12f, 0.f}), d[k]);
@@ -396,6 +397,15 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
 #pragma unroll
             for (int w = 0; w < kPT / 32; ++w) t += static_cast<double>(bsum[w][0]) + static_cast<double>(bsum[w][1]);
             bk.part[chunk] = t;
+        }
+        // dp, trial points and their split for the chunk's contiguous points, as
+        // contiguous runs
+        const int np = p1 - p0;
+        const float2* bff = reinterpret_cast<const float2*>(bout + 6 * kPT);
+        for (int i = threadIdx.x; i < 3 * np; i += kPT) {
+            bk.dp[3ll * p0 + i] = bout[i];
+            bk.tpts[3ll * p0 + i] = bout[3 * kPT + i];
+            bk.tpts_ff[3ll * p0 + i] = bff[i];
         }
         return;
     }
