@@ -208,8 +208,8 @@ def algorithmic_bytes(kernel: str, C: int, P: int, E: int) -> float:
 
 # DRAM bytes (read + write) per launch from one ncu capture on workload 5
 # (profiles/mixed_kernels_workload5_ncu.md), for the roofline's traffic field.
-NCU_TRAFFIC_W5 = {"point_pass_f32": 221.7e6 + 1596.7e6, "schur_point_pass_f32": 995.5e6 + 68.2e6,
-                  "schur_camera_pass_f32": 774.4e6 + 3.8e6, "cost_ff": 240.1e6 + 60.8e6}
+NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "schur_point_pass_f32": 992.6e6 + 66.4e6,
+                  "schur_camera_pass_f32": 774.4e6 + 3.8e6, "cost_ff": 239.9e6 + 61.0e6}
 
 HBM_KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
                "point_pass_f32", "cost_f64", "cost_ff")
