@@ -43,6 +43,7 @@ constexpr int kCamChunk = 1024;
 constexpr int kCheck = 8;       // most PCG iterations launched between host checks of the convergence flag
 constexpr long long kJudgeMin = 8;  // inner iterations a judged solve needs to be decisive
 constexpr int kJudgeAttempts = 2;    // indecisive judgements before block-Jacobi is kept for the solve
+constexpr double kShortInnerTol = 1e-2;  // inner tolerances this loose end every solve in a few iterations
 constexpr double kLooseTol = 1e-3;   // refinement targets at or above this run the fast (FP32) path
 
 constexpr int kUC = 32;        // cameras per block of the 9-threads-per-camera kernels
@@ -1190,10 +1191,12 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             judge_iters_[1] = it_l;
             // Solves shorter than kJudgeMin iterations are too short to compare:
             // keep block-Jacobi for now and judge again at the next inner solve.
-            // After kJudgeAttempts indecisive judgements (loose inner
-            // tolerances end every solve in a few iterations) block-Jacobi is
-            // kept: judging costs a second solve each time.
+            // After kJudgeAttempts indecisive judgements block-Jacobi is kept:
+            // judging costs a second solve each time. With an inner tolerance of
+            // kShortInnerTol or looser every later solve is as short, so one
+            // indecisive judgement settles it.
             ++judge_attempts_;
+            const int attempts = opts.pcg_tol >= kShortInnerTol ? 1 : kJudgeAttempts;
             const bool decisive = std::max(it_bj, it_l) >= kJudgeMin || !ok_bj || !ok_l;
             if (decisive && ok_l && (!ok_bj || it_l < it_bj)) {
                 learned_choice_ = 1;
@@ -1202,7 +1205,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                 it_count = it_l;
                 ok = ok_l;
             } else {
-                learned_choice_ = (decisive || judge_attempts_ >= kJudgeAttempts) ? 2 : 0;
+                learned_choice_ = (decisive || judge_attempts_ >= attempts) ? 2 : 0;
                 inner_rel2 = rel2_bj;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
