@@ -529,6 +529,7 @@ void LearnedPreconditioner::correct_factors(Solver& s, double lambda) {
 Solver::~Solver() {
     prof_reset();
     delete model_;
+    if (sync_ev_) cudaEventDestroy(sync_ev_);
 }
 
 void Solver::load_model(const std::string& path) {

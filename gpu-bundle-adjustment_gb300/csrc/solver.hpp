@@ -197,6 +197,7 @@ public:
     int C_, P_, E_, n_pad_ = 0;
     SolverForm form_;
     cudaStream_t stream_;
+    mutable cudaEvent_t sync_ev_ = nullptr;  // sync(): the event the host polls (created on first use)
     LearnedPreconditioner* model_ = nullptr;
 
     DevBuf<double> cams_, pts_, tcams_, tpts_, cams0_, pts0_;

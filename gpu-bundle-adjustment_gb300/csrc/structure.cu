@@ -382,7 +382,19 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     sync();
 }
 
-void Solver::sync() const { GBA_CUDA_CHECK(cudaStreamSynchronize(stream_)); }
+// Waits for the solver stream by polling an event: the host resumes as soon as
+// the stream drains, whatever scheduling mode the context was created with (a
+// yielding or blocking stream synchronisation adds tens of microseconds per
+// wait, and a solve waits some forty times). A device error ends the wait
+// with that error.
+void Solver::sync() const {
+    if (!sync_ev_) GBA_CUDA_CHECK(cudaEventCreateWithFlags(&sync_ev_, cudaEventDisableTiming));
+    GBA_CUDA_CHECK(cudaEventRecord(sync_ev_, stream_));
+    cudaError_t e;
+    while ((e = cudaEventQuery(sync_ev_)) == cudaErrorNotReady) {
+    }
+    GBA_CUDA_CHECK(e);
+}
 
 void Solver::set_params(const double* cams, const double* pts) {
     resid_valid_ = false;
