@@ -330,7 +330,30 @@ T* dalloc(long long n) {
     return p;
 }
 
+// Stream-ordered allocation from the device's memory pool (inference mode).
+template <typename T>
+T* palloc(long long n, cudaStream_t s) {
+    T* p = nullptr;
+    GBA_CUDA_CHECK(cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * n, s));
+    return p;
+}
+
 const char kMagic[8] = {'G', 'B', 'A', 'M', 'L', 'P', '0', '1'};
+
+std::vector<float> read_model(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open model " + path);
+    char magic[8];
+    int32_t dims[3];
+    f.read(magic, 8);
+    f.read(reinterpret_cast<char*>(dims), sizeof dims);
+    if (!f || std::memcmp(magic, kMagic, 8) != 0 || dims[0] != kMlpIn || dims[1] != kMlpH || dims[2] != kMlpOut)
+        throw std::runtime_error("not a gba MLP model: " + path);
+    std::vector<float> h(kMlpParams);
+    f.read(reinterpret_cast<char*>(h.data()), sizeof(float) * kMlpParams);
+    if (!f) throw std::runtime_error("truncated model " + path);
+    return h;
+}
 
 }  // namespace
 
@@ -351,6 +374,13 @@ void Mlp::alloc() {
 void Mlp::ensure_capacity(int B) {
     if (B <= cap_ && h1_) return;
     cap_ = std::max(B, std::max(cap_, 1));
+    if (inference_) {  // forward activations only
+        for (float* q : {h1_, h2_})
+            if (q) GBA_CUDA_CHECK(cudaFreeAsync(q, pool_stream_));
+        h1_ = palloc<float>(1ll * cap_ * kMlpH, pool_stream_);
+        h2_ = palloc<float>(1ll * cap_ * kMlpH, pool_stream_);
+        return;
+    }
     for (void* q : {static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(o_), static_cast<void*>(do_),
                     static_cast<void*>(dh2_), static_cast<void*>(dh1_), static_cast<void*>(loss_)})
         if (q) cudaFree(q);
@@ -376,22 +406,30 @@ Mlp::Mlp(int capacity, uint64_t seed) : cap_(capacity) {
 }
 
 Mlp::Mlp(const std::string& path, int capacity) : cap_(capacity) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) throw std::runtime_error("cannot open model " + path);
-    char magic[8];
-    int32_t dims[3];
-    f.read(magic, 8);
-    f.read(reinterpret_cast<char*>(dims), sizeof dims);
-    if (!f || std::memcmp(magic, kMagic, 8) != 0 || dims[0] != kMlpIn || dims[1] != kMlpH || dims[2] != kMlpOut)
-        throw std::runtime_error("not a gba MLP model: " + path);
-    std::vector<float> h(kMlpParams);
-    f.read(reinterpret_cast<char*>(h.data()), sizeof(float) * kMlpParams);
-    if (!f) throw std::runtime_error("truncated model " + path);
+    const std::vector<float> h = read_model(path);
     alloc();
     set_params(h.data());
 }
 
+Mlp::Mlp(const std::string& path, cudaStream_t stream)
+    : pool_stream_(stream), inference_(true), host_params_(read_model(path)) {
+    p_ = palloc<float>(kMlpParams, stream);
+    wb_ = palloc<__nv_bfloat16>(kBf16Count, stream);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(p_, host_params_.data(), sizeof(float) * kMlpParams, cudaMemcpyHostToDevice,
+                                   stream));
+    refresh_bf16(stream);
+}
+
+void Mlp::require_training() const {
+    if (inference_) throw std::logic_error("this MLP was loaded for inference only");
+}
+
 Mlp::~Mlp() {
+    if (inference_) {
+        for (void* q : {static_cast<void*>(p_), wb_, static_cast<void*>(h1_), static_cast<void*>(h2_)})
+            if (q) cudaFreeAsync(q, pool_stream_);
+        return;
+    }
     for (void* q : {static_cast<void*>(p_), static_cast<void*>(g_), static_cast<void*>(m_), static_cast<void*>(v_), wb_,
                     static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(o_), static_cast<void*>(do_),
                     static_cast<void*>(dh2_), static_cast<void*>(dh1_), static_cast<void*>(loss_)})
@@ -421,6 +459,7 @@ void Mlp::set_params(const float* host) {
 }
 
 void Mlp::grads(float* host) const {
+    require_training();
     GBA_CUDA_CHECK(cudaDeviceSynchronize());
     GBA_CUDA_CHECK(cudaMemcpy(host, g_, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
 }
@@ -449,6 +488,7 @@ void Mlp::forward(const float* feat, int B, float* out, cudaStream_t s) {
 
 double Mlp::loss_grad(const float* feat, const double* Shat, const double* Lhat, const double* g, const double* x,
                       int B, cudaStream_t s, double* baseline_loss) {
+    require_training();
     if (B <= 0) throw std::invalid_argument("empty batch");
     ensure_capacity(B);
     forward(feat, B, o_, s);
@@ -481,6 +521,7 @@ double Mlp::loss_grad(const float* feat, const double* Shat, const double* Lhat,
 }
 
 void Mlp::adam_step(float lr, float beta1, float beta2, float eps, cudaStream_t s) {
+    require_training();
     ++step_;
     const float c1 = 1.f - std::pow(beta1, static_cast<float>(step_));
     const float c2 = 1.f - std::pow(beta2, static_cast<float>(step_));
@@ -493,6 +534,7 @@ void Mlp::adam_step(float lr, float beta1, float beta2, float eps, cudaStream_t 
 
 void mlp_features(Solver& s, double lambda, float* feat) {
     if (!s.mlp_stats_.get()) {
+        StreamAllocScope scope(s.stream_);
         s.mlp_stats_.alloc(3ull * s.C_);
         camera_stats_kernel<<<s.C_, 256, 0, s.stream_>>>(s.cam_off_.get(), s.cam_slots_.get(), s.s_pt_.get(),
                                                           s.pt_off_.get(), s.C_, s.mlp_stats_.get());
@@ -503,19 +545,20 @@ void mlp_features(Solver& s, double lambda, float* feat) {
     GBA_LAUNCH_CHECK();
 }
 
-LearnedPreconditioner::LearnedPreconditioner(const std::string& path) : mlp_(path, 1) {}
+LearnedPreconditioner::LearnedPreconditioner(const std::string& path, cudaStream_t stream)
+    : mlp_(path, stream), stream_(stream) {}
 
 LearnedPreconditioner::~LearnedPreconditioner() {
-    if (feat_) cudaFree(feat_);
-    if (out_) cudaFree(out_);
+    if (feat_) cudaFreeAsync(feat_, stream_);
+    if (out_) cudaFreeAsync(out_, stream_);
 }
 
 void LearnedPreconditioner::correct_factors(Solver& s, double lambda) {
     if (cap_ < s.C_) {
-        if (feat_) cudaFree(feat_);
-        if (out_) cudaFree(out_);
-        feat_ = dalloc<float>(64ll * s.C_);
-        out_ = dalloc<float>(1ll * kMlpOut * s.C_);
+        if (feat_) GBA_CUDA_CHECK(cudaFreeAsync(feat_, stream_));
+        if (out_) GBA_CUDA_CHECK(cudaFreeAsync(out_, stream_));
+        feat_ = palloc<float>(64ll * s.C_, stream_);
+        out_ = palloc<float>(1ll * kMlpOut * s.C_, stream_);
         cap_ = s.C_;
     }
     mlp_features(s, lambda, feat_);
@@ -535,7 +578,7 @@ Solver::~Solver() {
 void Solver::load_model(const std::string& path) {
     if (form_ == SolverForm::Plain) throw std::invalid_argument("the learned preconditioner needs a mixed form");
     if (path.empty()) throw std::invalid_argument("learned form: empty model path");
-    auto* m = new LearnedPreconditioner(path);
+    auto* m = new LearnedPreconditioner(path, stream_);
     delete model_;
     model_ = m;
 }

@@ -44,6 +44,11 @@ class Mlp {
 public:
     Mlp(int capacity, uint64_t seed);               // random init, zero last layer
     Mlp(const std::string& path, int capacity);     // load a saved model
+    // Inference only (forward): a saved model whose parameters, BF16 weights
+    // and activations are allocated stream-ordered on `stream` (the device's
+    // memory pool: no driver allocation or device-wide synchronisation per
+    // solve) and uploaded on that stream; training calls throw.
+    Mlp(const std::string& path, cudaStream_t stream);
     ~Mlp();
     Mlp(const Mlp&) = delete;
     Mlp& operator=(const Mlp&) = delete;
@@ -70,7 +75,11 @@ public:
 private:
     void alloc();
     void refresh_bf16(cudaStream_t s);
+    void require_training() const;
     int cap_ = 0;
+    cudaStream_t pool_stream_ = nullptr;  // inference mode: allocations are stream-ordered on this stream
+    bool inference_ = false;
+    std::vector<float> host_params_;      // inference mode: the uploaded parameters (kept until the copy ends)
     long long step_ = 0;
     float* p_ = nullptr;   // FP32 masters (flat)
     float* g_ = nullptr;   // gradients (flat)
@@ -88,7 +97,8 @@ private:
 
 class LearnedPreconditioner {
 public:
-    explicit LearnedPreconditioner(const std::string& path);
+    // The model's buffers are allocated stream-ordered on the solver's stream.
+    LearnedPreconditioner(const std::string& path, cudaStream_t stream);
     ~LearnedPreconditioner();
     // Replaces the block-Jacobi factors in s.Pfac_ by the corrected factors
     // L_c F_c; S_cc (s.Sdiag_) and the factors must be current.
@@ -96,6 +106,7 @@ public:
 
 private:
     Mlp mlp_;
+    cudaStream_t stream_;
     float* feat_ = nullptr;
     float* out_ = nullptr;
     int cap_ = 0;
