@@ -268,7 +268,8 @@ public:
     }
     bool harvest_ = false;     // plain form: keep the damped diagonal blocks S_cc in Sdiag_
 
-    void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px);
+    void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px, const double* cams,
+                         const double* pts);
     void build_pairs();
     void sync() const;
 };

@@ -318,14 +318,17 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     cam_pre_.alloc(16ull * C);
     scal_.alloc(8);
     GBA_CUDA_CHECK(cudaMemsetAsync(counters_.get(), 0, 4 * sizeof(unsigned long long), stream_));
-    set_params(cams, pts);
     cams0_.alloc(9ull * C);
     pts0_.alloc(3ull * P);
+    resid_valid_ = false;
+    ff_holds_ = kFfNone;
+    // copies cams / pts to the device (after the observation indices) while it
+    // builds the structure; the stream has waited for them when this returns
+    build_structure(obs_cam, obs_pt, obs_px, cams, pts);
     GBA_CUDA_CHECK(cudaMemcpyAsync(cams0_.get(), cams_.get(), 9ull * C * sizeof(double), cudaMemcpyDeviceToDevice,
                                    stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(pts0_.get(), pts_.get(), 3ull * P * sizeof(double), cudaMemcpyDeviceToDevice,
                                    stream_));
-    build_structure(obs_cam, obs_pt, obs_px);
 
     // normal equations (both forms)
     U_.alloc(81ull * C);
@@ -415,13 +418,16 @@ void Solver::get_params(double* cams, double* pts) const {
     sync();
 }
 
-void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px) {
+void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px, const double* cams,
+                             const double* pts) {
     const int E = E_, P = P_, C = C_;
     DevBuf<int> d_oc(E), d_op(E), keys_sorted(E), iota(E);
     DevBuf<double> d_px(2ull * E);
-    // The pixels (16 B per observation, the bulk of the problem) cross on a
-    // side stream while the index check and the sort by point run; the main
-    // stream waits for them only before the gather that reads them.
+    // The observation indices cross first, alone on the link: the index check
+    // and the sort by point wait for them. The pixels (16 B per observation,
+    // the bulk of the problem) and the parameters follow on a side stream while
+    // the check and the sort run; the main stream waits for them only before
+    // the gather that reads the pixels.
     struct SideCopy {
         cudaStream_t s = nullptr;
         cudaEvent_t ready = nullptr, done = nullptr;
@@ -435,13 +441,15 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     GBA_CUDA_CHECK(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
     GBA_CUDA_CHECK(cudaEventCreateWithFlags(&side.ready, cudaEventDisableTiming));
     GBA_CUDA_CHECK(cudaEventCreateWithFlags(&side.done, cudaEventDisableTiming));
-    GBA_CUDA_CHECK(cudaEventRecord(side.ready, stream_));  // after d_px's stream-ordered allocation
+    GBA_CUDA_CHECK(cudaMemcpyAsync(d_oc.get(), obs_cam, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(d_op.get(), obs_pt, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    GBA_CUDA_CHECK(cudaEventRecord(side.ready, stream_));  // after the index copies and the stream-ordered allocations
     GBA_CUDA_CHECK(cudaStreamWaitEvent(side.s, side.ready, 0));
     GBA_CUDA_CHECK(
         cudaMemcpyAsync(d_px.get(), obs_px, 2ull * E * sizeof(double), cudaMemcpyHostToDevice, side.s));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cams_.get(), cams, 9ull * C * sizeof(double), cudaMemcpyHostToDevice, side.s));
+    GBA_CUDA_CHECK(cudaMemcpyAsync(pts_.get(), pts, 3ull * P * sizeof(double), cudaMemcpyHostToDevice, side.s));
     GBA_CUDA_CHECK(cudaEventRecord(side.done, side.s));
-    GBA_CUDA_CHECK(cudaMemcpyAsync(d_oc.get(), obs_cam, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
-    GBA_CUDA_CHECK(cudaMemcpyAsync(d_op.get(), obs_pt, E * sizeof(int), cudaMemcpyHostToDevice, stream_));
 
     order_.alloc(E);
     s_cam_.alloc(E);
