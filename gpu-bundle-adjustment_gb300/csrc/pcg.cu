@@ -88,15 +88,27 @@ __device__ __forceinline__ ff warp_total(ff v) {
 }
 
 // V'^-1 of a point (6 packed): FP32 copy, or FP32 copy + low parts.
+// A point's packed V'^-1 (6 floats, 24 B: 8-byte aligned) as three float2 loads.
 __device__ __forceinline__ void load_vinv(const float* __restrict__ hi, const float* __restrict__, long long p,
                                           float* v) {
+    const float2* h = reinterpret_cast<const float2*>(hi + 6 * p);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) v[k] = hi[6 * p + k];
+    for (int k = 0; k < 3; ++k) {
+        const float2 t = h[k];
+        v[2 * k] = t.x;
+        v[2 * k + 1] = t.y;
+    }
 }
 __device__ __forceinline__ void load_vinv(const float* __restrict__ hi, const float* __restrict__ lo, long long p,
                                           ff* v) {
+    const float2* h = reinterpret_cast<const float2*>(hi + 6 * p);
+    const float2* l = reinterpret_cast<const float2*>(lo + 6 * p);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) v[k] = {hi[6 * p + k], lo[6 * p + k]};
+    for (int k = 0; k < 3; ++k) {
+        const float2 a = h[k], b = l[k];
+        v[2 * k] = {a.x, b.x};
+        v[2 * k + 1] = {a.y, b.y};
+    }
 }
 
 // u_e: two values per slot (8 B in FP32, 16 B in float-float).
