@@ -266,8 +266,7 @@ __global__ void __launch_bounds__(kSumT) denom_finalize(const double* __restrict
 unsigned long long Solver::damp_invert_v(double lambda) {
     damp_launch(lambda);
     unsigned long long bad = 0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&bad, counters_.get() + 3, sizeof bad, cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{&bad, counters_.get() + 3, sizeof bad}});
     if (bad) add_nonspd(bad);
     return bad;
 }
@@ -275,8 +274,7 @@ unsigned long long Solver::damp_invert_v(double lambda) {
 // keep the cumulative non-SPD count (reference counters[1])
 void Solver::add_nonspd(unsigned long long n) {
     unsigned long long h[2];
-    GBA_CUDA_CHECK(cudaMemcpyAsync(h, counters_.get(), sizeof h, cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{h, counters_.get(), sizeof h}});
     h[1] += n;
     GBA_CUDA_CHECK(cudaMemcpyAsync(counters_.get(), h, sizeof h, cudaMemcpyHostToDevice, stream_));
     sync();
@@ -298,8 +296,7 @@ void Solver::damp_launch(double lambda) {
 double Solver::back_substitute(double lambda) {
     backsub_launch(lambda);
     double denom = 0.0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&denom, scal_.get() + 2, sizeof denom, cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{&denom, scal_.get() + 2, sizeof denom}});
     return denom;
 }
 

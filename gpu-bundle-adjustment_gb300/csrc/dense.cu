@@ -406,8 +406,7 @@ int Solver::schur_dense(double lambda) {
     dense_potrf(S_.get(), n_pad_, lda, info_.get(), stream_);
     prof_stop("dense_potrf", ev);
     int info = 0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&info, info_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{&info, info_.get(), sizeof info}});
     if (info != 0) return info;
     // solve in a copy so rhs stays the assembled right-hand side
     GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), rhs_.get(), n_pad_ * sizeof(double), cudaMemcpyDeviceToDevice,

@@ -750,8 +750,7 @@ double Solver::accumulate() {
                                                                  U_.get(), bc_.get());
     GBA_LAUNCH_CHECK();
     double sse = 0.0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&sse, scal_.get(), sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{&sse, scal_.get(), sizeof sse}});
     return sse;
 }
 
@@ -795,17 +794,14 @@ void Solver::prepare_ff(const double* cams, const double* pts) {
 double Solver::trial_cost() {
     trial_cost_launch(counters_.get());
     double sse = 0.0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&sse, scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{&sse, scal_.get() + 1, sizeof sse}});
     return sse;
 }
 
 void Solver::read_trial(double* denom, double* sse, unsigned long long* cost_anomalies) {
-    GBA_CUDA_CHECK(cudaMemcpyAsync(denom, scal_.get() + 2, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    GBA_CUDA_CHECK(cudaMemcpyAsync(sse, scal_.get() + 1, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    GBA_CUDA_CHECK(cudaMemcpyAsync(cost_anomalies, counters_.get() + 2, sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, stream_));
-    sync();
+    read_back({{denom, scal_.get() + 2, sizeof(double)},
+               {sse, scal_.get() + 1, sizeof(double)},
+               {cost_anomalies, counters_.get() + 2, sizeof(unsigned long long)}});
 }
 
 void Solver::zero_cost_scratch() {

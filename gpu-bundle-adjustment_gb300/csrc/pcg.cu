@@ -1115,13 +1115,11 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     if (learned && learned_choice_ == 1) model_->correct_factors(*this, lambda);
 
     double bnorm2 = 0.0;
-    GBA_CUDA_CHECK(cudaMemcpyAsync(&bnorm2, sc + S_NORM, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    if (nonspd_out)
-        GBA_CUDA_CHECK(cudaMemcpyAsync(nonspd_out, counters_.get() + 3, sizeof(unsigned long long),
-                                       cudaMemcpyDeviceToHost, stream_));
+    unsigned long long nonspd = 0;
     GBA_CUDA_CHECK(cudaMemsetAsync(dc_.get(), 0, n * sizeof(double), stream_));
     GBA_CUDA_CHECK(cudaMemcpyAsync(ref_r_.get(), rhs_.get(), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
-    sync();
+    read_back({{&bnorm2, sc + S_NORM, sizeof bnorm2}, {&nonspd, counters_.get() + 3, sizeof nonspd}});
+    if (nonspd_out) *nonspd_out = nonspd;
     if (nonspd_out && *nonspd_out) {  // a non-SPD damped point block: the trial is rejected
         st.rel_residual = NAN;
         return st;
@@ -1161,10 +1159,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         // point pass), so overshooting costs more than one extra check.
         int batch = std::max(1, std::min(prev_inner_ - 1, std::min(kCheck, opts.pcg_max_iters)));
         double h[9];
-        if (opts.pcg_max_iters <= 0) {  // no iteration: the state pcg_init_finalize left
-            GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
-            sync();
-        }
+        if (opts.pcg_max_iters <= 0) read_back({{h, sc, sizeof h}});  // the state pcg_init_finalize left
         for (int it = 0, next = 1; it < opts.pcg_max_iters; it += batch, batch = std::min(next, kCheck), next *= 2) {
             for (int j = 0; j < batch; ++j) {
                 implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
@@ -1178,8 +1173,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                                                         nub, opts.pcg_max_iters, sc);
                 GBA_LAUNCH_CHECK();
             }
-            GBA_CUDA_CHECK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, stream_));
-            sync();
+            read_back({{h, sc, sizeof h}});
             if (h[S_DONE] != 0.0) break;
         }
         *ok = h[S_DONE] != 2.0 && h[S_RR] <= h[S_TOL2] * h[S_BB];
@@ -1267,8 +1261,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         GBA_LAUNCH_CHECK();
         sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
         GBA_LAUNCH_CHECK();
-        GBA_CUDA_CHECK(cudaMemcpyAsync(&rnorm2, sc + S_NORM, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-        sync();
+        read_back({{&rnorm2, sc + S_NORM, sizeof rnorm2}});
         st.pcg_iterations += static_cast<long long>(iters);
         ++st.refine_steps;
         if (!std::isfinite(rnorm2)) break;

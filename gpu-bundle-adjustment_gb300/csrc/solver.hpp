@@ -18,6 +18,8 @@
 
 #include <cuda_runtime.h>
 
+#include <initializer_list>
+
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -272,6 +274,16 @@ public:
                          const double* pts);
     void build_pairs();
     void sync() const;
+    // Device -> host readback of a few scalars: each (dst, src, bytes) is
+    // queued as an asynchronous copy into a pinned staging buffer, one sync()
+    // completes them all, then they are copied to dst (host memory, pageable
+    // is fine). At most 4 KiB in total.
+    struct HostRead {
+        void* dst;
+        const void* src;
+        size_t bytes;
+    };
+    void read_back(std::initializer_list<HostRead> reads) const;
 };
 
 // Host-side checks of a BAL problem (sizes, null arrays, index ranges); throws

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <climits>
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -383,6 +384,36 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         pcg_s_.alloc(16);
     }
     sync();
+}
+
+namespace {
+// Pinned staging for scalar readbacks, one per host thread (a thread's solver
+// calls never overlap); allocated on first use and kept for the thread.
+constexpr size_t kPinnedBytes = 4096;
+struct PinnedScratch {
+    void* p = nullptr;
+    ~PinnedScratch() {
+        if (p) cudaFreeHost(p);
+    }
+};
+thread_local PinnedScratch t_pinned;
+}  // namespace
+
+void Solver::read_back(std::initializer_list<HostRead> reads) const {
+    if (!t_pinned.p) GBA_CUDA_CHECK(cudaMallocHost(&t_pinned.p, kPinnedBytes));
+    char* stage = static_cast<char*>(t_pinned.p);
+    size_t off = 0;
+    for (const HostRead& r : reads) {
+        if (off + r.bytes > kPinnedBytes) throw std::logic_error("read_back: more than the staging buffer");
+        GBA_CUDA_CHECK(cudaMemcpyAsync(stage + off, r.src, r.bytes, cudaMemcpyDeviceToHost, stream_));
+        off += (r.bytes + 15) & ~size_t{15};
+    }
+    sync();
+    off = 0;
+    for (const HostRead& r : reads) {
+        std::memcpy(r.dst, stage + off, r.bytes);
+        off += (r.bytes + 15) & ~size_t{15};
+    }
 }
 
 // Waits for the solver stream by polling an event: the host resumes as soon as
