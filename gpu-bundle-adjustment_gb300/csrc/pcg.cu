@@ -597,15 +597,20 @@ __device__ __forceinline__ double chunk_sum(const int* __restrict__ cam_chunk_of
 }
 
 // rhs = bc - sum partials; partial ||rhs||^2 per block.
+// rhs = bc - (chunk partials of the right-hand side pass), also copied to the
+// refinement's reference residual ref_r; dc (the refined step) starts at zero.
 __global__ void __launch_bounds__(kVT) rhs_finalize(const int* __restrict__ cam_chunk_off,
                                                    const double* __restrict__ part, const double* __restrict__ bc,
-                                                   int C, double* __restrict__ rhs, double* __restrict__ red) {
+                                                   int C, double* __restrict__ rhs, double* __restrict__ ref_r,
+                                                   double* __restrict__ dc, double* __restrict__ red) {
     __shared__ double sh[kVT / 32];
     const int i = blockIdx.x * kVT + threadIdx.x;
     double v = 0.0;
     if (i < 9 * C) {
         v = bc[i] - chunk_sum(cam_chunk_off, part, i / 9, i % 9, 54);  // the right-hand side pass writes 54 per chunk
         rhs[i] = v;
+        ref_r[i] = v;
+        dc[i] = 0.0;
     }
     const double t = block_sum<kVT>(v * v, sh);
     if (threadIdx.x == 0) red[blockIdx.x] = t;
@@ -1094,7 +1099,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     } else {
         implicit_parts<ff>(*this, static_cast<const ff*>(nullptr), 1.0, nullptr);
     }
-    rhs_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), bc_.get(), C_, rhs_.get(), red);
+    rhs_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), bc_.get(), C_, rhs_.get(),
+                                           ref_r_.get(), dc_.get(), red);
     GBA_LAUNCH_CHECK();
     sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
     GBA_LAUNCH_CHECK();
@@ -1116,8 +1122,6 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
 
     double bnorm2 = 0.0;
     unsigned long long nonspd = 0;
-    GBA_CUDA_CHECK(cudaMemsetAsync(dc_.get(), 0, n * sizeof(double), stream_));
-    GBA_CUDA_CHECK(cudaMemcpyAsync(ref_r_.get(), rhs_.get(), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
     read_back({{&bnorm2, sc + S_NORM, sizeof bnorm2}, {&nonspd, counters_.get() + 3, sizeof nonspd}});
     if (nonspd_out) *nonspd_out = nonspd;
     if (nonspd_out && *nonspd_out) {  // a non-SPD damped point block: the trial is rejected
