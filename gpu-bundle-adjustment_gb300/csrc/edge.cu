@@ -445,6 +445,10 @@ constexpr int kCamPre = 16;
 // cams32 (may be null): the FP32 Jacobian pass's per-camera record
 // (model::camera_constants, 28 floats: R, J_l, t, f, k1, k2, branch flag),
 // computed in FP64 and rounded.
+// One camera per thread in warp-sized blocks: the FP64 trigonometry of C
+// cameras spreads over all SMs' FP64 pipes (blocks of 128 used C / 128 SMs).
+constexpr int kPreT = 32;
+
 __global__ void camera_precompute_kernel(const double* __restrict__ cams, int C, double* __restrict__ pre,
                                          float2* __restrict__ preff, float* __restrict__ cams32) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -781,7 +785,7 @@ void Solver::cost_mixed(const double* cams, const double* pts, unsigned long lon
 // Float-float camera constants, FP32 cameras and float-float points of
 // (cams, pts), for the cost pass and the FP32 Jacobian pass.
 void Solver::prepare_ff(const double* cams, const double* pts) {
-    camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(
+    camera_precompute_kernel<<<ceil_div(C_, kPreT), kPreT, 0, stream_>>>(
         cams, C_, cam_pre_.get(), reinterpret_cast<float2*>(cam_pre_ff_.get()), cams32_.get());
     GBA_LAUNCH_CHECK();
     if (!(pts == tpts_.get() && pts_ff_trial_)) launch_split_ff(pts, 3ll * P_, pts_ff_.get(), stream_);
@@ -818,7 +822,7 @@ void Solver::trial_cost_launch(unsigned long long* anomalies) {
     if (form_ == SolverForm::Plain) {
         const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
         cudaEvent_t ev = prof_start();
-        camera_precompute_kernel<<<ceil_div(C_, 128), 128, 0, stream_>>>(tcams_.get(), C_, cam_pre_.get(), nullptr,
+        camera_precompute_kernel<<<ceil_div(C_, kPreT), kPreT, 0, stream_>>>(tcams_.get(), C_, cam_pre_.get(), nullptr,
                                                                          nullptr);
         GBA_LAUNCH_CHECK();
         cost_f64<<<n_pchunk_, kPT, 0, stream_>>>(pchunk_.get(), pt_off_.get(), s_cam_.get(), s_pt_.get(), spx,

@@ -285,6 +285,11 @@ __global__ void camera_stats_kernel(const int* __restrict__ cam_off, const int* 
     }
 }
 
+// Per-camera FP64 kernels (features, factor correction): one camera per
+// thread in warp-sized blocks, so that C cameras spread over all SMs' FP64
+// pipes.
+constexpr int kCamT = 32;
+
 __global__ void features_kernel(const double* __restrict__ Sdiag, const double* __restrict__ U,
                                 const float* __restrict__ stats, double lambda, int C, float* __restrict__ feat) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -540,7 +545,7 @@ void mlp_features(Solver& s, double lambda, float* feat) {
                                                           s.pt_off_.get(), s.C_, s.mlp_stats_.get());
         GBA_LAUNCH_CHECK();
     }
-    features_kernel<<<ceil_div(s.C_, 128), 128, 0, s.stream_>>>(s.Sdiag_.get(), s.U_.get(), s.mlp_stats_.get(),
+    features_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(s.Sdiag_.get(), s.U_.get(), s.mlp_stats_.get(),
                                                                  lambda, s.C_, feat);
     GBA_LAUNCH_CHECK();
 }
@@ -565,7 +570,7 @@ void LearnedPreconditioner::correct_factors(Solver& s, double lambda) {
     cudaEvent_t ev = s.prof_start();
     mlp_.forward(feat_, s.C_, out_, s.stream_);
     s.prof_stop("mlp_forward", ev);
-    correct_kernel<<<ceil_div(s.C_, 128), 128, 0, s.stream_>>>(out_, s.C_, s.Pfac_.get());
+    correct_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(out_, s.C_, s.Pfac_.get());
     GBA_LAUNCH_CHECK();
 }
 
