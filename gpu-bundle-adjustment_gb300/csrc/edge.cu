@@ -704,6 +704,14 @@ __global__ void eval_edges_kernel(const double* __restrict__ cams, const double*
 }  // namespace
 
 double Solver::accumulate() {
+    accumulate_launch();
+    double sse = 0.0;
+    read_back({{&sse, scal_.get(), sizeof sse}});
+    return sse;
+}
+
+// The normal-equation passes without the host read of the SSE (scal_[0]).
+void Solver::accumulate_launch() {
     const double2* spx = reinterpret_cast<const double2*>(s_px_.get());
     if (form_ == SolverForm::Plain) {
         cudaEvent_t ev = prof_start();
@@ -753,9 +761,6 @@ double Solver::accumulate() {
     camera_finalize<<<ceil_div(54ll * C_, 256), 256, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), C_,
                                                                  U_.get(), bc_.get());
     GBA_LAUNCH_CHECK();
-    double sse = 0.0;
-    read_back({{&sse, scal_.get(), sizeof sse}});
-    return sse;
 }
 
 // Mixed-form cost at (cams, pts): camera constants and points split to

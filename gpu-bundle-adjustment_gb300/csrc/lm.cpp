@@ -206,7 +206,13 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
             at_target = true;
             break;
         }
-        phase(res.t_accumulate, [&] { return s.accumulate(); });
+        // the new normal equations; the mixed forms already hold the SSE (the
+        // accepted trial's), so nothing is read back here
+        if (plain) {
+            phase(res.t_accumulate, [&] { return s.accumulate(); });
+        } else {
+            phase(res.t_accumulate, [&] { s.accumulate_launch(); return 0; });
+        }
     }
 
     res.final_cost = sse / 2.0;

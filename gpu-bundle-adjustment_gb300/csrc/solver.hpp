@@ -129,6 +129,7 @@ public:
     // Jacobians with FP64 accumulation (mixed). Returns the SSE; adds non-finite
     // edges to the anomaly counter.
     double accumulate();
+    void accumulate_launch();  // the same passes, SSE left in scal_[0] (no host read)
     // V' = V + lambda * max(diag V, 1e-12), inverted per point. Returns the number
     // of non-SPD blocks found by this call.
     unsigned long long damp_invert_v(double lambda);

@@ -86,3 +86,19 @@ def test_ragged_mixed_reaches_oracle_cost(gba, oracle, form):
     assert res.final_cost <= ref["final_cost"] * (1 + 1e-3)
     assert np.array_equal(run.cameras[-9:], prob.cameras[-9:])
     assert np.array_equal(run.points[-3:], prob.points[-3:])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_non_spd_point_blocks_reject_every_trial(gba, form):
+    """A negative damping makes every damped point block non-SPD: each trial is
+    rejected before its step is taken (reference semantics: a non-SPD V block
+    rejects the trial), lambda stays negative, and after max_inner_trials
+    rejections the solve ends in FAILURE at the initial cost."""
+    prob = gba.synthetic_custom(6, 300, 2, 5, 1.4, seed=31)
+    run = prob.copy()
+    res = gba.solve(run, form=form, initial_lambda=-1.5, max_inner_trials=3, max_iterations=2)
+    assert res.termination == "FAILURE"
+    assert res.iterations == 0 and res.trials == 3
+    assert res.final_cost == res.initial_cost
+    assert np.array_equal(run.cameras, prob.cameras) and np.array_equal(run.points, prob.points)
