@@ -117,7 +117,7 @@ __global__ void gather_obs_kernel(const int* __restrict__ order, const int* __re
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
         const int e = order[s];
         s_cam[s] = oc[e];
-        s_px[s] = make_double2(px[2 * e], px[2 * e + 1]);
+        s_px[s] = make_double2(px[2ll * e], px[2ll * e + 1]);
     }
 }
 
@@ -303,6 +303,10 @@ void validate_problem(int C, int P, int E, const double* cams, const double* pts
     if (C <= 0 || P <= 0 || E <= 0) throw std::invalid_argument("empty BAL problem");
     if (!cams || !pts || !obs_cam || !obs_pt || !obs_px) throw std::invalid_argument("null problem array");
     if (static_cast<long long>(C) * 9 > INT_MAX / 2) throw std::invalid_argument("too many cameras");
+    // 32-bit per-point and per-observation index arithmetic stays in range
+    // (both limits lie beyond what one GPU's memory holds)
+    if (static_cast<long long>(P) * 6 > INT_MAX) throw std::invalid_argument("too many points");
+    if (static_cast<long long>(E) * 2 > INT_MAX) throw std::invalid_argument("too many observations");
 }
 
 Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const int* obs_cam,

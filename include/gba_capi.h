@@ -88,7 +88,10 @@ void gba_lm_options_default(gba_lm_options* opts);
 
 /* LM solve of a BAL problem held in host arrays (BAL layout); cameras and
  * points are updated in place. Replaces gba::solve_bal_gpu
- * (reference include/gba/lm.hpp:34, src/lm.cu:371-724). [host] all arrays. */
+ * (reference include/gba/lm.hpp:34, src/lm.cu:371-724). [host] all arrays.
+ * Sizes (also gba_solver_create): at least one camera, point and observation;
+ * 9 C <= INT_MAX / 2, 6 P <= INT_MAX, 2 E <= INT_MAX; otherwise status 1
+ * before any array is read. Observation indices out of range: status 1. */
 int gba_solve_bal(int num_cameras, int num_points, int num_observations, double* cameras, double* points,
                   const int* obs_camera, const int* obs_point, const double* obs_pixel,
                   const gba_lm_options* opts, gba_lm_result* result);

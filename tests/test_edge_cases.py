@@ -102,3 +102,19 @@ def test_non_spd_point_blocks_reject_every_trial(gba, form):
     assert res.iterations == 0 and res.trials == 3
     assert res.final_cost == res.initial_cost
     assert np.array_equal(run.cameras, prob.cameras) and np.array_equal(run.points, prob.points)
+
+
+def test_oversized_problem_is_rejected(gba):
+    """Sizes past the solver's 32-bit index range are refused up front (status 1),
+    before any array is read or any device work starts: the arrays here are
+    tiny, only the counts are large."""
+    lib = gba.lib
+    import ctypes as C
+    one = np.zeros(9)
+    idx = np.zeros(1, np.int32)
+    for c, p, e in ((1, 400_000_000, 1), (1, 1, 1_100_000_000)):
+        rc = lib.gba_solver_create(c, p, e, one.ctypes.data_as(C.POINTER(C.c_double)),
+                                   one.ctypes.data_as(C.POINTER(C.c_double)), idx.ctypes.data_as(C.POINTER(C.c_int)),
+                                   idx.ctypes.data_as(C.POINTER(C.c_int)), one.ctypes.data_as(C.POINTER(C.c_double)),
+                                   0, None, C.byref(C.c_void_p()))
+        assert rc == 1, rc
