@@ -288,8 +288,8 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
     // instead of six strided loads per owner, no registers held), waited for
     // before the first barrier that precedes its use (233 instead of 269 us per
     // matvec on 8.8M observations). Float-float, and the back-substitution
-    // (whose larger shared footprint would shrink L1 under its strided row
-    // loads): the owners load it.
+    // (where the copy measured slower: 329-364 against 306 us): the owners
+    // load it.
     constexpr bool kSharedVinv = sizeof(T) == 4 && !kBack;
     T vinv[6];
     if constexpr (kSharedVinv) {
