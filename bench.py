@@ -93,7 +93,8 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
     PERIOD_MS = 100
 
-    def __init__(self):
+    def __init__(self, devices=("0",)):
+        self.devices = ",".join(devices)  # nvidia-smi -i: physical indices or UUIDs, one line per GPU and interval
         self.samples = []  # (datetime, [sm, max, 4 reasons])
         self.window = None
         self._p = None
@@ -101,9 +102,8 @@ class ClockSampler:
         self._t0 = None
 
     def start(self):
-        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
         try:
-            self._p = subprocess.Popen(["nvidia-smi", "-i", dev, f"--query-gpu={self.QUERY}",
+            self._p = subprocess.Popen(["nvidia-smi", "-i", self.devices, f"--query-gpu={self.QUERY}",
                                         "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                        stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
@@ -158,6 +158,14 @@ class ClockSampler:
         reasons = sorted({names[i] for s in picked for i in range(4) if s[2 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples_in_window": n_in, "samples_used": len(picked)}
+
+
+def smi_devices(world: int, count: int):
+    """nvidia-smi identifiers of the GPUs ranks 0..world-1 use on this node
+    (rank r on visible device r mod count)."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    ids = [v.strip() for v in vis.split(",")] if vis else [str(i) for i in range(max(count, 1))]
+    return [ids[r % len(ids)] for r in range(max(world, 1))]
 
 
 def _dist_env():
@@ -228,7 +236,10 @@ def run_ours(args):
     if world > 1 and not torch.distributed.is_initialized():
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", dev))
 
-    clocks = ClockSampler().start()  # long before the timed region (see ClockSampler)
+    # rank 0 samples every GPU of the run, long before the timed region (see ClockSampler)
+    clocks = ClockSampler(smi_devices(world, torch.cuda.device_count())) if rank == 0 else ClockSampler(())
+    if rank == 0:
+        clocks.start()
     prob = gba.synthetic(args.workload, args.seed)
     C, P, E = prob.num_cameras, prob.num_points, prob.num_observations
     ref = reference_cost(args.workload, args.seed)

@@ -83,3 +83,16 @@ def test_clock_summary_keeps_the_timed_window():
 
     s.window = None
     assert s.summary()["reasons"] == ["unsampled"]
+
+
+def test_clock_sampler_devices_follow_the_ranks(monkeypatch):
+    """Rank r runs on visible device r mod count; nvidia-smi gets the physical
+    identifiers (CUDA_VISIBLE_DEVICES entries when set)."""
+    bench = _load_bench()
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES", raising=False)
+    assert bench.smi_devices(1, 8) == ["0"]
+    assert bench.smi_devices(4, 8) == ["0", "1", "2", "3"]
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "3, 5")
+    assert bench.smi_devices(2, 2) == ["3", "5"]
+    assert bench.smi_devices(1, 2) == ["3"]
+    assert bench.ClockSampler(["3", "5"]).devices == "3,5"
