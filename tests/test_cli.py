@@ -55,9 +55,13 @@ def test_json_schema_and_file_output(tmp_path):
     assert printed["trajectory"][0] == printed["initial_cost"]
 
 
+MODEL = ROOT / "gpu-bundle-adjustment_gb300" / "models" / "bj_mlp.bin"
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("extra", [["--form=mixed"], ["--form=mixed", "--refine-tol=0.1", "--pcg-tol=0.1"],
-                                   ["--loss=huber", "--delta=2"], ["--form=mixed", "--loss=huber", "--delta=2"]])
+                                   ["--loss=huber", "--delta=2"], ["--form=mixed", "--loss=huber", "--delta=2"],
+                                   ["--form=learned", f"--model={MODEL}"]])
 def test_forms_and_loss(extra):
     r = _run(TINY, "--iterations=10", *extra)
     assert r.returncode == 0, r.stderr

@@ -149,6 +149,20 @@ def test_trained_model_beats_block_jacobi_held_out():
 
 
 @pytest.mark.skipif(not MODEL.exists(), reason="trained model not present")
+@pytest.mark.skipif(not MODEL.exists(), reason="trained model not present")
+def test_learned_huber_reaches_oracle_cost_workload1(gba, oracle):
+    """Huber loss through the learned form (judged preconditioner on the robust
+    system): final robust cost within 0.1% of the oracle's."""
+    prob = gba.synthetic(1)
+    ref, _, _ = oracle.solve(prob, max_iterations=15, huber_delta=1.0)
+    res = gba.solve(prob.copy(), max_iterations=15, form="learned", model_path=str(MODEL), loss="huber",
+                    huber_delta=1.0)
+    assert abs(res.initial_cost - ref["initial_cost"]) <= 1e-9 * ref["initial_cost"]
+    assert res.anomalies == 0
+    assert res.final_cost <= ref["final_cost"] * (1 + 1e-3)
+    assert res.learned_choice in (1, 2)
+
+
 def test_learned_lm_reaches_oracle_cost_and_reports_gain(gba, oracle):
     """Workload-1 solve with the learned preconditioner: same accuracy bar as
     the mixed form (0.1% of the FP64 oracle), and the PCG work of both forms."""
