@@ -108,6 +108,7 @@ void fill_result(const gba::LMResult& r, gba_lm_result* out) {
     out->learned_choice = r.learned_choice;
     out->judge_iters_block_jacobi = r.judge_iters_block_jacobi;
     out->judge_iters_learned = r.judge_iters_learned;
+    out->max_refine_residual = r.max_refine_residual;
     out->trajectory_len = static_cast<int>(r.trajectory.size());
     const int n = std::min<int>(out->trajectory_len, std::max(0, out->trajectory_capacity));
     for (int i = 0; i < n; ++i) {

@@ -81,6 +81,8 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
                 }
                 res.pcg_iterations += st.pcg_iterations;
                 res.refine_steps += st.refine_steps;
+                if (std::isfinite(st.rel_residual))
+                    res.max_refine_residual = std::max(res.max_refine_residual, st.rel_residual);
                 if (!std::isfinite(st.rel_residual)) {
                     lambda *= nu;
                     nu *= 2.0;
@@ -152,6 +154,8 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
                 const PcgStats st = phase(res.t_schur, [&] { return s.schur_pcg(lambda, opts, learned); });
                 res.pcg_iterations += st.pcg_iterations;
                 res.refine_steps += st.refine_steps;
+                if (std::isfinite(st.rel_residual))
+                    res.max_refine_residual = std::max(res.max_refine_residual, st.rel_residual);
                 if (!std::isfinite(st.rel_residual)) {
                     lambda *= nu;
                     nu *= 2.0;

@@ -84,6 +84,7 @@ class LMResultC(C.Structure):
         ("learned_choice", C.c_int),
         ("judge_iters_block_jacobi", C.c_longlong),
         ("judge_iters_learned", C.c_longlong),
+        ("max_refine_residual", C.c_double),
     ]
 
 
@@ -313,6 +314,7 @@ class LMResult:
     trajectory_time_s: list = field(default_factory=list)
     learned_choice: int = 0  # learned form: 1 learned, 2 block-Jacobi won the judged first inner solve
     judge_iters: tuple = (0, 0)  # that solve's inner PCG iterations: (block-Jacobi, learned)
+    max_refine_residual: float = 0.0  # mixed forms: largest relative residual of a refined Schur step
 
 
 def _result_struct(cap: int):
@@ -332,7 +334,7 @@ def _to_result(r, traj, ttime, cap) -> "LMResult":
         dict(setup=r.t_setup, accumulate=r.t_accumulate, damp=r.t_damp, schur=r.t_schur, backsub=r.t_backsub,
              cost=r.t_cost),
         traj[:n].tolist(), ttime[:n].tolist(), r.learned_choice,
-        (r.judge_iters_block_jacobi, r.judge_iters_learned),
+        (r.judge_iters_block_jacobi, r.judge_iters_learned), r.max_refine_residual,
     )
 
 

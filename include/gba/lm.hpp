@@ -71,6 +71,10 @@ struct LMResult {
     int trials = 0;                        // inner trials evaluated (accepted + rejected)
     long long pcg_iterations = 0;          // mixed: total inner PCG iterations
     int refine_steps = 0;                  // mixed: total FP64 refinement steps
+    // mixed: largest relative residual ||rhs - S dc|| / ||rhs|| of a refined
+    // Schur step over the solve's trials (float-float residual of the system
+    // the refinement solves), 0 for the plain form
+    double max_refine_residual = 0.0;
     double time_to_target_s = -1.0;        // first time cost <= LMOptions::target_cost, or -1
     // Learned form: which preconditioner won the judged first inner solve
     // (1 = learned, 2 = block-Jacobi, 0 = not judged) and its inner PCG

@@ -82,6 +82,7 @@ typedef struct gba_lm_result {
     int learned_choice;              /* learned form: 1 learned, 2 block-Jacobi won the judged solve */
     long long judge_iters_block_jacobi;
     long long judge_iters_learned;
+    double max_refine_residual;      /* mixed forms: largest relative residual of a refined Schur step */
 } gba_lm_result;
 
 void gba_lm_options_default(gba_lm_options* opts);

@@ -1,7 +1,10 @@
 """ORACLE (test infrastructure only): ctypes access to the CPU restatement of
-the reference LM (liboracle.so) and to the reference's own compiled BAL reader
-(_ref/libgba_ref_reader.so, present only where the reference checkout was
-available at build time). Only tests/, __graft_entry__.smoke() and bench.py's
+the reference LM (liboracle.so), to the reference's own compiled BAL reader
+(_ref/libgba_ref_reader.so) and to the reference's own LM driver run on the
+CPU (_ref/libgba_ref_lm_host.so: src/lm.cu compiled unmodified against the
+Eigen stand-in, its kernels executed by the CPU stand-in for the CUDA
+runtime). The _ref libraries exist only where the reference checkout was
+available at build time. Only tests/, __graft_entry__.smoke() and bench.py's
 CPU-baseline leg use this module, as the checker.
 """
 from __future__ import annotations
@@ -11,7 +14,7 @@ from pathlib import Path
 
 import numpy as np
 
-from build_oracle import ORACLE_SO, REF_SO, build_oracle, build_reference_reader
+from build_oracle import ORACLE_SO, REF_SO, build_oracle, build_reference_lm, build_reference_reader
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -159,3 +162,64 @@ class ReferenceReader:
                 np.empty(2 * e.value))
         self.lib.ref_load_bal(str(path).encode(), _d(arrs[0]), _d(arrs[1]), _i(arrs[2]), _i(arrs[3]), _d(arrs[4]))
         return arrs
+
+
+class ReferenceLM:
+    """The reference's own LM driver, gba::solve_bal_gpu (src/lm.cu:371-724,
+    compiled unmodified), run on the CPU: its host code (S assembly, LLT,
+    back-substitution, gain ratio, damping, termination) is the reference's;
+    its three kernels run as CPU restatements inside the CUDA-runtime stand-in
+    (oracle/ref_host_runtime.cpp). The per-iteration cost trajectory is
+    recovered at full precision from the stand-in's launch log: an accepted
+    trial is a cost launch followed by a re-accumulation (edge launch)."""
+
+    EDGE, COST, DAMP = 1, 2, 3
+
+    def __init__(self):
+        path = build_reference_lm()
+        if path is None or not Path(path).exists():
+            raise FileNotFoundError("reference LM driver not built (reference checkout unavailable)")
+        self.lib = C.CDLL(str(path))
+        self.lib.gba_ref_solve_bal.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, C.c_int,
+                                               C.c_double, C.c_double, C.c_int, C.c_int, _dp, _dp, _ip, _ip,
+                                               C.POINTER(C.c_ulonglong), _dp, C.c_char_p, C.c_int]
+        self.lib.gba_ref_events.argtypes = [C.c_int, _ip, _dp, C.POINTER(C.c_ulonglong)]
+        self.lib.gba_ref_events.restype = C.c_int
+        self.lib.gba_ref_events_clear.argtypes = []
+
+    def _events(self):
+        n = self.lib.gba_ref_events(0, None, None, None)
+        kinds, sse, cnt = np.zeros(n, np.int32), np.zeros(n), np.zeros(n, np.uint64)
+        self.lib.gba_ref_events(n, _i(kinds), _d(sse), cnt.ctypes.data_as(C.POINTER(C.c_ulonglong)))
+        return kinds, sse, cnt
+
+    def solve(self, prob, max_iterations=50, initial_lambda=1e-3, rel_decrease_tol=1e-6, max_inner_trials=16):
+        """Full solve on copies of the parameters; returns (result dict, cams, pts)."""
+        C_, P_, E_ = _args(prob)
+        cams, pts = prob.cameras.copy(), prob.points.copy()
+        init, fin, tt = C.c_double(), C.c_double(), C.c_double()
+        it, term, an = C.c_int(), C.c_int(), C.c_ulonglong()
+        err = C.create_string_buffer(512)
+        self.lib.gba_ref_events_clear()
+        st = self.lib.gba_ref_solve_bal(C_, P_, E_, _d(cams), _d(pts), _i(prob.obs_camera), _i(prob.obs_point),
+                                        _d(prob.obs_pixel), max_iterations, initial_lambda, rel_decrease_tol,
+                                        max_inner_trials, 0, C.byref(init), C.byref(fin), C.byref(it),
+                                        C.byref(term), C.byref(an), C.byref(tt), err, len(err))
+        if st != 0:
+            raise RuntimeError("reference solve_bal_gpu threw: " + err.value.decode())
+        kinds, sse, _ = self._events()
+        traj = [init.value]
+        pending = None
+        for k, s in zip(kinds[1:], sse[1:]):
+            if k == self.COST:
+                pending = s / 2.0
+            elif k == self.EDGE and pending is not None:
+                traj.append(pending)
+                pending = None
+        if len(traj) == it.value:  # the last accepted step ended the solve without a re-accumulation
+            traj.append(fin.value)
+        res = dict(initial_cost=init.value, final_cost=fin.value, iterations=it.value,
+                   termination={0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE"}.get(term.value, "?"),
+                   anomalies=an.value, trajectory=traj, trials=int(np.sum(kinds == self.DAMP)),
+                   total_time_s=tt.value)
+        return res, cams, pts

@@ -53,3 +53,53 @@ def rel_err(a, b):
     b = np.asarray(b, np.float64)
     scale = max(np.max(np.abs(b)), 1e-300)
     return float(np.max(np.abs(a - b)) / scale)
+
+
+def implicit_system(s, prob, lam):
+    """rhs and x -> S x of the mixed form's system, in numpy FP64 from the device's
+    own FP32 Jacobian records and FP64 U, V, bc, bp (the system the refinement solves)."""
+    C, P = prob.num_cameras, prob.num_points
+    J = np.hstack([s.download("Jc32").reshape(-1, 18), s.download("Jp32").reshape(-1, 6)]).astype(np.float64)
+    order = s.download("order")
+    cam = prob.obs_camera[order]
+    pt = prob.obs_point[order]
+    Jc = J[:, :18].reshape(-1, 2, 9)
+    Jp = J[:, 18:].reshape(-1, 2, 3)
+    U = s.download("U").reshape(C, 9, 9)
+    Ud = np.diagonal(U, axis1=1, axis2=2)
+    Ul = U + lam * np.einsum("ci,ij->cij", np.where(Ud > 0, Ud, 1e-12), np.eye(9))
+    Vp = s.download("V").reshape(P, 6)
+    V = np.empty((P, 3, 3))
+    for k, (i, j) in enumerate([(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]):
+        V[:, i, j] = Vp[:, k]
+        V[:, j, i] = Vp[:, k]
+    for i in range(3):
+        d = V[:, i, i].copy()
+        V[:, i, i] += lam * np.where(d > 0, d, 1e-12)
+    Vinv = np.linalg.inv(V)
+    bc, bp = s.download("bc").reshape(C, 9), s.download("bp").reshape(P, 3)
+
+    def point_step(dc):  # dp = V'^-1 (bp - sum_e W_e^T dc)
+        t = np.einsum("sri,si->sr", Jc, dc.reshape(C, 9)[cam])
+        g = np.zeros((P, 3))
+        np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
+        return np.einsum("pij,pj->pi", Vinv, bp - g).ravel()
+
+    def back(g):  # g (P,3) -> sum over slots of Jc^T Jp Vinv g, per camera
+        w = np.einsum("pij,pj->pi", Vinv, g)
+        u = np.einsum("sij,sj->si", Jp, w[pt])
+        out = np.zeros((C, 9))
+        np.add.at(out, cam, np.einsum("sri,sr->si", Jc, u))
+        return out
+
+    rhs = (bc - back(bp)).ravel()
+
+    def matvec(x):
+        x = x.reshape(C, 9)
+        t = np.einsum("sri,si->sr", Jc, x[cam])
+        g = np.zeros((P, 3))
+        np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
+        return (np.einsum("cij,cj->ci", Ul, x) - back(g)).ravel()
+
+    matvec.point_step = point_step
+    return rhs, matvec

@@ -11,7 +11,7 @@ reader cost to 1e-9).
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import implicit_system, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -106,56 +106,6 @@ def test_mixed_huber_reaches_oracle_cost_workload1(gba, oracle):
     assert res.final_cost <= ref["final_cost"] * (1 + 1e-3)
 
 
-def _implicit_system(s, prob, lam):
-    """rhs and x -> S x of the mixed form's system, in numpy FP64 from the device's
-    own FP32 Jacobian records and FP64 U, V, bc, bp (the system the refinement solves)."""
-    C, P = prob.num_cameras, prob.num_points
-    J = np.hstack([s.download("Jc32").reshape(-1, 18), s.download("Jp32").reshape(-1, 6)]).astype(np.float64)
-    order = s.download("order")
-    cam = prob.obs_camera[order]
-    pt = prob.obs_point[order]
-    Jc = J[:, :18].reshape(-1, 2, 9)
-    Jp = J[:, 18:].reshape(-1, 2, 3)
-    U = s.download("U").reshape(C, 9, 9)
-    Ud = np.diagonal(U, axis1=1, axis2=2)
-    Ul = U + lam * np.einsum("ci,ij->cij", np.where(Ud > 0, Ud, 1e-12), np.eye(9))
-    Vp = s.download("V").reshape(P, 6)
-    V = np.empty((P, 3, 3))
-    for k, (i, j) in enumerate([(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]):
-        V[:, i, j] = Vp[:, k]
-        V[:, j, i] = Vp[:, k]
-    for i in range(3):
-        d = V[:, i, i].copy()
-        V[:, i, i] += lam * np.where(d > 0, d, 1e-12)
-    Vinv = np.linalg.inv(V)
-    bc, bp = s.download("bc").reshape(C, 9), s.download("bp").reshape(P, 3)
-
-    def point_step(dc):  # dp = V'^-1 (bp - sum_e W_e^T dc)
-        t = np.einsum("sri,si->sr", Jc, dc.reshape(C, 9)[cam])
-        g = np.zeros((P, 3))
-        np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
-        return np.einsum("pij,pj->pi", Vinv, bp - g).ravel()
-
-    def back(g):  # g (P,3) -> sum over slots of Jc^T Jp Vinv g, per camera
-        w = np.einsum("pij,pj->pi", Vinv, g)
-        u = np.einsum("sij,sj->si", Jp, w[pt])
-        out = np.zeros((C, 9))
-        np.add.at(out, cam, np.einsum("sri,sr->si", Jc, u))
-        return out
-
-    rhs = (bc - back(bp)).ravel()
-
-    def matvec(x):
-        x = x.reshape(C, 9)
-        t = np.einsum("sri,si->sr", Jc, x[cam])
-        g = np.zeros((P, 3))
-        np.add.at(g, pt, np.einsum("srj,sr->sj", Jp, t))
-        return (np.einsum("cij,cj->ci", Ul, x) - back(g)).ravel()
-
-    matvec.point_step = point_step
-    return rhs, matvec
-
-
 def test_loose_target_fast_path(gba, small):
     """refine_tol >= 1e-3: FP32 right-hand side, the converged inner solve as its
     own check, FP32 back-substitution. The true residual of the step meets the
@@ -168,7 +118,7 @@ def test_loose_target_fast_path(gba, small):
         dc = s.download("dc")
         s.back_substitute(lam)
         dp = s.download("dp")
-        rhs, matvec = _implicit_system(s, small, lam)
+        rhs, matvec = implicit_system(s, small, lam)
     assert steps == 1 and 1 <= iters and relres <= 0.1
     true_rel = np.linalg.norm(rhs - matvec(dc)) / np.linalg.norm(rhs)
     assert true_rel <= 0.1 + 1e-4, (true_rel, relres)
@@ -196,7 +146,7 @@ def test_float_float_refinement_residual_is_fp64_accurate(gba, small):
         iters, steps, relres = s.schur_pcg(lam, refine_tol=1e-10, pcg_tol=1e-3, pcg_max_iters=500)
         rhs_dev = s.download("rhs")[:9 * small.num_cameras]
         dc = s.download("dc")
-        rhs, matvec = _implicit_system(s, small, lam)
+        rhs, matvec = implicit_system(s, small, lam)
     assert rel_err(rhs_dev, rhs) < 1e-12
     r = rhs - matvec(dc)
     true_rel = np.linalg.norm(r) / np.linalg.norm(rhs)
@@ -298,7 +248,7 @@ def test_long_tracks_refined_step(gba, oracle, long_tracks):
         dc = s.download("dc")
         s.back_substitute(lam)
         dp = s.download("dp")
-        rhs, matvec = _implicit_system(s, long_tracks, lam)
+        rhs, matvec = implicit_system(s, long_tracks, lam)
     assert rel_err(rhs_dev, rhs) < 1e-12
     assert relres <= 1e-10
     assert np.linalg.norm(rhs - matvec(dc)) / np.linalg.norm(rhs) <= 2e-10
