@@ -1,6 +1,7 @@
 """Build recipe of the test oracle (CPU). Test infrastructure only.
 
-  oracle/liboracle.so            CPU FP64 restatement of the reference LM (lm_oracle.cpp), g++
+  oracle/liboracle.so            CPU FP64 restatement of the reference LM (lm_oracle.cpp) and the
+                                 seeded workload generator (synthetic_oracle.cpp), g++
   oracle/_ref/libgba_ref_reader.so
                                  the reference's own src/bal_reader.cpp compiled from its
                                  source where it lies, plus ref_shim.cpp (extern "C" wrappers)
@@ -53,10 +54,10 @@ def _stale(out: Path, inputs) -> bool:
 
 
 def build_oracle() -> Path:
-    src = HERE / "lm_oracle.cpp"
-    if _stale(ORACLE_SO, [src]):
+    srcs = [HERE / "lm_oracle.cpp", HERE / "synthetic_oracle.cpp"]
+    if _stale(ORACLE_SO, srcs):
         tmp = ORACLE_SO.with_suffix(".so.tmp")
-        _run(["g++", *FLAGS, "-o", str(tmp), str(src), "-lpthread"])
+        _run(["g++", *FLAGS, "-o", str(tmp), *map(str, srcs), "-lpthread"])
         os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 

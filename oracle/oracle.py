@@ -50,7 +50,37 @@ _lib.oracle_solve_robust.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _
                                      C.c_double, C.c_double, C.c_int, C.c_int, _dp, _dp, _ip, _ip,
                                      C.POINTER(C.c_ulonglong), _dp, C.c_int, _ip]
 
+_lib.oracle_synthetic.argtypes = [C.c_int, C.c_ulonglong, _ip, _ip, _ip]
+_lib.oracle_synthetic_copy.argtypes = [_dp, _dp, _ip, _ip, _dp]
+
 TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE"}
+
+
+class Problem:
+    """BAL-layout arrays (the fields of gba::BALProblem) for the oracle's own use."""
+
+    def __init__(self, cameras, points, obs_camera, obs_point, obs_pixel):
+        self.cameras, self.points = cameras, points
+        self.obs_camera, self.obs_point, self.obs_pixel = obs_camera, obs_point, obs_pixel
+
+    num_cameras = property(lambda self: self.cameras.size // 9)
+    num_points = property(lambda self: self.points.size // 3)
+    num_observations = property(lambda self: self.obs_camera.size)
+
+    def arrays(self):
+        return self.cameras, self.points, self.obs_camera, self.obs_point, self.obs_pixel
+
+
+def synthetic(workload: int, seed: int | None = None) -> Problem:
+    """Seeded workload 1..5 from the oracle's own generator (bit-identical to the product's)."""
+    c, p, e = C.c_int(), C.c_int(), C.c_int()
+    if _lib.oracle_synthetic(workload, workload if seed is None else seed, C.byref(c), C.byref(p), C.byref(e)):
+        raise ValueError("workload id must be 1..5")
+    prob = Problem(np.empty(9 * c.value), np.empty(3 * p.value), np.empty(e.value, np.int32),
+                   np.empty(e.value, np.int32), np.empty(2 * e.value))
+    _lib.oracle_synthetic_copy(_d(prob.cameras), _d(prob.points), _i(prob.obs_camera), _i(prob.obs_point),
+                               _d(prob.obs_pixel))
+    return prob
 
 
 def residual_jacobian(cam, pt, obs):

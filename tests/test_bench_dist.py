@@ -96,3 +96,32 @@ def test_clock_sampler_devices_follow_the_ranks(monkeypatch):
     assert bench.smi_devices(2, 2) == ["3", "5"]
     assert bench.smi_devices(1, 2) == ["3"]
     assert bench.ClockSampler(["3", "5"]).devices == "3,5"
+
+
+def _run_bench(*argv):
+    import json
+    import subprocess
+
+    code = ("import sys, runpy; sys.argv = ['bench.py'] + sys.argv[1:]; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "print('LOADED', 'gba_gb300' in sys.modules)")
+    r = subprocess.run([sys.executable, "-c", code, *argv], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                       env={**os.environ, "RANK": "0", "WORLD_SIZE": "1"})
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    return json.loads(lines[-2]), lines[-1]
+
+
+def test_reference_arm_unavailable_at_workload5_without_the_library():
+    line, loaded = _run_bench("--impl", "reference")
+    assert line["impl"] == "reference" and "unavailable" in line
+    assert loaded == "LOADED False"
+
+
+def test_reference_arm_times_oracle_solves_to_target_workload1():
+    line, loaded = _run_bench("--impl", "reference", "--workload", "1", "--steps", "1", "--warmup", "0")
+    assert loaded == "LOADED False"  # the CPU arm never loads the product library
+    assert line["impl"] == "reference" and line["unit"] == "s" and line["value"] > 0
+    assert line["config"]["iterations_to_target"] is not None
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0

@@ -101,3 +101,12 @@ def test_oracle_reproduces_committed_reference_run_workload1(gba, oracle):
     assert h.hexdigest() == e["fingerprint"]
     o, _, _ = oracle.solve(prob, max_iterations=e["max_iterations"], threads=2)
     assert _traj_close(o["trajectory"], e["reference"]["trajectory"], e["reference"]["initial_cost"]) < 1e-9
+
+
+@pytest.mark.parametrize("workload,seed", [(1, 1), (2, 2), (4, 4)])
+def test_oracle_generator_bit_identical_to_product(gba, oracle, workload, seed):
+    """The CPU benchmark arm generates its problems with the oracle's own
+    generator (nothing of the product loaded): same bits as the product's."""
+    a, b = gba.synthetic(workload, seed), oracle.synthetic(workload, seed)
+    for x, y in zip(a.arrays(), b.arrays()):
+        assert x.dtype == y.dtype and np.array_equal(x, y)
