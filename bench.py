@@ -56,7 +56,7 @@ GOLDEN = ROOT / "tests" / "golden"
 
 METRIC = "LM solve s to <=1.001x oracle cost: plain FP64 vs mixed+learned PCG, 1 GB300"
 TARGET_FACTOR = 1.001
-MODEL = PKG / "models" / "bj_mlp.bin"
+MODEL = PKG / "models" / "coarse_mlp.bin"
 # FP64 DMMA peak (mma.sync.m8n8k4.f64 loop) probed on a GB300 of this pool; the
 # measured peaks file has no FP64 entry.
 FP64_DMMA_TFLOPS = 1.05

@@ -171,6 +171,26 @@ int gba_solver_features(gba_solver* s, double lambda, float* feat) {
     });
 }
 
+int gba_solver_set_preconditioner(gba_solver* s, int mode) {
+    return guarded([&] {
+        need(mode >= 0 && mode <= 2, "mode must be 0 (judge), 1 (learned) or 2 (block-Jacobi)");
+        S(s).precond_force_ = mode;
+    });
+}
+
+int gba_solver_judge_info(gba_solver* s, long long* iters, double* btx) {
+    return guarded([&] {
+        if (iters) {
+            iters[0] = S(s).judge_iters_[0];
+            iters[1] = S(s).judge_iters_[1];
+        }
+        if (btx) {
+            btx[0] = S(s).judge_btx_[0];
+            btx[1] = S(s).judge_btx_[1];
+        }
+    });
+}
+
 long long gba_mlp_num_params(void) { return gba::kMlpParams; }
 
 int gba_mlp_create(uint64_t seed, int cap, gba_mlp** out) {
@@ -226,13 +246,12 @@ int gba_mlp_forward(gba_mlp* m, const float* feat, int B, float* out, void* stre
     });
 }
 
-int gba_mlp_loss_grad(gba_mlp* m, const float* feat, const double* Shat, const double* Lhat, const double* g,
-                      const double* x, int B, void* stream, double* out_loss, double* out_base) {
+int gba_mlp_backward(gba_mlp* m, const float* feat, const float* d_out, int B, void* stream) {
     return guarded([&] {
-        need(m && feat && Shat && Lhat && g && x && B > 0, "bad argument");
-        const double l = reinterpret_cast<gba::Mlp*>(m)->loss_grad(feat, Shat, Lhat, g, x, B,
-                                                                  static_cast<cudaStream_t>(stream), out_base);
-        if (out_loss) *out_loss = l;
+        need(m && feat && d_out && B > 0, "bad argument");
+        auto st = static_cast<cudaStream_t>(stream);
+        reinterpret_cast<gba::Mlp*>(m)->backward(feat, d_out, B, st);
+        GBA_CUDA_CHECK(cudaStreamSynchronize(st));
     });
 }
 

@@ -1,14 +1,14 @@
-// Learned block-Jacobi correction: MLP training and inference kernels.
+// Learned coarse-space correction: MLP training and inference kernels.
 //
 //   GEMMs      mma.sync.m16n8k16 BF16 x BF16 -> FP32 (BF16 weights and
 //              activations in shared memory, FP32 accumulation and storage);
 //              one kernel with strided operand loads serves the forward
 //              (X W^T), input-gradient (dY W) and weight-gradient (dY^T X) shapes.
-//   loss       per-camera FP64 thread: the preconditioned block step, its error
-//              in the block norm, and the analytic gradient through the factor
-//              parametrisation (rank-2 form dl/dF_ij = -(c_i a_j + d_i b_j)).
+//   backward   from the loss gradient w.r.t. the outputs (the loss, the
+//              eigenvector share outside the coarse space, is a global function
+//              of all cameras' outputs; the training script forms its gradient).
 //   Adam       FP32 masters, BF16 copies refreshed after each step.
-//   inference  features of S_cc -> MLP -> corrected factor L_c F_c.
+//   inference  features of S_cc and the camera -> MLP -> coarse basis rows Z_c.
 // No reference counterpart (the reference has no iterative solver).
 
 #include <cuda_bf16.h>
@@ -149,120 +149,6 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     }
 }
 
-using blk::tri;
-
-// F from the 45 network outputs (packed lower).
-__device__ __forceinline__ void build_F(const float* o, double* F, double* th) {
-    for (int i = 0; i < 9; ++i)
-        for (int j = 0; j <= i; ++j) {
-            const int k = tri(i, j);
-            const double tk = tanh(static_cast<double>(o[k]));
-            th[k] = tk;
-            F[k] = (i == j) ? exp(0.5 * tk) : 0.5 * tk;
-        }
-}
-
-// Lt = L F (both packed lower).
-__device__ __forceinline__ void lower_mul(const double* L, const double* F, double* Lt) {
-    for (int i = 0; i < 9; ++i)
-        for (int j = 0; j <= i; ++j) {
-            double s = 0.0;
-            for (int k = j; k <= i; ++k) s += L[tri(i, k)] * F[tri(k, j)];
-            Lt[tri(i, j)] = s;
-        }
-}
-
-__device__ __forceinline__ void sym_mul(const double* S, const double* x, double* y) {  // packed symmetric
-    for (int i = 0; i < 9; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < 9; ++j) s += S[i >= j ? tri(i, j) : tri(j, i)] * x[j];
-        y[i] = s;
-    }
-}
-
-__device__ __forceinline__ void lowerT_vec(const double* L, const double* x, double* y) {  // y = L^T x
-    for (int j = 0; j < 9; ++j) {
-        double s = 0.0;
-        for (int i = j; i < 9; ++i) s += L[tri(i, j)] * x[i];
-        y[j] = s;
-    }
-}
-
-// Per-sample loss and gradient w.r.t. the 45 outputs (scaled by inv_b).
-__global__ void loss_kernel(const float* __restrict__ O, const double* __restrict__ Shat,
-                            const double* __restrict__ Lhat, const double* __restrict__ g,
-                            const double* __restrict__ x, int B, double inv_b, float* __restrict__ dO,
-                            double* __restrict__ loss) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
-    double S[45], L[45], F[45], th[45], Lt[45];
-    for (int k = 0; k < 45; ++k) {
-        S[k] = Shat[45ll * b + k];
-        L[k] = Lhat[45ll * b + k];
-    }
-    double gv[9], xv[9];
-    for (int k = 0; k < 9; ++k) {
-        gv[k] = g[9ll * b + k];
-        xv[k] = x[9ll * b + k];
-    }
-    float o[45];
-    for (int k = 0; k < 45; ++k) o[k] = O[48ll * b + k];
-    build_F(o, F, th);
-    lower_mul(L, F, Lt);
-    double y[9], y0[9], e[9], Se[9], Sx[9];
-    blk::chol9_solve(Lt, gv, y);
-    blk::chol9_solve(L, gv, y0);
-    sym_mul(S, xv, Sx);
-    double den = 0.0;
-    for (int k = 0; k < 9; ++k) den += xv[k] * Sx[k];
-    den = den > 1e-300 ? den : 1e-300;
-    for (int k = 0; k < 9; ++k) e[k] = y[k] - xv[k];
-    sym_mul(S, e, Se);
-    double num = 0.0;
-    for (int k = 0; k < 9; ++k) num += e[k] * Se[k];
-    // baseline (F = I)
-    double e0[9], Se0[9], num0 = 0.0;
-    for (int k = 0; k < 9; ++k) e0[k] = y0[k] - xv[k];
-    sym_mul(S, e0, Se0);
-    for (int k = 0; k < 9; ++k) num0 += e0[k] * Se0[k];
-    loss[2ll * b] = num / den;
-    loss[2ll * b + 1] = num0 / den;
-    if (!dO) return;
-    // gradient: gy = 2 S e / den, z = A^-1 gy, a = Lt^T y, bb = Lt^T z, c = L^T z, d = L^T y,
-    // dl/dF_ij = -(c_i a_j + d_i bb_j) (i >= j)
-    double gy[9], z[9], a[9], bv[9], c[9], d[9];
-    for (int k = 0; k < 9; ++k) gy[k] = 2.0 * Se[k] / den;
-    blk::chol9_solve(Lt, gy, z);
-    lowerT_vec(Lt, y, a);
-    lowerT_vec(Lt, z, bv);
-    lowerT_vec(L, z, c);
-    lowerT_vec(L, y, d);
-    for (int i = 0; i < 9; ++i)
-        for (int j = 0; j <= i; ++j) {
-            const int k = tri(i, j);
-            const double dF = -(c[i] * a[j] + d[i] * bv[j]);
-            const double dt = 0.5 * (1.0 - th[k] * th[k]);
-            const double dout = (i == j) ? dF * F[k] * dt : dF * dt;
-            dO[48ll * b + k] = static_cast<float>(dout * inv_b);
-        }
-    for (int k = 45; k < 48; ++k) dO[48ll * b + k] = 0.f;
-}
-
-__global__ void __launch_bounds__(256) mean2_kernel(const double* __restrict__ loss, int B, double* __restrict__ out) {
-    __shared__ double sh[8];
-    double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < B; i += 256) {
-        a += loss[2ll * i];
-        b += loss[2ll * i + 1];
-    }
-    const double ta = block_sum<256>(a, sh);
-    const double tb = block_sum<256>(b, sh);
-    if (threadIdx.x == 0) {
-        out[0] = ta / B;
-        out[1] = tb / B;
-    }
-}
-
 // ---- inference-side kernels
 
 // Per-camera track statistics: observations, sum of (track length - 1), mean track length.
@@ -291,7 +177,8 @@ __global__ void camera_stats_kernel(const int* __restrict__ cam_off, const int* 
 constexpr int kCamT = 32;
 
 __global__ void features_kernel(const double* __restrict__ Sdiag, const double* __restrict__ U,
-                                const float* __restrict__ stats, double lambda, int C, float* __restrict__ feat) {
+                                const float* __restrict__ stats, const double* __restrict__ cams, double lambda,
+                                int C, float* __restrict__ feat) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
     const double* S = Sdiag + 81ll * c;
@@ -312,20 +199,27 @@ __global__ void features_kernel(const double* __restrict__ Sdiag, const double* 
     f[46] = stats[3 * c + 1];
     f[47] = stats[3 * c + 2];
     f[48] = static_cast<float>(log10(lambda > 1e-300 ? lambda : 1e-300) / 10.0);
-    for (int i = 49; i < 64; ++i) f[i] = 0.f;
+    const double* cam = cams + 9ll * c;
+    for (int i = 0; i < 3; ++i) f[49 + i] = static_cast<float>(3.0 * cam[i]);
+    for (int i = 0; i < 3; ++i) f[52 + i] = static_cast<float>(0.5 * cam[3 + i]);
+    f[55] = static_cast<float>((cam[6] - 500.0) / 100.0);
+    f[56] = static_cast<float>(10.0 * cam[7]);
+    f[57] = static_cast<float>(100.0 * cam[8]);
+    for (int i = kMlpUsedIn; i < 64; ++i) f[i] = 0.f;
 }
 
-// Pfac_c <- L_c F_c (in place; both packed lower).
-__global__ void correct_kernel(const float* __restrict__ O, int C, double* __restrict__ Pfac) {
+// Coarse basis rows of camera c from the network outputs:
+// Z[j][9c + i] = o[9 i + j] * unit_i (unit 1, the focal-length row f_c).
+__global__ void basis_kernel(const float* __restrict__ O, const double* __restrict__ cams, int C,
+                             double* __restrict__ Z) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
-    double L[45], F[45], th[45], Lt[45];
-    for (int k = 0; k < 45; ++k) L[k] = Pfac[45ll * c + k];
-    float o[45];
-    for (int k = 0; k < 45; ++k) o[k] = O[48ll * c + k];
-    build_F(o, F, th);
-    lower_mul(L, F, Lt);
-    for (int k = 0; k < 45; ++k) Pfac[45ll * c + k] = Lt[k];
+    const double f = cams[9ll * c + 6];
+    const long long n = 9ll * C;
+    for (int i = 0; i < 9; ++i) {
+        const double unit = i == 6 ? f : 1.0;
+        for (int j = 0; j < kCoarse; ++j) Z[j * n + 9ll * c + i] = unit * O[static_cast<long long>(kMlpOut) * c + 9 * i + j];
+    }
 }
 
 template <typename T>
@@ -343,7 +237,7 @@ T* palloc(long long n, cudaStream_t s) {
     return p;
 }
 
-const char kMagic[8] = {'G', 'B', 'A', 'M', 'L', 'P', '0', '1'};
+const char kMagic[8] = {'G', 'B', 'A', 'M', 'L', 'P', '0', '2'};
 
 std::vector<float> read_model(const std::string& path) {
     std::ifstream f(path, std::ios::binary);
@@ -386,16 +280,13 @@ void Mlp::ensure_capacity(int B) {
         h2_ = palloc<float>(1ll * cap_ * kMlpH, pool_stream_);
         return;
     }
-    for (void* q : {static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(o_), static_cast<void*>(do_),
-                    static_cast<void*>(dh2_), static_cast<void*>(dh1_), static_cast<void*>(loss_)})
+    for (void* q : {static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(dh2_),
+                    static_cast<void*>(dh1_)})
         if (q) cudaFree(q);
     h1_ = dalloc<float>(1ll * cap_ * kMlpH);
     h2_ = dalloc<float>(1ll * cap_ * kMlpH);
-    o_ = dalloc<float>(1ll * cap_ * kMlpOut);
-    do_ = dalloc<float>(1ll * cap_ * kMlpOut);
     dh2_ = dalloc<float>(1ll * cap_ * kMlpH);
     dh1_ = dalloc<float>(1ll * cap_ * kMlpH);
-    loss_ = dalloc<double>(2ll * cap_ + 2);
 }
 
 Mlp::Mlp(int capacity, uint64_t seed) : cap_(capacity) {
@@ -407,7 +298,10 @@ Mlp::Mlp(int capacity, uint64_t seed) : cap_(capacity) {
     for (int r = 0; r < kMlpH; ++r)
         for (int c = 0; c < kMlpUsedIn; ++c) h[kW1 + 1ll * r * kMlpIn + c] = s1 * nd(rng);
     for (long long i = 0; i < 1ll * kMlpH * kMlpH; ++i) h[kW2 + i] = s2 * nd(rng);
-    set_params(h.data());  // W3 = 0, biases = 0: the network starts as plain block-Jacobi
+    const float s3 = 0.1f * s2;  // a small random last layer: a full-rank basis to start from
+    for (int r = 0; r < kMlpUsedOut; ++r)
+        for (int c = 0; c < kMlpH; ++c) h[kW3 + 1ll * r * kMlpH + c] = s3 * nd(rng);
+    set_params(h.data());
 }
 
 Mlp::Mlp(const std::string& path, int capacity) : cap_(capacity) {
@@ -436,8 +330,8 @@ Mlp::~Mlp() {
         return;
     }
     for (void* q : {static_cast<void*>(p_), static_cast<void*>(g_), static_cast<void*>(m_), static_cast<void*>(v_), wb_,
-                    static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(o_), static_cast<void*>(do_),
-                    static_cast<void*>(dh2_), static_cast<void*>(dh1_), static_cast<void*>(loss_)})
+                    static_cast<void*>(h1_), static_cast<void*>(h2_), static_cast<void*>(dh2_),
+                    static_cast<void*>(dh1_)})
         if (q) cudaFree(q);
 }
 
@@ -491,24 +385,17 @@ void Mlp::forward(const float* feat, int B, float* out, cudaStream_t s) {
     gemm(B, kMlpOut, kMlpH, h2_, kMlpH, 1, w3, 1, kMlpH, out, kMlpOut, p_ + kB3, false, nullptr, 0, s);
 }
 
-double Mlp::loss_grad(const float* feat, const double* Shat, const double* Lhat, const double* g, const double* x,
-                      int B, cudaStream_t s, double* baseline_loss) {
+void Mlp::backward(const float* feat, const float* dO, int B, cudaStream_t s) {
     require_training();
-    if (B <= 0) throw std::invalid_argument("empty batch");
-    ensure_capacity(B);
-    forward(feat, B, o_, s);
-    loss_kernel<<<ceil_div(B, 128), 128, 0, s>>>(o_, Shat, Lhat, g, x, B, 1.0 / B, do_, loss_);
-    GBA_LAUNCH_CHECK();
-    mean2_kernel<<<1, 256, 0, s>>>(loss_, B, loss_ + 2ll * cap_);
-    GBA_LAUNCH_CHECK();
+    if (B <= 0 || B > cap_) throw std::invalid_argument("backward: batch must be the last forward's (<= capacity)");
     const __nv_bfloat16* wb = static_cast<const __nv_bfloat16*>(wb_);
     const __nv_bfloat16* w2 = wb + 1ll * kMlpH * kMlpIn;
     const __nv_bfloat16* w3 = w2 + 1ll * kMlpH * kMlpH;
     // layer 3: dW3[n][k] = sum_m dO[m][n] H2[m][k]; db3; dH2 = (dO W3) * (H2 > 0)
-    gemm(kMlpOut, kMlpH, B, do_, 1, kMlpOut, h2_, kMlpH, 1, g_ + kW3, kMlpH, nullptr, false, nullptr, 0, s);
-    colsum_kernel<<<kMlpOut, 256, 0, s>>>(do_, B, kMlpOut, g_ + kB3);
+    gemm(kMlpOut, kMlpH, B, dO, 1, kMlpOut, h2_, kMlpH, 1, g_ + kW3, kMlpH, nullptr, false, nullptr, 0, s);
+    colsum_kernel<<<kMlpOut, 256, 0, s>>>(dO, B, kMlpOut, g_ + kB3);
     GBA_LAUNCH_CHECK();
-    gemm(B, kMlpH, kMlpOut, do_, kMlpOut, 1, w3, kMlpH, 1, dh2_, kMlpH, nullptr, false, h2_, kMlpH, s);
+    gemm(B, kMlpH, kMlpOut, dO, kMlpOut, 1, w3, kMlpH, 1, dh2_, kMlpH, nullptr, false, h2_, kMlpH, s);
     // layer 2
     gemm(kMlpH, kMlpH, B, dh2_, 1, kMlpH, h1_, kMlpH, 1, g_ + kW2, kMlpH, nullptr, false, nullptr, 0, s);
     colsum_kernel<<<kMlpH, 256, 0, s>>>(dh2_, B, kMlpH, g_ + kB2);
@@ -518,11 +405,6 @@ double Mlp::loss_grad(const float* feat, const double* Shat, const double* Lhat,
     gemm(kMlpH, kMlpIn, B, dh1_, 1, kMlpH, feat, kMlpIn, 1, g_ + kW1, kMlpIn, nullptr, false, nullptr, 0, s);
     colsum_kernel<<<kMlpH, 256, 0, s>>>(dh1_, B, kMlpH, g_ + kB1);
     GBA_LAUNCH_CHECK();
-    double h[2];
-    GBA_CUDA_CHECK(cudaMemcpyAsync(h, loss_ + 2ll * cap_, sizeof h, cudaMemcpyDeviceToHost, s));
-    GBA_CUDA_CHECK(cudaStreamSynchronize(s));
-    if (baseline_loss) *baseline_loss = h[1];
-    return h[0];
 }
 
 void Mlp::adam_step(float lr, float beta1, float beta2, float eps, cudaStream_t s) {
@@ -546,7 +428,7 @@ void mlp_features(Solver& s, double lambda, float* feat) {
         GBA_LAUNCH_CHECK();
     }
     features_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(s.Sdiag_.get(), s.U_.get(), s.mlp_stats_.get(),
-                                                                 lambda, s.C_, feat);
+                                                                 s.cams_.get(), lambda, s.C_, feat);
     GBA_LAUNCH_CHECK();
 }
 
@@ -558,7 +440,7 @@ LearnedPreconditioner::~LearnedPreconditioner() {
     if (out_) cudaFreeAsync(out_, stream_);
 }
 
-void LearnedPreconditioner::correct_factors(Solver& s, double lambda) {
+void LearnedPreconditioner::coarse_basis(Solver& s, double lambda, double* Z) {
     if (cap_ < s.C_) {
         if (feat_) GBA_CUDA_CHECK(cudaFreeAsync(feat_, stream_));
         if (out_) GBA_CUDA_CHECK(cudaFreeAsync(out_, stream_));
@@ -570,7 +452,7 @@ void LearnedPreconditioner::correct_factors(Solver& s, double lambda) {
     cudaEvent_t ev = s.prof_start();
     mlp_.forward(feat_, s.C_, out_, s.stream_);
     s.prof_stop("mlp_forward", ev);
-    correct_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(out_, s.C_, s.Pfac_.get());
+    basis_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(out_, s.cams_.get(), s.C_, Z);
     GBA_LAUNCH_CHECK();
 }
 

@@ -1,24 +1,30 @@
 #pragma once
-// Learned block-Jacobi correction for the mixed-form PCG.
+// Learned coarse-space correction of the block-Jacobi preconditioner (mixed-form PCG).
 //
-// Per camera c, a 3-layer MLP (inputs 49 -> 128 -> 128 -> 45; BF16 weights,
-// FP32 accumulation on the tensor cores, FP32 master weights for training)
-// maps features of the damped diagonal block S_cc to a lower-triangular factor
-// F_c with positive diagonal. The preconditioner block becomes
-//   M_c = (L_c F_c F_c^T L_c^T)^-1,   L_c = chol(S_cc),
-// which is SPD for any network output and equals block-Jacobi when F_c = I
-// (a zero last layer). Parametrisation of the 45 outputs o:
-//   F_ij = 0.5 tanh(o_ij) (i > j),   F_ii = exp(0.5 tanh(o_ii)).
-// Features (in the Jacobi-scaled space S^ = D^-1/2 S_cc D^-1/2, padded to 64):
-//   [0,36)  off-diagonal S^_ij, i > j (row order)
-//   [36,45) S_ii / (U_ii + lambda max(U_ii, 1e-12))   (share of the diagonal left after
-//           eliminating the points)
+// Block-Jacobi PCG on the reduced camera system converges slowly because of a
+// handful of very small eigenvalues of the Jacobi-preconditioned S: the
+// 7-dimensional similarity gauge of bundle adjustment (global rotation,
+// translation, scale: only the LM damping holds it) and a few soft
+// rotation/translation/focal modes. No block-diagonal correction reaches them
+// (they are global), so the learned part is a low-rank correction: per camera
+// c, a 3-layer MLP (inputs 58 -> 128 -> 128 -> 81; BF16 weights, FP32
+// accumulation on the tensor cores, FP32 master weights for training) maps the
+// camera's features to its 9 x kCoarse rows Z_c of a coarse basis Z (9C x
+// kCoarse). The preconditioner is the balancing two-level form
+//   M = P^T B^-1 P + Z E^-1 Z^T,   P = I - S Z E^-1 Z^T,   E = Z^T S Z,
+// with B the block-Jacobi blocks: SPD for any Z of full rank, and B^-1 itself
+// (block-Jacobi) when the coarse solve is disabled (E not SPD).
+// Output parametrisation: Z_c(i, j) = o[9 i + j] * unit_i, unit = 1 except the
+// focal-length row (f_c), so that every output is O(1).
+// Features (padded to 64):
+//   [0,36)  off-diagonal entries of the Jacobi-scaled block D^-1/2 S_cc D^-1/2, i > j (row order)
+//   [36,45) S_ii / (U_ii + lambda max(U_ii, 1e-12))
 //   45 log1p(observations of c) / 10, 46 log1p(sum over c's observations of (track length - 1)) / 15,
-//   47 mean track length / 10, 48 log10(lambda) / 10.
-// Training loss per camera (the block's step error in its own norm):
-//   l = (y - x*)^T S^ (y - x*) / (x*^T S^ x*),  y = M^_c g^_c,
-// with g the Schur right-hand side and x* the exact (dense FP64) step, both in
-// the scaled space.
+//   47 mean track length / 10, 48 log10(lambda) / 10,
+//   [49,52) 3 x angle-axis, [52,55) translation / 2, 55 (f - 500) / 100, 56 10 k1, 57 100 k2.
+// Training objective (train_preconditioner.py): the share of the lowest
+// eigenvectors of the block-Jacobi-preconditioned S (from systems the plain
+// solver assembles) that lies outside span(B^T Z).
 
 #include <cuda_runtime.h>
 
@@ -30,19 +36,20 @@ namespace gba {
 
 class Solver;
 
-constexpr int kMlpIn = 64;   // 49 features padded for the K = 16 MMA steps
+constexpr int kMlpIn = 64;   // 58 features padded for the K = 16 MMA steps
 constexpr int kMlpH = 128;
-constexpr int kMlpOut = 48;  // 45 outputs padded to a multiple of 16
-constexpr int kMlpUsedIn = 49;
-constexpr int kMlpUsedOut = 45;
+constexpr int kCoarse = 9;   // coarse basis columns
+constexpr int kMlpOut = 96;  // 81 outputs padded to a multiple of 16
+constexpr int kMlpUsedIn = 58;
+constexpr int kMlpUsedOut = 9 * kCoarse;
 
-// Flat FP32 parameter vector: W1[128x64] b1[128] W2[128x128] b2[128] W3[48x128] b3[48].
+// Flat FP32 parameter vector: W1[128x64] b1[128] W2[128x128] b2[128] W3[96x128] b3[96].
 constexpr long long kMlpParams =
     1ll * kMlpH * kMlpIn + kMlpH + 1ll * kMlpH * kMlpH + kMlpH + 1ll * kMlpOut * kMlpH + kMlpOut;
 
 class Mlp {
 public:
-    Mlp(int capacity, uint64_t seed);               // random init, zero last layer
+    Mlp(int capacity, uint64_t seed);               // random init (He; small last layer), zero biases
     Mlp(const std::string& path, int capacity);     // load a saved model
     // Inference only (forward): a saved model whose parameters, BF16 weights
     // and activations are allocated stream-ordered on `stream` (the device's
@@ -59,15 +66,14 @@ public:
     int capacity() const { return cap_; }
     void ensure_capacity(int B);
 
-    // out[B x 48] (FP32) = network(feat[B x 64]); device pointers.
+    // out[B x 96] (FP32) = network(feat[B x 64]); device pointers. Keeps the
+    // hidden activations for a following backward() on the same batch.
     void forward(const float* feat, int B, float* out, cudaStream_t s);
-    // Forward + loss + backward on a batch (device pointers: Shat, Lhat packed
-    // lower 45 per sample, g and x 9 per sample). Gradients kept for adam_step;
-    // returns the mean loss. If baseline_loss is non-null it receives the mean
-    // loss of F = I (plain block-Jacobi) on the same batch.
-    double loss_grad(const float* feat, const double* Shat, const double* Lhat, const double* g, const double* x,
-                     int B, cudaStream_t s, double* baseline_loss = nullptr);
-    void grads(float* host) const;  // flat gradient of the last loss_grad
+    // Gradient of a loss w.r.t. the parameters, given its gradient dO[B x 96]
+    // w.r.t. the outputs of the last forward() on feat (device pointers).
+    // Gradients kept for adam_step.
+    void backward(const float* feat, const float* dO, int B, cudaStream_t s);
+    void grads(float* host) const;  // flat gradient of the last backward
     void adam_step(float lr, float beta1, float beta2, float eps, cudaStream_t s);
 
     float* params_dev() const { return p_; }
@@ -89,10 +95,8 @@ private:
     float* h1_ = nullptr;  // activations [cap x 128]
     float* h2_ = nullptr;
     float* o_ = nullptr;   // [cap x 48]
-    float* do_ = nullptr;
     float* dh2_ = nullptr;
     float* dh1_ = nullptr;
-    double* loss_ = nullptr;  // [cap x 2] per-sample loss, baseline loss
 };
 
 class LearnedPreconditioner {
@@ -100,9 +104,9 @@ public:
     // The model's buffers are allocated stream-ordered on the solver's stream.
     LearnedPreconditioner(const std::string& path, cudaStream_t stream);
     ~LearnedPreconditioner();
-    // Replaces the block-Jacobi factors in s.Pfac_ by the corrected factors
-    // L_c F_c; S_cc (s.Sdiag_) and the factors must be current.
-    void correct_factors(Solver& s, double lambda);
+    // The coarse basis Z (kCoarse columns of 9C, column-major, FP64) at the
+    // solver's current cameras; S_cc (s.Sdiag_) must be current.
+    void coarse_basis(Solver& s, double lambda, double* Z);
 
 private:
     Mlp mlp_;
@@ -112,8 +116,8 @@ private:
     int cap_ = 0;
 };
 
-// Per-camera features of the current damped diagonal blocks (s.Sdiag_) into
-// feat[C x 64] (device).
+// Per-camera features of the current damped diagonal blocks (s.Sdiag_) and
+// cameras into feat[C x 64] (device).
 void mlp_features(Solver& s, double lambda, float* feat);
 
 }  // namespace gba

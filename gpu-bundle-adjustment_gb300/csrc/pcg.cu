@@ -19,8 +19,9 @@
 // solves on the FP32 operator; with refine_tol >= kLooseTol the right-hand side
 // is FP32 and a converged inner solve is its own check. The block-Jacobi blocks
 // are the 9x9 diagonal blocks S_cc (FP32 products, FP64 sums, FP64 Cholesky,
-// explicit inverses); the learned form replaces their factors by the
-// MLP-corrected ones (mlp.cu). PCG vectors and dot products are FP64 with
+// explicit inverses); the learned form adds a coarse-space correction whose
+// basis the MLP predicts (mlp.cu; the balancing two-level preconditioner
+// below). PCG vectors and dot products are FP64 with
 // deterministic reductions; all PCG control scalars live on the device and the
 // host polls a convergence flag after batches of iterations.
 //
@@ -59,7 +60,7 @@ constexpr int kUT = 9 * kUC;   // their block size
 // S_DONE, whose value every block of the writing kernel derives itself:
 //   pcg_update         reads S_RZ;            writes S_RZPREV, S_ITERS (and S_DONE on breakdown)
 //   pcg_direction      reads S_RZPREV, S_ITERS; writes S_RZ, S_RR, S_BETA, S_DONE
-enum { S_RZ = 0, S_ALPHA, S_BETA, S_RR, S_BB, S_DONE, S_ITERS, S_TOL2, S_NORM, S_RZPREV };
+enum { S_RZ = 0, S_ALPHA, S_BETA, S_RR, S_BB, S_DONE, S_ITERS, S_TOL2, S_NORM, S_RZPREV, S_BTX0, S_BTX1 };
 
 using ffa::ff;
 
@@ -696,14 +697,230 @@ __device__ __forceinline__ double apply_minv_row(const double* __restrict__ Minv
     return z;
 }
 
+// ---- balancing two-level preconditioner with the learned coarse basis Z
+// (kCoarse columns of n = 9C, column-major): z = M r with
+//   c1 = E^-1 Z^T r,  w = B^-1 (r - SZ c1),  c2 = E^-1 SZ^T w,  z = w + Z (c1 - c2),
+// E = Z^T S Z, SZ = S Z (both formed once per trial by coarse_prepare). E^-1 and
+// its SPD flag live in einv[0, kCoarse^2) and einv[kCoarse^2]; a flag of 0 (E not
+// SPD) zeroes c1 and c2, which leaves block-Jacobi.
+
+// Block partials of V^T v for the kCoarse columns of V (entry i of this
+// thread, vi its value; i past the end contributes 0): red[block * kCoarse + j].
+__device__ __forceinline__ void coarse_partials(const double* __restrict__ V, long long n, long long i, double vi,
+                                                double* sh, double* __restrict__ red) {
+#pragma unroll 1
+    for (int j = 0; j < kCoarse; ++j) {
+        const double t = block_sum<kUT>(i < n ? V[j * n + i] * vi : 0.0, sh);
+        if (threadIdx.x == 0) red[static_cast<long long>(blockIdx.x) * kCoarse + j] = t;
+    }
+}
+
+// c = E^-1 (sum over nb blocks of red[b * kCoarse + j]) in shared cs[kCoarse],
+// every block in the same order (warp j sums column j); 0 if E is not SPD.
+// Needs kUT / 32 == kCoarse warps.
+__device__ __forceinline__ void coarse_coeffs(const double* __restrict__ red, int nb,
+                                              const double* __restrict__ einv, double* tsum, double* cs) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double v = 0.0;
+    for (int b = lane; b < nb; b += 32) v += red[static_cast<long long>(b) * kCoarse + warp];
+    v = warp_sum(v);
+    if (lane == 0) tsum[warp] = v;
+    __syncthreads();
+    if (threadIdx.x < kCoarse) {
+        double c = 0.0;
+        if (einv[kCoarse * kCoarse] != 0.0) {
+#pragma unroll
+            for (int k = 0; k < kCoarse; ++k) c += einv[threadIdx.x * kCoarse + k] * tsum[k];
+        }
+        cs[threadIdx.x] = c;
+    }
+    __syncthreads();
+}
+
+// w = B^-1 (r - SZ c1) into w; block partials of SZ^T w. c1 from the Z^T r
+// partials (block 0 also stores it for coarse_z). At init (init != 0) the PCG
+// done flag is not consulted (it is set afterwards by pcg_init_finalize).
+__global__ void __launch_bounds__(kUT) coarse_w(const double* __restrict__ r, const double* __restrict__ SZ,
+                                               const double* __restrict__ Minv, const double* __restrict__ einv,
+                                               int C, const double* __restrict__ red_zr, int nb,
+                                               double* __restrict__ c1_out, double* __restrict__ w,
+                                               double* __restrict__ red_szw, const double* __restrict__ sc, int init) {
+    static_assert(kUT / 32 == kCoarse, "one warp per coarse column");
+    __shared__ double sh[kUT / 32];
+    __shared__ double rs[kUT];
+    __shared__ double tsum[kCoarse], c1[kCoarse];
+    __shared__ double bc;
+    if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
+    coarse_coeffs(red_zr, nb, einv, tsum, c1);
+    if (blockIdx.x == 0 && threadIdx.x < kCoarse) c1_out[threadIdx.x] = c1[threadIdx.x];
+    const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
+    const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
+    const long long n = 9ll * C, i = 9 * c + k;
+    double yi = 0.0;
+    if (c < C) {
+        yi = r[i];
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) yi -= SZ[j * n + i] * c1[j];
+    }
+    rs[threadIdx.x] = yi;
+    __syncthreads();
+    double wi = 0.0;
+    if (c < C) {
+        wi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+        w[i] = wi;
+    }
+    coarse_partials(SZ, n, i, wi, sh, red_szw);
+}
+
+// z = w + Z (c1 - c2) in place of w, c2 = E^-1 SZ^T w from the partials; the
+// partials of r.z; at init also p = z and its FP32 copy.
+__global__ void __launch_bounds__(kUT) coarse_z(const double* __restrict__ r, const double* __restrict__ Zc,
+                                               const double* __restrict__ einv, int C,
+                                               const double* __restrict__ red_szw, int nb,
+                                               const double* __restrict__ c1_in, double* __restrict__ z,
+                                               double* __restrict__ p, float* __restrict__ p32,
+                                               double* __restrict__ red_rz, const double* __restrict__ sc, int init) {
+    __shared__ double sh[kUT / 32];
+    __shared__ double tsum[kCoarse], c2[kCoarse];
+    __shared__ double bc;
+    if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
+    coarse_coeffs(red_szw, nb, einv, tsum, c2);
+    const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
+    const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
+    const long long n = 9ll * C, i = 9 * c + k;
+    double rz = 0.0;
+    if (c < C) {
+        double zi = z[i];
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) zi += Zc[j * n + i] * (c1_in[j] - c2[j]);
+        z[i] = zi;
+        if (init) {
+            p[i] = zi;
+            p32[kX32 * c + k] = static_cast<float>(zi);
+        }
+        rz = r[i] * zi;
+    }
+    const double t = block_sum<kUT>(rz, sh);
+    if (threadIdx.x == 0) red_rz[blockIdx.x] = t;
+}
+
+// FP32 copy of an FP64 camera vector in the matvec's padded layout.
+__global__ void __launch_bounds__(kVT) to_x32_kernel(const double* __restrict__ v, int n, float* __restrict__ x32) {
+    const int i = blockIdx.x * kVT + threadIdx.x;
+    if (i < n) {
+        const int c = i / 9;
+        x32[kX32 * c + (i - 9 * c)] = static_cast<float>(v[i]);
+    }
+}
+
+// y = U_lambda v - (chunk partials of the implicit product): one FP32 product S v.
+__global__ void __launch_bounds__(kVT) coarse_q_kernel(const int* __restrict__ cam_chunk_off,
+                                                      const double* __restrict__ part, const double* __restrict__ U,
+                                                      double lambda, const double* __restrict__ v, int C,
+                                                      double* __restrict__ y) {
+    const int i = blockIdx.x * kVT + threadIdx.x;
+    if (i < 9 * C) {
+        const int c = i / 9, k = i % 9;
+        y[i] = damped_u_row_dot(U + 81ll * c, k, lambda, v + 9ll * c) - chunk_sum(cam_chunk_off, part, c, k);
+    }
+}
+
+// Block partials of E = Z^T SZ: red[block * kCoarse^2 + a kCoarse + b] over the block's entries.
+__global__ void __launch_bounds__(kVT) coarse_gram_partials(const double* __restrict__ Zc,
+                                                           const double* __restrict__ SZ, long long n,
+                                                           double* __restrict__ red) {
+    __shared__ double sh[kVT / 32];
+    const long long i = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x;
+    double zv[kCoarse], sv[kCoarse];
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) {
+        zv[j] = i < n ? Zc[j * n + i] : 0.0;
+        sv[j] = i < n ? SZ[j * n + i] : 0.0;
+    }
+#pragma unroll 1
+    for (int a = 0; a < kCoarse; ++a)
+#pragma unroll 1
+        for (int b = 0; b < kCoarse; ++b) {
+            const double t = block_sum<kVT>(zv[a] * sv[b], sh);
+            if (threadIdx.x == 0) red[static_cast<long long>(blockIdx.x) * kCoarse * kCoarse + a * kCoarse + b] = t;
+        }
+}
+
+// E from the partials (fixed order), symmetrised; FP64 Cholesky and inverse by
+// one thread. einv[kCoarse^2] = 1 if E is SPD (relative pivot floor 1e-13), else 0.
+__global__ void __launch_bounds__(128) coarse_einv_kernel(const double* __restrict__ red, int nb,
+                                                         double* __restrict__ einv) {
+    constexpr int K = kCoarse, KK = kCoarse * kCoarse;
+    __shared__ double E[KK];
+    for (int t = threadIdx.x; t < KK; t += 128) {
+        double v = 0.0;
+        for (int b = 0; b < nb; ++b) v += red[static_cast<long long>(b) * KK + t];
+        E[t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double L[KK], dmax = 0.0;
+    for (int a = 0; a < K; ++a)
+        for (int b = 0; b < K; ++b) L[a * K + b] = 0.5 * (E[a * K + b] + E[b * K + a]);
+    for (int a = 0; a < K; ++a) dmax = fmax(dmax, L[a * K + a]);
+    bool ok = dmax > 0.0 && isfinite(dmax);
+    for (int k = 0; k < K && ok; ++k) {
+        double d = L[k * K + k];
+        for (int m = 0; m < k; ++m) d -= L[k * K + m] * L[k * K + m];
+        if (!(d > 1e-13 * dmax)) {
+            ok = false;
+            break;
+        }
+        const double l = sqrt(d);
+        L[k * K + k] = l;
+        for (int a = k + 1; a < K; ++a) {
+            double v = L[a * K + k];
+            for (int m = 0; m < k; ++m) v -= L[a * K + m] * L[k * K + m];
+            L[a * K + k] = v / l;
+        }
+    }
+    if (!ok) {
+        for (int t = 0; t <= KK; ++t) einv[t] = 0.0;
+        return;
+    }
+    // E^-1 = L^-T L^-1, column by column of the identity
+    for (int col = 0; col < K; ++col) {
+        double y[K];
+        for (int a = 0; a < K; ++a) {
+            double v = a == col ? 1.0 : 0.0;
+            for (int m = 0; m < a; ++m) v -= L[a * K + m] * y[m];
+            y[a] = v / L[a * K + a];
+        }
+        for (int a = K - 1; a >= 0; --a) {
+            double v = y[a];
+            for (int m = a + 1; m < K; ++m) v -= L[m * K + a] * y[m];
+            y[a] = v / L[a * K + a];
+        }
+        for (int a = 0; a < K; ++a) einv[a * K + col] = y[a];
+    }
+    einv[KK] = 1.0;
+}
+
+// Block partials of a . b (FP64).
+__global__ void __launch_bounds__(kVT) dot_partials(const double* __restrict__ a, const double* __restrict__ b, int n,
+                                                   double* __restrict__ red) {
+    __shared__ double sh[kVT / 32];
+    const int i = blockIdx.x * kVT + threadIdx.x;
+    const double t = block_sum<kVT>(i < n ? a[i] * b[i] : 0.0, sh);
+    if (threadIdx.x == 0) red[blockIdx.x] = t;
+}
+
 // alpha = rz / p.q (every block sums the p.q partials in the same order);
 // x += alpha p, r -= alpha q, z = M r; partials r.r and r.z. Nine threads per camera.
+// With a coarse basis Z (learned form; Zc non-null) z is left to coarse_w /
+// coarse_z: this kernel writes the partials of Z^T r (kCoarse per block) instead.
 __global__ void __launch_bounds__(kUT) pcg_update(double* __restrict__ x, double* __restrict__ r,
                                                  double* __restrict__ z, const double* __restrict__ p,
                                                  const double* __restrict__ q, const double* __restrict__ Minv, int C,
                                                  const double* __restrict__ red_pq, int n_pq,
                                                  double* __restrict__ red_rr, double* __restrict__ red_rz,
-                                                 double* __restrict__ sc) {
+                                                 double* __restrict__ sc, const double* __restrict__ Zc,
+                                                 double* __restrict__ red_zr) {
     __shared__ double sh[kUT / 32];
     __shared__ double rs[kUT];
     __shared__ double bc;
@@ -729,6 +946,12 @@ __global__ void __launch_bounds__(kUT) pcg_update(double* __restrict__ x, double
         x[i] += alpha * p[i];
         ri = r[i] - alpha * q[i];
         r[i] = ri;
+    }
+    if (Zc) {
+        coarse_partials(Zc, 9ll * C, i, c < C ? ri : 0.0, sh, red_zr);
+        const double a = block_sum<kUT>(ri * ri, sh);
+        if (threadIdx.x == 0) red_rr[blockIdx.x] = a;
+        return;
     }
     rs[threadIdx.x] = ri;
     __syncthreads();
@@ -785,10 +1008,13 @@ __global__ void __launch_bounds__(kVT) pcg_direction(double* __restrict__ p, flo
 }
 
 // x = 0, r = b, z = M b, p = z; partials b.b and r.z. Nine threads per camera.
+// With a coarse basis (Zc non-null): x = 0, r = b and the partials b.b and Z^T b;
+// coarse_w / coarse_z then form z = p and the r.z partials.
 __global__ void __launch_bounds__(kUT) pcg_init(double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
                                                double* __restrict__ p, float* __restrict__ p32,
                                                const double* __restrict__ b, const double* __restrict__ Minv, int C,
-                                               double* __restrict__ red_rr, double* __restrict__ red_rz) {
+                                               double* __restrict__ red_rr, double* __restrict__ red_rz,
+                                               const double* __restrict__ Zc, double* __restrict__ red_zr) {
     __shared__ double sh[kUT / 32];
     __shared__ double rs[kUT];
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
@@ -799,6 +1025,12 @@ __global__ void __launch_bounds__(kUT) pcg_init(double* __restrict__ x, double* 
         ri = b[i];
         x[i] = 0.0;
         r[i] = ri;
+    }
+    if (Zc) {
+        coarse_partials(Zc, 9ll * C, i, c < C ? ri : 0.0, sh, red_zr);
+        const double a = block_sum<kUT>(ri * ri, sh);
+        if (threadIdx.x == 0) red_rr[blockIdx.x] = a;
+        return;
     }
     rs[threadIdx.x] = ri;
     __syncthreads();
@@ -940,17 +1172,6 @@ __device__ __forceinline__ void inverse_from_factor_lane(double (&x)[45], double
         }
 }
 
-__global__ void __launch_bounds__(kSL) precond_inverse_lane(const double* __restrict__ L, int C,
-                                                           double* __restrict__ Minv) {
-    const int c = blockIdx.x * kSL + threadIdx.x;
-    if (c >= C) return;
-    const double* Lc = L + 45ll * c;
-    double x[45];
-#pragma unroll
-    for (int t = 0; t < 45; ++t) x[t] = Lc[t];
-    inverse_from_factor_lane(x, Minv + 81ll * c);
-}
-
 // One camera per lane: S_cc = U_lambda,c - (chunk sums from the right-hand
 // side pass, in chunk order), stored full FP64, its block-Jacobi factor and,
 // when Minv is given (no learned correction of the factor follows), the
@@ -990,23 +1211,6 @@ __global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict
 #pragma unroll
     for (int t = 0; t < 45; ++t) Lc[t] = a[t];
     if (Minv) inverse_from_factor_lane(a, Minv + 81ll * c);
-}
-
-// Block-Jacobi factors from stored diagonal blocks, one camera per lane.
-__global__ void __launch_bounds__(kSL) factor_blocks_lane(const double* __restrict__ Sdiag, int C,
-                                                         double* __restrict__ L) {
-    const int c = blockIdx.x * kSL + threadIdx.x;
-    if (c >= C) return;
-    const double* Sc = Sdiag + 81ll * c;
-    double a[45];
-#pragma unroll
-    for (int i = 0; i < 9; ++i)
-#pragma unroll
-        for (int j = 0; j <= i; ++j) a[blk::tri(i, j)] = Sc[9 * i + j];
-    chol9_lane(a);
-    double* Lc = L + 45ll * c;
-#pragma unroll
-    for (int t = 0; t < 45; ++t) Lc[t] = a[t];
 }
 
 }  // namespace
@@ -1105,20 +1309,15 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
     GBA_LAUNCH_CHECK();
 
-    // block-Jacobi blocks (partials from the right-hand side pass) and factors
-    // (+ learned correction)
-    // Pinv_ is current for Pfac_ (set by the fused inverse or the inverse kernel,
-    // cleared whenever the factors change).
-    bool pinv_valid = !(learned && learned_choice_ != 2);
+    // block-Jacobi blocks (partials from the right-hand side pass), factors and
+    // explicit inverses
     cudaEvent_t bj_ev = prof_start();
     sdiag_finalize_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
-                                                               C_, Sdiag_.get(), Pfac_.get(),
-                                                               pinv_valid ? Pinv_.get() : nullptr);
+                                                               C_, Sdiag_.get(), Pfac_.get(), Pinv_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("bj_blocks", bj_ev);
     if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
-    // Learned factors are used once they have won the judged solve (below).
-    if (learned && learned_choice_ == 1) model_->correct_factors(*this, lambda);
+    if (learned && precond_force_ != 0) learned_choice_ = precond_force_;
 
     double bnorm2 = 0.0;
     unsigned long long nonspd = 0;
@@ -1138,21 +1337,34 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     }
     double rnorm2 = bnorm2;
     const double tol2 = opts.refine_tol * opts.refine_tol * bnorm2;
-    // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_). Returns the
-    // iteration count; *ok = reached the inner tolerance without breakdown;
-    // inner_rel2 = its final ||r||^2 / ||b||^2.
+    // The learned coarse space (basis, S Z, E^-1) is formed once per trial, when
+    // an inner solve first needs it.
+    bool coarse_ready = false;
+    // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_), preconditioned by
+    // block-Jacobi, or by the balancing two-level form with the learned coarse
+    // basis (coarse). Returns the iteration count; *ok = reached the inner
+    // tolerance without breakdown; inner_rel2 = its final ||r||^2 / ||b||^2.
     double inner_rel2 = 0.0;
-    auto inner_pcg = [&](bool* ok) -> long long {
-        if (!pinv_valid) {
-            cudaEvent_t inv_ev = prof_start();
-            precond_inverse_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Pfac_.get(), C_, Pinv_.get());
-            GBA_LAUNCH_CHECK();
-            prof_stop("bj_inverse", inv_ev);
-            pinv_valid = true;
+    auto inner_pcg = [&](bool* ok, bool coarse) -> long long {
+        if (coarse && !coarse_ready) {
+            coarse_prepare(lambda);
+            coarse_ready = true;
         }
+        const double* Zc = coarse ? cz_.get() : nullptr;
+        double* red_zr = cred_.get();
+        double* red_szw = red_zr + 1ll * nub * kCoarse;
+        double* c1 = red_szw + 1ll * nub * kCoarse;
         pcg_init<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
-                                           ref_r_.get(), Pinv_.get(), C_, red, red2);
+                                           ref_r_.get(), Pinv_.get(), C_, red, red2, Zc, red_zr);
         GBA_LAUNCH_CHECK();
+        if (coarse) {
+            coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz_.get(), Pinv_.get(), ceinv_.get(), C_, red_zr, nub, c1,
+                                               pcg_z_.get(), red_szw, sc, 1);
+            GBA_LAUNCH_CHECK();
+            coarse_z<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), Zc, ceinv_.get(), C_, red_szw, nub, c1, pcg_z_.get(),
+                                               pcg_p_.get(), pcg_p32_.get(), red2, sc, 1);
+            GBA_LAUNCH_CHECK();
+        }
         pcg_init_finalize<<<1, 256, 0, stream_>>>(red, red2, nub, opts.pcg_tol, sc);
         GBA_LAUNCH_CHECK();
         // p.q partials (nvb) and r.r / r.z partials (nub) in disjoint ranges
@@ -1171,8 +1383,19 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                                                          pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
                 GBA_LAUNCH_CHECK();
                 pcg_update<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(),
-                                                     pcg_q_.get(), Pinv_.get(), C_, red_pq, nvb, red, red2, sc);
+                                                     pcg_q_.get(), Pinv_.get(), C_, red_pq, nvb, red, red2, sc, Zc,
+                                                     red_zr);
                 GBA_LAUNCH_CHECK();
+                if (coarse) {
+                    cudaEvent_t cev = prof_start();
+                    coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz_.get(), Pinv_.get(), ceinv_.get(), C_, red_zr,
+                                                       nub, c1, pcg_z_.get(), red_szw, sc, 0);
+                    GBA_LAUNCH_CHECK();
+                    coarse_z<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), Zc, ceinv_.get(), C_, red_szw, nub, c1,
+                                                       pcg_z_.get(), nullptr, nullptr, red2, sc, 0);
+                    GBA_LAUNCH_CHECK();
+                    prof_stop("coarse_apply", cev);
+                }
                 pcg_direction<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_p32_.get(), pcg_z_.get(), n, red, red2,
                                                         nub, opts.pcg_max_iters, sc);
                 GBA_LAUNCH_CHECK();
@@ -1185,25 +1408,39 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         prev_inner_ = static_cast<int>(h[S_ITERS]);
         return static_cast<long long>(h[S_ITERS]);
     };
+    // b . x of the inner solution pcg_x_ (b = ref_r_, the inner right-hand side) into sc[slot]
+    auto btx = [&](int slot) {
+        dot_partials<<<nvb, kVT, 0, stream_>>>(ref_r_.get(), pcg_x_.get(), n, red);
+        GBA_LAUNCH_CHECK();
+        sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, slot);
+        GBA_LAUNCH_CHECK();
+    };
     bool use_learned = learned && learned_choice_ == 1;
     for (int step = 0; step < opts.refine_max_steps && rnorm2 > tol2; ++step) {
         bool ok = false;
         long long it_count = 0;
         if (learned && learned_choice_ == 0) {
-            // Block-Jacobi judges the learned factors on the first inner solve of
-            // the LM solve: both preconditioners solve it, and the one that
-            // reaches the inner tolerance in fewer iterations serves for the rest
-            // of the solve. Both solves count in pcg_iterations.
+            // Block-Jacobi judges the learned correction on the first inner solve
+            // of the LM solve: both preconditioners solve it; the learned one
+            // serves the rest of the solve if it needed at most 4/5 of
+            // block-Jacobi's iterations and its step is no worse in the S-norm.
+            // For PCG iterates from x = 0, ||x* - x||_S^2 = b.x* - b.x, so the
+            // step with the larger b.x has the smaller S-norm error. Both solves
+            // count in pcg_iterations.
             bool ok_bj = false, ok_l = false;
-            const long long it_bj = inner_pcg(&ok_bj);
+            const long long it_bj = inner_pcg(&ok_bj, false);
             const double rel2_bj = inner_rel2;
+            btx(S_BTX0);
             GBA_CUDA_CHECK(cudaMemcpyAsync(judge_x_.get(), pcg_x_.get(), n * sizeof(double),
                                            cudaMemcpyDeviceToDevice, stream_));
-            model_->correct_factors(*this, lambda);
-            pinv_valid = false;
-            const long long it_l = inner_pcg(&ok_l);
+            const long long it_l = inner_pcg(&ok_l, true);
+            btx(S_BTX1);
+            double bx[2];
+            read_back({{bx, sc + S_BTX0, sizeof bx}});
             judge_iters_[0] = it_bj;
             judge_iters_[1] = it_l;
+            judge_btx_[0] = bx[0];
+            judge_btx_[1] = bx[1];
             // Solves shorter than kJudgeMin iterations are too short to compare:
             // keep block-Jacobi for now and judge again at the next inner solve.
             // After kJudgeAttempts indecisive judgements block-Jacobi is kept:
@@ -1213,7 +1450,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             ++judge_attempts_;
             const int attempts = opts.pcg_tol >= kShortInnerTol ? 1 : kJudgeAttempts;
             const bool decisive = std::max(it_bj, it_l) >= kJudgeMin || !ok_bj || !ok_l;
-            if (decisive && ok_l && (!ok_bj || it_l * kLearnedWinDen <= it_bj * kLearnedWinNum)) {
+            const bool no_worse = bx[1] >= bx[0] * (1.0 - opts.pcg_tol * opts.pcg_tol);
+            if (decisive && ok_l && (!ok_bj || (it_l * kLearnedWinDen <= it_bj * kLearnedWinNum && no_worse))) {
                 learned_choice_ = 1;
                 use_learned = true;
                 st.pcg_iterations += it_bj;
@@ -1224,27 +1462,21 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                 inner_rel2 = rel2_bj;
                 GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
                                                cudaMemcpyDeviceToDevice, stream_));
-                factor_blocks_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
-                GBA_LAUNCH_CHECK();
-                pinv_valid = false;
                 st.pcg_iterations += it_l;
                 it_count = it_bj;
                 ok = ok_bj;
             }
         } else {
-            it_count = inner_pcg(&ok);
+            it_count = inner_pcg(&ok, use_learned);
         }
         if (use_learned && !ok) {
-            // Block-Jacobi judges the learned factors: an inner solve that breaks
-            // down or misses its tolerance is redone with the plain blocks, which
-            // then serve for the rest of this trial.
-            factor_blocks_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(Sdiag_.get(), C_, Pfac_.get());
-            GBA_LAUNCH_CHECK();
-            pinv_valid = false;
+            // Block-Jacobi is the fallback: an inner solve with the coarse
+            // correction that breaks down or misses its tolerance is redone with
+            // block-Jacobi alone, which then serves for the rest of this trial.
             use_learned = false;
             ++st.fallbacks;
             st.pcg_iterations += it_count;
-            it_count = inner_pcg(&ok);
+            it_count = inner_pcg(&ok, false);
         }
         const double iters = static_cast<double>(it_count);
         if (fast && step == 0 && ok && inner_rel2 <= tol2 / bnorm2) {
@@ -1273,6 +1505,39 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     st.rel_residual = std::sqrt(rnorm2 / bnorm2);
     st.converged = rnorm2 <= tol2;
     return st;
+}
+
+// Learned coarse space for this trial: the basis Z from the network at the
+// current cameras, SZ = S Z (kCoarse FP32 implicit products, FP64 finalize), and
+// E^-1 = (Z^T S Z)^-1 (FP64 Cholesky on the device; flagged off if E is not SPD).
+void Solver::coarse_prepare(double lambda) {
+    const int n = 9 * C_;
+    const int nvb = ceil_div(n, kVT);
+    const int nub = ceil_div(C_, kUC);
+    const size_t need_red = 2ull * nub * kCoarse + kCoarse + 1ull * nvb * kCoarse * kCoarse;
+    if (!cz_.get()) {
+        StreamAllocScope scope(stream_);
+        cz_.alloc(1ull * kCoarse * n);
+        csz_.alloc(1ull * kCoarse * n);
+        ceinv_.alloc(kCoarse * kCoarse + 1);
+        cred_.alloc(need_red);
+    }
+    cudaEvent_t ev = prof_start();
+    model_->coarse_basis(*this, lambda, cz_.get());
+    for (int j = 0; j < kCoarse; ++j) {
+        to_x32_kernel<<<nvb, kVT, 0, stream_>>>(cz_.get() + 1ll * j * n, n, pcg_p32_.get());
+        GBA_LAUNCH_CHECK();
+        implicit_parts<float>(*this, pcg_p32_.get(), 0.0, nullptr);
+        coarse_q_kernel<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
+                                                  cz_.get() + 1ll * j * n, C_, csz_.get() + 1ll * j * n);
+        GBA_LAUNCH_CHECK();
+    }
+    double* gram = cred_.get() + 2ll * nub * kCoarse + kCoarse;
+    coarse_gram_partials<<<nvb, kVT, 0, stream_>>>(cz_.get(), csz_.get(), n, gram);
+    GBA_LAUNCH_CHECK();
+    coarse_einv_kernel<<<1, 128, 0, stream_>>>(gram, nvb, ceinv_.get());
+    GBA_LAUNCH_CHECK();
+    prof_stop("coarse_basis", ev);
 }
 
 }  // namespace gba

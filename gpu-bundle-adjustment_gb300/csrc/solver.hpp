@@ -249,10 +249,17 @@ public:
     DevBuf<float> g_cm_;     // per-slot G_e = Jp V'^-1 Jp^T (00, 01, 11, pad) at camera-major positions
     DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
     DevBuf<float> mlp_stats_;  // learned form: per-camera track statistics (3 per camera)
-    // Learned form, per solve: 0 = not judged yet, 1 = learned factors won the
-    // first inner solve, 2 = block-Jacobi won (used for the rest of the solve).
+    // learned form: coarse basis Z (kCoarse columns of 9C), S Z, E^-1 (+ SPD flag),
+    // and the partial sums of the balancing preconditioner and of E
+    DevBuf<double> cz_, csz_, ceinv_, cred_;
+    void coarse_prepare(double lambda);  // pcg.cu
+    // Learned form, per solve: 0 = not judged yet, 1 = the learned coarse
+    // correction won the first inner solve, 2 = block-Jacobi won (used for the
+    // rest of the solve).
     int learned_choice_ = 0;
+    int precond_force_ = 0;              // learned form: 0 judge, 1 always learned, 2 always block-Jacobi
     long long judge_iters_[2] = {0, 0};  // inner PCG iterations of the judged solve: block-Jacobi, learned
+    double judge_btx_[2] = {0, 0};       // b . x of the judged solve's two steps (larger: smaller S-norm error)
     int judge_attempts_ = 0;             // judgements made in this solve
     bool fast_solve_ = false;            // the last Schur solve ran the loose-target FP32 path
     int prev_inner_ = 0;                 // iterations of the last inner PCG solve (launch-batch predictor)

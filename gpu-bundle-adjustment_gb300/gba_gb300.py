@@ -150,8 +150,9 @@ _SIG = {
     "gba_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "gba_mlp_get_grads": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "gba_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
-    "gba_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
-                                    C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gba_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "gba_solver_set_preconditioner": (C.c_int, [C.c_void_p, C.c_int]),
+    "gba_solver_judge_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "gba_mlp_adam_step": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]),
     "gba_solver_buffer_size": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
     "gba_solver_download": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
@@ -472,6 +473,16 @@ class Solver:
     def reset_params(self) -> None:
         _check(lib.gba_solver_reset_params(self.h))
 
+    def set_preconditioner(self, mode: str = "judge") -> None:
+        """Learned form: "judge" (default), "learned" (always) or "block-jacobi" (never learned)."""
+        _check(lib.gba_solver_set_preconditioner(self.h, {"judge": 0, "learned": 1, "block-jacobi": 2}[mode]))
+
+    def judge_info(self):
+        """Last judged solve: ((block-Jacobi, learned) PCG iterations, (block-Jacobi, learned) b.x)."""
+        it, bx = (C.c_longlong * 2)(), (C.c_double * 2)()
+        _check(lib.gba_solver_judge_info(self.h, it, bx))
+        return (it[0], it[1]), (bx[0], bx[1])
+
     def set_loss(self, loss: str = "none", delta: float = 1.0) -> None:
         _check(lib.gba_solver_set_loss(self.h, LOSSES[loss], delta))
 
@@ -535,9 +546,11 @@ def solver_features(solver: "Solver", lam: float, feat_dev: int) -> None:
 
 
 class Mlp:
-    """The learned block-Jacobi correction network (gba_mlp)."""
+    """The learned coarse-basis network (gba_mlp): per-camera features (64) -> 96 outputs,
+    the first 81 of which are the camera's 9 x 9 rows of the coarse basis (row-major)."""
 
     NUM_PARAMS = int(lib.gba_mlp_num_params())
+    N_IN, N_OUT, N_USED_OUT, K = 64, 96, 81, 9
 
     def __init__(self, seed: int = 0, capacity: int = 4096, path=None):
         h = C.c_void_p()
@@ -578,11 +591,9 @@ class Mlp:
     def forward(self, feat_dev: int, batch: int, out_dev: int, stream: int = 0) -> None:
         _check(lib.gba_mlp_forward(self.h, feat_dev, batch, out_dev, stream or None))
 
-    def loss_grad(self, feat: int, Shat: int, Lhat: int, g: int, x: int, batch: int, stream: int = 0):
-        loss, base = C.c_double(), C.c_double()
-        _check(lib.gba_mlp_loss_grad(self.h, feat, Shat, Lhat, g, x, batch, stream or None, C.byref(loss),
-                                     C.byref(base)))
-        return loss.value, base.value
+    def backward(self, feat_dev: int, d_out_dev: int, batch: int, stream: int = 0) -> None:
+        """Parameter gradients from d(loss)/d(outputs) of the last forward on feat_dev."""
+        _check(lib.gba_mlp_backward(self.h, feat_dev, d_out_dev, batch, stream or None))
 
     def adam_step(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
                   stream: int = 0) -> None:

@@ -1,16 +1,31 @@
-"""Trains the learned block-Jacobi correction on the GPU with this library's own
-MLP kernels (gba_mlp_*), from (S_cc, right-hand side, exact step) triples that
-the plain FP64 solver generates.
+"""Trains the learned coarse-space correction of block-Jacobi PCG on the GPU with
+this library's own MLP kernels (gba_mlp_forward / gba_mlp_backward /
+gba_mlp_adam_step), from reduced camera systems that the plain FP64 solver
+assembles.
 
-  python train_preconditioner.py [--out models/bj_mlp.bin] [--steps 3000]
+  python train_preconditioner.py [--out models/coarse_mlp.bin] [--epochs 300]
 
-Harvest: plain-form LM solves of the 257-camera workload (2) and the
-1,000-camera workload (3), seeds as listed in HARVEST; at every inner trial the
-damped diagonal blocks S_cc, the Schur right-hand side g and the exact dense
-step x* = S^-1 g are kept for every camera (Jacobi-scaled, see mlp.hpp).
-Training: Adam on the mean per-camera block-norm step error; 10% of the
-triples are held out. The report (JSON beside the model) gives the held-out
-loss of the network and of plain block-Jacobi (the network at zero output).
+Why a coarse space: the Jacobi-preconditioned reduced camera system
+B^-1/2 S B^-T/2 (B the 9x9 diagonal blocks) has a handful of eigenvalues far
+below the rest: the 7-dimensional similarity gauge of bundle adjustment (only
+the LM damping holds it) and a few soft modes. They set block-Jacobi PCG's
+iteration count at tight tolerances, and a block-diagonal correction cannot
+touch them. The network predicts, per camera, its rows Z_c (9 x 9) of a basis
+whose span should contain those eigenvectors; the solver then adds the
+balancing two-level correction built from Z (see csrc/mlp.hpp).
+
+Harvest: plain-form LM solves driven stage by stage on the HARVEST problems; at
+each inner trial (up to PER_PROBLEM per problem) the dense S is factored on
+the device; its factor, the diagonal blocks S_cc, the features and the cameras
+are kept, and the M lowest eigenvectors of the Jacobi-preconditioned S are
+computed on the host.
+
+Loss per system: the weighted share of those eigenvectors outside span(B^T Z)
+(coarse_loss_and_grad, the gradient w.r.t. the network outputs in closed
+form); the network's parameter gradients come from the library's backward
+kernels. Adam, one system per step. The report (JSON beside the model) gives
+the held-out loss and the evaluation solves (block-Jacobi vs learned, inner
+PCG iterations at the strict Schur targets).
 """
 from __future__ import annotations
 
@@ -25,17 +40,19 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 sys.path.insert(0, str(PKG))
 
+K = 9            # coarse basis columns per camera
+M_EIG = 9        # lowest eigenvectors per system in the loss
+PER_PROBLEM = 12
 # (problem, seed, LM iterations); a problem is a workload id or the generator
 # parameters (cameras, points, track_min, track_max, alpha, outlier share,
-# outlier sigma). The last two have the track and outlier statistics of
-# workload 5 at a size the plain dense solver handles in seconds.
+# outlier sigma). The last one has the track and outlier statistics of
+# workload 5 at a size whose dense S the host eigensolver handles in seconds.
 HARVEST = [
-    (2, 2, 30), (2, 12, 30), (3, 3, 25), (3, 13, 25),
-    ((1000, 300000, 2, 200, 2.2, 0.05, 20.0), 21, 20),
-    ((600, 180000, 2, 200, 2.2, 0.05, 20.0), 22, 20),
+    (2, 2, 20), (2, 12, 20), (2, 22, 20), (2, 32, 20),
+    ((400, 120000, 2, 200, 2.2, 0.05, 20.0), 21, 15),
 ]
-# held-out problems on which the trained network is compared with block-Jacobi
-EVALUATE = [(4, 4), ((2000, 600000, 2, 200, 2.2, 0.05, 20.0), 31)]
+# held-out problems: block-Jacobi vs learned solves at the strict Schur targets
+EVALUATE = [(2, 42), (4, 4)]
 
 
 def make_problem(gba, spec, seed):
@@ -45,25 +62,68 @@ def make_problem(gba, spec, seed):
     return gba.synthetic_custom(C, P, kmin, kmax, alpha, ofrac, osig, seed)
 
 
-def _tri():
-    return [(i, j) for i in range(9) for j in range(i + 1)]
+def units(cams):
+    """Row units of the basis: 1, except the focal-length row (f of the camera)."""
+    u = np.ones((cams.shape[0], 9))
+    u[:, 6] = cams[:, 6]
+    return u
 
 
-TRI = _tri()
+def coarse_loss_and_grad(O, cams, Bl, V, w=None):
+    """Loss = sum_i w_i (1 - |Q v_i|^2) / sum w, Q the orthogonal projector onto
+    span(Zh), Zh_c = B_c^T Z_c, Z_c(i, j) = O_c[9 i + j] * unit_i; V (9C x m)
+    orthonormal eigenvectors of the Jacobi-preconditioned S, B_c (lower) the
+    Cholesky factors of its diagonal blocks. Returns (loss, dloss/dO (C x
+    O.shape[1], zero past column 81), per-vector captured share)."""
+    C = O.shape[0]
+    m = V.shape[1]
+    w = np.ones(m) if w is None else np.asarray(w, np.float64)
+    u = units(cams)
+    Z = O[:, :9 * K].astype(np.float64).reshape(C, 9, K) * u[:, :, None]
+    Zh = np.einsum("cji,cjk->cik", Bl, Z).reshape(9 * C, K)
+    G = Zh.T @ Zh
+    Ginv = np.linalg.inv(G)
+    T = Ginv @ (Zh.T @ V)                      # K x m: coefficients of Q v_i
+    PV = Zh @ T
+    cap = np.einsum("ij,ij->j", V, PV)
+    loss = float(np.sum(w * (1.0 - cap)) / np.sum(w))
+    dZh = -2.0 * ((V - PV) * w) @ T.T / np.sum(w)     # 9C x K
+    dZ = np.einsum("cij,cjk->cik", Bl, dZh.reshape(C, 9, K))
+    dO = np.zeros_like(O, dtype=np.float64)
+    dO[:, :9 * K] = (dZ * u[:, :, None]).reshape(C, 9 * K)
+    return loss, dO, cap
+
+
+def jacobi_eigvecs(L, Sdiag, C, m):
+    """Lowest m eigenvectors of B^-1 S B^-T, S = L L^T (n x n lower factor), B_c =
+    chol(S_cc); returns (eigenvalues, eigenvectors, B (C, 9, 9))."""
+    import scipy.linalg as sl
+
+    n = 9 * C
+    Bl = np.linalg.cholesky(Sdiag)
+    G = np.empty((n, n))
+    for c in range(C):
+        G[9 * c:9 * c + 9] = sl.solve_triangular(Bl[c], L[9 * c:9 * c + 9], lower=True)
+    A = G @ G.T
+    ev, V = sl.eigh(A, subset_by_index=[0, m - 1])
+    return ev, V, Bl
 
 
 def harvest(gba, torch, spec, seed: int, iterations: int, lam0: float = 1e-3):
-    """Plain-form LM run driven stage by stage; returns per-camera training triples."""
+    """Plain-form LM run driven stage by stage; returns systems
+    {feat, cams, B, V, ev, lam}."""
     prob = make_problem(gba, spec, seed)
     C = prob.num_cameras
-    feats, blocks, gs, xs = [], [], [], []
+    systems = []
     feat_dev = torch.empty((C, 64), dtype=torch.float32, device="cuda")
+    raw = []
     with gba.Solver(prob, "plain") as s:
         gba.solver_set_harvest(s, True)
         sse = s.accumulate()
         lam = lam0
+        _, _, _, n_pad = s.dims()
         for _ in range(iterations):
-            nu, accepted = 2.0, False
+            nu, accepted, rel = 2.0, False, 0.0
             for _trial in range(16):
                 if s.damp_invert_v(lam):
                     lam, nu = lam * nu, nu * 2
@@ -73,10 +133,10 @@ def harvest(gba, torch, spec, seed: int, iterations: int, lam0: float = 1e-3):
                     continue
                 gba.solver_features(s, lam, feat_dev.data_ptr())
                 torch.cuda.synchronize()
-                feats.append(feat_dev.cpu().numpy().copy())
-                blocks.append(s.download("Sdiag").reshape(C, 9, 9))
-                gs.append(s.download("rhs")[:9 * C].reshape(C, 9))
-                xs.append(s.download("dc").reshape(C, 9))
+                cams, _ = s.get_params()
+                L = s.download("S").reshape(n_pad, n_pad).T[:9 * C, :9 * C]  # column-major -> [row, col]
+                raw.append(dict(feat=feat_dev.cpu().numpy().copy(), cams=cams.reshape(C, 9).copy(),
+                                Sdiag=s.download("Sdiag").reshape(C, 9, 9).copy(), L=np.tril(L), lam=lam))
                 denom = s.back_substitute(lam)
                 if not denom > 0:
                     lam, nu = lam * nu, nu * 2
@@ -98,33 +158,18 @@ def harvest(gba, torch, spec, seed: int, iterations: int, lam0: float = 1e-3):
             if not accepted or rel < 1e-6:
                 break
             s.accumulate()
-    return np.concatenate(feats), np.concatenate(blocks), np.concatenate(gs), np.concatenate(xs)
-
-
-def scale(blocks, gs, xs):
-    """Jacobi-scaled packed S^, its Cholesky factor, g^ and x^; drops blocks that
-    are not numerically SPD."""
-    d = np.sqrt(np.maximum(np.einsum("bii->bi", blocks), 1e-300))
-    Sh = blocks / (d[:, :, None] * d[:, None, :])
-    keep = np.ones(len(blocks), bool)
-    Lh = np.zeros_like(Sh)
-    for b in range(len(blocks)):
-        try:
-            Lh[b] = np.linalg.cholesky(Sh[b])
-        except np.linalg.LinAlgError:
-            keep[b] = False
-    ii = np.array([i for i, _ in TRI])
-    jj = np.array([j for _, j in TRI])
-    pk = lambda M: M[:, ii, jj]  # noqa: E731
-    ok = keep & np.isfinite(xs).all(1) & (np.abs(xs).sum(1) > 0)
-    return ok, pk(Sh), pk(Lh), gs / d, xs * d
+    keep = np.unique(np.linspace(0, len(raw) - 1, min(PER_PROBLEM, len(raw))).astype(int))
+    for i in keep:
+        r = raw[i]
+        ev, V, Bl = jacobi_eigvecs(r["L"], r["Sdiag"], C, M_EIG)
+        systems.append(dict(feat=r["feat"], cams=r["cams"], B=Bl, V=V, ev=ev, lam=r["lam"]))
+    return systems
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=str(PKG / "models" / "bj_mlp.bin"))
-    ap.add_argument("--steps", type=int, default=3000)
-    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--out", default=str(PKG / "models" / "coarse_mlp.bin"))
+    ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
@@ -137,54 +182,58 @@ def main():
     import gba_gb300 as gba
 
     t0 = time.time()
-    F, Sb, G, X = [], [], [], []
+    systems = []
     for spec, seed, iters in HARVEST:
-        f, s, g, x = harvest(gba, torch, spec, seed, iters)
-        F.append(f)
-        Sb.append(s)
-        G.append(g)
-        X.append(x)
-        print(f"harvested {spec} seed {seed}: {len(f)} camera samples", flush=True)
-    F, Sb, G, X = map(np.concatenate, (F, Sb, G, X))
-    ok, Sh, Lh, Gh, Xh = scale(Sb, G, X)
-    F, Sh, Lh, Gh, Xh = F[ok], Sh[ok], Lh[ok], Gh[ok], Xh[ok]
-    n = len(F)
+        got = harvest(gba, torch, spec, seed, iters)
+        systems += [dict(s, problem=str(spec), seed=seed) for s in got]
+        print(f"harvested {spec} seed {seed}: {len(got)} systems ({time.time() - t0:.0f} s)", flush=True)
     rng = np.random.default_rng(args.seed)
-    perm = rng.permutation(n)
-    n_val = max(1, n // 10)
-    val, tr = perm[:n_val], perm[n_val:]
-    dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dt)  # noqa: E731
-    D = {k: dev(v, torch.float64) for k, v in (("S", Sh), ("L", Lh), ("g", Gh), ("x", Xh))}
-    D["f"] = dev(F, torch.float32)
+    perm = rng.permutation(len(systems))
+    n_val = max(1, len(systems) // 8)
+    val, tr = [systems[i] for i in perm[:n_val]], [systems[i] for i in perm[n_val:]]
+    cap = max(s["feat"].shape[0] for s in systems)
+    mlp = gba.Mlp(seed=args.seed, capacity=cap)
+    out_dev = torch.empty((cap, gba.Mlp.N_OUT), dtype=torch.float32, device="cuda")
+    feats = [torch.from_numpy(s["feat"]).cuda() for s in systems]
+    fidx = {id(s): i for i, s in enumerate(systems)}
 
-    mlp = gba.Mlp(seed=args.seed, capacity=max(args.batch, n_val))
+    def run(sysd, train):
+        f = feats[fidx[id(sysd)]]
+        C = f.shape[0]
+        mlp.forward(f.data_ptr(), C, out_dev.data_ptr())
+        O = out_dev[:C].cpu().numpy()
+        loss, dO, capt = coarse_loss_and_grad(O, sysd["cams"], sysd["B"], sysd["V"])
+        if train:
+            d = torch.from_numpy(dO.astype(np.float32)).cuda()
+            mlp.backward(f.data_ptr(), d.data_ptr(), C)
+        return loss, capt
 
-    def batch_ptrs(idx):
-        t = torch.from_numpy(idx).to("cuda")
-        parts = {k: v.index_select(0, t).contiguous() for k, v in D.items()}
-        return parts, [parts[k].data_ptr() for k in ("f", "S", "L", "g", "x")]
-
-    vparts, vptr = batch_ptrs(val)
-    v0, vb = mlp.loss_grad(*vptr, len(val))
-    history = [(0, v0, vb)]
-    for step in range(1, args.steps + 1):
-        idx = rng.choice(tr, size=min(args.batch, len(tr)), replace=False)
-        parts, ptr = batch_ptrs(idx)
-        loss, _ = mlp.loss_grad(*ptr, len(idx))
-        lr = args.lr * (0.5 * (1 + np.cos(np.pi * step / args.steps)))  # cosine decay
-        mlp.adam_step(lr)
-        if step % 250 == 0 or step == args.steps:
-            vl, vb = mlp.loss_grad(*vptr, len(val))
-            history.append((step, vl, vb))
-            print(f"step {step}: train {loss:.4f} held-out {vl:.4f} (block-Jacobi {vb:.4f})", flush=True)
+    history = []
+    steps = args.epochs * len(tr)
+    step = 0
+    for ep in range(args.epochs):
+        tot = 0.0
+        for i in rng.permutation(len(tr)):
+            loss, _ = run(tr[i], True)
+            lr = args.lr * 0.5 * (1 + np.cos(np.pi * step / steps))
+            mlp.adam_step(lr)
+            tot += loss
+            step += 1
+        if ep % 25 == 0 or ep == args.epochs - 1:
+            vl = float(np.mean([run(s, False)[0] for s in val]))
+            history.append((ep, tot / len(tr), vl))
+            print(f"epoch {ep}: train {tot / len(tr):.4f} held-out {vl:.4f}", flush=True)
     out = Path(args.out)
     out.parent.mkdir(parents=True, exist_ok=True)
     mlp.save(out)
+    held_cap = np.mean([run(s, False)[1] for s in val], axis=0)
+
     evaluation = []
+    strict = dict(refine_tol=1e-8, pcg_tol=1e-4, max_iterations=30)
     for spec, seed in EVALUATE:
         prob = make_problem(gba, spec, seed)
-        bj = gba.solve(prob.copy(), form="mixed", max_iterations=30)
-        le = gba.solve(prob.copy(), form="learned", model_path=str(out), max_iterations=30)
+        bj = gba.solve(prob.copy(), form="mixed", **strict)
+        le = gba.solve(prob.copy(), form="learned", model_path=str(out), **strict)
         evaluation.append({
             "problem": spec, "seed": seed, "cameras": prob.num_cameras, "observations": prob.num_observations,
             "block_jacobi": {"pcg_iterations": bj.pcg_iterations, "final_cost": bj.final_cost,
@@ -197,11 +246,12 @@ def main():
         print(json.dumps(evaluation[-1]), flush=True)
     report = {
         "evaluation": evaluation,
-        "samples": int(n), "held_out": int(n_val), "harvest": HARVEST, "steps": args.steps, "batch": args.batch,
-        "lr": args.lr, "seconds": time.time() - t0,
-        "held_out_loss": history[-1][1], "held_out_block_jacobi_loss": history[-1][2],
+        "systems": len(systems), "held_out": n_val, "harvest": HARVEST, "epochs": args.epochs, "lr": args.lr,
+        "seconds": time.time() - t0, "held_out_loss": history[-1][2],
+        "held_out_captured_share_per_eigenvector": held_cap.tolist(),
+        "held_out_eigenvalues_mean": np.mean([s["ev"] for s in val], axis=0).tolist(),
         "history": history,
-        "loss": "mean over cameras of (y - x*)^T S^ (y - x*) / (x*^T S^ x*), y = learned block step",
+        "loss": f"share of the {M_EIG} lowest eigenvectors of the Jacobi-preconditioned S outside span(B^T Z)",
     }
     out.with_suffix(".json").write_text(json.dumps(report, indent=1))
     print(json.dumps({k: v for k, v in report.items() if k != "history"}))

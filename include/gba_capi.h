@@ -204,19 +204,28 @@ int gba_release_cached_memory(void);
 
 /* ------------------------------------------------------------ learned preconditioner
  * No reference counterpart (the reference has no iterative solver). The MLP
- * maps per-camera features of the damped diagonal block S_cc (49, padded to
- * 64 floats) to 45 outputs (padded to 48) that correct the block's Cholesky
- * factor; see gpu-bundle-adjustment_gb300/csrc/mlp.hpp for the layout. */
+ * maps per-camera features (58, padded to 64 floats: the damped diagonal block
+ * S_cc, track statistics, the camera's parameters) to the camera's 9 x 9 rows
+ * of a coarse basis Z (81 outputs, padded to 96); the learned form's PCG adds
+ * the coarse-space correction of block-Jacobi built from Z. Layouts in
+ * gpu-bundle-adjustment_gb300/csrc/mlp.hpp. */
 
 /* Plain form: also keep the damped diagonal blocks S_cc (GBA_BUF_SDIAG) at each
  * gba_solver_schur_dense (training-data harvest). */
 int gba_solver_set_harvest(gba_solver* s, int enable);
-/* Features of the current S_cc blocks at damping lambda. [device] feat (C x 64 float). */
+/* Features of the current S_cc blocks and cameras at damping lambda. [device] feat (C x 64 float). */
 int gba_solver_features(gba_solver* s, double lambda, float* feat);
+/* Learned form: 0 = block-Jacobi judges the learned correction on the first
+ * inner solve of each LM solve (default), 1 = always use it, 2 = never. */
+int gba_solver_set_preconditioner(gba_solver* s, int mode);
+/* Learned form, last judged solve: inner PCG iterations and b.x of the
+ * block-Jacobi and the learned steps (the larger b.x has the smaller S-norm
+ * error). [host] iters (2), btx (2). */
+int gba_solver_judge_info(gba_solver* s, long long* iters, double* btx);
 
 typedef struct gba_mlp gba_mlp;
 long long gba_mlp_num_params(void);
-/* New network (He-initialised hidden layers, zero output layer = plain block-Jacobi). */
+/* New network (He-initialised hidden layers, small random output layer, zero biases). */
 int gba_mlp_create(uint64_t seed, int batch_capacity, gba_mlp** out);
 int gba_mlp_load(const char* path, int batch_capacity, gba_mlp** out);
 int gba_mlp_save(const gba_mlp* m, const char* path);
@@ -225,15 +234,12 @@ void gba_mlp_destroy(gba_mlp* m);
 int gba_mlp_get_params(const gba_mlp* m, float* params);
 int gba_mlp_set_params(gba_mlp* m, const float* params);
 int gba_mlp_get_grads(const gba_mlp* m, float* grads);
-/* out (B x 48) = network(feat (B x 64)). [device] */
+/* out (B x 96) = network(feat (B x 64)); keeps the activations for gba_mlp_backward. [device] */
 int gba_mlp_forward(gba_mlp* m, const float* feat, int batch, float* out, void* stream);
-/* Forward + per-camera loss + backward on a batch. [device] feat (B x 64 float),
- * Shat / Lhat (B x 45 double, packed lower: Jacobi-scaled S_cc and its Cholesky
- * factor), g / x (B x 9 double: scaled right-hand side and exact step).
- * out_loss: mean loss; out_baseline: mean loss of plain block-Jacobi. */
-int gba_mlp_loss_grad(gba_mlp* m, const float* feat, const double* Shat, const double* Lhat, const double* g,
-                      const double* x, int batch, void* stream, double* out_loss, double* out_baseline);
-/* One Adam step with the gradients of the last gba_mlp_loss_grad. */
+/* Parameter gradients of a loss from its gradient d_out (B x 96 float) w.r.t.
+ * the outputs of the last gba_mlp_forward on the same feat. [device] */
+int gba_mlp_backward(gba_mlp* m, const float* feat, const float* d_out, int batch, void* stream);
+/* One Adam step with the gradients of the last gba_mlp_backward. */
 int gba_mlp_adam_step(gba_mlp* m, float lr, float beta1, float beta2, float eps, void* stream);
 
 enum {

@@ -55,7 +55,7 @@ def test_json_schema_and_file_output(tmp_path):
     assert printed["trajectory"][0] == printed["initial_cost"]
 
 
-MODEL = ROOT / "gpu-bundle-adjustment_gb300" / "models" / "bj_mlp.bin"
+MODEL = ROOT / "gpu-bundle-adjustment_gb300" / "models" / "coarse_mlp.bin"
 
 
 @pytest.mark.gpu

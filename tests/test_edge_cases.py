@@ -15,7 +15,7 @@ import pytest
 
 from conftest import PKG, rel_err
 
-MODEL = PKG / "models" / "bj_mlp.bin"
+MODEL = PKG / "models" / "coarse_mlp.bin"
 
 
 def _ragged(gba):

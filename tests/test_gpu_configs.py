@@ -99,3 +99,68 @@ def test_mixed_workload3_first_step_true_residual(gba):
     assert relres <= 1e-8
     assert true_rel <= 1.01e-8, (true_rel, relres)
     assert abs(true_rel - relres) <= 1e-10
+
+
+MODEL = GOLDEN.parents[1] / "gpu-bundle-adjustment_gb300" / "models" / "coarse_mlp.bin"
+
+
+@pytest.mark.skipif(not MODEL.exists() or "w4" not in RUNS, reason="trained model or workload 4 run missing")
+def test_learned_vs_block_jacobi_vs_exact_workload4(gba):
+    """Workload 4 (workload 3's shape, seed 4): the learned coarse correction
+    against block-Jacobi alone and the exact dense step, on the same trial
+    (lambda 1e-3 at the initial parameters) and over whole solves.
+      - inner PCG iterations of the step refined to 1e-8 (PCG tolerance 1e-4):
+        the learned form needs at most 80% of block-Jacobi's;
+      - S-norm step error ||dc - dc*||_S / ||dc*||_S after 10 PCG iterations
+        (dc* the plain form's exact FP64 step, S its dense FP64 system): the
+        learned one is smaller; refined, both reach the FP32-Jacobian floor;
+      - whole LM solves at the strict targets: the learned form's PCG work is at
+        most 80% of block-Jacobi's and both final costs are within 0.1% of the
+        reference driver's."""
+    prob, e = _problem(gba, "w4")
+    lam = 1e-3
+    C = prob.num_cameras
+    with gba.Solver(prob, "plain") as s:
+        s.accumulate()
+        assert s.damp_invert_v(lam) == 0
+        assert s.schur_dense(lam) == 0
+        _, _, _, n_pad = s.dims()
+        L = np.tril(s.download("S").reshape(n_pad, n_pad).T[:9 * C, :9 * C])
+        dc_exact = s.download("dc")
+
+    def snorm(x):
+        y = L.T @ x
+        return float(np.sqrt(y @ y))
+
+    ref_norm = snorm(dc_exact)
+    out = {}
+    for mode in ("block-jacobi", "learned"):
+        with gba.Solver(prob, "learned") as s:
+            s.load_model(MODEL)
+            s.set_preconditioner(mode)
+            s.accumulate()
+            assert s.damp_invert_v(lam) == 0
+            iters, _, relres = s.schur_pcg(lam, learned=True, refine_tol=1e-8, pcg_tol=1e-4, pcg_max_iters=500)
+            dc = s.download("dc")
+            s.schur_pcg(lam, learned=True, refine_tol=1e-30, refine_max_steps=1, pcg_tol=0.0, pcg_max_iters=10)
+            dc10 = s.download("dc")
+        out[mode] = dict(iters=iters, relres=relres, err=snorm(dc - dc_exact) / ref_norm,
+                         err10=snorm(dc10 - dc_exact) / ref_norm)
+    bj, le = out["block-jacobi"], out["learned"]
+    print(f"w4 one trial: {out}")
+    assert bj["relres"] <= 1e-8 and le["relres"] <= 1e-8
+    assert le["iters"] <= 0.8 * bj["iters"], out
+    assert le["err10"] < bj["err10"], out
+    assert max(bj["err"], le["err"]) < 1e-3, out
+    strict = dict(refine_tol=1e-8, pcg_tol=1e-4, max_iterations=40)
+    ref_final = e["reference"]["final_cost"]
+    r_bj = gba.solve(prob.copy(), form="mixed", **strict)
+    r_le = gba.solve(prob.copy(), form="learned", model_path=str(MODEL), **strict)
+    print(f"w4 solves: block-Jacobi {r_bj.pcg_iterations} PCG / {r_bj.final_cost:.12g}; learned "
+          f"{r_le.pcg_iterations} PCG / {r_le.final_cost:.12g} (choice {r_le.learned_choice}); "
+          f"reference {ref_final:.12g}")
+    assert r_le.learned_choice == 1
+    assert r_le.pcg_iterations <= 0.8 * r_bj.pcg_iterations
+    for r in (r_bj, r_le):
+        assert r.anomalies == 0 and r.final_cost <= ref_final * (1 + 1e-3)
+        assert r.max_refine_residual <= 1e-8

@@ -189,54 +189,36 @@ def test_oracle_lm_converges_on_small_problem(gba, oracle):
     assert abs(res["initial_cost"] - gba.total_squared_error(prob) / 2) <= 1e-9 * res["initial_cost"]
 
 
-def _block_sample(rng, mlp_oracle):
-    M = rng.normal(size=(9, 9))
-    S = M @ M.T + 9 * np.eye(9)
-    S *= np.outer(np.logspace(0, 3, 9), np.logspace(0, 3, 9))  # badly scaled like camera blocks
-    g = rng.normal(size=9)
-    x = np.linalg.solve(S, g) * (1 + 0.3 * rng.normal(size=9))
-    return mlp_oracle.scaled_sample(S, g, x)
-
-
-def test_mlp_oracle_loss_gradient_vs_finite_differences():
-    """The analytic (rank-2) gradient of the block step-error loss that the GPU
-    loss kernel implements, against central differences."""
+def test_mlp_oracle_backward_through_coarse_loss_vs_finite_differences():
+    """The oracle's backward pass, fed the closed-form gradient of the coarse
+    loss (train_preconditioner.coarse_loss_and_grad), against central
+    differences of the composed loss w.r.t. the network parameters (FP64)."""
     import mlp_oracle
-
-    rng = np.random.default_rng(11)
-    for _ in range(5):
-        Sh, Lh, gh, xh = _block_sample(rng, mlp_oracle)
-        o = rng.normal(0, 0.4, 45)
-        an = mlp_oracle.sample_loss_grad(o, Sh, Lh, gh, xh)
-        fd = np.zeros(45)
-        for k in range(45):
-            e = np.zeros(45)
-            e[k] = 1e-6
-            fd[k] = (mlp_oracle.sample_loss(o + e, Sh, Lh, gh, xh) - mlp_oracle.sample_loss(o - e, Sh, Lh, gh, xh)) / 2e-6
-        assert np.max(np.abs(an - fd)) < 1e-6 * max(1.0, np.max(np.abs(fd)))
-
-
-def test_mlp_oracle_backward_vs_finite_differences():
-    import mlp_oracle
+    import train_preconditioner as tp
 
     rng = np.random.default_rng(12)
-    B = 3
-    samples = [_block_sample(rng, mlp_oracle) for _ in range(B)]
-    S, L, g, x = (np.array([s[i] for s in samples]) for i in range(4))
-    feat = np.zeros((B, 64))
-    feat[:, :49] = rng.normal(0, 0.5, (B, 49))
+    C, m = 5, 4
+    V, _ = np.linalg.qr(rng.standard_normal((9 * C, m)))
+    Bl = np.tril(rng.standard_normal((C, 9, 9))) + 3 * np.eye(9)[None]
+    cams = np.zeros((C, 9))
+    cams[:, 6] = rng.uniform(400, 600, C)
+    feat = np.zeros((C, 64))
+    feat[:, :mlp_oracle.USED_IN] = rng.normal(0, 0.5, (C, mlp_oracle.USED_IN))
     p = mlp_oracle.unpack(np.zeros(mlp_oracle.N_PARAMS))
-    p["W1"][:, :49] = rng.normal(0, 0.3, (128, 49))
+    p["W1"][:, :mlp_oracle.USED_IN] = rng.normal(0, 0.3, (128, mlp_oracle.USED_IN))
     p["b1"][:] = 0.05
     p["W2"][:] = rng.normal(0, 0.1, (128, 128))
-    p["W3"][:45] = rng.normal(0, 0.05, (45, 128))
+    p["W3"][:81] = rng.normal(0, 0.05, (81, 128))
+    p["b3"][:81] = rng.normal(0, 0.05, 81)
     flat = mlp_oracle.pack(p)
-    _, _, grad = mlp_oracle.loss_and_grads(flat, feat, S, L, g, x, emulate_bf16=False)
 
     def loss_at(v):
         o, _ = mlp_oracle.forward(v, feat, emulate_bf16=False)
-        return np.mean([mlp_oracle.sample_loss(o[b, :45], S[b], L[b], g[b], x[b]) for b in range(B)])
+        return tp.coarse_loss_and_grad(o, cams, Bl, V)[0]
 
+    o, _ = mlp_oracle.forward(flat, feat, emulate_bf16=False)
+    _, dO, _ = tp.coarse_loss_and_grad(o, cams, Bl, V)
+    grad = mlp_oracle.backward(flat, feat, dO, emulate_bf16=False)
     sizes = np.cumsum([0] + [int(np.prod(s)) for _, s in mlp_oracle.SIZES])
     idx = [sizes[0] + 5, sizes[1] + 3, sizes[2] + 700, sizes[3] + 9, sizes[4] + 129, sizes[5] + 2]
     for i in idx:
