@@ -17,7 +17,12 @@
 // serialised by the caller. Host code reaches the array only through the
 // address cudaGetSymbolAddress returns for the current device (the symbol
 // itself is a host-side stand-in); the first call on each device looks that
-// address up, so that first call should come before any stream capture.
+// address up, so that first call should come before any stream capture. The
+// address is cached per device ordinal for the life of the process: it is
+// stale after cudaDeviceReset destroys the device's primary context, and the
+// entry point must not be called on that device after such a reset. The
+// observation indices are not range-checked (the call receives no camera or
+// point counts): they must lie inside the caller's arrays.
 
 #include <mutex>
 
@@ -94,7 +99,8 @@ std::mutex g_addr_mutex;
 double* g_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device (looked up once
-// per device, with that device current).
+// per device, with that device current; valid until the device's primary
+// context is destroyed, e.g. by cudaDeviceReset).
 double* scratch_address() {
     int dev = 0;
     GBA_CUDA_CHECK(cudaGetDevice(&dev));

@@ -303,7 +303,13 @@ int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info,
  * library holds until exit; all calls share it (each call writes every slot it
  * reads), so calls that overlap on the GPU race and must be serialised by the
  * caller. The first call on a device looks up that array's device address;
- * make that first call before any stream capture. */
+ * make that first call before any stream capture. The looked-up address is
+ * kept for the life of the process: after cudaDeviceReset (or anything else
+ * that destroys the device's primary context) it is stale, so do not call
+ * this entry point again on that device after such a reset.
+ * Precondition, not checked (the call takes no camera or point counts):
+ * every obs_camera[i] lies in [0, C) and every obs_point[i] in [0, P) of the
+ * caller's cameras / points arrays. */
 int gba_cost_noalloc(const double* cameras, const double* points, const int* obs_camera, const int* obs_point,
                      const double* obs_pixel, int num_observations, double* out_sse,
                      unsigned long long* out_nonfinite, void* stream);
