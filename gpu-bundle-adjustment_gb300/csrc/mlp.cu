@@ -209,15 +209,18 @@ __global__ void features_kernel(const double* __restrict__ Sdiag, const double* 
 }
 
 // Coarse basis rows of camera c from the network outputs:
-// Z[j][9c + i] = o[9 i + j] * unit_i (unit 1, the focal-length row f_c).
-__global__ void basis_kernel(const float* __restrict__ O, const double* __restrict__ cams, int C,
-                             double* __restrict__ Z) {
+// Z[j][9c + i] = o[9 i + j] * unit_i (unit 1, the focal-length row f_c). A camera
+// without observations gets zero rows: its block of S is decoupled (only the
+// damping's 1e-12 floor), its right-hand side zero, and its step must stay zero.
+__global__ void basis_kernel(const float* __restrict__ O, const double* __restrict__ cams,
+                             const int* __restrict__ cam_off, int C, double* __restrict__ Z) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
     const double f = cams[9ll * c + 6];
+    const bool observed = cam_off[c + 1] > cam_off[c];
     const long long n = 9ll * C;
     for (int i = 0; i < 9; ++i) {
-        const double unit = i == 6 ? f : 1.0;
+        const double unit = !observed ? 0.0 : i == 6 ? f : 1.0;
         for (int j = 0; j < kCoarse; ++j) Z[j * n + 9ll * c + i] = unit * O[static_cast<long long>(kMlpOut) * c + 9 * i + j];
     }
 }
@@ -452,7 +455,7 @@ void LearnedPreconditioner::coarse_basis(Solver& s, double lambda, double* Z) {
     cudaEvent_t ev = s.prof_start();
     mlp_.forward(feat_, s.C_, out_, s.stream_);
     s.prof_stop("mlp_forward", ev);
-    basis_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(out_, s.cams_.get(), s.C_, Z);
+    basis_kernel<<<ceil_div(s.C_, kCamT), kCamT, 0, s.stream_>>>(out_, s.cams_.get(), s.cam_off_.get(), s.C_, Z);
     GBA_LAUNCH_CHECK();
 }
 
