@@ -221,18 +221,15 @@ def algorithmic_bytes(unit: str, C: int, P: int, E: int) -> float:
 
 
 def design_bytes(unit: str, C: int, P: int, E: int) -> float:
-    """DRAM bytes this implementation's kernels move per unit (its own layout; the
-    point-side passes recompute the FP32 Jacobian rows instead of storing them)."""
+    """Bytes this implementation's kernels move per unit (its own layout)."""
     if unit == "matvec":
-        # point pass: s_cam, s_pt, cam_pos, robust scale 16 + u write 8 per slot; V'^-1 24, CSR 4 and the
-        # FP32 point 16 per point; camera records (112 B) and x (48 B) per camera (L2-resident);
-        # camera pass: camera record 80 + u 8 per slot
-        return E * (24.0 + 88.0) + P * 44.0 + C * 160.0
+        # point pass: Jc32 72 + Jp32 24 + s_cam, s_pt, cam_pos 12 + u 8 per slot, V'^-1 24 + CSR 4 per
+        # point, x 36 per camera; camera pass: camera record 80 + u 8 per slot
+        return E * (116.0 + 88.0) + P * 28.0 + C * 36.0
     if unit == "edge":
-        # point pass: s_cam, s_pt, cam_pos, r 20 in, camera record 80 + robust scale 4 out per slot; point
-        # 24 in, FP32 point 16 and V / bp 72 out per point, camera record 112 per camera; camera pass:
-        # record 80 per slot
-        return E * (104.0 + 80.0) + P * 112.0 + C * 112.0
+        # point pass: indices + r 20 in, Jc32 + Jp32 96 + camera record 80 out per slot, point 24 in and
+        # V / bp 72 out per point, camera record 112 per camera; camera pass: record 80 per slot
+        return E * (196.0 + 80.0) + P * 96.0 + C * 112.0
     if unit == "cost":
         return E * 32.0 + P * 24.0 + C * 128.0
     raise KeyError(unit)
@@ -244,8 +241,10 @@ UNITS = {"matvec": ("schur_point_pass_f32", "schur_camera_pass_f32"),
 
 # DRAM bytes (read + write) per launch from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum, --clock-control none) of each kernel at workload 5; copied
-# here, not measured in this run. Empty until captured for the current kernels.
-NCU_TRAFFIC_W5: dict = {}
+# here, not measured in this run.
+NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "camera_pass_f32": None,
+                  "schur_point_pass_f32": 992.6e6 + 66.4e6, "schur_camera_pass_f32": 774.4e6 + 3.8e6,
+                  "cost_ff": 239.9e6 + 61.0e6}
 
 KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
            "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "cost_ff",

@@ -544,7 +544,6 @@ int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out) {
     return guarded([&] {
         need(out != nullptr, "null argument");
         need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_JP32, "bad buffer id");
-        if (buffer == GBA_BUF_JC32 || buffer == GBA_BUF_JP32) S(s).materialize_jacobians();
         size_t bytes = 0;
         S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &bytes);
         *out = bytes;
@@ -555,7 +554,6 @@ int gba_solver_download(gba_solver* s, int buffer, void* dst, size_t bytes) {
     return guarded([&] {
         need(dst != nullptr, "null destination");
         need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_JP32, "bad buffer id");
-        if (buffer == GBA_BUF_JC32 || buffer == GBA_BUF_JP32) S(s).materialize_jacobians();
         size_t have = 0;
         const void* src = S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &have);
         need(src != nullptr, "buffer not held by this solver form");
@@ -569,7 +567,6 @@ int gba_solver_device_ptr(gba_solver* s, int buffer, void** out) {
     return guarded([&] {
         need(out != nullptr, "null argument");
         need(buffer >= GBA_BUF_U && buffer <= GBA_BUF_JP32, "bad buffer id");
-        if (buffer == GBA_BUF_JC32 || buffer == GBA_BUF_JP32) S(s).materialize_jacobians();
         size_t have = 0;
         *out = const_cast<void*>(S(s).buffer(static_cast<gba::Solver::Buf>(buffer), &have));
     });

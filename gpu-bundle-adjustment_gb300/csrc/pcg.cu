@@ -28,7 +28,6 @@
 // No reference counterpart: the reference solves S densely on the host.
 
 #include "blocks.cuh"
-#include "camera_model.cuh"
 #include "common.cuh"
 #include "ff.cuh"
 #include "mlp.hpp"
@@ -159,54 +158,23 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// The slot's FP32 Jacobian rows J = [Jc(18), Jp(6)] at the linearisation point,
-// recomputed (matrix-free: no per-slot rows are stored) from the camera's FP32
-// record (cams32, 28 floats: R, J_l, t, f, k1, k2, branch flag), the point
-// (pts32) and the slot's robust scale w, with the same function and inputs as
-// the normal-equation pass (edge.cu) that accumulated U, V and the camera
-// records from them: w = 0 (a non-finite slot) zeroes the rows, w != 1 scales them.
-constexpr int kCamRec32 = 28;
-__device__ __forceinline__ void slot_jacobian(const float* __restrict__ cams32, int c,
-                                              const float4* __restrict__ pts32, int p, float w, float* J) {
-    float cam[kCamRec32];
-    const float4* c4 = reinterpret_cast<const float4*>(cams32 + static_cast<long long>(kCamRec32) * c);
+// J = [Jc(18), Jp(6)] of slot s
+__device__ __forceinline__ void load_j(const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long s,
+                                       float* J) {
+    const float2* qc = reinterpret_cast<const float2*>(Jc32 + 18 * s);
 #pragma unroll
-    for (int k = 0; k < kCamRec32 / 4; ++k) {
-        const float4 t = __ldg(c4 + k);
-        cam[4 * k] = t.x;
-        cam[4 * k + 1] = t.y;
-        cam[4 * k + 2] = t.z;
-        cam[4 * k + 3] = t.w;
+    for (int k = 0; k < 9; ++k) {
+        const float2 v = qc[k];
+        J[2 * k] = v.x;
+        J[2 * k + 1] = v.y;
     }
-    const float4 xp = __ldg(pts32 + p);
-    const float X[3] = {xp.x, xp.y, xp.z};
-    const float obs[2] = {0.f, 0.f};
-    float r[2];
-    model::residual_jacobian_pre(cam, X, obs, r, J, J + 18);
-    if (w == 0.f) {
+    const float2* qp = reinterpret_cast<const float2*>(Jp32 + 6 * s);
 #pragma unroll
-        for (int q = 0; q < 24; ++q) J[q] = 0.f;
-    } else if (w != 1.f) {
-#pragma unroll
-        for (int q = 0; q < 24; ++q) J[q] *= w;
+    for (int k = 0; k < 3; ++k) {
+        const float2 v = qp[k];
+        J[18 + 2 * k] = v.x;
+        J[19 + 2 * k] = v.y;
     }
-}
-
-// Jacobian rows of the slot into Jc32 (18) / Jp32 (6), slot order (inspection only).
-__global__ void __launch_bounds__(256) materialize_jacobians_kernel(const int* __restrict__ s_cam,
-                                                                   const int* __restrict__ s_pt,
-                                                                   const float* __restrict__ cams32,
-                                                                   const float4* __restrict__ pts32,
-                                                                   const float* __restrict__ jw, int E,
-                                                                   float* __restrict__ Jc32, float* __restrict__ Jp32) {
-    const int s = blockIdx.x * 256 + threadIdx.x;
-    if (s >= E) return;
-    float J[24];
-    slot_jacobian(cams32, s_cam[s], pts32, s_pt[s], jw[s], J);
-#pragma unroll
-    for (int k = 0; k < 18; ++k) Jc32[18ll * s + k] = J[k];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) Jp32[6ll * s + k] = J[18 + k];
 }
 
 // w = V'^-1 z (3x3 packed symmetric)
@@ -280,10 +248,10 @@ struct BacksubOut {
 // xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
 // kRhs: the right-hand side instantiation (xt = null, a = 1, also G).
 template <typename T, bool kBack = false, bool kRhs = false>
-__global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 3 : 4) : 2) schur_point_pass(const int4* __restrict__ prange, const int* __restrict__ pchunk, const int* __restrict__ pt_off,
+__global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int4* __restrict__ prange, const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
-                                                       const int* __restrict__ cam_pos, const float* __restrict__ cams32,
-                                                       const float4* __restrict__ pts32, const float* __restrict__ jw,
+                                                       const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
+                                                       const float* __restrict__ Jp32,
                                                        const float* __restrict__ vinv_hi,
                                                        const float* __restrict__ vinv_lo,
                                                        const double* __restrict__ bp, const T* __restrict__ xt,
@@ -346,13 +314,12 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 3 : 4) : 2) sch
             if (s < s1) {
                 key = s_pt[s];
                 q = cam_pos[s];
-                const int c = s_cam[s];
                 float J[24];
-                slot_jacobian(cams32, c, pts32, key, jw[s], J);
+                load_j(Jc32, Jp32, s, J);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
                 T xv[9];
-                load_x(xt, c, xv);
+                load_x(xt, s_cam[s], xv);
                 T t0 = zero<T>(), t1 = zero<T>();
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
@@ -410,10 +377,14 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 3 : 4) : 2) sch
         if (s < s1) {
             key = s_pt[s];
             q = cam_pos[s];
-            float J[24];
-            slot_jacobian(cams32, s_cam[s], pts32, key, jw[s], J);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
+            const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
+            const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
+            jp[0] = j01.x;
+            jp[1] = j01.y;
+            jp[2] = j23.x;
+            jp[3] = j23.y;
+            jp[4] = j45.x;
+            jp[5] = j45.y;
         }
     }
     if constexpr (kSharedVinv) {
@@ -503,9 +474,9 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 3 : 4) : 2) sch
     }
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int p = s_pt[s];
-        float J[24];
-        slot_jacobian(cams32, s_cam[s], pts32, p, jw[s], J);
-        const float* j = J + 18;
+        const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
+        const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
+        const float j[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
         T u0, u1;
         jp_times(j, wsh[p - p0][0], wsh[p - p0][1], wsh[p - p0][2], u0, u1);
         const long long q = cam_pos[s];
@@ -1255,7 +1226,7 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     float4* g = rhs ? reinterpret_cast<float4*>(s.g_cm_.get()) : nullptr;
     cudaEvent_t ev = s.prof_start();
     (rhs ? schur_point_pass<T, false, true> : schur_point_pass<T, false, false>)<<<s.n_pchunk_, kPT, 0, s.stream_>>>(reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
-                                                           s.s_pt_.get(), s.cam_pos_.get(), s.cams32_.get(), reinterpret_cast<const float4*>(s.jpts32_.get()), s.jw_.get(),
+                                                           s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
                                                            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
                                                            u, done, BacksubOut{}, g);
     GBA_LAUNCH_CHECK();
@@ -1293,11 +1264,11 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
                         s.dp_.get(), s.tpts_.get(), reinterpret_cast<float2*>(s.pts_ff_.get()), part};
     if (s.fast_solve_) {
         schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.cams32_.get(), reinterpret_cast<const float4*>(s.jpts32_.get()), s.jw_.get(),
+            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), nullptr, s.bp_.get(), s.pcg_p32_.get(), -1.0, nullptr, nullptr, bk, nullptr);
     } else {
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.cams32_.get(), reinterpret_cast<const float4*>(s.jpts32_.get()), s.jw_.get(),
+            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
             nullptr, nullptr, bk, nullptr);
     }
@@ -1568,23 +1539,6 @@ void Solver::coarse_prepare(double lambda) {
     coarse_einv_kernel<<<1, 128, 0, stream_>>>(gram, nvb, ceinv_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_basis", ev);
-}
-
-// Per-slot FP32 Jacobian rows at the linearisation point into Jc32_ / Jp32_
-// (allocated on first use): for inspection; no solve reads them.
-void Solver::materialize_jacobians() {
-    if (form_ == SolverForm::Plain) return;
-    if (!Jc32_.get()) {
-        Jc32_.alloc(18ull * E_);
-        Jp32_.alloc(6ull * E_);
-    }
-    if (E_ > 0) {
-        materialize_jacobians_kernel<<<ceil_div(E_, 256), 256, 0, stream_>>>(
-            s_cam_.get(), s_pt_.get(), cams32_.get(), reinterpret_cast<const float4*>(jpts32_.get()), jw_.get(), E_,
-            Jc32_.get(), Jp32_.get());
-        GBA_LAUNCH_CHECK();
-    }
-    sync();
 }
 
 }  // namespace gba

@@ -218,14 +218,7 @@ public:
     DevBuf<int> pchunk4_;  // per point chunk, int4 {first point, end point, first slot, end slot}
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
-    // mixed: the point-side passes recompute each slot's FP32 Jacobian rows from the
-    // linearisation point's camera record (cams32_), FP32 point (jpts32_, 4 floats per
-    // point) and robust scale (jw_, per slot: sqrt(rho') or 0 for a non-finite slot),
-    // bit-identical to the rows the normal-equation pass accumulated; Jc32_ / Jp32_
-    // (18 and 6 floats per slot, slot order) are only materialised for inspection
-    DevBuf<float> jpts32_, jw_;
-    DevBuf<float> Jc32_, Jp32_;
-    void materialize_jacobians();  // pcg.cu
+    DevBuf<float> Jc32_, Jp32_;  // mixed: FP32 Jacobian rows per slot, slot order (18 and 6 floats)
     DevBuf<float> J32c_;    // mixed: camera record [Jc(18), r(2)] per slot in camera-major position
     DevBuf<float> Vinv32_;  // mixed: FP32 copy of V'^-1 (6 per point) for the FP32 matvec
     DevBuf<float> Vinv32lo_;  // mixed: V'^-1 - Vinv32_ rounded to FP32 (float-float matvec)

@@ -359,8 +359,8 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         info_.alloc(1);
         build_pairs();
     } else {
-        jw_.alloc(E);
-        jpts32_.alloc(4ull * P);
+        Jc32_.alloc(18ull * E);
+        Jp32_.alloc(6ull * E);
         J32c_.alloc(20ull * E);
         judge_x_.alloc(9ull * C);
         Vinv32_.alloc(6ull * P);

@@ -254,13 +254,13 @@ enum {
     GBA_BUF_DC = 8,       /* double[9 C] */
     GBA_BUF_DP = 9,       /* double[3 P] */
     GBA_BUF_ORDER = 10,   /* int[E]  original observation index of each slot */
-    GBA_BUF_JC32 = 11,    /* float[18 E] Jc (2x9 row-major) per slot (mixed forms; recomputed on request, the solve keeps none) */
+    GBA_BUF_JC32 = 11,    /* float[18 E] Jc (2x9 row-major) per slot (mixed forms) */
     GBA_BUF_SDIAG = 12,   /* double[81 C] S diagonal blocks (mixed form) */
     GBA_BUF_CAMS = 13,    /* double[9 C] current cameras */
     GBA_BUF_PTS = 14,     /* double[3 P] current points */
     GBA_BUF_TRIAL_CAMS = 15,
     GBA_BUF_TRIAL_PTS = 16,
-    GBA_BUF_JP32 = 17     /* float[6 E]  Jp (2x3 row-major) per slot (mixed forms; recomputed on request) */
+    GBA_BUF_JP32 = 17     /* float[6 E]  Jp (2x3 row-major) per slot (mixed forms) */
 };
 /* Size in bytes of a solver buffer (0 if the form does not hold it). */
 int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out_bytes);
