@@ -804,25 +804,177 @@ __global__ void __launch_bounds__(kUT) coarse_z(const double* __restrict__ r, co
     if (threadIdx.x == 0) red_rz[blockIdx.x] = t;
 }
 
-// FP32 copy of an FP64 camera vector in the matvec's padded layout.
-__global__ void __launch_bounds__(kVT) to_x32_kernel(const double* __restrict__ v, int n, float* __restrict__ x32) {
-    const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < n) {
-        const int c = i / 9;
-        x32[kX32 * c + (i - 9 * c)] = static_cast<float>(v[i]);
+// ---- S Z for all kCoarse basis columns in one implicit product (instead of
+// kCoarse single products): the Jacobian rows are read once per slot.
+
+constexpr int kZs = 84;  // floats per camera of the FP32 basis copy Z32 (9 x 9, padded to 16-byte multiples)
+
+// Z32[c][i][j] = Z[j][9c + i] (FP32), the per-camera rows the point pass gathers.
+__global__ void __launch_bounds__(kVT) coarse_z32_kernel(const double* __restrict__ Zc, int C,
+                                                        float* __restrict__ Z32) {
+    const int t = blockIdx.x * kVT + threadIdx.x;
+    if (t >= 81 * C) return;
+    const int c = t / 81, r = t - 81 * c, i = r / 9, j = r - 9 * i;
+    Z32[static_cast<long long>(kZs) * c + r] = static_cast<float>(Zc[static_cast<long long>(j) * 9 * C + 9ll * c + i]);
+}
+
+// Point pass of S Z (FP32, as schur_point_pass for one vector): per slot and
+// column j, a = Jc Z_c(:, j) and v = Jp^T a; per point t_j = sum over its slots
+// (warp segmented scans and ordered segment sums), w_j = V'^-1 t_j; per slot
+// u_j = Jp w_j, 18 floats stored at the slot's camera-major position.
+__global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restrict__ prange,
+                                                            const int* __restrict__ pt_off,
+                                                            const int* __restrict__ s_cam,
+                                                            const int* __restrict__ s_pt,
+                                                            const int* __restrict__ cam_pos,
+                                                            const float* __restrict__ Jc32,
+                                                            const float* __restrict__ Jp32,
+                                                            const float* __restrict__ vinv_hi,
+                                                            const float* __restrict__ Z32, float* __restrict__ u9) {
+    __shared__ float seg[kPT][3];
+    __shared__ float wsh[kPT][3 * kCoarse];
+    const int4 rg = prange[blockIdx.x];
+    const int p0 = rg.x, p1 = rg.y, s0 = rg.z, s1 = rg.w;
+    const int my_p = p0 + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int my_b = 0, my_e = 0;
+    if (my_p < p1) {
+        my_b = pt_off[my_p];
+        my_e = pt_off[my_p + 1];
+    }
+    float t[3 * kCoarse];
+#pragma unroll
+    for (int k = 0; k < 3 * kCoarse; ++k) t[k] = 0.f;
+    for (int base = s0; base < s1; base += kPT) {
+        const int s = base + threadIdx.x;
+        int key = -1;
+        float J[24];
+        const float* Zc = Z32;
+        if (s < s1) {
+            key = s_pt[s];
+            load_j(Jc32, Jp32, s, J);
+            Zc = Z32 + static_cast<long long>(kZs) * s_cam[s];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 24; ++k) J[k] = 0.f;
+        }
+        const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) {
+            float a0 = 0.f, a1 = 0.f;
+            if (s < s1) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) {
+                    const float z = __ldg(Zc + 9 * i + j);
+                    a0 = fmaf(J[i], z, a0);
+                    a1 = fmaf(J[9 + i], z, a1);
+                }
+            }
+            float v0 = J[18] * a0 + J[21] * a1, v1 = J[19] * a0 + J[22] * a1, v2 = J[20] * a0 + J[23] * a1;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const float u0 = __shfl_up_sync(0xffffffffu, v0, d);
+                const float u1 = __shfl_up_sync(0xffffffffu, v1, d);
+                const float u2 = __shfl_up_sync(0xffffffffu, v2, d);
+                const int kd = __shfl_up_sync(0xffffffffu, key, d);
+                if (lane >= d && kd == key) {
+                    v0 += u0;
+                    v1 += u1;
+                    v2 += u2;
+                }
+            }
+            if (lane == 31 || knext != key) {
+                seg[threadIdx.x][0] = v0;
+                seg[threadIdx.x][1] = v1;
+                seg[threadIdx.x][2] = v2;
+            }
+            __syncthreads();
+            if (my_p < p1) {
+                const int b = max(my_b, base) - base, e = min(my_e, base + kPT) - base;
+                for (int w = b >> 5; b < e && w <= (e - 1) >> 5; ++w) {
+                    const int q = min(e - 1, 32 * w + 31);
+                    t[3 * j] += seg[q][0];
+                    t[3 * j + 1] += seg[q][1];
+                    t[3 * j + 2] += seg[q][2];
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (my_p < p1) {
+        float vi[6];
+        load_vinv(vinv_hi, nullptr, my_p, vi);
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) {
+            float w0, w1, w2;
+            apply_vinv(vi, t[3 * j], t[3 * j + 1], t[3 * j + 2], w0, w1, w2);
+            wsh[threadIdx.x][3 * j] = w0;
+            wsh[threadIdx.x][3 * j + 1] = w1;
+            wsh[threadIdx.x][3 * j + 2] = w2;
+        }
+    }
+    __syncthreads();
+    for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
+        const int pl = s_pt[s] - p0;
+        const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
+        const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
+        const float jp[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
+        float2* out = reinterpret_cast<float2*>(u9 + 18ll * cam_pos[s]);
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) {
+            const float w0 = wsh[pl][3 * j], w1 = wsh[pl][3 * j + 1], w2 = wsh[pl][3 * j + 2];
+            out[j] = make_float2(jp[0] * w0 + jp[1] * w1 + jp[2] * w2, jp[3] * w0 + jp[4] * w1 + jp[5] * w2);
+        }
     }
 }
 
-// y = U_lambda v - (chunk partials of the implicit product): one FP32 product S v.
-__global__ void __launch_bounds__(kVT) coarse_q_kernel(const int* __restrict__ cam_chunk_off,
-                                                      const double* __restrict__ part, const double* __restrict__ U,
-                                                      double lambda, const double* __restrict__ v, int C,
-                                                      double* __restrict__ y) {
-    const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < 9 * C) {
-        const int c = i / 9, k = i % 9;
-        y[i] = damped_u_row_dot(U + 81ll * c, k, lambda, v + 9ll * c) - chunk_sum(cam_chunk_off, part, c, k);
+// Camera pass of S Z: per camera chunk, the partials sum_e Jc_e^T u_e,j for all
+// columns (81 per chunk at part[81 chunk + 9 i + j]); thread (g, j): positions
+// g, g + 16, ... of the chunk for column j, FP32 sums, groups added in FP64.
+constexpr int kC9 = 16 * kCoarse;
+__global__ void __launch_bounds__(kC9) coarse_camera_pass9(const int* __restrict__ cchunk_begin,
+                                                          const int* __restrict__ cchunk_cam,
+                                                          const int* __restrict__ cam_off,
+                                                          const float* __restrict__ J32c,
+                                                          const float* __restrict__ u9, double* __restrict__ part) {
+    __shared__ float sh[16][81];
+    const int k = blockIdx.x;
+    const int b = cchunk_begin[k], c = cchunk_cam[k];
+    const int e = min(b + kCamChunk, cam_off[c + 1]);
+    const int g = threadIdx.x / kCoarse, j = threadIdx.x - kCoarse * g;
+    float acc[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) acc[i] = 0.f;
+    for (int q = b + g; q < e; q += 16) {
+        const float* rec = J32c + 20ll * q;
+        const float2 u = reinterpret_cast<const float2*>(u9 + 18ll * q)[j];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) acc[i] = fmaf(__ldg(rec + i), u.x, fmaf(__ldg(rec + 9 + i), u.y, acc[i]));
     }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) sh[g][9 * i + j] = acc[i];
+    __syncthreads();
+    if (threadIdx.x < 81) {
+        double v = 0.0;
+#pragma unroll
+        for (int gg = 0; gg < 16; ++gg) v += static_cast<double>(sh[gg][threadIdx.x]);
+        part[81ll * k + threadIdx.x] = v;
+    }
+}
+
+// SZ[j][9c + i] = (U_lambda Z_j)_(c, i) - sum over the camera's chunks of part[81 q + 9 i + j] (FP64).
+__global__ void __launch_bounds__(kVT) coarse_sz_finalize(const int* __restrict__ cam_chunk_off,
+                                                         const double* __restrict__ part,
+                                                         const double* __restrict__ U, double lambda,
+                                                         const double* __restrict__ Zc, int C,
+                                                         double* __restrict__ SZ) {
+    const int t = blockIdx.x * kVT + threadIdx.x;
+    if (t >= 81 * C) return;
+    const int c = t / 81, r = t - 81 * c, i = r / 9, j = r - 9 * i;
+    const long long n = 9ll * C;
+    double sum = 0.0;
+    for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) sum += part[81ll * q + r];
+    SZ[j * n + 9ll * c + i] = damped_u_row_dot(U + 81ll * c, i, lambda, Zc + j * n + 9ll * c) - sum;
 }
 
 // Block partials of E = Z^T SZ: red[block * kCoarse^2 + a kCoarse + b] over the block's entries.
@@ -1509,7 +1661,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
 }
 
 // Learned coarse space for this trial: the basis Z from the network at the
-// current cameras, SZ = S Z (kCoarse FP32 implicit products, FP64 finalize), and
+// current cameras, SZ = S Z (one FP32 implicit product for all kCoarse columns,
+// FP64 finalize), and
 // E^-1 = (Z^T S Z)^-1 (FP64 Cholesky on the device; flagged off if E is not SPD).
 void Solver::coarse_prepare(double lambda) {
     const int n = 9 * C_;
@@ -1522,17 +1675,26 @@ void Solver::coarse_prepare(double lambda) {
         csz_.alloc(1ull * kCoarse * n);
         ceinv_.alloc(kCoarse * kCoarse + 1);
         cred_.alloc(need_red);
+        cz32_.alloc(1ull * kZs * C_);
+        cu9_.alloc(18ull * E_);
+        cpart9_.alloc(81ull * std::max(n_cchunk_, 1));
     }
     cudaEvent_t ev = prof_start();
     model_->coarse_basis(*this, lambda, cz_.get());
-    for (int j = 0; j < kCoarse; ++j) {
-        to_x32_kernel<<<nvb, kVT, 0, stream_>>>(cz_.get() + 1ll * j * n, n, pcg_p32_.get());
-        GBA_LAUNCH_CHECK();
-        implicit_parts<float>(*this, pcg_p32_.get(), 0.0, nullptr);
-        coarse_q_kernel<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
-                                                  cz_.get() + 1ll * j * n, C_, csz_.get() + 1ll * j * n);
+    coarse_z32_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, cz32_.get());
+    GBA_LAUNCH_CHECK();
+    coarse_point_pass9<<<n_pchunk_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(),
+                                                       s_cam_.get(), s_pt_.get(), cam_pos_.get(), Jc32_.get(),
+                                                       Jp32_.get(), Vinv32_.get(), cz32_.get(), cu9_.get());
+    GBA_LAUNCH_CHECK();
+    if (n_cchunk_ > 0) {
+        coarse_camera_pass9<<<n_cchunk_, kC9, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(), cam_off_.get(),
+                                                            J32c_.get(), cu9_.get(), cpart9_.get());
         GBA_LAUNCH_CHECK();
     }
+    coarse_sz_finalize<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cam_chunk_off_.get(), cpart9_.get(), U_.get(),
+                                                                      lambda, cz_.get(), C_, csz_.get());
+    GBA_LAUNCH_CHECK();
     double* gram = cred_.get() + 2ll * nub * kCoarse + kCoarse;
     coarse_gram_partials<<<nvb, kVT, 0, stream_>>>(cz_.get(), csz_.get(), n, gram);
     GBA_LAUNCH_CHECK();

@@ -251,7 +251,8 @@ public:
     DevBuf<float> mlp_stats_;  // learned form: per-camera track statistics (3 per camera)
     // learned form: coarse basis Z (kCoarse columns of 9C), S Z, E^-1 (+ SPD flag),
     // and the partial sums of the balancing preconditioner and of E
-    DevBuf<double> cz_, csz_, ceinv_, cred_;
+    DevBuf<double> cz_, csz_, ceinv_, cred_, cpart9_;
+    DevBuf<float> cz32_, cu9_;  // FP32 per-camera basis rows; per-slot u of the product S Z (18 floats)
     void coarse_prepare(double lambda);  // pcg.cu
     // Learned form, per solve: 0 = not judged yet, 1 = the learned coarse
     // correction won the first inner solve, 2 = block-Jacobi won (used for the
