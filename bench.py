@@ -249,7 +249,7 @@ NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "camera_pass_f32": None,
 KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
            "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "cost_ff",
            "backsub", "schur_rhs_point_pass", "schur_rhs_camera_pass", "mlp_forward", "schur_assemble",
-           "dense_potrf", "coarse_basis", "coarse_apply")
+           "dense_potrf", "coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram", "coarse_apply")
 
 
 def _breakdown(solver, steps):

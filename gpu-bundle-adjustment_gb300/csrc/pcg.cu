@@ -977,25 +977,36 @@ __global__ void __launch_bounds__(kVT) coarse_sz_finalize(const int* __restrict_
     SZ[j * n + 9ll * c + i] = damped_u_row_dot(U + 81ll * c, i, lambda, Zc + j * n + 9ll * c) - sum;
 }
 
-// Block partials of E = Z^T SZ: red[block * kCoarse^2 + a kCoarse + b] over the block's entries.
+// Block partials of E = Z^T SZ: red[block * kCoarse^2 + a kCoarse + b] over the
+// block's entries (one per thread): warp shuffle sums per pair, then the warps'
+// sums in warp order (one barrier).
 __global__ void __launch_bounds__(kVT) coarse_gram_partials(const double* __restrict__ Zc,
                                                            const double* __restrict__ SZ, long long n,
                                                            double* __restrict__ red) {
-    __shared__ double sh[kVT / 32];
+    constexpr int KK = kCoarse * kCoarse;
+    __shared__ double wsum[kVT / 32][KK];
     const long long i = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double zv[kCoarse], sv[kCoarse];
 #pragma unroll
     for (int j = 0; j < kCoarse; ++j) {
         zv[j] = i < n ? Zc[j * n + i] : 0.0;
         sv[j] = i < n ? SZ[j * n + i] : 0.0;
     }
-#pragma unroll 1
+#pragma unroll
     for (int a = 0; a < kCoarse; ++a)
-#pragma unroll 1
+#pragma unroll
         for (int b = 0; b < kCoarse; ++b) {
-            const double t = block_sum<kVT>(zv[a] * sv[b], sh);
-            if (threadIdx.x == 0) red[static_cast<long long>(blockIdx.x) * kCoarse * kCoarse + a * kCoarse + b] = t;
+            const double t = warp_sum(zv[a] * sv[b]);
+            if (lane == 0) wsum[warp][a * kCoarse + b] = t;
         }
+    __syncthreads();
+    if (threadIdx.x < KK) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < kVT / 32; ++w) v += wsum[w][threadIdx.x];
+        red[static_cast<long long>(blockIdx.x) * KK + threadIdx.x] = v;
+    }
 }
 
 // E from the partials (fixed order), symmetrised; FP64 Cholesky and inverse by
@@ -1683,15 +1694,20 @@ void Solver::coarse_prepare(double lambda) {
     model_->coarse_basis(*this, lambda, cz_.get());
     coarse_z32_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, cz32_.get());
     GBA_LAUNCH_CHECK();
+    cudaEvent_t ev1 = prof_start();
     coarse_point_pass9<<<n_pchunk_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(),
                                                        s_cam_.get(), s_pt_.get(), cam_pos_.get(), Jc32_.get(),
                                                        Jp32_.get(), Vinv32_.get(), cz32_.get(), cu9_.get());
     GBA_LAUNCH_CHECK();
+    prof_stop("coarse_point_pass9", ev1);
     if (n_cchunk_ > 0) {
+        ev1 = prof_start();
         coarse_camera_pass9<<<n_cchunk_, kC9, 0, stream_>>>(cchunk_begin_.get(), cchunk_cam_.get(), cam_off_.get(),
                                                             J32c_.get(), cu9_.get(), cpart9_.get());
         GBA_LAUNCH_CHECK();
+        prof_stop("coarse_camera_pass9", ev1);
     }
+    ev1 = prof_start();
     coarse_sz_finalize<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cam_chunk_off_.get(), cpart9_.get(), U_.get(),
                                                                       lambda, cz_.get(), C_, csz_.get());
     GBA_LAUNCH_CHECK();
@@ -1700,6 +1716,7 @@ void Solver::coarse_prepare(double lambda) {
     GBA_LAUNCH_CHECK();
     coarse_einv_kernel<<<1, 128, 0, stream_>>>(gram, nvb, ceinv_.get());
     GBA_LAUNCH_CHECK();
+    prof_stop("coarse_gram", ev1);
     prof_stop("coarse_basis", ev);
 }
 
