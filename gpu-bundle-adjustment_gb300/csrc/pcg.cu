@@ -818,10 +818,11 @@ __global__ void __launch_bounds__(kVT) coarse_z32_kernel(const double* __restric
     Z32[static_cast<long long>(kZs) * c + r] = static_cast<float>(Zc[static_cast<long long>(j) * 9 * C + 9ll * c + i]);
 }
 
-// Point pass of S Z (FP32, as schur_point_pass for one vector): per slot and
-// column j, a = Jc Z_c(:, j) and v = Jp^T a; per point t_j = sum over its slots
-// (warp segmented scans and ordered segment sums), w_j = V'^-1 t_j; per slot
-// u_j = Jp w_j, 18 floats stored at the slot's camera-major position.
+// Point pass of S Z (FP32, as schur_point_pass for one vector): per slot,
+// a_j = Jc Z_c(:, j) for all columns (the camera's 9 x 9 rows read as float4
+// runs) and v_j = Jp^T a_j (27 values); per point t_j = sum over its slots (one
+// warp segmented scan of the 27 values and ordered segment sums), w_j = V'^-1 t_j;
+// per slot u_j = Jp w_j, 18 floats stored at the slot's camera-major position.
 __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restrict__ prange,
                                                             const int* __restrict__ pt_off,
                                                             const int* __restrict__ s_cam,
@@ -831,8 +832,9 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
                                                             const float* __restrict__ Jp32,
                                                             const float* __restrict__ vinv_hi,
                                                             const float* __restrict__ Z32, float* __restrict__ u9) {
-    __shared__ float seg[kPT][3];
-    __shared__ float wsh[kPT][3 * kCoarse];
+    constexpr int KV = 3 * kCoarse;
+    __shared__ float seg[kPT][KV + 1];  // warp-segment sums (27 per slot), at each segment's last slot
+    float* wsh = &seg[0][0];            // reused for w (27 per point) once the sums are taken
     const int4 rg = prange[blockIdx.x];
     const int p0 = rg.x, p1 = rg.y, s0 = rg.z, s1 = rg.w;
     const int my_p = p0 + threadIdx.x;
@@ -842,64 +844,67 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
         my_b = pt_off[my_p];
         my_e = pt_off[my_p + 1];
     }
-    float t[3 * kCoarse];
+    float t[KV];
 #pragma unroll
-    for (int k = 0; k < 3 * kCoarse; ++k) t[k] = 0.f;
+    for (int k = 0; k < KV; ++k) t[k] = 0.f;
     for (int base = s0; base < s1; base += kPT) {
         const int s = base + threadIdx.x;
         int key = -1;
-        float J[24];
-        const float* Zc = Z32;
+        float v[KV];
+#pragma unroll
+        for (int k = 0; k < KV; ++k) v[k] = 0.f;
         if (s < s1) {
             key = s_pt[s];
+            float J[24];
             load_j(Jc32, Jp32, s, J);
-            Zc = Z32 + static_cast<long long>(kZs) * s_cam[s];
-        } else {
+            const float4* z4 = reinterpret_cast<const float4*>(Z32 + static_cast<long long>(kZs) * s_cam[s]);
+            float Z[kZs];
 #pragma unroll
-            for (int k = 0; k < 24; ++k) J[k] = 0.f;
+            for (int q = 0; q < kZs / 4; ++q) {
+                const float4 z = __ldg(z4 + q);
+                Z[4 * q] = z.x;
+                Z[4 * q + 1] = z.y;
+                Z[4 * q + 2] = z.z;
+                Z[4 * q + 3] = z.w;
+            }
+#pragma unroll
+            for (int j = 0; j < kCoarse; ++j) {
+                float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) {
+                    a0 = fmaf(J[i], Z[9 * i + j], a0);
+                    a1 = fmaf(J[9 + i], Z[9 * i + j], a1);
+                }
+                v[3 * j] = J[18] * a0 + J[21] * a1;
+                v[3 * j + 1] = J[19] * a0 + J[22] * a1;
+                v[3 * j + 2] = J[20] * a0 + J[23] * a1;
+            }
         }
         const int knext = __shfl_down_sync(0xffffffffu, key, 1);
 #pragma unroll
-        for (int j = 0; j < kCoarse; ++j) {
-            float a0 = 0.f, a1 = 0.f;
-            if (s < s1) {
+        for (int d = 1; d < 32; d <<= 1) {
+            const int kd = __shfl_up_sync(0xffffffffu, key, d);
+            const bool take = lane >= d && kd == key;
 #pragma unroll
-                for (int i = 0; i < 9; ++i) {
-                    const float z = __ldg(Zc + 9 * i + j);
-                    a0 = fmaf(J[i], z, a0);
-                    a1 = fmaf(J[9 + i], z, a1);
-                }
+            for (int k = 0; k < KV; ++k) {
+                const float u = __shfl_up_sync(0xffffffffu, v[k], d);
+                if (take) v[k] += u;
             }
-            float v0 = J[18] * a0 + J[21] * a1, v1 = J[19] * a0 + J[22] * a1, v2 = J[20] * a0 + J[23] * a1;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const float u0 = __shfl_up_sync(0xffffffffu, v0, d);
-                const float u1 = __shfl_up_sync(0xffffffffu, v1, d);
-                const float u2 = __shfl_up_sync(0xffffffffu, v2, d);
-                const int kd = __shfl_up_sync(0xffffffffu, key, d);
-                if (lane >= d && kd == key) {
-                    v0 += u0;
-                    v1 += u1;
-                    v2 += u2;
-                }
-            }
-            if (lane == 31 || knext != key) {
-                seg[threadIdx.x][0] = v0;
-                seg[threadIdx.x][1] = v1;
-                seg[threadIdx.x][2] = v2;
-            }
-            __syncthreads();
-            if (my_p < p1) {
-                const int b = max(my_b, base) - base, e = min(my_e, base + kPT) - base;
-                for (int w = b >> 5; b < e && w <= (e - 1) >> 5; ++w) {
-                    const int q = min(e - 1, 32 * w + 31);
-                    t[3 * j] += seg[q][0];
-                    t[3 * j + 1] += seg[q][1];
-                    t[3 * j + 2] += seg[q][2];
-                }
-            }
-            __syncthreads();
         }
+        if (lane == 31 || knext != key) {
+#pragma unroll
+            for (int k = 0; k < KV; ++k) seg[threadIdx.x][k] = v[k];
+        }
+        __syncthreads();
+        if (my_p < p1) {
+            const int b = max(my_b, base) - base, e = min(my_e, base + kPT) - base;
+            for (int w = b >> 5; b < e && w <= (e - 1) >> 5; ++w) {
+                const int q = min(e - 1, 32 * w + 31);
+#pragma unroll
+                for (int k = 0; k < KV; ++k) t[k] += seg[q][k];
+            }
+        }
+        __syncthreads();
     }
     if (my_p < p1) {
         float vi[6];
@@ -908,9 +913,9 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
         for (int j = 0; j < kCoarse; ++j) {
             float w0, w1, w2;
             apply_vinv(vi, t[3 * j], t[3 * j + 1], t[3 * j + 2], w0, w1, w2);
-            wsh[threadIdx.x][3 * j] = w0;
-            wsh[threadIdx.x][3 * j + 1] = w1;
-            wsh[threadIdx.x][3 * j + 2] = w2;
+            wsh[threadIdx.x * (KV + 1) + 3 * j] = w0;
+            wsh[threadIdx.x * (KV + 1) + 3 * j + 1] = w1;
+            wsh[threadIdx.x * (KV + 1) + 3 * j + 2] = w2;
         }
     }
     __syncthreads();
@@ -919,10 +924,11 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
         const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
         const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
         const float jp[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
+        const float* w = wsh + pl * (KV + 1);
         float2* out = reinterpret_cast<float2*>(u9 + 18ll * cam_pos[s]);
 #pragma unroll
         for (int j = 0; j < kCoarse; ++j) {
-            const float w0 = wsh[pl][3 * j], w1 = wsh[pl][3 * j + 1], w2 = wsh[pl][3 * j + 2];
+            const float w0 = w[3 * j], w1 = w[3 * j + 1], w2 = w[3 * j + 2];
             out[j] = make_float2(jp[0] * w0 + jp[1] * w1 + jp[2] * w2, jp[3] * w0 + jp[4] * w1 + jp[5] * w2);
         }
     }
