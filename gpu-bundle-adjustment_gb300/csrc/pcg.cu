@@ -27,6 +27,8 @@
 //
 // No reference counterpart: the reference solves S densely on the host.
 
+#include <cuda_bf16.h>
+
 #include "blocks.cuh"
 #include "common.cuh"
 #include "ff.cuh"
@@ -807,15 +809,22 @@ __global__ void __launch_bounds__(kUT) coarse_z(const double* __restrict__ r, co
 // ---- S Z for all kCoarse basis columns in one implicit product (instead of
 // kCoarse single products): the Jacobian rows are read once per slot.
 
-constexpr int kZs = 84;  // floats per camera of the FP32 basis copy Z32 (9 x 9, padded to 16-byte multiples)
+constexpr int kZs = 88;  // BF16 values per camera of the basis copy Zb (9 x 9, padded to 16-byte multiples)
 
-// Z32[c][i][j] = Z[j][9c + i] (FP32), the per-camera rows the point pass gathers.
-__global__ void __launch_bounds__(kVT) coarse_z32_kernel(const double* __restrict__ Zc, int C,
-                                                        float* __restrict__ Z32) {
+// The basis is used at BF16 precision: Zb[c][i][j] = bf16(Z[j][9c + i]), the
+// per-camera rows the point pass gathers (176 B per camera), and Z itself is
+// overwritten by the same rounded values, so that S Z, E = Z^T S Z and the
+// preconditioner all use one basis (any full-rank basis is valid; the rounding
+// moves its span by ~4e-3 relative).
+__global__ void __launch_bounds__(kVT) coarse_zb_kernel(double* __restrict__ Zc, int C,
+                                                       __nv_bfloat16* __restrict__ Zb) {
     const int t = blockIdx.x * kVT + threadIdx.x;
     if (t >= 81 * C) return;
     const int c = t / 81, r = t - 81 * c, i = r / 9, j = r - 9 * i;
-    Z32[static_cast<long long>(kZs) * c + r] = static_cast<float>(Zc[static_cast<long long>(j) * 9 * C + 9ll * c + i]);
+    double* z = Zc + static_cast<long long>(j) * 9 * C + 9ll * c + i;
+    const __nv_bfloat16 b = __float2bfloat16_rn(static_cast<float>(*z));
+    Zb[static_cast<long long>(kZs) * c + r] = b;
+    *z = static_cast<double>(__bfloat162float(b));
 }
 
 // Point pass of S Z (FP32, as schur_point_pass for one vector): per slot,
@@ -831,7 +840,8 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
                                                             const float* __restrict__ Jc32,
                                                             const float* __restrict__ Jp32,
                                                             const float* __restrict__ vinv_hi,
-                                                            const float* __restrict__ Z32, float* __restrict__ u9) {
+                                                            const __nv_bfloat16* __restrict__ Zb,
+                                                            float* __restrict__ u9) {
     constexpr int KV = 3 * kCoarse;
     __shared__ float seg[kPT][KV + 1];  // warp-segment sums (27 per slot), at each segment's last slot
     float* wsh = &seg[0][0];            // reused for w (27 per point) once the sums are taken
@@ -857,15 +867,17 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
             key = s_pt[s];
             float J[24];
             load_j(Jc32, Jp32, s, J);
-            const float4* z4 = reinterpret_cast<const float4*>(Z32 + static_cast<long long>(kZs) * s_cam[s]);
+            const uint4* z4 = reinterpret_cast<const uint4*>(Zb + static_cast<long long>(kZs) * s_cam[s]);
             float Z[kZs];
 #pragma unroll
-            for (int q = 0; q < kZs / 4; ++q) {
-                const float4 z = __ldg(z4 + q);
-                Z[4 * q] = z.x;
-                Z[4 * q + 1] = z.y;
-                Z[4 * q + 2] = z.z;
-                Z[4 * q + 3] = z.w;
+            for (int q = 0; q < kZs / 8; ++q) {
+                const uint4 z = __ldg(z4 + q);
+                const uint32_t w[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    Z[8 * q + 2 * h] = __uint_as_float(w[h] << 16);             // low BF16 of the word
+                    Z[8 * q + 2 * h + 1] = __uint_as_float(w[h] & 0xffff0000u);  // high BF16
+                }
             }
 #pragma unroll
             for (int j = 0; j < kCoarse; ++j) {
@@ -1692,18 +1704,18 @@ void Solver::coarse_prepare(double lambda) {
         csz_.alloc(1ull * kCoarse * n);
         ceinv_.alloc(kCoarse * kCoarse + 1);
         cred_.alloc(need_red);
-        cz32_.alloc(1ull * kZs * C_);
+        czb_.alloc(1ull * kZs * C_);
         cu9_.alloc(18ull * E_);
         cpart9_.alloc(81ull * std::max(n_cchunk_, 1));
     }
     cudaEvent_t ev = prof_start();
     model_->coarse_basis(*this, lambda, cz_.get());
-    coarse_z32_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, cz32_.get());
+    coarse_zb_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, czb_.get());
     GBA_LAUNCH_CHECK();
     cudaEvent_t ev1 = prof_start();
     coarse_point_pass9<<<n_pchunk_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(),
                                                        s_cam_.get(), s_pt_.get(), cam_pos_.get(), Jc32_.get(),
-                                                       Jp32_.get(), Vinv32_.get(), cz32_.get(), cu9_.get());
+                                                       Jp32_.get(), Vinv32_.get(), czb_.get(), cu9_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_point_pass9", ev1);
     if (n_cchunk_ > 0) {

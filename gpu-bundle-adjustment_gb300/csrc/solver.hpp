@@ -16,6 +16,7 @@
 //                  column-major, lower triangle), rhs, dc, dp
 //   Schur (mixed)  PCG vectors (9C) and block-Jacobi factors (81C)
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <initializer_list>
@@ -252,7 +253,8 @@ public:
     // learned form: coarse basis Z (kCoarse columns of 9C), S Z, E^-1 (+ SPD flag),
     // and the partial sums of the balancing preconditioner and of E
     DevBuf<double> cz_, csz_, ceinv_, cred_, cpart9_;
-    DevBuf<float> cz32_, cu9_;  // FP32 per-camera basis rows; per-slot u of the product S Z (18 floats)
+    DevBuf<__nv_bfloat16> czb_;  // BF16 per-camera basis rows (the basis is used at BF16 precision)
+    DevBuf<float> cu9_;          // per-slot u of the product S Z (18 floats)
     void coarse_prepare(double lambda);  // pcg.cu
     // Learned form, per solve: 0 = not judged yet, 1 = the learned coarse
     // correction won the first inner solve, 2 = block-Jacobi won (used for the

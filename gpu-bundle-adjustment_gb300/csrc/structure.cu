@@ -85,6 +85,7 @@ template class DevBuf<unsigned long long>;
 template class DevBuf<unsigned int>;
 template class DevBuf<unsigned char>;
 template class DevBuf<long long>;
+template class DevBuf<__nv_bfloat16>;
 
 namespace {
 std::atomic<unsigned long long> g_launches{0};
