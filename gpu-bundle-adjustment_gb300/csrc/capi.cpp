@@ -82,6 +82,8 @@ gba::LMOptions to_options(const gba_lm_options* o) {
     r.loss = static_cast<gba::Loss>(o->loss);
     r.huber_delta = o->huber_delta;
     need(r.loss == gba::Loss::None || r.huber_delta > 0.0, "huber_delta must be positive");
+    need(o->schur_layout >= GBA_SCHUR_AUTO && o->schur_layout <= GBA_SCHUR_BAND, "bad schur_layout");
+    r.schur_layout = o->schur_layout;
     return r;
 }
 
@@ -109,6 +111,7 @@ void fill_result(const gba::LMResult& r, gba_lm_result* out) {
     out->judge_iters_block_jacobi = r.judge_iters_block_jacobi;
     out->judge_iters_learned = r.judge_iters_learned;
     out->max_refine_residual = r.max_refine_residual;
+    out->schur_band_rows = r.schur_band_rows;
     out->trajectory_len = static_cast<int>(r.trajectory.size());
     const int n = std::min<int>(out->trajectory_len, std::max(0, out->trajectory_capacity));
     for (int i = 0; i < n; ++i) {
@@ -147,6 +150,7 @@ void gba_lm_options_default(gba_lm_options* o) {
     o->stop_at_target = 0;
     o->loss = GBA_LOSS_NONE;
     o->huber_delta = d.huber_delta;
+    o->schur_layout = GBA_SCHUR_AUTO;
 }
 
 unsigned long long gba_launch_count(void) { return gba::launch_count(); }
@@ -394,6 +398,18 @@ int gba_host_problem_synthetic_custom(int C, int P, int kmin, int kmax, double a
     });
 }
 
+int gba_host_problem_synthetic_local(int C, int P, int kmin, int kmax, double alpha, int window, uint64_t seed,
+                                     gba_host_problem** out) {
+    return guarded([&] {
+        need(out != nullptr && window > 0, "bad argument (window must be positive)");
+        gba::SyntheticConfig cfg{C, P, kmin, kmax, alpha, 0.0, 0.0};
+        cfg.window = window;
+        auto h = std::make_unique<gba_host_problem>();
+        h->p = gba::make_synthetic(cfg, seed, nullptr);
+        *out = h.release();
+    });
+}
+
 int gba_host_problem_launch_bounds(int num_points, gba_host_problem** out) {
     return guarded([&] {
         need(out != nullptr && num_points > 0, "bad argument");
@@ -601,7 +617,7 @@ int gba_dense_potrf(double* A, int n, int lda, int* info, void* stream) {
     return guarded([&] {
         need(A && info, "null argument");
         need(n > 0 && n % 64 == 0 && lda >= n, "n must be a positive multiple of 64 and lda >= n");
-        gba::dense_potrf(A, n, lda, info, static_cast<cudaStream_t>(stream));
+        gba::dense_potrf(A, n, lda, n / 64 - 1, info, static_cast<cudaStream_t>(stream));
     });
 }
 
@@ -609,7 +625,45 @@ int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info,
     return guarded([&] {
         need(L && b && info, "null argument");
         need(n > 0 && n % 64 == 0 && lda >= n, "n must be a positive multiple of 64 and lda >= n");
-        gba::dense_potrs(L, n, lda, b, info, static_cast<cudaStream_t>(stream));
+        gba::dense_potrs(L, n, lda, n / 64 - 1, b, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_band_potrf(double* AB, int n, int ldb, int bt, int* info, void* stream) {
+    return guarded([&] {
+        need(AB && info, "null argument");
+        need(n > 0 && n % 64 == 0, "n must be a positive multiple of 64");
+        need(bt >= 0 && ldb >= (bt + 2) * 64, "ldb must be at least (bt + 2) * 64");
+        gba::dense_potrf(AB, n, ldb - 1, bt, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_band_potrs(const double* LB, int n, int ldb, int bt, double* b, const int* info, void* stream) {
+    return guarded([&] {
+        need(LB && b && info, "null argument");
+        need(n > 0 && n % 64 == 0, "n must be a positive multiple of 64");
+        need(bt >= 0 && ldb >= (bt + 2) * 64, "ldb must be at least (bt + 2) * 64");
+        gba::dense_potrs(LB, n, ldb - 1, bt, b, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_solver_set_schur_layout(gba_solver* s, int layout) {
+    return guarded([&] {
+        need(layout >= GBA_SCHUR_AUTO && layout <= GBA_SCHUR_BAND, "unknown Schur layout");
+        need(S(s).form() == gba::SolverForm::Plain, "the Schur layout applies to the plain form");
+        S(s).set_schur_layout(layout);
+    });
+}
+
+int gba_solver_schur_band(gba_solver* s, int* band_rows, int* band_tiles, int* perm) {
+    return guarded([&] {
+        auto& so = S(s);
+        if (band_rows) *band_rows = so.band_mode_ ? so.band_ldb_ : 0;
+        if (band_tiles) *band_tiles = so.band_mode_ ? so.band_bt_ : 0;
+        if (perm && so.band_mode_) {
+            GBA_CUDA_CHECK(cudaMemcpy(perm, so.cam_perm_.get(), so.cam_perm_.size() * sizeof(int),
+                                      cudaMemcpyDeviceToHost));
+        }
     });
 }
 

@@ -14,6 +14,16 @@
 //     trailing update C -= A B^T with mma.sync.m8n8k4 FP64 (DMMA).
 // S is column-major, n_pad x n_pad (n_pad = 9C rounded up to 64, identity on
 // the padding), lower triangle meaningful; the upper triangle is never read.
+//
+// Band layout (for camera graphs of local covisibility, where S is mostly
+// zero): cameras are renumbered by reverse Cuthill-McKee so the nonzero blocks
+// gather near the diagonal, and S keeps per column only the ldb rows from the
+// diagonal down: element (i, j), 0 <= i - j < ldb, at S[i + j (ldb - 1)]. Every
+// kernel below addresses S as A[i + j lda], so the same kernels run on the band
+// with lda = ldb - 1; the panel loops stop bt tiles below the diagonal tile
+// (Cholesky creates no fill outside the band). Writes to the strict upper
+// triangle of a diagonal tile (i - j in [-63, -1]) land in rows ldb - 63 ..
+// ldb - 1 of the previous column, which ldb = (bt + 2) 64 keeps outside the band.
 
 #include "common.cuh"
 #include "solver.hpp"
@@ -47,7 +57,7 @@ __global__ void __launch_bounds__(288) assemble_kernel(const int* __restrict__ b
                                                       const int* __restrict__ block_cf, const int* __restrict__ pe,
                                                       const int* __restrict__ pf, const double* __restrict__ T,
                                                       const double* __restrict__ W, int nblocks, int lda,
-                                                      double* __restrict__ S) {
+                                                      const int* __restrict__ perm, double* __restrict__ S) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long b = t / 9;
     const int i = static_cast<int>(t % 9);
@@ -62,21 +72,31 @@ __global__ void __launch_bounds__(288) assemble_kernel(const int* __restrict__ b
 #pragma unroll
         for (int j = 0; j < 9; ++j) acc[j] += t0 * Wf[3 * j] + t1 * Wf[3 * j + 1] + t2 * Wf[3 * j + 2];
     }
-    const long long row = 9ll * block_ce[b] + i;
-    const long long col0 = 9ll * block_cf[b];
+    const int pe_ = perm ? perm[block_ce[b]] : block_ce[b];
+    const int pf_ = perm ? perm[block_cf[b]] : block_cf[b];
+    if (pe_ >= pf_) {
+        const long long row = 9ll * pe_ + i;
+        const long long col0 = 9ll * pf_;
 #pragma unroll
-    for (int j = 0; j < 9; ++j) S[row + (col0 + j) * lda] = -acc[j];
+        for (int j = 0; j < 9; ++j) S[row + (col0 + j) * lda] = -acc[j];
+    } else {  // the renumbering put the block above the diagonal: store its transpose
+        const long long col = 9ll * pe_ + i;
+        const long long row0 = 9ll * pf_;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) S[(row0 + j) + col * lda] = -acc[j];
+    }
 }
 
 // Diagonal blocks += U_c + lambda * max(diag U_c, 1e-12); identity on padding.
 __global__ void add_damped_u_kernel(const double* __restrict__ U, double lambda, int C, int n_pad, int lda,
-                                    double* __restrict__ S) {
+                                    const int* __restrict__ perm, double* __restrict__ S) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < 81 * C) {
         const int c = t / 81, i = (t % 81) / 9, j = t % 9;
         double v = U[t];
         if (i == j) v += lambda * (v > 0.0 ? v : 1e-12);
-        S[(9ll * c + i) + (9ll * c + j) * lda] += v;
+        const long long pc = perm ? perm[c] : c;
+        S[(9 * pc + i) + (9 * pc + j) * lda] += v;
     } else if (t < 81 * C + (n_pad - 9 * C)) {
         const long long r = 9ll * C + (t - 81 * C);
         S[r + r * lda] = 1.0;
@@ -84,12 +104,27 @@ __global__ void add_damped_u_kernel(const double* __restrict__ U, double lambda,
 }
 
 // Copies the assembled diagonal blocks S_cc (lower triangle mirrored) to Sdiag.
-__global__ void extract_diag_blocks(const double* __restrict__ S, int C, int lda, double* __restrict__ Sdiag) {
+__global__ void extract_diag_blocks(const double* __restrict__ S, int C, int lda, const int* __restrict__ perm,
+                                    double* __restrict__ Sdiag) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 81 * C) return;
     const int c = t / 81, i = (t % 81) / 9, j = t % 9;
     const int r = i >= j ? i : j, q = i >= j ? j : i;
-    Sdiag[t] = S[(9ll * c + r) + (9ll * c + q) * lda];
+    const long long pc = perm ? perm[c] : c;
+    Sdiag[t] = S[(9 * pc + r) + (9 * pc + q) * lda];
+}
+
+// x[9 perm(c) + k] = v[9c + k] (to_band) or v[9c + k] = x[9 perm(c) + k].
+__global__ void permute_cameras(const int* __restrict__ perm, int C, bool to_band, const double* __restrict__ in,
+                                double* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 9 * C) return;
+    const int c = t / 9, k = t % 9;
+    const long long pos = 9ll * perm[c] + k;
+    if (to_band)
+        out[pos] = in[t];
+    else
+        out[t] = in[pos];
 }
 
 // rhs_c = bc_c - sum_{e in c} T_e bp_{p(e)}; one CTA per camera, ordered sums.
@@ -310,14 +345,14 @@ __global__ void trsv_upper_diag(const double* __restrict__ L, int j0, int lda, d
     b[j0 + t] = x[t];
 }
 
-// y[0 : j0) -= L[j0:j0+NB, 0:j0]^T x_j; one warp per output row i (reads column i of L).
-__global__ void gemv_upper_above(const double* __restrict__ L, int j0, int lda, double* __restrict__ b,
+// y[i0 : j0) -= L[j0:j0+NB, i0:j0]^T x_j; one warp per output row i (reads column i of L).
+__global__ void gemv_upper_above(const double* __restrict__ L, int i0, int j0, int lda, double* __restrict__ b,
                                  const int* __restrict__ info) {
     __shared__ double x[NB];
     if (*info) return;
     if (threadIdx.x < NB) x[threadIdx.x] = b[j0 + threadIdx.x];
     __syncthreads();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int warp = i0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (warp >= j0) return;
     const double* col = L + (long long)warp * lda + j0;
     double s = col[lane] * x[lane] + col[lane + 32] * x[lane + 32];
@@ -327,8 +362,11 @@ __global__ void gemv_upper_above(const double* __restrict__ L, int j0, int lda, 
 
 }  // namespace
 
-void dense_potrf(double* A, int n, int lda, int* info, cudaStream_t s) {
-    if (n % NB != 0 || lda < n) throw std::invalid_argument("dense_potrf: n must be a multiple of 64, lda >= n");
+// bt: tiles below the diagonal tile that hold nonzeros (n / 64 - 1 for a
+// dense matrix; lda = ldb - 1 with ldb >= (bt + 2) 64 for a band).
+void dense_potrf(double* A, int n, int lda, int bt, int* info, cudaStream_t s) {
+    if (n % NB != 0 || bt < 0 || (bt < n / NB - 1 ? lda + 1 < (bt + 2) * NB : lda < n))
+        throw std::invalid_argument("dense_potrf: n must be a multiple of 64 and lda hold the band");
     GBA_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
     static bool attr = false;
     const int smem = 2 * NB * kSP * sizeof(double);
@@ -343,8 +381,11 @@ void dense_potrf(double* A, int n, int lda, int* info, cudaStream_t s) {
         const int j0 = jb * NB;
         potrf_diag_kernel<<<1, 256, 0, s>>>(A, j0, lda, info);
         GBA_LAUNCH_CHECK();
-        const int below = nt - jb - 1;
-        if (below == 0) break;
+        const int below = std::min(nt - jb - 1, bt);
+        if (below == 0) {
+            if (jb == nt - 1) break;
+            continue;
+        }
         trsm_panel_kernel<<<below, 256, tsmem, s>>>(A, j0, lda, info);
         GBA_LAUNCH_CHECK();
         const long long tiles = (long long)below * (below + 1) / 2;
@@ -353,15 +394,17 @@ void dense_potrf(double* A, int n, int lda, int* info, cudaStream_t s) {
     }
 }
 
-void dense_potrs(const double* L, int n, int lda, double* b, const int* info, cudaStream_t s) {
-    if (n % NB != 0 || lda < n) throw std::invalid_argument("dense_potrs: n must be a multiple of 64, lda >= n");
+void dense_potrs(const double* L, int n, int lda, int bt, double* b, const int* info, cudaStream_t s) {
+    if (n % NB != 0 || bt < 0 || (bt < n / NB - 1 ? lda + 1 < (bt + 2) * NB : lda < n))
+        throw std::invalid_argument("dense_potrs: n must be a multiple of 64 and lda hold the band");
     const int nt = n / NB;
     for (int jb = 0; jb < nt; ++jb) {
         const int j0 = jb * NB;
         trsv_lower_diag<<<1, NB, 0, s>>>(L, j0, lda, b, info);
         GBA_LAUNCH_CHECK();
-        if (j0 + NB < n) {
-            gemv_lower_below<<<ceil_div(n - j0 - NB, 256), 256, 0, s>>>(L, j0, n, lda, b, info);
+        const int r_end = static_cast<int>(std::min<long long>(n, j0 + NB + (long long)bt * NB));
+        if (j0 + NB < r_end) {
+            gemv_lower_below<<<ceil_div(r_end - j0 - NB, 256), 256, 0, s>>>(L, j0, r_end, lda, b, info);
             GBA_LAUNCH_CHECK();
         }
     }
@@ -369,15 +412,36 @@ void dense_potrs(const double* L, int n, int lda, double* b, const int* info, cu
         const int j0 = jb * NB;
         trsv_upper_diag<<<1, NB, 0, s>>>(L, j0, lda, b, info);
         GBA_LAUNCH_CHECK();
-        if (j0 > 0) {
-            gemv_upper_above<<<ceil_div(32ll * j0, 256), 256, 0, s>>>(L, j0, lda, b, info);
+        const int i0 = std::max(0, j0 - bt * NB);
+        if (j0 > i0) {
+            gemv_upper_above<<<ceil_div(32ll * (j0 - i0), 256), 256, 0, s>>>(L, i0, j0, lda, b, info);
             GBA_LAUNCH_CHECK();
         }
     }
 }
 
+void Solver::ensure_schur_storage() {
+    const int want = schur_layout_;
+    if (S_.get() && schur_layout_planned_ == want) return;
+    bool band = false;
+    if (want == 2) {
+        plan_schur_band();
+        band = true;
+    } else if (want == 0 && C_ >= 2 && 3ll * n_blocks_ <= static_cast<long long>(C_) * C_) {
+        plan_schur_band();  // a band can only pay with at most ~1/3 of the blocks present
+        band = band_beneficial_;
+    }
+    band_mode_ = band;
+    S_.release();
+    S_.alloc(static_cast<size_t>(n_pad_) * (band ? band_ldb_ : n_pad_));
+    schur_layout_planned_ = want;
+}
+
 int Solver::schur_dense(double lambda) {
-    const int lda = n_pad_;
+    ensure_schur_storage();
+    const int lda = band_mode_ ? band_ldb_ - 1 : n_pad_;
+    const int bt = band_mode_ ? band_bt_ : n_pad_ / NB - 1;
+    const int* perm = band_mode_ ? cam_perm_.get() : nullptr;
     compute_T_kernel<<<std::min(ceil_div(E_, 256), 32 * device_sm_count()), 256, 0, stream_>>>(
         W_.get(), Vinv_.get(), s_pt_.get(), E_, T_.get());
     GBA_LAUNCH_CHECK();
@@ -386,12 +450,12 @@ int Solver::schur_dense(double lambda) {
         cudaEvent_t ev = prof_start();
         assemble_kernel<<<ceil_div(9ll * n_blocks_, 288), 288, 0, stream_>>>(
             block_off_.get(), block_ce_.get(), block_cf_.get(), pair_e_.get(), pair_f_.get(), T_.get(), W_.get(),
-            n_blocks_, lda, S_.get());
+            n_blocks_, lda, perm, S_.get());
         GBA_LAUNCH_CHECK();
         prof_stop("schur_assemble", ev);
     }
     add_damped_u_kernel<<<ceil_div(81ll * C_ + (n_pad_ - 9 * C_), 256), 256, 0, stream_>>>(U_.get(), lambda, C_,
-                                                                                        n_pad_, lda, S_.get());
+                                                                                        n_pad_, lda, perm, S_.get());
     GBA_LAUNCH_CHECK();
     GBA_CUDA_CHECK(cudaMemsetAsync(rhs_.get(), 0, rhs_.size() * sizeof(double), stream_));
     rhs_kernel<<<C_, 128, 0, stream_>>>(cam_off_.get(), cam_slots_.get(), s_pt_.get(), T_.get(), bp_.get(),
@@ -399,21 +463,33 @@ int Solver::schur_dense(double lambda) {
     GBA_LAUNCH_CHECK();
     if (harvest_) {
         if (!Sdiag_.get()) Sdiag_.alloc(81ull * C_);
-        extract_diag_blocks<<<ceil_div(81ll * C_, 256), 256, 0, stream_>>>(S_.get(), C_, lda, Sdiag_.get());
+        extract_diag_blocks<<<ceil_div(81ll * C_, 256), 256, 0, stream_>>>(S_.get(), C_, lda, perm, Sdiag_.get());
         GBA_LAUNCH_CHECK();
     }
     cudaEvent_t ev = prof_start();
-    dense_potrf(S_.get(), n_pad_, lda, info_.get(), stream_);
+    dense_potrf(S_.get(), n_pad_, lda, bt, info_.get(), stream_);
     prof_stop("dense_potrf", ev);
     int info = 0;
     read_back({{&info, info_.get(), sizeof info}});
     if (info != 0) return info;
-    // solve in a copy so rhs stays the assembled right-hand side
-    GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), rhs_.get(), n_pad_ * sizeof(double), cudaMemcpyDeviceToDevice,
-                                   stream_));
-    dense_potrs(S_.get(), n_pad_, lda, pcg_x_.get(), info_.get(), stream_);
-    GBA_CUDA_CHECK(cudaMemcpyAsync(dc_.get(), pcg_x_.get(), 9ull * C_ * sizeof(double), cudaMemcpyDeviceToDevice,
-                                   stream_));
+    // solve in a copy so rhs stays the assembled right-hand side (in the band
+    // layout the copy is in the renumbered camera order; the padding stays 0)
+    if (band_mode_) {
+        GBA_CUDA_CHECK(cudaMemsetAsync(pcg_x_.get(), 0, n_pad_ * sizeof(double), stream_));
+        permute_cameras<<<ceil_div(9 * C_, 256), 256, 0, stream_>>>(perm, C_, true, rhs_.get(), pcg_x_.get());
+        GBA_LAUNCH_CHECK();
+    } else {
+        GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), rhs_.get(), n_pad_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                                       stream_));
+    }
+    dense_potrs(S_.get(), n_pad_, lda, bt, pcg_x_.get(), info_.get(), stream_);
+    if (band_mode_) {
+        permute_cameras<<<ceil_div(9 * C_, 256), 256, 0, stream_>>>(perm, C_, false, pcg_x_.get(), dc_.get());
+        GBA_LAUNCH_CHECK();
+    } else {
+        GBA_CUDA_CHECK(cudaMemcpyAsync(dc_.get(), pcg_x_.get(), 9ull * C_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                                       stream_));
+    }
     sync();
     return 0;
 }

@@ -46,6 +46,7 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
 
     s.begin_solve();
     s.set_loss(opts.loss, opts.huber_delta);
+    if (plain) s.set_schur_layout(opts.schur_layout);
     double sse = phase(res.t_accumulate, [&] { return s.accumulate(); });
     res.initial_cost = sse / 2.0;
     res.trajectory.push_back(res.initial_cost);
@@ -221,6 +222,7 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
 
     res.final_cost = sse / 2.0;
     res.anomalies = s.anomalies();
+    res.schur_band_rows = s.band_mode_ ? s.band_ldb_ : 0;
     res.learned_choice = s.learned_choice_;
     res.judge_iters_block_jacobi = s.judge_iters_[0];
     res.judge_iters_learned = s.judge_iters_[1];

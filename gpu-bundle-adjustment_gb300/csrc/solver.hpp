@@ -280,6 +280,20 @@ public:
         huber_delta_ = d;
     }
     bool harvest_ = false;     // plain form: keep the damped diagonal blocks S_cc in Sdiag_
+    // plain form: storage of S. The camera graph (the nonzero 9x9 blocks) is
+    // ordered by reverse Cuthill-McKee at set-up (cam_perm_: camera -> position);
+    // in band mode S holds, per column, the band_ldb_ rows from the diagonal
+    // down (element (i, j) at S_[i + j (band_ldb_ - 1)]), band_bt_ = 64-row
+    // tiles below the diagonal tile that the band reaches.
+    int schur_layout_ = 0;     // 0 auto, 1 dense, 2 band
+    int schur_layout_planned_ = -1;  // the layout S_ was allocated for
+    bool band_mode_ = false;
+    bool band_beneficial_ = false;
+    int band_ldb_ = 0, band_bt_ = 0;
+    DevBuf<int> cam_perm_;
+    void set_schur_layout(int layout) { schur_layout_ = layout; }
+    void plan_schur_band();       // structure.cu: ordering and band size from the block list
+    void ensure_schur_storage();  // dense.cu: allocates S for the chosen layout
 
     void build_structure(const int* obs_cam, const int* obs_pt, const double* obs_px, const double* cams,
                          const double* pts);
@@ -313,11 +327,14 @@ void mixed_back_substitute(Solver& s, double lambda, double* part);
 void launch_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n,
                                      cudaStream_t s);
 void launch_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, cudaStream_t s);
-// Blocked dense Cholesky (lower, column-major). n must be a multiple of 64,
-// lda >= n. info (device int) = 0 on success, else the 1-based failed column.
-void dense_potrf(double* A, int n, int lda, int* info, cudaStream_t s);
+// Blocked Cholesky (lower, column-major), element (i, j) at A[i + j lda]. n
+// must be a multiple of 64. Dense: bt = n / 64 - 1, lda >= n. Band of bt
+// 64-row tiles below the diagonal tile: lda = ldb - 1, ldb >= (bt + 2) 64 rows
+// kept per column from the diagonal down. info (device int) = 0 on success,
+// else the 1-based failed column.
+void dense_potrf(double* A, int n, int lda, int bt, int* info, cudaStream_t s);
 // Solves L L^T x = b in place (b on the device, length n), L from dense_potrf.
-void dense_potrs(const double* L, int n, int lda, double* b, const int* info, cudaStream_t s);
+void dense_potrs(const double* L, int n, int lda, int bt, double* b, const int* info, cudaStream_t s);
 // Residual + Jacobian for E independent observations (device pointers, original
 // layout). Jc, Jp may be null. FP64 or FP32 arithmetic.
 void launch_eval_edges_f64(const double* cams, const double* pts, const int* oc, const int* op,

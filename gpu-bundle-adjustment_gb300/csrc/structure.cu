@@ -353,8 +353,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         W_.alloc(27ull * E);
         JcR_.alloc(20ull * E);
         T_.alloc(27ull * E);
-        n_pad_ = ((9 * C + 63) / 64) * 64;
-        S_.alloc(static_cast<size_t>(n_pad_) * n_pad_);
+        n_pad_ = ((9 * C + 63) / 64) * 64;  // S itself is allocated at the first dense Schur step
         rhs_.alloc(n_pad_);
         pcg_x_.alloc(n_pad_);  // dense solve work vector
         info_.alloc(1);
@@ -676,6 +675,79 @@ void Solver::build_pairs() {
     }
     block_split_kernel<<<grid_for(nb), 256, 0, stream_>>>(ukey.get(), nb, C, block_ce_.get(), block_cf_.get());
     GBA_LAUNCH_CHECK();
+    sync();
+}
+
+// Reverse Cuthill-McKee order of the camera graph (cameras adjacent when they
+// share a point: the nonzero off-diagonal blocks of S), its block bandwidth,
+// and whether a band holding it is at most a third of the dense matrix. Each
+// component is started from a camera of least degree; neighbours are visited
+// in increasing degree (ties by index), and the whole order is reversed. The
+// cameras' own order is kept when its bandwidth is no larger.
+// Host work O(blocks log), once per solver (the block list is fixed).
+void Solver::plan_schur_band() {
+    const int C = C_, nb = n_blocks_;
+    std::vector<int> ce(nb), cf(nb);
+    if (nb > 0) {
+        GBA_CUDA_CHECK(cudaMemcpyAsync(ce.data(), block_ce_.get(), nb * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        GBA_CUDA_CHECK(cudaMemcpyAsync(cf.data(), block_cf_.get(), nb * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        sync();
+    }
+    std::vector<int> deg(C, 0);
+    for (int b = 0; b < nb; ++b)
+        if (ce[b] != cf[b]) {
+            ++deg[ce[b]];
+            ++deg[cf[b]];
+        }
+    std::vector<int> off(C + 1, 0);
+    for (int c = 0; c < C; ++c) off[c + 1] = off[c] + deg[c];
+    std::vector<int> adj(off[C]), fill(off.begin(), off.end() - 1);
+    for (int b = 0; b < nb; ++b)
+        if (ce[b] != cf[b]) {
+            adj[fill[ce[b]]++] = cf[b];
+            adj[fill[cf[b]]++] = ce[b];
+        }
+    for (int c = 0; c < C; ++c)
+        std::sort(adj.begin() + off[c], adj.begin() + off[c + 1],
+                  [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; });
+    std::vector<int> order;
+    order.reserve(C);
+    std::vector<char> seen(C, 0);
+    std::vector<int> by_degree(C);
+    for (int c = 0; c < C; ++c) by_degree[c] = c;
+    std::stable_sort(by_degree.begin(), by_degree.end(), [&](int a, int b) { return deg[a] < deg[b]; });
+    for (int start : by_degree) {
+        if (seen[start]) continue;
+        size_t head = order.size();
+        order.push_back(start);
+        seen[start] = 1;
+        while (head < order.size()) {
+            const int u = order[head++];
+            for (int k = off[u]; k < off[u + 1]; ++k)
+                if (!seen[adj[k]]) {
+                    seen[adj[k]] = 1;
+                    order.push_back(adj[k]);
+                }
+        }
+    }
+    std::vector<int> perm(C);
+    for (int i = 0; i < C; ++i) perm[order[C - 1 - i]] = i;
+    int w = 0, w_given = 0;
+    for (int b = 0; b < nb; ++b) {
+        w = std::max(w, std::abs(perm[ce[b]] - perm[cf[b]]));
+        w_given = std::max(w_given, std::abs(ce[b] - cf[b]));
+    }
+    if (w_given <= w) {  // the cameras' own order is at least as narrow (e.g. a sequential capture)
+        for (int c = 0; c < C; ++c) perm[c] = c;
+        w = w_given;
+    }
+    const int band_rows = 9 * (w + 1);
+    constexpr int kTile = 64;
+    band_bt_ = (band_rows - 1 + kTile - 1) / kTile;
+    band_ldb_ = (band_bt_ + 2) * kTile;
+    band_beneficial_ = 3ll * band_ldb_ <= n_pad_;
+    cam_perm_.alloc(C);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(cam_perm_.get(), perm.data(), C * sizeof(int), cudaMemcpyHostToDevice, stream_));
     sync();
 }
 

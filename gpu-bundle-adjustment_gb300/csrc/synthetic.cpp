@@ -100,10 +100,25 @@ BALProblem make_synthetic(const SyntheticConfig& cfg, uint64_t seed, BALProblem*
     truth.num_cameras = C;
     truth.num_points = P;
     truth.cameras.resize(9ull * C);
+    const bool local = cfg.window > 0;
+    constexpr double kSpacing = 0.5;  // local mode: distance between consecutive camera centres
+    std::vector<double> centres(local ? 3ull * C : 0);
     for (int c = 0; c < C; ++c) {
         double* cam = truth.camera(c);
         for (int i = 0; i < 3; ++i) cam[i] = rng.normal(0.1);
-        for (int i = 3; i < 6; ++i) cam[i] = rng.normal(1.0);
+        if (local) {
+            // centre (0.5 c, ~0, ~0), t = -R centre
+            const double ctr[3] = {kSpacing * c, rng.normal(0.1), rng.normal(0.1)};
+            const double rot[9] = {cam[0], cam[1], cam[2], 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            double rc[3];
+            to_camera(rot, ctr, rc);  // R centre (the record's translation is zero)
+            for (int i = 0; i < 3; ++i) {
+                cam[3 + i] = -rc[i];
+                centres[3ull * c + i] = ctr[i];
+            }
+        } else {
+            for (int i = 3; i < 6; ++i) cam[i] = rng.normal(1.0);
+        }
         cam[6] = rng.uniform(400.0, 600.0);
         cam[7] = rng.normal(1e-2);
         cam[8] = rng.normal(1e-4);
@@ -111,13 +126,13 @@ BALProblem make_synthetic(const SyntheticConfig& cfg, uint64_t seed, BALProblem*
     truth.points.resize(3ull * P);
     for (int p = 0; p < P; ++p) {
         double* X = truth.point(p);
-        X[0] = rng.uniform(-3.0, 3.0);
+        X[0] = local ? rng.uniform(-1.0, kSpacing * (C - 1) + 1.0) : rng.uniform(-3.0, 3.0);
         X[1] = rng.uniform(-3.0, 3.0);
         X[2] = rng.uniform(-10.0, -3.0);
     }
 
     // discrete power-law track lengths, inverse CDF over [min, max]
-    const int kmax = std::min(cfg.track_max, C);
+    const int kmax = std::min(cfg.track_max, local ? std::min(C, 2 * cfg.window + 1) : C);
     std::vector<double> cdf;
     double tot = 0.0;
     for (int k = cfg.track_min; k <= kmax; ++k) tot += std::pow(static_cast<double>(k), -cfg.track_alpha);
@@ -141,8 +156,10 @@ BALProblem make_synthetic(const SyntheticConfig& cfg, uint64_t seed, BALProblem*
         const int want = cfg.track_min + static_cast<int>(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
         chosen.clear();
         const double* X = truth.point(p);
+        const int c_near = local ? std::min(C - 1, std::max(0, static_cast<int>(std::lround(X[0] / kSpacing)))) : 0;
         for (int attempt = 0; attempt < 64 * C && static_cast<int>(chosen.size()) < want; ++attempt) {
-            const int c = rng.below(C);
+            const int c = local ? c_near - cfg.window + rng.below(2 * cfg.window + 1) : rng.below(C);
+            if (c < 0 || c >= C) continue;
             if (used[c]) continue;
             double Pc[3];
             to_camera(truth.camera(c), X, Pc);
@@ -179,7 +196,25 @@ BALProblem make_synthetic(const SyntheticConfig& cfg, uint64_t seed, BALProblem*
         prob.obs_pixel[2 * i + 1] = obs[i].y;
     }
     prob.cameras = truth.cameras;
-    for (double& v : prob.cameras) v += rng.normal(0.01);
+    if (local) {
+        // the centre (not the translation, which grows with the distance from
+        // the origin) and the rotation are perturbed, so every camera moves by
+        // the same amount whatever its place on the path
+        for (int c = 0; c < C; ++c) {
+            double* cam = prob.camera(c);
+            double n[9];
+            for (double& v : n) v = rng.normal(0.01);
+            for (int i = 0; i < 3; ++i) cam[i] += n[i];
+            const double ctr[3] = {centres[3ull * c] + n[3], centres[3ull * c + 1] + n[4], centres[3ull * c + 2] + n[5]};
+            const double rot[9] = {cam[0], cam[1], cam[2], 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            double rc[3];
+            to_camera(rot, ctr, rc);
+            for (int i = 0; i < 3; ++i) cam[3 + i] = -rc[i];
+            for (int i = 6; i < 9; ++i) cam[i] += n[i];
+        }
+    } else {
+        for (double& v : prob.cameras) v += rng.normal(0.01);
+    }
     prob.points = truth.points;
     for (double& v : prob.points) v += rng.normal(0.05);
     if (truth_out) {

@@ -15,6 +15,11 @@ struct SyntheticConfig {
     double track_alpha;        // discrete power law P(k) ~ k^-alpha on [min, max]
     double outlier_fraction;   // share of observations with outlier noise
     double outlier_sigma;      // px
+    // > 0: spatially local covisibility, as along a camera path: camera c's
+    // centre lies at x = 0.5 c on the x axis, points spread along the path, and
+    // a point's track takes cameras within +-window of the camera nearest to it
+    // (the camera graph is then a band); 0: cameras anywhere, tracks drawn from all
+    int window = 0;
 };
 
 // Workloads 1..5:

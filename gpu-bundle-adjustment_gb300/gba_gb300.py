@@ -22,6 +22,7 @@ LIB_PATH = PKG / "lib" / "libgba_gb300.so"
 GBA_OK = 0
 FORMS = {"plain": 0, "mixed": 1, "learned": 2}
 LOSSES = {"none": 0, "huber": 1}
+SCHUR_LAYOUTS = {"auto": 0, "dense": 1, "band": 2}
 TERMINATION = {0: "CONVERGENCE", 1: "MAX_ITERATIONS", 2: "FAILURE", 3: "TARGET_COST"}
 BUF = {
     "U": 0, "V": 1, "bc": 2, "bp": 3, "W": 4, "Vinv": 5, "S": 6, "rhs": 7, "dc": 8, "dp": 9,
@@ -56,6 +57,7 @@ class LMOptions(C.Structure):
         ("stop_at_target", C.c_int),
         ("loss", C.c_int),
         ("huber_delta", C.c_double),
+        ("schur_layout", C.c_int),
     ]
 
 
@@ -85,6 +87,7 @@ class LMResultC(C.Structure):
         ("judge_iters_block_jacobi", C.c_longlong),
         ("judge_iters_learned", C.c_longlong),
         ("max_refine_residual", C.c_double),
+        ("schur_band_rows", C.c_int),
     ]
 
 
@@ -111,6 +114,8 @@ _SIG = {
     "gba_host_problem_synthetic": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "gba_host_problem_synthetic_custom": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                                     C.c_double, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "gba_host_problem_synthetic_local": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                                   C.c_uint64, C.POINTER(C.c_void_p)]),
     "gba_host_problem_launch_bounds": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "gba_host_problem_dims": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
     "gba_host_problem_copy": (C.c_int, [C.c_void_p, _dp, _dp, _ip, _ip, _dp]),
@@ -152,6 +157,10 @@ _SIG = {
     "gba_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "gba_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "gba_solver_set_preconditioner": (C.c_int, [C.c_void_p, C.c_int]),
+    "gba_solver_set_schur_layout": (C.c_int, [C.c_void_p, C.c_int]),
+    "gba_solver_schur_band": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
+    "gba_band_potrf": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "gba_band_potrs": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gba_solver_judge_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "gba_mlp_adam_step": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]),
     "gba_solver_buffer_size": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
@@ -250,6 +259,15 @@ def synthetic_custom(num_cameras: int, num_points: int, track_min: int = 2, trac
     return _from_handle(h)
 
 
+def synthetic_local(num_cameras: int, num_points: int, track_min: int = 2, track_max: int = 8,
+                    alpha: float = 1.5, window: int = 10, seed: int = 1) -> BALProblem:
+    """Seeded problem with spatially local covisibility: the camera graph is a band of half-width ~window."""
+    h = C.c_void_p()
+    _check(lib.gba_host_problem_synthetic_local(num_cameras, num_points, track_min, track_max, alpha, window, seed,
+                                                C.byref(h)))
+    return _from_handle(h)
+
+
 def launch_bounds_problem(num_points: int = 400000) -> BALProblem:
     h = C.c_void_p()
     _check(lib.gba_host_problem_launch_bounds(num_points, C.byref(h)))
@@ -292,6 +310,8 @@ def default_options(**kw) -> LMOptions:
             v = FORMS[v] if isinstance(v, str) else v
         if k == "loss":
             v = LOSSES[v] if isinstance(v, str) else v
+        if k == "schur_layout":
+            v = SCHUR_LAYOUTS[v] if isinstance(v, str) else v
         if k == "model_path" and v is not None:
             v = str(v).encode()
         setattr(o, k, v)
@@ -316,6 +336,7 @@ class LMResult:
     learned_choice: int = 0  # learned form: 1 learned, 2 block-Jacobi won the judged first inner solve
     judge_iters: tuple = (0, 0)  # that solve's inner PCG iterations: (block-Jacobi, learned)
     max_refine_residual: float = 0.0  # mixed forms: largest relative residual of a refined Schur step
+    schur_band_rows: int = 0  # plain form: rows of the band S was stored in (0: dense)
 
 
 def _result_struct(cap: int):
@@ -335,7 +356,7 @@ def _to_result(r, traj, ttime, cap) -> "LMResult":
         dict(setup=r.t_setup, accumulate=r.t_accumulate, damp=r.t_damp, schur=r.t_schur, backsub=r.t_backsub,
              cost=r.t_cost),
         traj[:n].tolist(), ttime[:n].tolist(), r.learned_choice,
-        (r.judge_iters_block_jacobi, r.judge_iters_learned), r.max_refine_residual,
+        (r.judge_iters_block_jacobi, r.judge_iters_learned), r.max_refine_residual, r.schur_band_rows,
     )
 
 
@@ -477,6 +498,20 @@ class Solver:
         """Learned form: "judge" (default), "learned" (always) or "block-jacobi" (never learned)."""
         _check(lib.gba_solver_set_preconditioner(self.h, {"judge": 0, "learned": 1, "block-jacobi": 2}[mode]))
 
+    def set_schur_layout(self, layout: str = "auto") -> None:
+        """Plain form: storage of S, "auto", "dense" or "band" (from the next schur_dense on)."""
+        _check(lib.gba_solver_set_schur_layout(self.h, SCHUR_LAYOUTS[layout]))
+
+    def schur_band(self):
+        """After schur_dense: (ldb, bt, perm) of the band S is stored in; (0, 0, None) when dense."""
+        ldb, bt = C.c_int(), C.c_int()
+        _check(lib.gba_solver_schur_band(self.h, C.byref(ldb), C.byref(bt), None))
+        if ldb.value == 0:
+            return 0, 0, None
+        perm = np.empty(self.dims()[0], np.int32)
+        _check(lib.gba_solver_schur_band(self.h, None, None, perm.ctypes.data_as(_ip)))
+        return ldb.value, bt.value, perm
+
     def judge_info(self):
         """Last judged solve: ((block-Jacobi, learned) PCG iterations, (block-Jacobi, learned) b.x)."""
         it, bx = (C.c_longlong * 2)(), (C.c_double * 2)()
@@ -529,6 +564,14 @@ def dense_potrf(A: int, n: int, lda: int, info: int, stream: int = 0) -> None:
 
 def dense_potrs(L: int, n: int, lda: int, b: int, info: int, stream: int = 0) -> None:
     _check(lib.gba_dense_potrs(L, n, lda, b, info, stream or None))
+
+
+def band_potrf(AB: int, n: int, ldb: int, bt: int, info: int, stream: int = 0) -> None:
+    _check(lib.gba_band_potrf(AB, n, ldb, bt, info, stream or None))
+
+
+def band_potrs(LB: int, n: int, ldb: int, bt: int, b: int, info: int, stream: int = 0) -> None:
+    _check(lib.gba_band_potrs(LB, n, ldb, bt, b, info, stream or None))
 
 
 def eval_edges(precision: int, cams: int, pts: int, oc: int, op: int, px: int, E: int, r: int, Jc: int = 0,

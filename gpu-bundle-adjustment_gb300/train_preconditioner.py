@@ -118,6 +118,7 @@ def harvest(gba, torch, spec, seed: int, iterations: int, lam0: float = 1e-3):
     feat_dev = torch.empty((C, 64), dtype=torch.float32, device="cuda")
     raw = []
     with gba.Solver(prob, "plain") as s:
+        s.set_schur_layout("dense")  # the eigenvectors are taken of the dense factor
         gba.solver_set_harvest(s, True)
         sse = s.accumulate()
         lam = lam0

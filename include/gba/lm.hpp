@@ -64,6 +64,10 @@ struct LMOptions {
     bool stop_at_target = false;  // end the solve ("TARGET_COST") once cost <= target_cost
     Loss loss = Loss::None;       // robust loss; cost = sum rho(|r|^2) / 2
     double huber_delta = 1.0;     // Huber threshold (px)
+    // plain form: storage of S (0 auto, 1 dense, 2 band of the cameras in reverse
+    // Cuthill-McKee order; auto takes the band when it is at most a third of the
+    // dense matrix)
+    int schur_layout = 0;
 };
 
 struct LMResult {
@@ -85,6 +89,7 @@ struct LMResult {
     // Schur step over the solve's trials (float-float residual of the system
     // the refinement solves), 0 for the plain form
     double max_refine_residual = 0.0;
+    int schur_band_rows = 0;  // plain form: rows of the band S was stored in (0: dense)
     double time_to_target_s = -1.0;        // first time cost <= LMOptions::target_cost, or -1
     // Learned form: which preconditioner won the judged first inner solve
     // (1 = learned, 2 = block-Jacobi, 0 = not judged) and its inner PCG

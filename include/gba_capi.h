@@ -56,7 +56,15 @@ typedef struct gba_lm_options {
     int stop_at_target;       /* 0; 1 = end the solve once cost <= target_cost */
     int loss;                 /* GBA_LOSS_NONE (0) or GBA_LOSS_HUBER (1) */
     double huber_delta;       /* 1.0 */
+    int schur_layout;         /* plain form: GBA_SCHUR_AUTO (0), GBA_SCHUR_DENSE (1) or GBA_SCHUR_BAND (2) */
 } gba_lm_options;
+
+/* Storage of the plain form's reduced camera system S: dense (9C)^2, or a band
+ * of the cameras reordered by reverse Cuthill-McKee on the camera graph (block
+ * rows of S within the band, the factor keeps the band). AUTO takes the band
+ * when it holds at most a third of the dense matrix (sparse covisibility, e.g.
+ * sequential captures); random covisibility stays dense. */
+enum { GBA_SCHUR_AUTO = 0, GBA_SCHUR_DENSE = 1, GBA_SCHUR_BAND = 2 };
 
 enum { GBA_LOSS_NONE = 0, GBA_LOSS_HUBER = 1 };
 
@@ -83,6 +91,7 @@ typedef struct gba_lm_result {
     long long judge_iters_block_jacobi;
     long long judge_iters_learned;
     double max_refine_residual;      /* mixed forms: largest relative residual of a refined Schur step */
+    int schur_band_rows;             /* plain form: rows of the band S was stored in, 0 if dense */
 } gba_lm_result;
 
 void gba_lm_options_default(gba_lm_options* opts);
@@ -125,6 +134,12 @@ int gba_host_problem_synthetic(int workload, uint64_t seed, gba_host_problem** o
 int gba_host_problem_synthetic_custom(int num_cameras, int num_points, int track_min, int track_max,
                                       double track_alpha, double outlier_fraction, double outlier_sigma,
                                       uint64_t seed, gba_host_problem** out);
+/* Same generator with spatially local covisibility (no reference counterpart):
+ * camera centres along a path (x = 0.5 c), each point's track drawn from the
+ * cameras within +-window of the camera nearest to it, so the camera graph is
+ * a band, as in sequential captures. */
+int gba_host_problem_synthetic_local(int num_cameras, int num_points, int track_min, int track_max,
+                                     double track_alpha, int window, uint64_t seed, gba_host_problem** out);
 /* The reference launch-bounds regression problem (tests/test_launch_bounds.cpp:28-80). */
 int gba_host_problem_launch_bounds(int num_points, gba_host_problem** out);
 int gba_host_problem_dims(const gba_host_problem* p, int* num_cameras, int* num_points, int* num_observations);
@@ -159,6 +174,14 @@ int gba_solver_damp_invert_v(gba_solver* s, double lambda, unsigned long long* o
 /* Plain form: dense S assembly + FP64 DMMA Cholesky + solve (reference
  * src/lm.cu:488-604). out_info: 0, or the failed pivot column (1-based). */
 int gba_solver_schur_dense(gba_solver* s, double lambda, int* out_info);
+/* Plain form: storage of S from the next gba_solver_schur_dense on
+ * (GBA_SCHUR_AUTO / DENSE / BAND; gba_solve takes gba_lm_options.schur_layout). */
+int gba_solver_set_schur_layout(gba_solver* s, int layout);
+/* Plain form, after gba_solver_schur_dense: the band S is stored in (rows per
+ * column ldb and tiles below the diagonal tile bt; 0 and 0 for dense S) and, for
+ * a band, the camera order (perm[c] = position of camera c). [host] band_rows,
+ * band_tiles (may be NULL), perm (C ints, may be NULL). */
+int gba_solver_schur_band(gba_solver* s, int* band_rows, int* band_tiles, int* perm);
 /* Mixed forms: PCG + FP64 refinement (no reference counterpart). */
 int gba_solver_schur_pcg(gba_solver* s, double lambda, const gba_lm_options* opts, int learned,
                          long long* out_pcg_iters, int* out_refine_steps, double* out_rel_residual);
@@ -249,7 +272,8 @@ enum {
     GBA_BUF_BP = 3,       /* double[3 P] */
     GBA_BUF_W = 4,        /* double[27 E]  9x3 row-major per slot (plain form) */
     GBA_BUF_VINV = 5,     /* double[6 P]   packed */
-    GBA_BUF_S = 6,        /* double[n_pad^2] column-major (plain form; factor after schur_dense) */
+    GBA_BUF_S = 6,        /* double[n_pad^2] column-major, or the band double[n_pad * ldb] (plain form;
+                             factor after schur_dense) */
     GBA_BUF_RHS = 7,      /* double[n_pad] (plain) or [9 C] (mixed) */
     GBA_BUF_DC = 8,       /* double[9 C] */
     GBA_BUF_DP = 9,       /* double[3 P] */
@@ -288,6 +312,17 @@ int gba_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, void* 
 int gba_dense_potrf(double* A, int n, int lda, int* info, void* stream);
 /* Solves L L^T x = b in place after gba_dense_potrf (reference src/lm.cu:604). [device] */
 int gba_dense_potrs(const double* L, int n, int lda, double* b, const int* info, void* stream);
+
+/* The same Cholesky on a symmetric band matrix in band storage: per column the
+ * ldb rows from the diagonal down, element (i, j), 0 <= i - j < ldb, at
+ * AB[(i - j) + j * ldb]; nonzeros no more than bt 64-row tiles below each
+ * diagonal 64 x 64 tile; ldb >= (bt + 2) * 64 (the last 64 rows of each column
+ * are work space). No counterpart in the reference, whose dense LLT
+ * (src/lm.cu:598-604) this replaces when the plain form's camera graph is a
+ * band (GBA_SCHUR_BAND). n multiple of 64. [device] AB, info. */
+int gba_band_potrf(double* AB, int n, int ldb, int bt, int* info, void* stream);
+/* Solves L L^T x = b in place after gba_band_potrf. [device] */
+int gba_band_potrs(const double* LB, int n, int ldb, int bt, double* b, const int* info, void* stream);
 
 /* FP64 reprojection cost that allocates no device memory (no counterpart in the
  * reference). For callers that cannot let a library allocate: host frameworks

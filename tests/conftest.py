@@ -103,3 +103,17 @@ def implicit_system(s, prob, lam):
 
     matvec.point_step = point_step
     return rhs, matvec
+
+
+def shuffle_cameras(prob, seed):
+    """The same problem with its cameras renumbered by a seeded permutation:
+    returns (problem, new_index) with camera c of prob at new_index[c]."""
+    rng = np.random.default_rng(seed)
+    C = prob.num_cameras
+    new_index = rng.permutation(C).astype(np.int32)
+    cams = np.empty_like(prob.cameras).reshape(C, 9)
+    cams[new_index] = prob.cameras.reshape(C, 9)
+    out = prob.copy()
+    out.cameras = cams.ravel()
+    out.obs_camera = new_index[prob.obs_camera]
+    return out, new_index

@@ -121,6 +121,7 @@ def test_learned_vs_block_jacobi_vs_exact_workload4(gba):
     lam = 1e-3
     C = prob.num_cameras
     with gba.Solver(prob, "plain") as s:
+        s.set_schur_layout("dense")
         s.accumulate()
         assert s.damp_invert_v(lam) == 0
         assert s.schur_dense(lam) == 0

@@ -40,6 +40,7 @@ def system(gba, torch_cuda):
     prob = gba.synthetic_custom(C, 3000, 2, 8, 1.6, seed=17)
     lam = 1e-3
     with gba.Solver(prob, "plain") as s:
+        s.set_schur_layout("dense")
         gba.solver_set_harvest(s, True)
         s.accumulate()
         assert s.damp_invert_v(lam) == 0

@@ -203,6 +203,7 @@ def test_assembled_S_matches_oracle(gba, oracle, small):
     S_ref = np.tril(ref["S"])
     S_ref = S_ref + np.tril(S_ref, -1).T
     with gba.Solver(small, "plain") as s:
+        s.set_schur_layout("dense")
         _, _, _, n_pad = s.dims()
         s.accumulate()
         s.damp_invert_v(lam)
