@@ -220,8 +220,13 @@ def algorithmic_bytes(unit: str, C: int, P: int, E: int) -> float:
     raise KeyError(unit)
 
 
-def design_bytes(unit: str, C: int, P: int, E: int) -> float:
+def design_bytes(unit: str, C: int, P: int, E: int, windowed: bool = False) -> float:
     """Bytes this implementation's kernels move per unit (its own layout)."""
+    if unit == "matvec" and windowed:
+        # per window: point pass Jc32 72 + Jp32 24 + s_cam, s_pt 8 + u 8 (written) per slot, V'^-1 24 +
+        # CSR 4 per point, x 36 per camera; camera pass: window slot index 4 per slot from HBM, the
+        # window's Jc32 and u again from L2; partials 72 B per camera segment (~ per camera and window)
+        return E * 116.0 + P * 28.0 + C * 36.0
     if unit == "matvec":
         # point pass: Jc32 72 + Jp32 24 + s_cam, s_pt, cam_pos 12 + u 8 per slot, V'^-1 24 + CSR 4 per
         # point, x 36 per camera; camera pass: camera record 80 + u 8 per slot
@@ -235,21 +240,26 @@ def design_bytes(unit: str, C: int, P: int, E: int) -> float:
     raise KeyError(unit)
 
 
-UNITS = {"matvec": ("schur_point_pass_f32", "schur_camera_pass_f32"),
+UNITS = {"matvec": ("schur_matvec_f32", "schur_point_pass_f32", "schur_camera_pass_f32"),
          "edge": ("point_pass_f32", "camera_pass_f32"),
          "cost": ("cost_ff",)}
 
 # DRAM bytes (read + write) per launch from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum, --clock-control none) of each kernel at workload 5; copied
 # here, not measured in this run.
-NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "camera_pass_f32": None,
+NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "camera_pass_f32": None, "schur_matvec_f32": None,
                   "schur_point_pass_f32": 992.6e6 + 66.4e6, "schur_camera_pass_f32": 774.4e6 + 3.8e6,
                   "cost_ff": 239.9e6 + 61.0e6}
 
-KERNELS = ("schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff", "schur_camera_pass_ff",
+KERNELS = ("schur_matvec_f32", "schur_point_pass_f32", "schur_camera_pass_f32", "schur_point_pass_ff",
+           "schur_camera_pass_ff",
            "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "cost_ff",
            "backsub", "schur_rhs_point_pass", "schur_rhs_camera_pass", "mlp_forward", "schur_assemble",
-           "dense_potrf", "coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram", "coarse_apply")
+           "dense_potrf", "coarse_prepare", "coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram",
+           "coarse_apply")
+# stages that contain others (their times are not additional)
+NESTED = {"coarse_prepare": ["coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram"],
+          "coarse_basis": ["mlp_forward"]}
 
 
 def _breakdown(solver, steps):
@@ -258,6 +268,8 @@ def _breakdown(solver, steps):
         n_k, ms_k = solver.kernel_stats(name)
         if n_k:
             out[name] = {"launches": n_k, "ms_per_step": ms_k / steps}
+            if name in NESTED:
+                out[name]["contains"] = NESTED[name]
     return out
 
 
@@ -280,7 +292,11 @@ def roofline_mixed(solver, breakdown, C, P, E, workload, seed):
         solver.schur_pcg(1e-3, refine_tol=1e-30, refine_max_steps=1, pcg_tol=0.0, pcg_max_iters=64)
         source = "64 full-work PCG iterations (lambda 1e-3) on the resident problem, CUDA events per launch"
     per_unit_s, launches, traffic = 0.0, None, 0.0
-    for k in UNITS[unit]:
+    names = UNITS[unit]
+    windowed = unit == "matvec" and solver.kernel_stats("schur_matvec_f32")[0] > 0
+    if unit == "matvec":  # the windowed product is timed as one stage; the two-pass one per pass
+        names = ("schur_matvec_f32",) if windowed else names[1:]
+    for k in names:
         n, ms = solver.kernel_stats(k)
         if unit == "matvec":
             n = min(n, 64)
@@ -296,8 +312,8 @@ def roofline_mixed(solver, breakdown, C, P, E, workload, seed):
             "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of these kernels at workload 5, "
                                "one capture, copied into bench.py (not measured in this run)") if traffic else None,
-            "kernel": "+".join(UNITS[unit]), "work_unit": unit, "algorithmic_bytes": alg,
-            "design_bytes": design_bytes(unit, C, P, E), "launches": launches,
+            "kernel": "+".join(names), "work_unit": unit, "algorithmic_bytes": alg,
+            "design_bytes": design_bytes(unit, C, P, E, windowed), "launches": launches,
             "avg_unit_us": per_unit_s * 1e6, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs, copy)",
             "per_launch_source": source}
 
@@ -380,6 +396,43 @@ def plain_denominator(torch, gba, prob, args, target):
                 "roofline": roofline_potrf(solver, prob.num_cameras), "measured": "in this run (CUDA events)"}
     finally:
         solver.close()
+
+
+def plain_band(torch, gba, args):
+    """The plain FP64 form on a camera path (local covisibility: S is a band):
+    the same LM solve with S stored as a band (reverse Cuthill-McKee order, band
+    Cholesky) and dense, CUDA events around each solve."""
+    prob = gba.synthetic_local(1200, 120000, 2, 8, 1.5, 10, seed=8)
+    out = {"workload": f"camera path: {prob.num_cameras} cameras / {prob.num_points} points / "
+                       f"{prob.num_observations} observations, tracks within +-10 cameras, seed 8",
+           "max_iterations": 10}
+    runs = {}
+    for layout in ("band", "dense"):
+        stream = torch.cuda.Stream()
+        solver = gba.Solver(prob, "plain", stream=stream.cuda_stream)
+        try:
+            solver.profile(True)
+            opts = dict(form="plain", max_iterations=10, schur_layout=layout)
+            solver.run(**opts)  # warm-up: allocates S, plans the band
+            solver.profile_reset()
+            solver.reset_params()
+            torch.cuda.synchronize()
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            r = solver.run(**opts)
+            end.record(stream)
+            torch.cuda.synchronize()
+            n_f, f_ms = solver.kernel_stats("dense_potrf")
+            runs[layout] = r
+            out[layout] = {"solve_s": start.elapsed_time(end) / 1e3, "iterations": r.iterations,
+                           "trials": r.trials, "final_cost": r.final_cost, "band_rows": r.schur_band_rows,
+                           "factorisations": n_f, "factor_ms_each": f_ms / n_f if n_f else None}
+        finally:
+            solver.close()
+    tb, td = runs["band"].trajectory, runs["dense"].trajectory
+    out["max_rel_cost_difference"] = (max(abs(a - b) / b for a, b in zip(tb, td)) if len(tb) == len(td) else None)
+    out["dense_over_band"] = out["dense"]["solve_s"] / out["band"]["solve_s"]
+    return out
 
 
 def cpu_pair(torch, gba, args):
@@ -582,6 +635,8 @@ def run_ours(args):
         line["plain_fp64_form"] = plain_denominator(torch, gba, prob, args, target)
         pl = line["plain_fp64_form"]["time_to_target_s"]
         line["plain_over_chosen"] = pl / line["value"] if pl else None
+    if rank == 0 and world == 1 and not args.no_band:
+        line["plain_band"] = plain_band(torch, gba, args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(prob, final.iterations)
         if args.cpu_pair_workload:
@@ -656,6 +711,7 @@ def main():
     ap.add_argument("--no-inexact", action="store_true", help="skip the inexact-Newton extra measurement")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 solve to the target")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-band", action="store_true", help="skip the plain form's band-vs-dense camera-path solve")
     ap.add_argument("--cpu-pair-workload", type=int, default=2)
     ap.add_argument("--reference-max-cameras", type=int, default=300,
                     help="largest workload (cameras) the CPU arm solves; above it prints unavailable")

@@ -84,6 +84,7 @@ gba::LMOptions to_options(const gba_lm_options* o) {
     need(r.loss == gba::Loss::None || r.huber_delta > 0.0, "huber_delta must be positive");
     need(o->schur_layout >= GBA_SCHUR_AUTO && o->schur_layout <= GBA_SCHUR_BAND, "bad schur_layout");
     r.schur_layout = o->schur_layout;
+    r.deterministic = o->deterministic != 0;
     return r;
 }
 
@@ -151,6 +152,7 @@ void gba_lm_options_default(gba_lm_options* o) {
     o->loss = GBA_LOSS_NONE;
     o->huber_delta = d.huber_delta;
     o->schur_layout = GBA_SCHUR_AUTO;
+    o->deterministic = 0;
 }
 
 unsigned long long gba_launch_count(void) { return gba::launch_count(); }
@@ -644,6 +646,15 @@ int gba_band_potrs(const double* LB, int n, int ldb, int bt, double* b, const in
         need(n > 0 && n % 64 == 0, "n must be a positive multiple of 64");
         need(bt >= 0 && ldb >= (bt + 2) * 64, "ldb must be at least (bt + 2) * 64");
         gba::dense_potrs(LB, n, ldb - 1, bt, b, info, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int gba_solver_set_matvec(gba_solver* s, int mode, int* out_one_pass) {
+    return guarded([&] {
+        need(S(s).form() != gba::SolverForm::Plain, "the PCG product belongs to the mixed forms");
+        need(mode >= -1 && mode <= 2, "matvec mode: -1 query, 0 auto, 1 two-pass, 2 one-pass");
+        if (mode >= 0) S(s).set_matvec(mode);
+        if (out_one_pass) *out_one_pass = S(s).one_pass_;
     });
 }
 

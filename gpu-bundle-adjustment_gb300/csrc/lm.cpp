@@ -46,7 +46,10 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
 
     s.begin_solve();
     s.set_loss(opts.loss, opts.huber_delta);
-    if (plain) s.set_schur_layout(opts.schur_layout);
+    if (plain)
+        s.set_schur_layout(opts.schur_layout);
+    else
+        s.set_matvec(opts.deterministic ? 1 : 0);
     double sse = phase(res.t_accumulate, [&] { return s.accumulate(); });
     res.initial_cost = sse / 2.0;
     res.trajectory.push_back(res.initial_cost);

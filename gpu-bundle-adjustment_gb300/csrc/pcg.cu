@@ -230,6 +230,30 @@ __device__ __forceinline__ float4 jp_vinv_jpt(const float* j, const float* vi) {
                        m[3] * j[3] + m[4] * j[4] + m[5] * j[5], 0.f);
 }
 
+// y += Jc^T u for one slot (FP32, device-memory atomics: two float4 and one
+// float into a 12-float accumulator of the slot's camera). The slot's Jacobian
+// rows are re-read here; the point pass loaded them moments before, so they
+// come from L1 or L2, not HBM.
+template <typename T>
+__device__ __forceinline__ void accumulate_jct_u(const float* __restrict__ jc, T u0, T u1, T* y) {
+    if constexpr (sizeof(T) == 4) {
+        const float2* q = reinterpret_cast<const float2*>(jc);
+        float Jc[18];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const float2 v = q[t];
+            Jc[2 * t] = v.x;
+            Jc[2 * t + 1] = v.y;
+        }
+        float r[9];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) r[t] = fmaf(Jc[t], u0, Jc[9 + t] * u1);
+        atomicAdd(reinterpret_cast<float4*>(y), make_float4(r[0], r[1], r[2], r[3]));
+        atomicAdd(reinterpret_cast<float4*>(y) + 1, make_float4(r[4], r[5], r[6], r[7]));
+        atomicAdd(y + 8, r[8]);
+    }
+}
+
 // Back-substitution outputs of the point pass (kBack): dp = V'^-1 (bp - W^T dc),
 // trial points, and per-chunk partials of the gain denominator's point terms.
 struct BacksubOut {
@@ -249,7 +273,7 @@ struct BacksubOut {
 // position so that the camera pass reads it contiguously. With kBack (a = -1,
 // xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
 // kRhs: the right-hand side instantiation (xt = null, a = 1, also G).
-template <typename T, bool kBack = false, bool kRhs = false>
+template <typename T, bool kBack = false, bool kRhs = false, bool kAcc = false>
 __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int4* __restrict__ prange, const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                        const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
@@ -315,13 +339,14 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
             key = -1;
             if (s < s1) {
                 key = s_pt[s];
-                q = cam_pos[s];
+                const int cam = s_cam[s];
+                q = cam_pos[s];  // kAcc: the slot's accumulator
                 float J[24];
                 load_j(Jc32, Jp32, s, J);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
                 T xv[9];
-                load_x(xt, s_cam[s], xv);
+                load_x(xt, cam, xv);
                 T t0 = zero<T>(), t1 = zero<T>();
 #pragma unroll
                 for (int k = 0; k < 9; ++k) {
@@ -464,12 +489,16 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
         return;
     }
     __syncthreads();
-    // u_e = Jp_e w_p for every slot of the chunk, stored camera-major
+    // u_e = Jp_e w_p for every slot of the chunk, stored camera-major (kAcc:
+    // Jc_e^T u_e added into the camera's accumulators)
     if (single) {
         if (s0 + static_cast<int>(threadIdx.x) < s1) {
             T u0, u1;
             jp_times(jp, wsh[key - p0][0], wsh[key - p0][1], wsh[key - p0][2], u0, u1);
-            store_u(u_cm, q, u0, u1);
+            if constexpr (kAcc)
+                accumulate_jct_u(Jc32 + 18ll * (s0 + threadIdx.x), u0, u1, u_cm + static_cast<long long>(kX32) * q);
+            else
+                store_u(u_cm, q, u0, u1);
             if (g_cm) g_cm[q] = jp_vinv_jpt(jp, vsh[key - p0]);
         }
         return;
@@ -481,9 +510,13 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
         const float j[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
         T u0, u1;
         jp_times(j, wsh[p - p0][0], wsh[p - p0][1], wsh[p - p0][2], u0, u1);
-        const long long q = cam_pos[s];
-        store_u(u_cm, q, u0, u1);
-        if (g_cm) g_cm[q] = jp_vinv_jpt(j, vsh[p - p0]);
+        if constexpr (kAcc) {
+            accumulate_jct_u(Jc32 + 18ll * s, u0, u1, u_cm + static_cast<long long>(kX32) * cam_pos[s]);
+        } else {
+            const long long q = cam_pos[s];
+            store_u(u_cm, q, u0, u1);
+            if (g_cm) g_cm[q] = jp_vinv_jpt(j, vsh[p - p0]);
+        }
     }
 }
 
@@ -651,6 +684,34 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize(const int* __restrict__ ca
     if (i < 9 * C) {
         const int c = i / 9, k = i % 9;
         const double qi = damped_u_row_dot(U + 81ll * c, k, lambda, p + 9ll * c) - chunk_sum(cam_chunk_off, part, c, k);
+        q[i] = qi;
+        v = p[i] * qi;
+    }
+    const double t = block_sum<kVT>(v, sh);
+    if (threadIdx.x == 0) red[blockIdx.x] = t;
+}
+
+// pcg_q_finalize for the one-pass product: q = U_lambda p - sum of the
+// camera's accumulators (12 floats each, 9 used; camera c's at [acc_off[c],
+// acc_off[c + 1])) in FP64, which it clears for the next product.
+__global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y, const int* __restrict__ acc_off,
+                                                         const double* __restrict__ U, double lambda,
+                                                         const double* __restrict__ p, int C,
+                                                         double* __restrict__ q, double* __restrict__ red,
+                                                         const double* __restrict__ sc) {
+    __shared__ double sh[kVT / 32];
+    if (sc[S_DONE] != 0.0) return;
+    const int i = blockIdx.x * kVT + threadIdx.x;
+    double v = 0.0;
+    if (i < 9 * C) {
+        const int c = i / 9, k = i % 9;
+        double sum = 0.0;
+        for (int r = acc_off[c]; r < acc_off[c + 1]; ++r) {
+            float* yr = y + static_cast<long long>(kX32) * r + k;
+            sum += static_cast<double>(*yr);
+            *yr = 0.f;
+        }
+        const double qi = damped_u_row_dot(U + 81ll * c, k, lambda, p + 9ll * c) - sum;
         q[i] = qi;
         v = p[i] * qi;
     }
@@ -1428,6 +1489,18 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     }
 }
 
+// The one-pass FP32 product (schur_point_pass with kAcc): y = sum over slots of
+// Jc^T u, accumulated in device memory (acc_id_: the slot's accumulator).
+static void implicit_parts_acc(Solver& s, const float* x, const double* done) {
+    cudaEvent_t ev = s.prof_start();
+    schur_point_pass<float, false, false, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
+        reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
+        s.s_pt_.get(), s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.Vinv32_.get(), nullptr, s.bp_.get(), x,
+        0.0, s.y_acc_.get(), done, BacksubOut{}, nullptr);
+    GBA_LAUNCH_CHECK();
+    s.prof_stop("schur_matvec_f32", ev);
+}
+
 void launch_split_ff(const double* x, long long n, float* out, cudaStream_t s) {
     if (n <= 0) return;
     split_kernel<<<ceil_div(n, kVT), kVT, 0, s>>>(x, n, out);
@@ -1559,9 +1632,15 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         if (opts.pcg_max_iters <= 0) read_back({{h, sc, sizeof h}});  // the state pcg_init_finalize left
         for (int it = 0, next = 1; it < opts.pcg_max_iters; it += batch, batch = std::min(next, kCheck), next *= 2) {
             for (int j = 0; j < batch; ++j) {
-                implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
-                pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
-                                                         pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                if (one_pass_) {
+                    implicit_parts_acc(*this, pcg_p32_.get(), done);
+                    pcg_q_finalize_acc<<<nvb, kVT, 0, stream_>>>(y_acc_.get(), acc_off_.get(), U_.get(), lambda,
+                                                                 pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                } else {
+                    implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
+                    pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(),
+                                                             lambda, pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                }
                 GBA_LAUNCH_CHECK();
                 pcg_update<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(),
                                                      pcg_q_.get(), Pinv_.get(), C_, red_pq, nvb, red, red2, sc, Zc,
@@ -1709,10 +1788,12 @@ void Solver::coarse_prepare(double lambda) {
         cpart9_.alloc(81ull * std::max(n_cchunk_, 1));
     }
     cudaEvent_t ev = prof_start();
+    cudaEvent_t ev1 = prof_start();
     model_->coarse_basis(*this, lambda, cz_.get());
     coarse_zb_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, czb_.get());
     GBA_LAUNCH_CHECK();
-    cudaEvent_t ev1 = prof_start();
+    prof_stop("coarse_basis", ev1);
+    ev1 = prof_start();
     coarse_point_pass9<<<n_pchunk_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(),
                                                        s_cam_.get(), s_pt_.get(), cam_pos_.get(), Jc32_.get(),
                                                        Jp32_.get(), Vinv32_.get(), czb_.get(), cu9_.get());
@@ -1735,7 +1816,18 @@ void Solver::coarse_prepare(double lambda) {
     coarse_einv_kernel<<<1, 128, 0, stream_>>>(gram, nvb, ceinv_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_gram", ev1);
-    prof_stop("coarse_basis", ev);
+    prof_stop("coarse_prepare", ev);
+}
+
+void Solver::set_matvec(int mode) {
+    if (form_ == SolverForm::Plain) throw std::invalid_argument("the PCG product belongs to the mixed forms");
+    if (mode < 0 || mode > 2) throw std::invalid_argument("matvec mode: 0 auto, 1 two-pass, 2 one-pass");
+    one_pass_ = mode != 1;
+    if (one_pass_ && !y_acc_.get()) {
+        const size_t n = static_cast<size_t>(kX32) * std::max(n_acc_, 1);
+        y_acc_.alloc(n);
+        GBA_CUDA_CHECK(cudaMemsetAsync(y_acc_.get(), 0, n * sizeof(float), stream_));
+    }
 }
 
 }  // namespace gba

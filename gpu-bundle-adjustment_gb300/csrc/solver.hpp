@@ -226,6 +226,19 @@ public:
     DevBuf<float> dcff_;      // mixed: float-float copy of dc (hi, lo per entry) for the refinement residual
     DevBuf<float> pcg_p32_; // mixed: FP32 copy of the PCG direction for the FP32 matvec
     DevBuf<int> cam_pos_;   // camera-major position of each slot (inverse of cam_slots_)
+    // mixed: the one-pass FP32 PCG product (pcg.cu): the point pass adds each
+    // slot's Jc^T u into an accumulator of its camera (y_acc_, 12 floats each)
+    // instead of leaving u for a camera pass; else the two-pass product. A
+    // camera has one accumulator per kAccSlots of its observations (its
+    // camera-major positions), so that no FP32 accumulator sums more terms
+    // than a camera-pass chunk: camera c's at [acc_off_[c], acc_off_[c + 1]),
+    // the slot's in acc_id_.
+    static constexpr int kAccSlots = 256;
+    bool one_pass_ = false;
+    int n_acc_ = 0;
+    DevBuf<int> acc_id_, acc_off_;
+    DevBuf<float> y_acc_;
+    void set_matvec(int mode);  // 0 auto (one pass), 1 two-pass (deterministic), 2 one-pass
     DevBuf<double> cam_pre_;  // per-camera rotation matrix, translation, intrinsics (16 per camera)
     DevBuf<float> cam_pre_ff_;  // mixed: the same as float-float pairs (32 floats per camera)
     DevBuf<float> pts_ff_;      // mixed: float-float copy of the points being costed (6 floats per point)
@@ -333,6 +346,7 @@ void launch_batch_inverse3_spd(const double* A, double* Ainv, int* ok, int n, cu
 // kept per column from the diagonal down. info (device int) = 0 on success,
 // else the 1-based failed column.
 void dense_potrf(double* A, int n, int lda, int bt, int* info, cudaStream_t s);
+
 // Solves L L^T x = b in place (b on the device, length n), L from dense_potrf.
 void dense_potrs(const double* L, int n, int lda, int bt, double* b, const int* info, cudaStream_t s);
 // Residual + Jacobian for E independent observations (device pointers, original

@@ -219,6 +219,16 @@ __global__ void gather_cm_kernel(const int* __restrict__ cam_slots, const int* _
 }
 
 // offsets[k] = first position i with keys[i] >= k, for k = 0..nk (keys sorted).
+// acc_id[s] = acc_off[cam(s)] + (camera-major position of s - cam_off[cam(s)]) / per
+__global__ void acc_id_kernel(const int* __restrict__ s_cam, const int* __restrict__ cam_pos,
+                              const int* __restrict__ cam_off, const int* __restrict__ acc_off, int E, int per,
+                              int* __restrict__ acc_id) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+        const int c = s_cam[s];
+        acc_id[s] = acc_off[c] + (cam_pos[s] - cam_off[c]) / per;
+    }
+}
+
 __global__ void csr_offsets_kernel(const int* __restrict__ keys, int n, int nk, int* __restrict__ off) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int prev = i == 0 ? -1 : keys[i - 1];
@@ -386,6 +396,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         u_.alloc(2ull * E);
         g_cm_.alloc(4ull * E);
         pcg_s_.alloc(16);
+        set_matvec(0);
     }
     sync();
 }
@@ -594,6 +605,20 @@ void Solver::build_structure(const int* obs_cam, const int* obs_pt, const double
     }
     cam_chunk_off[C] = static_cast<int>(cbeg.size());
     n_cchunk_ = static_cast<int>(cbeg.size());
+    if (form_ != SolverForm::Plain) {  // the one-pass product's accumulators
+        std::vector<int> acc_off(C + 1, 0);
+        for (int c = 0; c < C; ++c)
+            acc_off[c + 1] = acc_off[c] + (h_cam_off[c + 1] - h_cam_off[c] + kAccSlots - 1) / kAccSlots;
+        n_acc_ = acc_off[C];
+        acc_off_.alloc(C + 1ull);
+        acc_id_.alloc(E);
+        GBA_CUDA_CHECK(cudaMemcpyAsync(acc_off_.get(), acc_off.data(), (C + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                                       stream_));
+        acc_id_kernel<<<grid_for(E), 256, 0, stream_>>>(s_cam_.get(), cam_pos_.get(), cam_off_.get(), acc_off_.get(),
+                                                        E, kAccSlots, acc_id_.get());
+        GBA_LAUNCH_CHECK();
+        sync();  // acc_off dies at scope exit
+    }
 
     cchunk_begin_.alloc(std::max<size_t>(cbeg.size(), 1));
     cchunk_cam_.alloc(std::max<size_t>(ccam.size(), 1));

@@ -58,6 +58,7 @@ class LMOptions(C.Structure):
         ("loss", C.c_int),
         ("huber_delta", C.c_double),
         ("schur_layout", C.c_int),
+        ("deterministic", C.c_int),
     ]
 
 
@@ -158,6 +159,7 @@ _SIG = {
     "gba_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "gba_solver_set_preconditioner": (C.c_int, [C.c_void_p, C.c_int]),
     "gba_solver_set_schur_layout": (C.c_int, [C.c_void_p, C.c_int]),
+    "gba_solver_set_matvec": (C.c_int, [C.c_void_p, C.c_int, _ip]),
     "gba_solver_schur_band": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
     "gba_band_potrf": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "gba_band_potrs": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -497,6 +499,14 @@ class Solver:
     def set_preconditioner(self, mode: str = "judge") -> None:
         """Learned form: "judge" (default), "learned" (always) or "block-jacobi" (never learned)."""
         _check(lib.gba_solver_set_preconditioner(self.h, {"judge": 0, "learned": 1, "block-jacobi": 2}[mode]))
+
+    def set_matvec(self, mode: str = "auto") -> bool:
+        """Mixed forms: the FP32 PCG product, "auto", "two-pass", "one-pass" or "query";
+        returns whether the one-pass product is in use."""
+        v = C.c_int()
+        _check(lib.gba_solver_set_matvec(self.h, {"query": -1, "auto": 0, "two-pass": 1, "one-pass": 2}[mode],
+                                         C.byref(v)))
+        return bool(v.value)
 
     def set_schur_layout(self, layout: str = "auto") -> None:
         """Plain form: storage of S, "auto", "dense" or "band" (from the next schur_dense on)."""

@@ -68,6 +68,9 @@ struct LMOptions {
     // Cuthill-McKee order; auto takes the band when it is at most a third of the
     // dense matrix)
     int schur_layout = 0;
+    // mixed forms: 1 = the ordered two-pass FP32 PCG product (bit-identical
+    // reruns); 0 = the one-pass product (atomic adds: reruns agree to rounding)
+    int deterministic = 0;
 };
 
 struct LMResult {

@@ -57,6 +57,8 @@ typedef struct gba_lm_options {
     int loss;                 /* GBA_LOSS_NONE (0) or GBA_LOSS_HUBER (1) */
     double huber_delta;       /* 1.0 */
     int schur_layout;         /* plain form: GBA_SCHUR_AUTO (0), GBA_SCHUR_DENSE (1) or GBA_SCHUR_BAND (2) */
+    int deterministic;        /* mixed forms: 0 = one-pass PCG product; 1 = ordered two-pass product,
+                                 bit-identical reruns (gba_solver_set_matvec) */
 } gba_lm_options;
 
 /* Storage of the plain form's reduced camera system S: dense (9C)^2, or a band
@@ -174,6 +176,16 @@ int gba_solver_damp_invert_v(gba_solver* s, double lambda, unsigned long long* o
 /* Plain form: dense S assembly + FP64 DMMA Cholesky + solve (reference
  * src/lm.cu:488-604). out_info: 0, or the failed pivot column (1-based). */
 int gba_solver_schur_dense(gba_solver* s, double lambda, int* out_info);
+/* Mixed forms: the FP32 product S p inside PCG. 0 (default) and 2 = one pass
+ * over the observations, adding each observation's Jc^T u into per-camera
+ * accumulators with device atomics (its Jacobian rows read once from HBM; the
+ * order of the atomic adds varies between runs, so results agree to FP32
+ * rounding, not bit for bit); 1 = two passes (point pass, then camera pass
+ * over a camera-major copy of the Jacobian rows; ordered sums, bit-identical
+ * reruns); -1 = query only. The refinement residual, right-hand side and
+ * back-substitution are the ordered two-pass products in every mode.
+ * [host] out_one_pass (may be NULL): 1 if the one-pass product is in use. */
+int gba_solver_set_matvec(gba_solver* s, int mode, int* out_one_pass);
 /* Plain form: storage of S from the next gba_solver_schur_dense on
  * (GBA_SCHUR_AUTO / DENSE / BAND; gba_solve takes gba_lm_options.schur_layout). */
 int gba_solver_set_schur_layout(gba_solver* s, int layout);
@@ -210,7 +222,10 @@ int gba_solver_reset_params(gba_solver* s);
  * schur_assemble, dense_potrf, backsub (plain form); point_pass_f32,
  * camera_pass_f32, cost_ff, schur_rhs_point_pass, schur_rhs_camera_pass,
  * schur_point_pass_f32, schur_camera_pass_f32, schur_point_pass_ff,
- * schur_camera_pass_ff, backsub, mlp_forward (mixed forms). */
+ * schur_camera_pass_ff, backsub (mixed forms); coarse_prepare (the learned
+ * form's whole coarse-space set-up per trial), within it coarse_basis (the MLP
+ * and the basis; mlp_forward within that), coarse_point_pass9,
+ * coarse_camera_pass9, coarse_gram; coarse_apply (the correction inside PCG). */
 int gba_solver_profile(gba_solver* s, int enable);
 int gba_solver_kernel_stats(gba_solver* s, const char* name, long long* out_launches, double* out_total_ms);
 int gba_solver_profile_reset(gba_solver* s);
