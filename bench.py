@@ -255,7 +255,7 @@ KERNELS = ("schur_matvec_f32", "schur_point_pass_f32", "schur_camera_pass_f32", 
            "schur_camera_pass_ff",
            "point_pass_f32", "camera_pass_f32", "point_pass_f64", "camera_pass_f64", "cost_f64", "cost_ff",
            "backsub", "schur_rhs_point_pass", "schur_rhs_camera_pass", "mlp_forward", "schur_assemble",
-           "dense_potrf", "coarse_prepare", "coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram",
+           "dense_potrf", "pcg_q_finalize", "coarse_prepare", "coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram",
            "coarse_apply")
 # stages that contain others (their times are not additional)
 NESTED = {"coarse_prepare": ["coarse_basis", "coarse_point_pass9", "coarse_camera_pass9", "coarse_gram"],

@@ -14,6 +14,13 @@ namespace gba {
 // passes: 9 used, padded to 48 B so that a gather is two float4 and a float.
 constexpr int kX32 = 12;
 
+// The mixed forms' FP32 Jacobian rows are stored component-major: component k
+// of slot s at Jc32[k js + s] (k < 18: row 0 then row 1 of the 2 x 9 camera
+// block) and Jp32[k js + s] (k < 6), js = the slot count rounded up to 32.
+// A warp's load or store of one component is then 128 contiguous bytes (the
+// row-major 72- and 24-byte records cost 4x the L1 wavefronts).
+inline long long jacobian_stride(long long E) { return (E + 31) / 32 * 32; }
+
 // Thrown by the host driver on CUDA failure (the C-ABI layer converts it to a
 // status code; nothing throws across the ABI).
 struct CudaError : std::runtime_error {

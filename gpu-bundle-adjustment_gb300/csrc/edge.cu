@@ -209,8 +209,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
     const int4* __restrict__ prange, const int* __restrict__ pt_off, const int* __restrict__ s_cam,
     const int* __restrict__ s_pt, const float* __restrict__ cams32,
     const float2* __restrict__ ptsff, const float2* __restrict__ r_cur, const int* __restrict__ cam_pos,
-    float* __restrict__ Jc32, float* __restrict__ Jp32, float* __restrict__ J32c, double* __restrict__ V, double* __restrict__ bp,
-    unsigned long long* __restrict__ counters, float delta) {
+    float* __restrict__ Jc32, float* __restrict__ Jp32, long long js, float* __restrict__ J32c,
+    double* __restrict__ V, double* __restrict__ bp, unsigned long long* __restrict__ counters, float delta) {
     __shared__ float seg[9][kPT];  // warp-segment sums, at each segment's last slot
     __shared__ unsigned long long redu[kPT / 32];
     __shared__ __align__(16) float stg[kPT * kStg];  // this pass's rows, per slot (kStg floats)
@@ -271,6 +271,11 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
                 for (int q = 0; q < 24; ++q) J[q] = 0.f;
                 r[0] = r[1] = 0.f;
             }
+            // component-major rows: lane-contiguous stores
+#pragma unroll
+            for (int k = 0; k < 18; ++k) Jc32[k * js + s] = J[k];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) Jp32[k * js + s] = J[18 + k];
             float4* st = reinterpret_cast<float4*>(stg + kStg * threadIdx.x);
 #pragma unroll
             for (int k = 0; k < 4; ++k) st[k] = make_float4(J[4 * k], J[4 * k + 1], J[4 * k + 2], J[4 * k + 3]);
@@ -288,25 +293,13 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
             for (int i = 0; i < 3; ++i) v[6 + i] = -(Jp[i] * r[0] + Jp[3 + i] * r[1]);
         }
         {
-            // The warp's slots are contiguous: write their rows as contiguous
-            // runs (256 B per instruction) and each camera record by five
-            // adjacent lanes, instead of one 8- or 16-byte piece per lane
-            // (4x fewer L2 store requests; 891 -> 582 us per launch on the
-            // 8.8M-observation workload).
+            // Each camera record (camera-major) is written by five adjacent
+            // lanes from the staging buffer, instead of one 16-byte piece per
+            // lane (4x fewer L2 store requests).
             __syncwarp();
             const int w0 = base + (threadIdx.x & ~31);
             const int n = max(0, min(32, s1 - w0));
             const float* ws = stg + kStg * (threadIdx.x & ~31);
-            float2* gc = reinterpret_cast<float2*>(Jc32 + 18ll * w0);
-            for (int t = lane; t < 9 * n; t += 32) {
-                const int j = t / 9, k = t - 9 * j;
-                gc[t] = *reinterpret_cast<const float2*>(ws + kStg * j + 2 * k);
-            }
-            float2* gp = reinterpret_cast<float2*>(Jp32 + 6ll * w0);
-            for (int t = lane; t < 3 * n; t += 32) {
-                const int j = t / 3, k = t - 3 * j;
-                gp[t] = *reinterpret_cast<const float2*>(ws + kStg * j + 20 + 2 * k);
-            }
             for (int t = lane; t < 5 * n; t += 32) {
                 const int j = t / 5, k = t - 5 * j;
                 const long long qj = __float_as_int(ws[kStg * j + 26]);
@@ -747,7 +740,7 @@ void Solver::accumulate_launch() {
         cudaEvent_t ev = prof_start();
         point_pass_f32<<<n_pchunk_, kPT, 0, stream_>>>(
             reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(), s_cam_.get(), s_pt_.get(), cams32_.get(), reinterpret_cast<const float2*>(pts_ff_.get()), rc, cam_pos_.get(), Jc32_.get(), Jp32_.get(),
-            J32c_.get(), V_.get(), bp_.get(), counters_.get(), static_cast<float>(huber_delta_));
+            js_, J32c_.get(), V_.get(), bp_.get(), counters_.get(), static_cast<float>(huber_delta_));
         GBA_LAUNCH_CHECK();
         prof_stop("point_pass_f32", ev);
         if (n_cchunk_ > 0) {

@@ -160,23 +160,17 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// J = [Jc(18), Jp(6)] of slot s
-__device__ __forceinline__ void load_j(const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long s,
-                                       float* J) {
-    const float2* qc = reinterpret_cast<const float2*>(Jc32 + 18 * s);
+// J = [Jc(18), Jp(6)] of slot s (component-major rows, stride js)
+__device__ __forceinline__ void load_j(const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long js,
+                                       long long s, float* J) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        const float2 v = qc[k];
-        J[2 * k] = v.x;
-        J[2 * k + 1] = v.y;
-    }
-    const float2* qp = reinterpret_cast<const float2*>(Jp32 + 6 * s);
+    for (int k = 0; k < 18; ++k) J[k] = Jc32[k * js + s];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float2 v = qp[k];
-        J[18 + 2 * k] = v.x;
-        J[19 + 2 * k] = v.y;
-    }
+    for (int k = 0; k < 6; ++k) J[18 + k] = Jp32[k * js + s];
+}
+__device__ __forceinline__ void load_jp(const float* __restrict__ Jp32, long long js, long long s, float* jp) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) jp[k] = Jp32[k * js + s];
 }
 
 // w = V'^-1 z (3x3 packed symmetric)
@@ -235,16 +229,12 @@ __device__ __forceinline__ float4 jp_vinv_jpt(const float* j, const float* vi) {
 // rows are re-read here; the point pass loaded them moments before, so they
 // come from L1 or L2, not HBM.
 template <typename T>
-__device__ __forceinline__ void accumulate_jct_u(const float* __restrict__ jc, T u0, T u1, T* y) {
+__device__ __forceinline__ void accumulate_jct_u(const float* __restrict__ Jc32, long long js, long long s, T u0,
+                                                 T u1, T* y) {
     if constexpr (sizeof(T) == 4) {
-        const float2* q = reinterpret_cast<const float2*>(jc);
         float Jc[18];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const float2 v = q[t];
-            Jc[2 * t] = v.x;
-            Jc[2 * t + 1] = v.y;
-        }
+        for (int t = 0; t < 18; ++t) Jc[t] = Jc32[t * js + s];
         float r[9];
 #pragma unroll
         for (int t = 0; t < 9; ++t) r[t] = fmaf(Jc[t], u0, Jc[9 + t] * u1);
@@ -277,7 +267,7 @@ template <typename T, bool kBack = false, bool kRhs = false, bool kAcc = false>
 __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int4* __restrict__ prange, const int* __restrict__ pchunk, const int* __restrict__ pt_off,
                                                        const int* __restrict__ s_cam, const int* __restrict__ s_pt,
                                                        const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
-                                                       const float* __restrict__ Jp32,
+                                                       const float* __restrict__ Jp32, long long js,
                                                        const float* __restrict__ vinv_hi,
                                                        const float* __restrict__ vinv_lo,
                                                        const double* __restrict__ bp, const T* __restrict__ xt,
@@ -342,7 +332,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
                 const int cam = s_cam[s];
                 q = cam_pos[s];  // kAcc: the slot's accumulator
                 float J[24];
-                load_j(Jc32, Jp32, s, J);
+                load_j(Jc32, Jp32, js, s, J);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) jp[k] = J[18 + k];
                 T xv[9];
@@ -404,14 +394,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
         if (s < s1) {
             key = s_pt[s];
             q = cam_pos[s];
-            const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
-            const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
-            jp[0] = j01.x;
-            jp[1] = j01.y;
-            jp[2] = j23.x;
-            jp[3] = j23.y;
-            jp[4] = j45.x;
-            jp[5] = j45.y;
+            load_jp(Jp32, js, s, jp);
         }
     }
     if constexpr (kSharedVinv) {
@@ -496,7 +479,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
             T u0, u1;
             jp_times(jp, wsh[key - p0][0], wsh[key - p0][1], wsh[key - p0][2], u0, u1);
             if constexpr (kAcc)
-                accumulate_jct_u(Jc32 + 18ll * (s0 + threadIdx.x), u0, u1, u_cm + static_cast<long long>(kX32) * q);
+                accumulate_jct_u(Jc32, js, s0 + threadIdx.x, u0, u1, u_cm + static_cast<long long>(kX32) * q);
             else
                 store_u(u_cm, q, u0, u1);
             if (g_cm) g_cm[q] = jp_vinv_jpt(jp, vsh[key - p0]);
@@ -505,13 +488,12 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
     }
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int p = s_pt[s];
-        const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
-        const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
-        const float j[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
+        float j[6];
+        load_jp(Jp32, js, s, j);
         T u0, u1;
         jp_times(j, wsh[p - p0][0], wsh[p - p0][1], wsh[p - p0][2], u0, u1);
         if constexpr (kAcc) {
-            accumulate_jct_u(Jc32 + 18ll * s, u0, u1, u_cm + static_cast<long long>(kX32) * cam_pos[s]);
+            accumulate_jct_u(Jc32, js, s, u0, u1, u_cm + static_cast<long long>(kX32) * cam_pos[s]);
         } else {
             const long long q = cam_pos[s];
             store_u(u_cm, q, u0, u1);
@@ -616,6 +598,183 @@ __global__ void __launch_bounds__(kCT) schur_camera_pass(const int* __restrict__
     }
 }
 
+// ---------------------------------------------------------------- one-pass product, warp chunks
+// The one-pass FP32 product over warp chunks: whole points packed into runs of
+// at most 32 slots, one run per warp, so that a point's slots never leave the
+// warp. Per slot (lane): v = Jp^T (Jc x), an inclusive segmented scan over the
+// warp gives each point's sum z at its last lane, which applies V'^-1 (loaded
+// by every lane of the point up front: one request per point), and every lane
+// takes its point's w from that lane (match + shuffle); then Jc^T (Jp w) goes
+// into the slot's accumulator. No shared memory and no barrier: a warp's
+// chain is loads -> shuffles -> atomics, and 64 warps per SM hide it. Points
+// with more than 32 observations go through the chunked point pass.
+constexpr int kMWarps = 8;  // warps per CTA
+__global__ void __launch_bounds__(32 * kMWarps) schur_matvec_warp(
+    const int2* __restrict__ wchunk, int n_wchunk, const int* __restrict__ s_cam, const int* __restrict__ s_pt,
+    const int* __restrict__ acc_id, const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long js,
+    const float* __restrict__ vinv, const float* __restrict__ x, float* __restrict__ y,
+    const double* __restrict__ done) {
+    if (done && *done != 0.0) return;
+    const int wid = blockIdx.x * kMWarps + (threadIdx.x >> 5);
+    if (wid >= n_wchunk) return;  // whole warps leave together
+    const int lane = threadIdx.x & 31;
+    const int2 r = wchunk[wid];
+    const int s = r.x + lane;
+    const bool has = s < r.y;
+    int key = -1, aid = 0;
+    float J[24], vi[6];
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    if (has) {
+        key = s_pt[s];
+        aid = acc_id[s];
+        float xv[9];
+        load_x(x, s_cam[s], xv);
+        load_vinv(vinv, nullptr, key, vi);
+        load_j(Jc32, Jp32, js, s, J);
+        float t0 = 0.f, t1 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            t0 = fmaf(J[c], xv[c], t0);
+            t1 = fmaf(J[9 + c], xv[c], t1);
+        }
+        v0 = fmaf(J[18], t0, J[21] * t1);
+        v1 = fmaf(J[19], t0, J[22] * t1);
+        v2 = fmaf(J[20], t0, J[23] * t1);
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float u0 = __shfl_up_sync(0xffffffffu, v0, d);
+        const float u1 = __shfl_up_sync(0xffffffffu, v1, d);
+        const float u2 = __shfl_up_sync(0xffffffffu, v2, d);
+        const int kd = __shfl_up_sync(0xffffffffu, key, d);
+        if (lane >= d && kd == key) {
+            v0 += u0;
+            v1 += u1;
+            v2 += u2;
+        }
+    }
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    if (has) apply_vinv(vi, v0, v1, v2, w0, w1, w2);  // meaningful at the point's last lane
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    const int last = 31 - __clz(grp);
+    w0 = __shfl_sync(0xffffffffu, w0, last);
+    w1 = __shfl_sync(0xffffffffu, w1, last);
+    w2 = __shfl_sync(0xffffffffu, w2, last);
+    if (has) {
+        float u0, u1;
+        jp_times(J + 18, w0, w1, w2, u0, u1);
+        float q[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) q[c] = fmaf(J[c], u0, J[9 + c] * u1);
+        float* ya = y + static_cast<long long>(kX32) * aid;
+        atomicAdd(reinterpret_cast<float4*>(ya), make_float4(q[0], q[1], q[2], q[3]));
+        atomicAdd(reinterpret_cast<float4*>(ya) + 1, make_float4(q[4], q[5], q[6], q[7]));
+        atomicAdd(ya + 8, q[8]);
+    }
+}
+
+// The one-pass product for points with 33 to 256 observations: a CTA takes
+// a list of such points (not consecutive) whose slots total at most 256 and
+// lays them out as one virtual chunk (thread t: the t-th slot of the list);
+// the point pass of schur_point_pass follows, then Jc^T u into the slot's
+// accumulator. lchunk[k] = {first entry in lpts, entries}.
+__global__ void __launch_bounds__(kPT) schur_matvec_long(
+    const int2* __restrict__ lchunk, const int* __restrict__ lpts, const int* __restrict__ pt_off,
+    const int* __restrict__ s_cam, const int* __restrict__ acc_id, const float* __restrict__ Jc32,
+    const float* __restrict__ Jp32, long long js, const float* __restrict__ vinv, const float* __restrict__ x,
+    float* __restrict__ y, const double* __restrict__ done) {
+    constexpr int kMaxPts = kPT / 33 + 1;  // points of more than 32 slots in 256
+    __shared__ int pb[kMaxPts + 1], ps[kMaxPts], pid[kMaxPts];  // virtual begin, first real slot, point
+    __shared__ float seg[kPT][3];
+    __shared__ float wsh[kMaxPts][3];
+    if (done && *done != 0.0) return;
+    const int2 lc = lchunk[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0) {
+        int v = 0;
+        for (int j = 0; j < lc.y; ++j) {
+            const int p = lpts[lc.x + j];
+            pid[j] = p;
+            ps[j] = pt_off[p];
+            pb[j] = v;
+            v += pt_off[p + 1] - ps[j];
+        }
+        pb[lc.y] = v;
+    }
+    __syncthreads();
+    const int n = pb[lc.y];
+    int key = -1, aid = 0;
+    long long sl = 0;
+    float J[24];
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    if (tid < n) {
+        int j = 0;
+        while (tid >= pb[j + 1]) ++j;
+        key = j;
+        sl = ps[j] + (tid - pb[j]);
+        aid = acc_id[sl];
+        float xv[9];
+        load_x(x, s_cam[sl], xv);
+        load_j(Jc32, Jp32, js, sl, J);
+        float t0 = 0.f, t1 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            t0 = fmaf(J[c], xv[c], t0);
+            t1 = fmaf(J[9 + c], xv[c], t1);
+        }
+        v0 = fmaf(J[18], t0, J[21] * t1);
+        v1 = fmaf(J[19], t0, J[22] * t1);
+        v2 = fmaf(J[20], t0, J[23] * t1);
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float u0 = __shfl_up_sync(0xffffffffu, v0, d);
+        const float u1 = __shfl_up_sync(0xffffffffu, v1, d);
+        const float u2 = __shfl_up_sync(0xffffffffu, v2, d);
+        const int kd = __shfl_up_sync(0xffffffffu, key, d);
+        if (lane >= d && kd == key) {
+            v0 += u0;
+            v1 += u1;
+            v2 += u2;
+        }
+    }
+    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    if (lane == 31 || knext != key) {
+        seg[tid][0] = v0;
+        seg[tid][1] = v1;
+        seg[tid][2] = v2;
+    }
+    __syncthreads();
+    if (tid < lc.y) {  // owner of point entry tid: its warp segments in order
+        const int b = pb[tid], e = pb[tid + 1];
+        float z0 = 0.f, z1 = 0.f, z2 = 0.f;
+        for (int w = b >> 5; w <= (e - 1) >> 5; ++w) {
+            const int q = min(e - 1, 32 * w + 31);
+            z0 += seg[q][0];
+            z1 += seg[q][1];
+            z2 += seg[q][2];
+        }
+        float vi[6], w0, w1, w2;
+        load_vinv(vinv, nullptr, pid[tid], vi);
+        apply_vinv(vi, z0, z1, z2, w0, w1, w2);
+        wsh[tid][0] = w0;
+        wsh[tid][1] = w1;
+        wsh[tid][2] = w2;
+    }
+    __syncthreads();
+    if (tid < n) {
+        float u0, u1;
+        jp_times(J + 18, wsh[key][0], wsh[key][1], wsh[key][2], u0, u1);
+        float q[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) q[c] = fmaf(J[c], u0, J[9 + c] * u1);
+        float* ya = y + static_cast<long long>(kX32) * aid;
+        atomicAdd(reinterpret_cast<float4*>(ya), make_float4(q[0], q[1], q[2], q[3]));
+        atomicAdd(reinterpret_cast<float4*>(ya) + 1, make_float4(q[4], q[5], q[6], q[7]));
+        atomicAdd(ya + 8, q[8]);
+    }
+}
+
 __device__ __forceinline__ double damped_u_row_dot(const double* __restrict__ Uc, int k, double lambda,
                                                    const double* __restrict__ xc) {
     double s = 0.0;
@@ -691,9 +850,12 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize(const int* __restrict__ ca
     if (threadIdx.x == 0) red[blockIdx.x] = t;
 }
 
-// pcg_q_finalize for the one-pass product: q = U_lambda p - sum of the
+// pcg_q_finalize for the one-pass product: q = U_lambda p - the sum of the
 // camera's accumulators (12 floats each, 9 used; camera c's at [acc_off[c],
-// acc_off[c + 1])) in FP64, which it clears for the next product.
+// acc_off[c + 1])), which it clears for the next product. One warp per camera
+// (cameras strided over the grid's warps; the grid has one warp per camera):
+// lanes take the accumulators in turn as float4 runs, then a warp reduction;
+// one p.q partial per block.
 __global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y, const int* __restrict__ acc_off,
                                                          const double* __restrict__ U, double lambda,
                                                          const double* __restrict__ p, int C,
@@ -701,21 +863,44 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y,
                                                          const double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
     if (sc[S_DONE] != 0.0) return;
-    const int i = blockIdx.x * kVT + threadIdx.x;
-    double v = 0.0;
-    if (i < 9 * C) {
-        const int c = i / 9, k = i % 9;
-        double sum = 0.0;
-        for (int r = acc_off[c]; r < acc_off[c + 1]; ++r) {
-            float* yr = y + static_cast<long long>(kX32) * r + k;
-            sum += static_cast<double>(*yr);
-            *yr = 0.f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double pq = 0.0;
+    for (int c = blockIdx.x * (kVT / 32) + warp; c < C; c += gridDim.x * (kVT / 32)) {
+        // FP32 sums (a lane's accumulators, then the warp tree: as few terms
+        // per sum as the two-pass camera pass), FP64 from the total on
+        float a[9];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) a[t] = 0.f;
+        for (int r = acc_off[c] + lane; r < acc_off[c + 1]; r += 32) {
+            float* yr = y + static_cast<long long>(kX32) * r;
+            const float4 A = reinterpret_cast<float4*>(yr)[0], B = reinterpret_cast<float4*>(yr)[1];
+            const float c8 = yr[8];
+            a[0] += A.x;
+            a[1] += A.y;
+            a[2] += A.z;
+            a[3] += A.w;
+            a[4] += B.x;
+            a[5] += B.y;
+            a[6] += B.z;
+            a[7] += B.w;
+            a[8] += c8;
+            reinterpret_cast<float4*>(yr)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+            reinterpret_cast<float4*>(yr)[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            yr[8] = 0.f;
         }
-        const double qi = damped_u_row_dot(U + 81ll * c, k, lambda, p + 9ll * c) - sum;
-        q[i] = qi;
-        v = p[i] * qi;
+        double mine = 0.0;
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const float v = warp_sum(a[t]);
+            if (lane == t) mine = static_cast<double>(v);
+        }
+        if (lane < 9) {
+            const double qi = damped_u_row_dot(U + 81ll * c, lane, lambda, p + 9ll * c) - mine;
+            q[9ll * c + lane] = qi;
+            pq += p[9ll * c + lane] * qi;
+        }
     }
-    const double t = block_sum<kVT>(v, sh);
+    const double t = block_sum<kVT>(pq, sh);
     if (threadIdx.x == 0) red[blockIdx.x] = t;
 }
 
@@ -899,7 +1084,7 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
                                                             const int* __restrict__ s_pt,
                                                             const int* __restrict__ cam_pos,
                                                             const float* __restrict__ Jc32,
-                                                            const float* __restrict__ Jp32,
+                                                            const float* __restrict__ Jp32, long long js,
                                                             const float* __restrict__ vinv_hi,
                                                             const __nv_bfloat16* __restrict__ Zb,
                                                             float* __restrict__ u9) {
@@ -927,7 +1112,7 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
         if (s < s1) {
             key = s_pt[s];
             float J[24];
-            load_j(Jc32, Jp32, s, J);
+            load_j(Jc32, Jp32, js, s, J);
             const uint4* z4 = reinterpret_cast<const uint4*>(Zb + static_cast<long long>(kZs) * s_cam[s]);
             float Z[kZs];
 #pragma unroll
@@ -994,9 +1179,8 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
     __syncthreads();
     for (int s = s0 + threadIdx.x; s < s1; s += kPT) {
         const int pl = s_pt[s] - p0;
-        const float2* Jp2 = reinterpret_cast<const float2*>(Jp32 + 6ll * s);
-        const float2 j01 = Jp2[0], j23 = Jp2[1], j45 = Jp2[2];
-        const float jp[6] = {j01.x, j01.y, j23.x, j23.y, j45.x, j45.y};
+        float jp[6];
+        load_jp(Jp32, js, s, jp);
         const float* w = wsh + pl * (KV + 1);
         float2* out = reinterpret_cast<float2*>(u9 + 18ll * cam_pos[s]);
 #pragma unroll
@@ -1468,7 +1652,7 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     float4* g = rhs ? reinterpret_cast<float4*>(s.g_cm_.get()) : nullptr;
     cudaEvent_t ev = s.prof_start();
     (rhs ? schur_point_pass<T, false, true> : schur_point_pass<T, false, false>)<<<s.n_pchunk_, kPT, 0, s.stream_>>>(reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
-                                                           s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
+                                                           s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_,
                                                            s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), x, a,
                                                            u, done, BacksubOut{}, g);
     GBA_LAUNCH_CHECK();
@@ -1493,11 +1677,25 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
 // Jc^T u, accumulated in device memory (acc_id_: the slot's accumulator).
 static void implicit_parts_acc(Solver& s, const float* x, const double* done) {
     cudaEvent_t ev = s.prof_start();
-    schur_point_pass<float, false, false, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-        reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(),
-        s.s_pt_.get(), s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.Vinv32_.get(), nullptr, s.bp_.get(), x,
-        0.0, s.y_acc_.get(), done, BacksubOut{}, nullptr);
-    GBA_LAUNCH_CHECK();
+    if (s.n_wchunk_ > 0) {
+        schur_matvec_warp<<<ceil_div(s.n_wchunk_, kMWarps), 32 * kMWarps, 0, s.stream_>>>(
+            reinterpret_cast<const int2*>(s.wchunk_.get()), s.n_wchunk_, s.s_cam_.get(), s.s_pt_.get(),
+            s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), x, s.y_acc_.get(), done);
+        GBA_LAUNCH_CHECK();
+    }
+    if (s.n_lchunk_ > 0) {  // points with 33 to 256 observations, packed per CTA
+        schur_matvec_long<<<s.n_lchunk_, kPT, 0, s.stream_>>>(
+            reinterpret_cast<const int2*>(s.lchunk_.get()), s.lpts_.get(), s.pt_off_.get(), s.s_cam_.get(),
+            s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), x, s.y_acc_.get(), done);
+        GBA_LAUNCH_CHECK();
+    }
+    if (s.n_huge_ > 0) {  // points with more than 256 observations, one range each
+        schur_point_pass<float, false, false, true><<<s.n_huge_, kPT, 0, s.stream_>>>(
+            reinterpret_cast<const int4*>(s.huge_range_.get()), nullptr, s.pt_off_.get(), s.s_cam_.get(),
+            s.s_pt_.get(), s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), nullptr,
+            s.bp_.get(), x, 0.0, s.y_acc_.get(), done, BacksubOut{}, nullptr);
+        GBA_LAUNCH_CHECK();
+    }
     s.prof_stop("schur_matvec_f32", ev);
 }
 
@@ -1518,11 +1716,11 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
                         s.dp_.get(), s.tpts_.get(), reinterpret_cast<float2*>(s.pts_ff_.get()), part};
     if (s.fast_solve_) {
         schur_point_pass<float, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
+            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_,
             s.Vinv32_.get(), nullptr, s.bp_.get(), s.pcg_p32_.get(), -1.0, nullptr, nullptr, bk, nullptr);
     } else {
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
-            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(),
+            reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_,
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
             nullptr, nullptr, bk, nullptr);
     }
@@ -1623,6 +1821,9 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         GBA_LAUNCH_CHECK();
         // p.q partials (nvb) and r.r / r.z partials (nub) in disjoint ranges
         double* red_pq = red2 + nub + 1;
+        // p.q partials: one per finalize block (one warp per camera for the
+        // one-pass product's accumulators)
+        const int npq = one_pass_ ? ceil_div(C_, kVT / 32) : nvb;
         // Launch batches sized from the previous inner solve's iteration count
         // (then 1, 2, 4, 8, 8, ...): a launch after convergence returns at once
         // but still dispatches its whole grid (tens of microseconds for the
@@ -1634,16 +1835,21 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             for (int j = 0; j < batch; ++j) {
                 if (one_pass_) {
                     implicit_parts_acc(*this, pcg_p32_.get(), done);
-                    pcg_q_finalize_acc<<<nvb, kVT, 0, stream_>>>(y_acc_.get(), acc_off_.get(), U_.get(), lambda,
+                    cudaEvent_t fev = prof_start();
+                    pcg_q_finalize_acc<<<npq, kVT, 0, stream_>>>(y_acc_.get(), acc_off_.get(), U_.get(), lambda,
                                                                  pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                    GBA_LAUNCH_CHECK();
+                    prof_stop("pcg_q_finalize", fev);
                 } else {
                     implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
+                    cudaEvent_t fev = prof_start();
                     pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(),
                                                              lambda, pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                    GBA_LAUNCH_CHECK();
+                    prof_stop("pcg_q_finalize", fev);
                 }
-                GBA_LAUNCH_CHECK();
                 pcg_update<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(),
-                                                     pcg_q_.get(), Pinv_.get(), C_, red_pq, nvb, red, red2, sc, Zc,
+                                                     pcg_q_.get(), Pinv_.get(), C_, red_pq, npq, red, red2, sc, Zc,
                                                      red_zr);
                 GBA_LAUNCH_CHECK();
                 if (coarse) {
@@ -1796,7 +2002,7 @@ void Solver::coarse_prepare(double lambda) {
     ev1 = prof_start();
     coarse_point_pass9<<<n_pchunk_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(),
                                                        s_cam_.get(), s_pt_.get(), cam_pos_.get(), Jc32_.get(),
-                                                       Jp32_.get(), Vinv32_.get(), czb_.get(), cu9_.get());
+                                                       Jp32_.get(), js_, Vinv32_.get(), czb_.get(), cu9_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_point_pass9", ev1);
     if (n_cchunk_ > 0) {
@@ -1827,6 +2033,61 @@ void Solver::set_matvec(int mode) {
         const size_t n = static_cast<size_t>(kX32) * std::max(n_acc_, 1);
         y_acc_.alloc(n);
         GBA_CUDA_CHECK(cudaMemsetAsync(y_acc_.get(), 0, n * sizeof(float), stream_));
+        // warp chunks: whole points packed greedily into runs of at most 32
+        // slots; points with more observations get a range of their own
+        std::vector<int> off(P_ + 1);
+        GBA_CUDA_CHECK(cudaMemcpyAsync(off.data(), pt_off_.get(), (P_ + 1ull) * sizeof(int), cudaMemcpyDeviceToHost,
+                                       stream_));
+        sync();
+        std::vector<int2> wc, lc;
+        std::vector<int> lp;
+        std::vector<int4> hr;
+        int b = -1, e = -1, lsum = 0;
+        for (int p = 0; p < P_; ++p) {
+            const int n = off[p + 1] - off[p];
+            if (n == 0) continue;
+            if (n > kPT) {
+                hr.push_back(make_int4(p, p + 1, off[p], off[p + 1]));
+                continue;
+            }
+            if (n > 32) {  // into the current long-point CTA list, or a new one
+                if (lc.empty() || lsum + n > kPT) {
+                    lc.push_back(make_int2(static_cast<int>(lp.size()), 0));
+                    lsum = 0;
+                }
+                lp.push_back(p);
+                ++lc.back().y;
+                lsum += n;
+                continue;
+            }
+            if (b >= 0 && (off[p] != e || off[p + 1] - b > 32)) {
+                wc.push_back(make_int2(b, e));
+                b = -1;
+            }
+            if (b < 0) b = off[p];
+            e = off[p + 1];
+        }
+        if (b >= 0) wc.push_back(make_int2(b, e));
+        n_wchunk_ = static_cast<int>(wc.size());
+        n_lchunk_ = static_cast<int>(lc.size());
+        n_huge_ = static_cast<int>(hr.size());
+        wchunk_.alloc(2 * std::max<size_t>(wc.size(), 1));
+        lchunk_.alloc(2 * std::max<size_t>(lc.size(), 1));
+        lpts_.alloc(std::max<size_t>(lp.size(), 1));
+        huge_range_.alloc(4 * std::max<size_t>(hr.size(), 1));
+        if (!wc.empty())
+            GBA_CUDA_CHECK(cudaMemcpyAsync(wchunk_.get(), wc.data(), wc.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                           stream_));
+        if (!lc.empty()) {
+            GBA_CUDA_CHECK(cudaMemcpyAsync(lchunk_.get(), lc.data(), lc.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                           stream_));
+            GBA_CUDA_CHECK(cudaMemcpyAsync(lpts_.get(), lp.data(), lp.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                           stream_));
+        }
+        if (!hr.empty())
+            GBA_CUDA_CHECK(cudaMemcpyAsync(huge_range_.get(), hr.data(), hr.size() * sizeof(int4),
+                                           cudaMemcpyHostToDevice, stream_));
+        sync();
     }
 }
 

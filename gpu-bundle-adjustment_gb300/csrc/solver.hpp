@@ -219,7 +219,8 @@ public:
     DevBuf<int> pchunk4_;  // per point chunk, int4 {first point, end point, first slot, end slot}
     // normal equations
     DevBuf<double> U_, bc_, V_, bp_, W_, JcR_, Vinv_;
-    DevBuf<float> Jc32_, Jp32_;  // mixed: FP32 Jacobian rows per slot, slot order (18 and 6 floats)
+    DevBuf<float> Jc32_, Jp32_;  // mixed: FP32 Jacobian rows, slot order, component-major (stride js_)
+    long long js_ = 0;
     DevBuf<float> J32c_;    // mixed: camera record [Jc(18), r(2)] per slot in camera-major position
     DevBuf<float> Vinv32_;  // mixed: FP32 copy of V'^-1 (6 per point) for the FP32 matvec
     DevBuf<float> Vinv32lo_;  // mixed: V'^-1 - Vinv32_ rounded to FP32 (float-float matvec)
@@ -231,11 +232,19 @@ public:
     // instead of leaving u for a camera pass; else the two-pass product. A
     // camera has one accumulator per kAccSlots of its observations (its
     // camera-major positions), so that no FP32 accumulator sums more terms
-    // than a camera-pass chunk: camera c's at [acc_off_[c], acc_off_[c + 1]),
-    // the slot's in acc_id_.
-    static constexpr int kAccSlots = 256;
+    // than a camera-pass thread and warp do (with 256 terms the refinement to
+    // 1e-8 on workload 3 ran out of steps): camera c's at [acc_off_[c],
+    // acc_off_[c + 1]), the slot's in acc_id_.
+    static constexpr int kAccSlots = 32;
     bool one_pass_ = false;
     int n_acc_ = 0;
+    // its work: warp chunks (whole points, at most 32 slots: int2 {first,
+    // end slot}); points with 33 to 256 observations in lists of at most 256
+    // slots per CTA (lchunk_: int2 {first entry of lpts_, entries}); longer
+    // points as ranges (int4 {p, p + 1, first slot, end slot}) for the
+    // chunked point pass
+    int n_wchunk_ = 0, n_lchunk_ = 0, n_huge_ = 0;
+    DevBuf<int> wchunk_, lchunk_, lpts_, huge_range_;
     DevBuf<int> acc_id_, acc_off_;
     DevBuf<float> y_acc_;
     void set_matvec(int mode);  // 0 auto (one pass), 1 two-pass (deterministic), 2 one-pass

@@ -358,7 +358,8 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
     cam_part_.alloc(54ull * std::max(n_cchunk_, 1));
     // block partials: the largest single reduction, or the PCG layout
     // [r.r | r.z | p.q] = max(9C/256, C/32) + C/32 + 9C/256 (+ separators)
-    red_part_.alloc(std::max(n_pchunk_, ceil_div(P, 256)) + 2 * ceil_div(9ll * C, 256) + 2 * ceil_div(C, 32) + 64);
+    red_part_.alloc(std::max(n_pchunk_, ceil_div(P, 256)) + 2 * ceil_div(9ll * C, 256) + 2 * ceil_div(C, 32) +
+                    ceil_div(C, 8) + 64);
     if (form_ == SolverForm::Plain) {
         W_.alloc(27ull * E);
         JcR_.alloc(20ull * E);
@@ -369,8 +370,9 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         info_.alloc(1);
         build_pairs();
     } else {
-        Jc32_.alloc(18ull * E);
-        Jp32_.alloc(6ull * E);
+        js_ = jacobian_stride(E);
+        Jc32_.alloc(18ull * js_);
+        Jp32_.alloc(6ull * js_);
         J32c_.alloc(20ull * E);
         judge_x_.alloc(9ull * C);
         Vinv32_.alloc(6ull * P);

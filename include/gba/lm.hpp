@@ -56,7 +56,7 @@ struct LMOptions {
     // ---- additive ----
     SolverForm form = SolverForm::Plain;
     double refine_tol = 1e-8;     // mixed: FP64 refinement stops at ||rhs - S dc|| <= tol ||rhs||
-    int refine_max_steps = 8;     // mixed: FP64 refinement steps per trial
+    int refine_max_steps = 12;    // mixed: FP64 refinement steps per trial (most take 2-4)
     double pcg_tol = 1e-4;        // mixed: relative residual target of each inner FP32 PCG solve
     int pcg_max_iters = 200;      // mixed: PCG iteration cap per inner solve
     std::string model_path;       // learned form: MLP weights file (gba_mlp binary)

@@ -48,7 +48,7 @@ typedef struct gba_lm_options {
     int verbose;              /* 0 */
     int form;                 /* GBA_FORM_* (plain) */
     double refine_tol;        /* 1e-8 */
-    int refine_max_steps;     /* 8 */
+    int refine_max_steps;     /* 12 */
     double pcg_tol;           /* 1e-4 */
     int pcg_max_iters;        /* 200 */
     const char* model_path;   /* learned-form weights, or NULL */

@@ -59,7 +59,7 @@ def implicit_system(s, prob, lam):
     """rhs and x -> S x of the mixed form's system, in numpy FP64 from the device's
     own FP32 Jacobian records and FP64 U, V, bc, bp (the system the refinement solves)."""
     C, P = prob.num_cameras, prob.num_points
-    J = np.hstack([s.download("Jc32").reshape(-1, 18), s.download("Jp32").reshape(-1, 6)]).astype(np.float64)
+    J = jacobian_rows(s).astype(np.float64)
     order = s.download("order")
     cam = prob.obs_camera[order]
     pt = prob.obs_point[order]
@@ -117,3 +117,12 @@ def shuffle_cameras(prob, seed):
     out.cameras = cams.ravel()
     out.obs_camera = new_index[prob.obs_camera]
     return out, new_index
+
+
+def jacobian_rows(s):
+    """The mixed form's FP32 Jacobian rows as (E, 24) = [Jc (2 x 9 row-major), Jp
+    (2 x 3)] per slot, from their component-major device layout."""
+    E = s.dims()[2]
+    jc = s.download("Jc32").reshape(18, -1)[:, :E]
+    jp = s.download("Jp32").reshape(6, -1)[:, :E]
+    return np.vstack([jc, jp]).T

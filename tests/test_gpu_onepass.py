@@ -1,6 +1,6 @@
 """GPU: the one-pass FP32 PCG product (the point pass adds each observation's
-Jc^T u into per-camera accumulators, so its Jacobian rows are read once from
-HBM) against the ordered two-pass product, and whole solves against the oracle.
+Jc^T u into per-camera accumulators of at most 32 terms, so its Jacobian rows
+are read once from HBM) against the ordered two-pass product, and whole solves against the oracle.
 
 The two products sum the same FP32 terms in different orders, so PCG's
 iterates differ by rounding: refined to 1e-10 both steps solve the same
