@@ -246,8 +246,10 @@ UNITS = {"matvec": ("schur_matvec_f32", "schur_point_pass_f32", "schur_camera_pa
 
 # DRAM bytes (read + write) per launch from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum, --clock-control none) of each kernel at workload 5; copied
-# here, not measured in this run.
-NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "camera_pass_f32": None, "schur_matvec_f32": None,
+# here, not measured in this run (profiles/schur_matvec_onepass.md,
+# profiles/mixed_kernels_workload5_ncu.md).
+NCU_TRAFFIC_W5 = {"point_pass_f32": 221.5e6 + 1596.8e6, "camera_pass_f32": None,
+                  "schur_matvec_f32": 861.7e6 + 11.5e6 + 368.1e6 + 9.2e6,  # schur_matvec_warp + schur_matvec_long
                   "schur_point_pass_f32": 992.6e6 + 66.4e6, "schur_camera_pass_f32": 774.4e6 + 3.8e6,
                   "cost_ff": 239.9e6 + 61.0e6}
 

@@ -5,7 +5,10 @@
 //   bench_bal <problem.txt[.bz2]> [--iterations=N] [--lambda=D] [--json=PATH] [--verbose]
 //   exit 1 = arguments / IO, 2 = solver initial cost differs from the reader's
 //   cost by more than 1e-9 max(1, |c|), 3 = device anomaly counter non-zero.
-// Additive flags: --synthetic=W (workload 1..5 instead of a file), --seed=S,
+// Additive flags: --synthetic=W (workload 1..5 instead of a file),
+// --custom=C,P,KMIN,KMAX,ALPHA[,WINDOW] (the seeded generator at other sizes:
+// cameras, points, track lengths KMIN..KMAX with P(k) ~ k^-ALPHA, and with
+// WINDOW > 0 tracks within +-WINDOW cameras along a path), --seed=S,
 // --form=plain|mixed|learned, --model=PATH, --target-cost=D, --refine-tol=D and
 // --pcg-tol=D (mixed forms' Schur solve targets), and the loss flags
 // of the reference's Ceres benchmark (benchmarks/bench_ceres.cpp:10-11,117-131):
@@ -35,6 +38,7 @@ struct Args {
     std::string json;
     bool verbose = false;
     int synthetic = 0;
+    std::string custom;
     unsigned long long seed = 0;
     bool seed_set = false;
     std::string form = "plain";
@@ -47,7 +51,8 @@ struct Args {
 
 [[noreturn]] void usage_error(const std::string& msg) {
     std::fprintf(stderr, "%s\nusage: bench_bal <problem.txt[.bz2]> [--iterations=N] [--lambda=D] [--json=PATH] "
-                         "[--verbose] [--synthetic=1..5 --seed=S] [--form=plain|mixed|learned] [--model=PATH] "
+                         "[--verbose] [--synthetic=1..5 | --custom=C,P,KMIN,KMAX,ALPHA[,WINDOW]] [--seed=S] "
+                         "[--form=plain|mixed|learned] [--model=PATH] "
                          "[--target-cost=D] [--loss=none|huber] [--delta=D] [--refine-tol=D] [--pcg-tol=D]\n",
                  msg.c_str());
     std::exit(1);
@@ -67,6 +72,7 @@ Args parse(int argc, char** argv) {
             else if (const char* v = val("--lambda=")) a.lambda = std::stod(v);
             else if (const char* v = val("--json=")) a.json = v;
             else if (const char* v = val("--synthetic=")) a.synthetic = std::stoi(v);
+            else if (const char* v = val("--custom=")) a.custom = v;
             else if (const char* v = val("--seed=")) { a.seed = std::stoull(v); a.seed_set = true; }
             else if (const char* v = val("--form=")) a.form = v;
             else if (const char* v = val("--model=")) a.model = v;
@@ -81,7 +87,8 @@ Args parse(int argc, char** argv) {
             usage_error("bad value: " + s);
         }
     }
-    if (a.file.empty() == (a.synthetic == 0)) usage_error("give exactly one of a problem file or --synthetic=W");
+    if ((a.file.empty() ? 0 : 1) + (a.synthetic ? 1 : 0) + (a.custom.empty() ? 0 : 1) != 1)
+        usage_error("give exactly one of a problem file, --synthetic=W or --custom=...");
     if (a.loss != "none" && a.loss != "huber") usage_error("unknown loss: " + a.loss);
     if (a.loss == "huber" && !(a.delta > 0.0)) usage_error("--delta must be positive");
     return a;
@@ -98,6 +105,18 @@ int main(int argc, char** argv) {
             const unsigned long long seed = args.seed_set ? args.seed : static_cast<unsigned long long>(args.synthetic);
             bal = gba::make_synthetic(gba::synthetic_config(args.synthetic), seed);
             name = "synthetic:" + std::to_string(args.synthetic) + ":seed" + std::to_string(seed);
+        } else if (!args.custom.empty()) {
+            gba::SyntheticConfig cfg{};
+            int window = 0;
+            const int n = std::sscanf(args.custom.c_str(), "%d,%d,%d,%d,%lf,%d", &cfg.num_cameras, &cfg.num_points,
+                                      &cfg.track_min, &cfg.track_max, &cfg.track_alpha, &window);
+            if (n < 5 || cfg.num_cameras <= 0 || cfg.num_points <= 0 || cfg.track_min < 1 ||
+                cfg.track_max < cfg.track_min)
+                usage_error("bad --custom: " + args.custom);
+            cfg.window = window;
+            const unsigned long long seed = args.seed_set ? args.seed : 1ull;
+            bal = gba::make_synthetic(cfg, seed);
+            name = "custom:" + args.custom + ":seed" + std::to_string(seed);
         } else {
             bal = gba::load_bal(args.file);
         }

@@ -690,16 +690,17 @@ __global__ void __launch_bounds__(kPT) schur_matvec_long(
     if (done && *done != 0.0) return;
     const int2 lc = lchunk[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < lc.y) {  // the list's points in parallel, then their prefix
+        const int p = lpts[lc.x + tid];
+        const int o0 = pt_off[p], o1 = pt_off[p + 1];
+        pid[tid] = p;
+        ps[tid] = o0;
+        pb[tid + 1] = o1 - o0;
+    }
+    __syncwarp();
     if (tid == 0) {
-        int v = 0;
-        for (int j = 0; j < lc.y; ++j) {
-            const int p = lpts[lc.x + j];
-            pid[j] = p;
-            ps[j] = pt_off[p];
-            pb[j] = v;
-            v += pt_off[p + 1] - ps[j];
-        }
-        pb[lc.y] = v;
+        pb[0] = 0;
+        for (int j = 1; j <= lc.y; ++j) pb[j] += pb[j - 1];
     }
     __syncthreads();
     const int n = pb[lc.y];
@@ -1188,6 +1189,179 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
             const float w0 = w[3 * j], w1 = w[3 * j + 1], w2 = w[3 * j + 2];
             out[j] = make_float2(jp[0] * w0 + jp[1] * w1 + jp[2] * w2, jp[3] * w0 + jp[4] * w1 + jp[5] * w2);
         }
+    }
+}
+
+// a_j = Jc Z_c(:, j) for the nine columns, from the camera's BF16 rows (Zb,
+// kZs values per camera) read as 16-byte runs and consumed as they arrive, and
+// v_j = Jp^T a_j (27 values: v[3 j + k]).
+__device__ __forceinline__ void coarse_slot_v(const float* J, const __nv_bfloat16* __restrict__ Zb, int cam,
+                                              float* v) {
+    float a0[kCoarse], a1[kCoarse];
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) a0[j] = a1[j] = 0.f;
+    const uint4* z4 = reinterpret_cast<const uint4*>(Zb + static_cast<long long>(kZs) * cam);
+#pragma unroll
+    for (int q = 0; q < kZs / 8; ++q) {
+        const uint4 z = __ldg(z4 + q);
+        const uint32_t w[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+            const int r = 8 * q + h;  // entry (i, j) = (r / 9, r % 9) of the camera's 9 x 9 rows
+            if (r < 81) {
+                const float zv = (h & 1) ? __uint_as_float(w[h >> 1] & 0xffff0000u) : __uint_as_float(w[h >> 1] << 16);
+                a0[r % 9] = fmaf(J[r / 9], zv, a0[r % 9]);
+                a1[r % 9] = fmaf(J[9 + r / 9], zv, a1[r % 9]);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) {
+        v[3 * j] = fmaf(J[18], a0[j], J[21] * a1[j]);
+        v[3 * j + 1] = fmaf(J[19], a0[j], J[22] * a1[j]);
+        v[3 * j + 2] = fmaf(J[20], a0[j], J[23] * a1[j]);
+    }
+}
+
+// Point pass of S Z over warp chunks (whole points of at most 32 slots per
+// warp; as schur_matvec_warp): per slot v_j = Jp^T Jc Z_c(:, j), a segmented
+// scan of the 27 values over the warp, w_j = V'^-1 t_j at each point's last
+// lane, every lane takes its point's w (match + shuffle) and stores u_j = Jp w_j
+// (18 floats) at its camera-major position for coarse_camera_pass9.
+__global__ void __launch_bounds__(32 * kMWarps) coarse_point_pass9_warp(
+    const int2* __restrict__ wchunk, int n_wchunk, const int* __restrict__ s_cam, const int* __restrict__ s_pt,
+    const int* __restrict__ cam_pos, const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long js,
+    const float* __restrict__ vinv, const __nv_bfloat16* __restrict__ Zb, float* __restrict__ u9) {
+    constexpr int KV = 3 * kCoarse;
+    const int wid = blockIdx.x * kMWarps + (threadIdx.x >> 5);
+    if (wid >= n_wchunk) return;  // whole warps leave together
+    const int lane = threadIdx.x & 31;
+    const int2 r = wchunk[wid];
+    const int s = r.x + lane;
+    const bool has = s < r.y;
+    int key = -1;
+    long long q = 0;
+    float J[24], vi[6], v[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) v[k] = 0.f;
+    if (has) {
+        key = s_pt[s];
+        q = cam_pos[s];
+        load_j(Jc32, Jp32, js, s, J);
+        load_vinv(vinv, nullptr, key, vi);
+        coarse_slot_v(J, Zb, s_cam[s], v);
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int kd = __shfl_up_sync(0xffffffffu, key, d);
+        const bool take = lane >= d && kd == key;
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+            const float u = __shfl_up_sync(0xffffffffu, v[k], d);
+            if (take) v[k] += u;
+        }
+    }
+    if (has) {  // meaningful at the point's last lane
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) apply_vinv(vi, v[3 * j], v[3 * j + 1], v[3 * j + 2], v[3 * j], v[3 * j + 1],
+                                                    v[3 * j + 2]);
+    }
+    const int last = 31 - __clz(__match_any_sync(0xffffffffu, key));
+#pragma unroll
+    for (int k = 0; k < KV; ++k) v[k] = __shfl_sync(0xffffffffu, v[k], last);
+    if (has) {
+        float2* out = reinterpret_cast<float2*>(u9 + 18 * q);
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j)
+            out[j] = make_float2(fmaf(J[18], v[3 * j], fmaf(J[19], v[3 * j + 1], J[20] * v[3 * j + 2])),
+                                 fmaf(J[21], v[3 * j], fmaf(J[22], v[3 * j + 1], J[23] * v[3 * j + 2])));
+    }
+}
+
+// Point pass of S Z for points with 33 to 256 observations: a CTA takes a
+// list of them as one virtual chunk (as schur_matvec_long); per point the
+// warps' segment sums in order (shared memory), then u_j = Jp w_j per slot.
+__global__ void __launch_bounds__(kPT) coarse_point_pass9_list(
+    const int2* __restrict__ lchunk, const int* __restrict__ lpts, const int* __restrict__ pt_off,
+    const int* __restrict__ s_cam, const int* __restrict__ cam_pos, const float* __restrict__ Jc32,
+    const float* __restrict__ Jp32, long long js, const float* __restrict__ vinv,
+    const __nv_bfloat16* __restrict__ Zb, float* __restrict__ u9) {
+    constexpr int KV = 3 * kCoarse;
+    constexpr int kMaxPts = kPT / 33 + 1;
+    __shared__ int pb[kMaxPts + 1], ps[kMaxPts], pid[kMaxPts];
+    __shared__ float seg[kPT][KV + 1];
+    __shared__ float wsh[kMaxPts][KV];
+    const int2 lc = lchunk[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < lc.y) {
+        const int p = lpts[lc.x + tid];
+        const int o0 = pt_off[p], o1 = pt_off[p + 1];
+        pid[tid] = p;
+        ps[tid] = o0;
+        pb[tid + 1] = o1 - o0;
+    }
+    __syncwarp();
+    if (tid == 0) {
+        pb[0] = 0;
+        for (int j = 1; j <= lc.y; ++j) pb[j] += pb[j - 1];
+    }
+    __syncthreads();
+    const int n = pb[lc.y];
+    int key = -1;
+    long long sl = 0;
+    float J[24], v[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) v[k] = 0.f;
+    if (tid < n) {
+        int j = 0;
+        while (tid >= pb[j + 1]) ++j;
+        key = j;
+        sl = ps[j] + (tid - pb[j]);
+        load_j(Jc32, Jp32, js, sl, J);
+        coarse_slot_v(J, Zb, s_cam[sl], v);
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int kd = __shfl_up_sync(0xffffffffu, key, d);
+        const bool take = lane >= d && kd == key;
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+            const float u = __shfl_up_sync(0xffffffffu, v[k], d);
+            if (take) v[k] += u;
+        }
+    }
+    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    if (lane == 31 || knext != key) {
+#pragma unroll
+        for (int k = 0; k < KV; ++k) seg[tid][k] = v[k];
+    }
+    __syncthreads();
+    // the points' sums, one thread per (point, value): the warps' segment
+    // ends in order
+    if (tid < KV * lc.y) {
+        const int j = tid / KV, k = tid - KV * j;
+        const int b = pb[j], e = pb[j + 1];
+        float t = 0.f;
+        for (int w = b >> 5; w <= (e - 1) >> 5; ++w) t += seg[min(e - 1, 32 * w + 31)][k];
+        wsh[j][k] = t;
+    }
+    __syncthreads();
+    // w = V'^-1 t, one thread per (point, column)
+    if (tid < kCoarse * lc.y) {
+        const int j = tid / kCoarse, c = tid - kCoarse * j;
+        float vi[6];
+        load_vinv(vinv, nullptr, pid[j], vi);
+        float* w = wsh[j] + 3 * c;
+        apply_vinv(vi, w[0], w[1], w[2], w[0], w[1], w[2]);
+    }
+    __syncthreads();
+    if (tid < n) {
+        const float* w = wsh[key];
+        float2* out = reinterpret_cast<float2*>(u9 + 18ll * cam_pos[sl]);
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j)
+            out[j] = make_float2(fmaf(J[18], w[3 * j], fmaf(J[19], w[3 * j + 1], J[20] * w[3 * j + 2])),
+                                 fmaf(J[21], w[3 * j], fmaf(J[22], w[3 * j + 1], J[23] * w[3 * j + 2])));
     }
 }
 
@@ -2000,10 +2174,25 @@ void Solver::coarse_prepare(double lambda) {
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_basis", ev1);
     ev1 = prof_start();
-    coarse_point_pass9<<<n_pchunk_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(pchunk4_.get()), pt_off_.get(),
-                                                       s_cam_.get(), s_pt_.get(), cam_pos_.get(), Jc32_.get(),
-                                                       Jp32_.get(), js_, Vinv32_.get(), czb_.get(), cu9_.get());
-    GBA_LAUNCH_CHECK();
+    if (n_wchunk_ > 0) {
+        coarse_point_pass9_warp<<<ceil_div(n_wchunk_, kMWarps), 32 * kMWarps, 0, stream_>>>(
+            reinterpret_cast<const int2*>(wchunk_.get()), n_wchunk_, s_cam_.get(), s_pt_.get(), cam_pos_.get(),
+            Jc32_.get(), Jp32_.get(), js_, Vinv32_.get(), czb_.get(), cu9_.get());
+        GBA_LAUNCH_CHECK();
+    }
+    if (n_lchunk_ > 0) {
+        coarse_point_pass9_list<<<n_lchunk_, kPT, 0, stream_>>>(
+            reinterpret_cast<const int2*>(lchunk_.get()), lpts_.get(), pt_off_.get(), s_cam_.get(), cam_pos_.get(),
+            Jc32_.get(), Jp32_.get(), js_, Vinv32_.get(), czb_.get(), cu9_.get());
+        GBA_LAUNCH_CHECK();
+    }
+    if (n_huge_ > 0) {
+        coarse_point_pass9<<<n_huge_, kPT, 0, stream_>>>(reinterpret_cast<const int4*>(huge_range_.get()),
+                                                         pt_off_.get(), s_cam_.get(), s_pt_.get(), cam_pos_.get(),
+                                                         Jc32_.get(), Jp32_.get(), js_, Vinv32_.get(), czb_.get(),
+                                                         cu9_.get());
+        GBA_LAUNCH_CHECK();
+    }
     prof_stop("coarse_point_pass9", ev1);
     if (n_cchunk_ > 0) {
         ev1 = prof_start();
@@ -2033,62 +2222,69 @@ void Solver::set_matvec(int mode) {
         const size_t n = static_cast<size_t>(kX32) * std::max(n_acc_, 1);
         y_acc_.alloc(n);
         GBA_CUDA_CHECK(cudaMemsetAsync(y_acc_.get(), 0, n * sizeof(float), stream_));
-        // warp chunks: whole points packed greedily into runs of at most 32
-        // slots; points with more observations get a range of their own
-        std::vector<int> off(P_ + 1);
-        GBA_CUDA_CHECK(cudaMemcpyAsync(off.data(), pt_off_.get(), (P_ + 1ull) * sizeof(int), cudaMemcpyDeviceToHost,
-                                       stream_));
-        sync();
-        std::vector<int2> wc, lc;
-        std::vector<int> lp;
-        std::vector<int4> hr;
-        int b = -1, e = -1, lsum = 0;
-        for (int p = 0; p < P_; ++p) {
-            const int n = off[p + 1] - off[p];
-            if (n == 0) continue;
-            if (n > kPT) {
-                hr.push_back(make_int4(p, p + 1, off[p], off[p + 1]));
-                continue;
-            }
-            if (n > 32) {  // into the current long-point CTA list, or a new one
-                if (lc.empty() || lsum + n > kPT) {
-                    lc.push_back(make_int2(static_cast<int>(lp.size()), 0));
-                    lsum = 0;
-                }
-                lp.push_back(p);
-                ++lc.back().y;
-                lsum += n;
-                continue;
-            }
-            if (b >= 0 && (off[p] != e || off[p + 1] - b > 32)) {
-                wc.push_back(make_int2(b, e));
-                b = -1;
-            }
-            if (b < 0) b = off[p];
-            e = off[p + 1];
-        }
-        if (b >= 0) wc.push_back(make_int2(b, e));
-        n_wchunk_ = static_cast<int>(wc.size());
-        n_lchunk_ = static_cast<int>(lc.size());
-        n_huge_ = static_cast<int>(hr.size());
-        wchunk_.alloc(2 * std::max<size_t>(wc.size(), 1));
-        lchunk_.alloc(2 * std::max<size_t>(lc.size(), 1));
-        lpts_.alloc(std::max<size_t>(lp.size(), 1));
-        huge_range_.alloc(4 * std::max<size_t>(hr.size(), 1));
-        if (!wc.empty())
-            GBA_CUDA_CHECK(cudaMemcpyAsync(wchunk_.get(), wc.data(), wc.size() * sizeof(int2), cudaMemcpyHostToDevice,
-                                           stream_));
-        if (!lc.empty()) {
-            GBA_CUDA_CHECK(cudaMemcpyAsync(lchunk_.get(), lc.data(), lc.size() * sizeof(int2), cudaMemcpyHostToDevice,
-                                           stream_));
-            GBA_CUDA_CHECK(cudaMemcpyAsync(lpts_.get(), lp.data(), lp.size() * sizeof(int), cudaMemcpyHostToDevice,
-                                           stream_));
-        }
-        if (!hr.empty())
-            GBA_CUDA_CHECK(cudaMemcpyAsync(huge_range_.get(), hr.data(), hr.size() * sizeof(int4),
-                                           cudaMemcpyHostToDevice, stream_));
-        sync();
     }
+}
+
+// Point groups of the warp-level point passes (the one-pass product and the
+// coarse S Z): whole points packed greedily into runs of at most 32 slots
+// (wchunk_), points with 33 to 256 observations into lists of at most 256
+// slots (lchunk_, lpts_), longer points as single ranges (huge_range_).
+void Solver::build_point_groups() {
+    // warp chunks: whole points packed greedily into runs of at most 32
+    // slots; points with more observations get a range of their own
+    std::vector<int> off(P_ + 1);
+    GBA_CUDA_CHECK(cudaMemcpyAsync(off.data(), pt_off_.get(), (P_ + 1ull) * sizeof(int), cudaMemcpyDeviceToHost,
+                                   stream_));
+    sync();
+    std::vector<int2> wc, lc;
+    std::vector<int> lp;
+    std::vector<int4> hr;
+    int b = -1, e = -1, lsum = 0;
+    for (int p = 0; p < P_; ++p) {
+        const int n = off[p + 1] - off[p];
+        if (n == 0) continue;
+        if (n > kPT) {
+            hr.push_back(make_int4(p, p + 1, off[p], off[p + 1]));
+            continue;
+        }
+        if (n > 32) {  // into the current long-point CTA list, or a new one
+            if (lc.empty() || lsum + n > kPT) {
+                lc.push_back(make_int2(static_cast<int>(lp.size()), 0));
+                lsum = 0;
+            }
+            lp.push_back(p);
+            ++lc.back().y;
+            lsum += n;
+            continue;
+        }
+        if (b >= 0 && (off[p] != e || off[p + 1] - b > 32)) {
+            wc.push_back(make_int2(b, e));
+            b = -1;
+        }
+        if (b < 0) b = off[p];
+        e = off[p + 1];
+    }
+    if (b >= 0) wc.push_back(make_int2(b, e));
+    n_wchunk_ = static_cast<int>(wc.size());
+    n_lchunk_ = static_cast<int>(lc.size());
+    n_huge_ = static_cast<int>(hr.size());
+    wchunk_.alloc(2 * std::max<size_t>(wc.size(), 1));
+    lchunk_.alloc(2 * std::max<size_t>(lc.size(), 1));
+    lpts_.alloc(std::max<size_t>(lp.size(), 1));
+    huge_range_.alloc(4 * std::max<size_t>(hr.size(), 1));
+    if (!wc.empty())
+        GBA_CUDA_CHECK(cudaMemcpyAsync(wchunk_.get(), wc.data(), wc.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                       stream_));
+    if (!lc.empty()) {
+        GBA_CUDA_CHECK(cudaMemcpyAsync(lchunk_.get(), lc.data(), lc.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                       stream_));
+        GBA_CUDA_CHECK(cudaMemcpyAsync(lpts_.get(), lp.data(), lp.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                       stream_));
+    }
+    if (!hr.empty())
+        GBA_CUDA_CHECK(cudaMemcpyAsync(huge_range_.get(), hr.data(), hr.size() * sizeof(int4),
+                                       cudaMemcpyHostToDevice, stream_));
+    sync();
 }
 
 }  // namespace gba

@@ -238,13 +238,14 @@ public:
     static constexpr int kAccSlots = 32;
     bool one_pass_ = false;
     int n_acc_ = 0;
-    // its work: warp chunks (whole points, at most 32 slots: int2 {first,
-    // end slot}); points with 33 to 256 observations in lists of at most 256
-    // slots per CTA (lchunk_: int2 {first entry of lpts_, entries}); longer
-    // points as ranges (int4 {p, p + 1, first slot, end slot}) for the
-    // chunked point pass
+    // the warp-level point passes' work: warp chunks (whole points, at most
+    // 32 slots: int2 {first, end slot}); points with 33 to 256 observations in
+    // lists of at most 256 slots per CTA (lchunk_: int2 {first entry of lpts_,
+    // entries}); longer points as ranges (int4 {p, p + 1, first slot, end
+    // slot}) for the chunked point passes
     int n_wchunk_ = 0, n_lchunk_ = 0, n_huge_ = 0;
     DevBuf<int> wchunk_, lchunk_, lpts_, huge_range_;
+    void build_point_groups();  // pcg.cu
     DevBuf<int> acc_id_, acc_off_;
     DevBuf<float> y_acc_;
     void set_matvec(int mode);  // 0 auto (one pass), 1 two-pass (deterministic), 2 one-pass

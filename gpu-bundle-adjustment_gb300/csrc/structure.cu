@@ -398,6 +398,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         u_.alloc(2ull * E);
         g_cm_.alloc(4ull * E);
         pcg_s_.alloc(16);
+        build_point_groups();
         set_matvec(0);
     }
     sync();

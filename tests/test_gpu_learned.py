@@ -159,10 +159,14 @@ def random_model(gba, tmp_path_factory):
     return path
 
 
-def test_two_level_pcg_refined_step_equals_block_jacobi(gba, random_model):
+@pytest.mark.parametrize("tracks", ["short", "long"])
+def test_two_level_pcg_refined_step_equals_block_jacobi(gba, random_model, tracks):
     """Any full-rank basis gives an SPD preconditioner: forced on, the refined
-    Schur step equals the block-Jacobi one (same system, refined to 1e-10)."""
-    prob = gba.synthetic_custom(30, 4000, 2, 8, 1.6, seed=23)
+    Schur step equals the block-Jacobi one (same system, refined to 1e-10).
+    Long tracks (40 to 300 observations) take the coarse product's list and
+    single-point passes besides the warp pass."""
+    prob = (gba.synthetic_custom(30, 4000, 2, 8, 1.6, seed=23) if tracks == "short"
+            else gba.synthetic_custom(400, 1500, 40, 300, 1.0, seed=23))
     lam = 1e-3
     steps = []
     for mode in ("block-jacobi", "learned"):
