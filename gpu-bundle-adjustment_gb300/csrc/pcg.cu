@@ -957,10 +957,26 @@ __device__ __forceinline__ double apply_minv_row(const double* __restrict__ Minv
 // thread, vi its value; i past the end contributes 0): red[block * kCoarse + j].
 __device__ __forceinline__ void coarse_partials(const double* __restrict__ V, long long n, long long i, double vi,
                                                 double* sh, double* __restrict__ red) {
-#pragma unroll 1
-    for (int j = 0; j < kCoarse; ++j) {
-        const double t = block_sum<kUT>(i < n ? V[j * n + i] * vi : 0.0, sh);
-        if (threadIdx.x == 0) red[static_cast<long long>(blockIdx.x) * kCoarse + j] = t;
+    // the nine block sums at once: warp shuffle trees (independent, so they
+    // interleave), one barrier, then the warps' sums in warp order
+    __shared__ double wpart[kUT / 32][kCoarse];
+    (void)sh;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double v[kCoarse];
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) v[j] = i < n ? V[j * n + i] * vi : 0.0;
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) v[j] = warp_sum(v[j]);
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < kCoarse; ++j) wpart[warp][j] = v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < kCoarse) {
+        double t = 0.0;
+#pragma unroll
+        for (int w = 0; w < kUT / 32; ++w) t += wpart[w][threadIdx.x];
+        red[static_cast<long long>(blockIdx.x) * kCoarse + threadIdx.x] = t;
     }
 }
 
@@ -1448,14 +1464,18 @@ __global__ void __launch_bounds__(kVT) coarse_gram_partials(const double* __rest
 
 // E from the partials (fixed order), symmetrised; FP64 Cholesky and inverse by
 // one thread. einv[kCoarse^2] = 1 if E is SPD (relative pivot floor 1e-13), else 0.
-__global__ void __launch_bounds__(128) coarse_einv_kernel(const double* __restrict__ red, int nb,
-                                                         double* __restrict__ einv) {
+constexpr int kEinvT = 1024;
+__global__ void __launch_bounds__(kEinvT) coarse_einv_kernel(const double* __restrict__ red, int nb,
+                                                            double* __restrict__ einv) {
     constexpr int K = kCoarse, KK = kCoarse * kCoarse;
     __shared__ double E[KK];
-    for (int t = threadIdx.x; t < KK; t += 128) {
+    // entry t of E: one warp sums the nb block partials (lanes strided, then a shuffle tree)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int t = warp; t < KK; t += kEinvT / 32) {
         double v = 0.0;
-        for (int b = 0; b < nb; ++b) v += red[static_cast<long long>(b) * KK + t];
-        E[t] = v;
+        for (int b = lane; b < nb; b += 32) v += red[static_cast<long long>(b) * KK + t];
+        v = warp_sum(v);
+        if (lane == 0) E[t] = v;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;
@@ -1971,7 +1991,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     // basis (coarse). Returns the iteration count; *ok = reached the inner
     // tolerance without breakdown; inner_rel2 = its final ||r||^2 / ||b||^2.
     double inner_rel2 = 0.0;
-    auto inner_pcg = [&](bool* ok, bool coarse) -> long long {
+    auto inner_pcg = [&](bool* ok, bool coarse, int max_iters) -> long long {
         if (coarse && !coarse_ready) {
             coarse_prepare(lambda);
             coarse_ready = true;
@@ -2002,10 +2022,10 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         // (then 1, 2, 4, 8, 8, ...): a launch after convergence returns at once
         // but still dispatches its whole grid (tens of microseconds for the
         // point pass), so overshooting costs more than one extra check.
-        int batch = std::max(1, std::min(prev_inner_ - 1, std::min(kCheck, opts.pcg_max_iters)));
+        int batch = std::max(1, std::min(prev_inner_ - 1, std::min(kCheck, max_iters)));
         double h[9];
-        if (opts.pcg_max_iters <= 0) read_back({{h, sc, sizeof h}});  // the state pcg_init_finalize left
-        for (int it = 0, next = 1; it < opts.pcg_max_iters; it += batch, batch = std::min(next, kCheck), next *= 2) {
+        if (max_iters <= 0) read_back({{h, sc, sizeof h}});  // the state pcg_init_finalize left
+        for (int it = 0, next = 1; it < max_iters; it += batch, batch = std::min(next, kCheck), next *= 2) {
             for (int j = 0; j < batch; ++j) {
                 if (one_pass_) {
                     implicit_parts_acc(*this, pcg_p32_.get(), done);
@@ -2037,7 +2057,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                     prof_stop("coarse_apply", cev);
                 }
                 pcg_direction<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_p32_.get(), pcg_z_.get(), n, red, red2,
-                                                        nub, opts.pcg_max_iters, sc);
+                                                        nub, max_iters, sc);
                 GBA_LAUNCH_CHECK();
             }
             read_back({{h, sc, sizeof h}});
@@ -2065,16 +2085,21 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             // serves the rest of the solve if it needed at most 4/5 of
             // block-Jacobi's iterations and its step is no worse in the S-norm.
             // For PCG iterates from x = 0, ||x* - x||_S^2 = b.x* - b.x, so the
-            // step with the larger b.x has the smaller S-norm error. Both solves
+            // step with the larger b.x has the smaller S-norm error. The learned
+            // solve runs first; block-Jacobi then stops once it has used 5/4 of
+            // the learned iterations, past which it cannot win. Both solves
             // count in pcg_iterations.
             bool ok_bj = false, ok_l = false;
-            const long long it_bj = inner_pcg(&ok_bj, false);
-            const double rel2_bj = inner_rel2;
-            btx(S_BTX0);
+            const long long it_l = inner_pcg(&ok_l, true, opts.pcg_max_iters);
+            const double rel2_l = inner_rel2;
+            btx(S_BTX1);
             GBA_CUDA_CHECK(cudaMemcpyAsync(judge_x_.get(), pcg_x_.get(), n * sizeof(double),
                                            cudaMemcpyDeviceToDevice, stream_));
-            const long long it_l = inner_pcg(&ok_l, true);
-            btx(S_BTX1);
+            const long long cap =
+                ok_l ? std::min<long long>(opts.pcg_max_iters, (it_l * kLearnedWinDen + kLearnedWinNum - 1) / kLearnedWinNum)
+                     : opts.pcg_max_iters;
+            const long long it_bj = inner_pcg(&ok_bj, false, static_cast<int>(cap));
+            btx(S_BTX0);
             double bx[2];
             read_back({{bx, sc + S_BTX0, sizeof bx}});
             judge_iters_[0] = it_bj;
@@ -2094,20 +2119,23 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             if (decisive && ok_l && (!ok_bj || (it_l * kLearnedWinDen <= it_bj * kLearnedWinNum && no_worse))) {
                 learned_choice_ = 1;
                 use_learned = true;
+                inner_rel2 = rel2_l;
+                GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
+                                               cudaMemcpyDeviceToDevice, stream_));
                 st.pcg_iterations += it_bj;
                 it_count = it_l;
                 ok = ok_l;
             } else {
+                // block-Jacobi's solve is in pcg_x_ (it ran last, and was not
+                // stopped early: a stopped run leaves ok_bj false, and the
+                // learned solve, converged, wins then)
                 learned_choice_ = (decisive || judge_attempts_ >= attempts) ? 2 : 0;
-                inner_rel2 = rel2_bj;
-                GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
-                                               cudaMemcpyDeviceToDevice, stream_));
                 st.pcg_iterations += it_l;
                 it_count = it_bj;
                 ok = ok_bj;
             }
         } else {
-            it_count = inner_pcg(&ok, use_learned);
+            it_count = inner_pcg(&ok, use_learned, opts.pcg_max_iters);
         }
         if (use_learned && !ok && precond_force_ != 1) {
             // Block-Jacobi is the fallback: an inner solve with the coarse
@@ -2117,7 +2145,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             use_learned = false;
             ++st.fallbacks;
             st.pcg_iterations += it_count;
-            it_count = inner_pcg(&ok, false);
+            it_count = inner_pcg(&ok, false, opts.pcg_max_iters);
         }
         const double iters = static_cast<double>(it_count);
         if (fast && step == 0 && ok && inner_rel2 <= tol2 / bnorm2) {
@@ -2208,7 +2236,7 @@ void Solver::coarse_prepare(double lambda) {
     double* gram = cred_.get() + 2ll * nub * kCoarse + kCoarse;
     coarse_gram_partials<<<nvb, kVT, 0, stream_>>>(cz_.get(), csz_.get(), n, gram);
     GBA_LAUNCH_CHECK();
-    coarse_einv_kernel<<<1, 128, 0, stream_>>>(gram, nvb, ceinv_.get());
+    coarse_einv_kernel<<<1, kEinvT, 0, stream_>>>(gram, nvb, ceinv_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_gram", ev1);
     prof_stop("coarse_prepare", ev);

@@ -96,7 +96,8 @@ struct LMResult {
     double time_to_target_s = -1.0;        // first time cost <= LMOptions::target_cost, or -1
     // Learned form: which preconditioner won the judged first inner solve
     // (1 = learned, 2 = block-Jacobi, 0 = not judged) and its inner PCG
-    // iterations with block-Jacobi and with the learned factors.
+    // iterations with block-Jacobi (stopped at 5/4 of the learned count, past
+    // which it cannot win) and with the learned coarse correction.
     int learned_choice = 0;
     long long judge_iters_block_jacobi = 0, judge_iters_learned = 0;
     // Phase wall times (device-synchronised): setup, accumulate, damp+V^-1,

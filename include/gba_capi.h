@@ -90,7 +90,8 @@ typedef struct gba_lm_result {
     int trajectory_capacity;
     int trajectory_len;
     int learned_choice;              /* learned form: 1 learned, 2 block-Jacobi won the judged solve */
-    long long judge_iters_block_jacobi;
+    long long judge_iters_block_jacobi;  /* the judged solve's block-Jacobi iterations (stopped at 5/4 of the
+                                            learned count, when it could no longer win) */
     long long judge_iters_learned;
     double max_refine_residual;      /* mixed forms: largest relative residual of a refined Schur step */
     int schur_band_rows;             /* plain form: rows of the band S was stored in, 0 if dense */
@@ -258,7 +259,9 @@ int gba_solver_features(gba_solver* s, double lambda, float* feat);
 int gba_solver_set_preconditioner(gba_solver* s, int mode);
 /* Learned form, last judged solve: inner PCG iterations and b.x of the
  * block-Jacobi and the learned steps (the larger b.x has the smaller S-norm
- * error). [host] iters (2), btx (2). */
+ * error). The learned solve runs first; block-Jacobi's stops once it has used
+ * 5/4 of the learned iterations (it cannot win past that). [host] iters (2),
+ * btx (2). */
 int gba_solver_judge_info(gba_solver* s, long long* iters, double* btx);
 
 typedef struct gba_mlp gba_mlp;
