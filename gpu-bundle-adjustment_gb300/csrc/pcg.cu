@@ -1468,7 +1468,8 @@ constexpr int kEinvT = 1024;
 __global__ void __launch_bounds__(kEinvT) coarse_einv_kernel(const double* __restrict__ red, int nb,
                                                             double* __restrict__ einv) {
     constexpr int K = kCoarse, KK = kCoarse * kCoarse;
-    __shared__ double E[KK];
+    __shared__ double E[KK], L[KK];
+    __shared__ int ok;
     // entry t of E: one warp sums the nb block partials (lanes strided, then a shuffle tree)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int t = warp; t < KK; t += kEinvT / 32) {
@@ -1478,47 +1479,54 @@ __global__ void __launch_bounds__(kEinvT) coarse_einv_kernel(const double* __res
         if (lane == 0) E[t] = v;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    double L[KK], dmax = 0.0;
-    for (int a = 0; a < K; ++a)
-        for (int b = 0; b < K; ++b) L[a * K + b] = 0.5 * (E[a * K + b] + E[b * K + a]);
-    for (int a = 0; a < K; ++a) dmax = fmax(dmax, L[a * K + a]);
-    bool ok = dmax > 0.0 && isfinite(dmax);
-    for (int k = 0; k < K && ok; ++k) {
-        double d = L[k * K + k];
-        for (int m = 0; m < k; ++m) d -= L[k * K + m] * L[k * K + m];
-        if (!(d > 1e-13 * dmax)) {
-            ok = false;
-            break;
+    if (threadIdx.x == 0) {  // Cholesky of the symmetrised E (9 x 9)
+        double dmax = 0.0;
+        for (int a = 0; a < K; ++a)
+            for (int b = 0; b < K; ++b) L[a * K + b] = 0.5 * (E[a * K + b] + E[b * K + a]);
+        for (int a = 0; a < K; ++a) dmax = fmax(dmax, L[a * K + a]);
+        bool good = dmax > 0.0 && isfinite(dmax);
+        for (int k = 0; k < K && good; ++k) {
+            double d = L[k * K + k];
+            for (int m = 0; m < k; ++m) d -= L[k * K + m] * L[k * K + m];
+            if (!(d > 1e-13 * dmax)) {
+                good = false;
+                break;
+            }
+            const double l = sqrt(d);
+            L[k * K + k] = l;
+            for (int a = k + 1; a < K; ++a) {
+                double v = L[a * K + k];
+                for (int m = 0; m < k; ++m) v -= L[a * K + m] * L[k * K + m];
+                L[a * K + k] = v / l;
+            }
         }
-        const double l = sqrt(d);
-        L[k * K + k] = l;
-        for (int a = k + 1; a < K; ++a) {
-            double v = L[a * K + k];
-            for (int m = 0; m < k; ++m) v -= L[a * K + m] * L[k * K + m];
-            L[a * K + k] = v / l;
-        }
+        ok = good;
     }
+    __syncthreads();
     if (!ok) {
-        for (int t = 0; t <= KK; ++t) einv[t] = 0.0;
+        for (int t = threadIdx.x; t <= KK; t += kEinvT) einv[t] = 0.0;
         return;
     }
-    // E^-1 = L^-T L^-1, column by column of the identity
-    for (int col = 0; col < K; ++col) {
+    // E^-1 = L^-T L^-1, one column of the identity per thread
+    if (threadIdx.x < K) {
+        const int col = threadIdx.x;
         double y[K];
+#pragma unroll
         for (int a = 0; a < K; ++a) {
             double v = a == col ? 1.0 : 0.0;
             for (int m = 0; m < a; ++m) v -= L[a * K + m] * y[m];
             y[a] = v / L[a * K + a];
         }
+#pragma unroll
         for (int a = K - 1; a >= 0; --a) {
             double v = y[a];
             for (int m = a + 1; m < K; ++m) v -= L[m * K + a] * y[m];
             y[a] = v / L[a * K + a];
         }
+#pragma unroll
         for (int a = 0; a < K; ++a) einv[a * K + col] = y[a];
     }
-    einv[KK] = 1.0;
+    if (threadIdx.x == 0) einv[KK] = 1.0;
 }
 
 // Block partials of a . b (FP64).
