@@ -652,18 +652,51 @@ def run_ours(args):
 # ----------------------------------------------------------------- the CPU arm
 
 def run_reference(args):
-    """The oracle's LM solve on the host cores, nothing of this library loaded."""
+    """The oracle's LM solve on the host cores, nothing of this library loaded.
+    Workloads whose dense reduced camera system does not fit a few minutes of
+    CPU time (more than --reference-max-cameras cameras) are timed on a bounded
+    sample per step (cpu_sample: the normal equations over all observations
+    plus the dense Cholesky at n = 4,608, scaled to the full system; a lower
+    bound on the solve, as its sample string says)."""
     rank, world = _dist_env()
     if rank != 0:
         return
     C = {1: 16, 2: 257, 3: 1000, 4: 1000, 5: 5000}.get(args.workload)
-    if C is None or C > args.reference_max_cameras:
-        n = 9 * (C or 0)
-        print(json.dumps({"impl": "reference", "unavailable": (
-            f"the CPU LM solve of workload {args.workload} factors a dense {n} x {n} FP64 system on the host "
-            f"cores every trial (about {n ** 3 / 3:.1e} flop, ~10^3-10^4 s per solve on 16 cores), which does "
-            f"not fit the run; the measured CPU/GPU pair is the ours-arm key cpu_pair "
-            f"(workload {args.cpu_pair_workload})")}))
+    if C is not None and C > args.reference_max_cameras:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+
+        prob = oracle.synthetic(args.workload, args.seed)
+        ref = reference_entry(args.workload, args.seed)
+        target = ref["final_cost"] * TARGET_FACTOR if ref else None
+        traj = None
+        f = GOLDEN / "workload_reference.json"
+        if f.exists():
+            traj = json.loads(f.read_text()).get(f"{args.workload}:{args.seed}", {}).get("trajectory")
+        iters = next((i for i, c in enumerate(traj) if c <= target), None) if (traj and target) else None
+        iters = iters or args.max_iterations
+        samples = []
+        for i in range(args.warmup + args.steps):
+            smp = cpu_sample(prob, iters)
+            if i >= args.warmup:
+                samples.append(smp)
+        v = sum(x["value"] for x in samples) / len(samples)
+        line = {
+            "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded BAL-shaped generator)",
+            "config": {"workload": f"workload{args.workload}: {prob.num_cameras} cameras / {prob.num_points} "
+                                   f"points / {prob.num_observations} observations, seed {args.seed}",
+                       "form": "plain (CPU oracle)", "target_cost": target, "iterations_to_target": iters},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "s", "cores": samples[-1]["cores"], "kind": "port",
+                             "extrapolated": True, "sample": "per step: " + samples[-1]["sample"]},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+    if C is None:
+        print(json.dumps({"impl": "reference", "unavailable": f"unknown workload {args.workload}"}))
         return
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
@@ -716,7 +749,7 @@ def main():
     ap.add_argument("--no-band", action="store_true", help="skip the plain form's band-vs-dense camera-path solve")
     ap.add_argument("--cpu-pair-workload", type=int, default=2)
     ap.add_argument("--reference-max-cameras", type=int, default=300,
-                    help="largest workload (cameras) the CPU arm solves; above it prints unavailable")
+                    help="largest workload (cameras) the CPU arm solves whole; above it, a bounded sample per step")
     args = ap.parse_args()
     if args.seed is None:
         args.seed = args.workload
