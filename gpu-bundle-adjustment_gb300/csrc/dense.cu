@@ -161,8 +161,13 @@ __global__ void __launch_bounds__(128) rhs_kernel(const int* __restrict__ cam_of
 // ---------------------------------------------------------------- Cholesky
 
 // Factor the NB x NB diagonal block at (j0, j0) in shared memory.
+// The pivot's square root and its reciprocal are taken once per column (by
+// thread 0) and the column is scaled by multiplication: FP64 square roots and
+// divisions expand into many instructions on GB300's narrow FP64 pipe, and the
+// kernel runs on one SM, on the factorisation's critical path.
 __global__ void __launch_bounds__(256) potrf_diag_kernel(double* __restrict__ A, int j0, int lda, int* __restrict__ info) {
     __shared__ double a[NB][NB + 1];  // a[col][row]
+    __shared__ double lk[2];          // L_kk, 1 / L_kk
     __shared__ int failed;
     if (*info) return;
     const int tid = threadIdx.x;
@@ -181,10 +186,15 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double* __restrict__ A,
             }
             break;  // every thread read the same pivot
         }
-        const double lkk = sqrt(piv);
+        if (tid == 0) {
+            const double lkk = sqrt(piv);
+            lk[0] = lkk;
+            lk[1] = 1.0 / lkk;
+        }
         __syncthreads();
-        for (int r = k + 1 + tid; r < NB; r += 256) a[k][r] /= lkk;
-        if (tid == 0) a[k][k] = lkk;
+        const double inv = lk[1];
+        for (int r = k + 1 + tid; r < NB; r += 256) a[k][r] *= inv;
+        if (tid == 0) a[k][k] = lk[0];
         __syncthreads();
         for (int idx = tid; idx < NB * NB; idx += 256) {
             const int r = idx % NB, c = idx / NB;
@@ -209,15 +219,17 @@ __global__ void __launch_bounds__(256) trsm_panel_kernel(double* __restrict__ A,
     if (*info) return;
     const int tid = threadIdx.x;
     const long long r0 = j0 + NB + (long long)NB * blockIdx.x;
+    __shared__ double rinv[NB];  // 1 / L_kk, one division per column
     for (int idx = tid; idx < NB * NB; idx += 256) {
         const int r = idx % NB, c = idx / NB;
         L[c][r] = r >= c ? A[(j0 + r) + (long long)(j0 + c) * lda] : 0.0;
         X[c][r] = A[(r0 + r) + (long long)(j0 + c) * lda];
     }
+    if (tid < NB) rinv[tid] = 1.0 / A[(j0 + tid) + (long long)(j0 + tid) * lda];
     __syncthreads();
     for (int k = 0; k < NB; ++k) {
-        const double d = L[k][k];
-        for (int r = tid; r < NB; r += 256) X[k][r] /= d;
+        const double d = rinv[k];
+        for (int r = tid; r < NB; r += 256) X[k][r] *= d;
         __syncthreads();
         for (int idx = tid; idx < NB * NB; idx += 256) {
             const int r = idx % NB, c = idx / NB;
@@ -295,21 +307,38 @@ __global__ void __launch_bounds__(256) syrk_update_kernel(double* __restrict__ A
 
 // ---------------------------------------------------------------- triangular solves
 
-// y_j = L_jj^{-1} b_j (forward) for the diagonal block at j0; one CTA.
+// The diagonal block L_jj (lower triangle) and the reciprocals of its diagonal
+// into shared memory: the triangular solves below then take their 64 dependent
+// steps from shared memory, with multiplications (one division per column).
+__device__ __forceinline__ void load_diag_tile(const double* __restrict__ L, int j0, int lda, double (*t)[NB + 1],
+                                               double* rinv) {
+    for (int idx = threadIdx.x; idx < NB * NB; idx += NB) {
+        const int r = idx % NB, c = idx / NB;
+        t[c][r] = r >= c ? L[(j0 + r) + (long long)(j0 + c) * lda] : 0.0;
+    }
+    __syncthreads();
+    rinv[threadIdx.x] = 1.0 / t[threadIdx.x][threadIdx.x];
+    __syncthreads();
+}
+
+// y_j = L_jj^{-1} b_j (forward) for the diagonal block at j0; one CTA of NB threads.
 __global__ void trsv_lower_diag(const double* __restrict__ L, int j0, int lda, double* __restrict__ b,
                                 const int* __restrict__ info) {
     __shared__ double x[NB];
+    __shared__ double t[NB][NB + 1];  // t[col][row]
+    __shared__ double rinv[NB];
     if (*info) return;
-    const int t = threadIdx.x;  // NB threads
-    x[t] = b[j0 + t];
+    const int tr = threadIdx.x;  // NB threads
+    load_diag_tile(L, j0, lda, t, rinv);
+    x[tr] = b[j0 + tr];
     __syncthreads();
     for (int k = 0; k < NB; ++k) {
-        if (t == k) x[k] /= L[(j0 + k) + (long long)(j0 + k) * lda];
+        if (tr == k) x[k] *= rinv[k];
         __syncthreads();
-        if (t > k) x[t] -= L[(j0 + t) + (long long)(j0 + k) * lda] * x[k];
+        if (tr > k) x[tr] -= t[k][tr] * x[k];
         __syncthreads();
     }
-    b[j0 + t] = x[t];
+    b[j0 + tr] = x[tr];
 }
 
 // b[j0+NB : n) -= L[j0+NB:n, j0:j0+NB] b[j0 : j0+NB); thread per row.
@@ -327,22 +356,25 @@ __global__ void gemv_lower_below(const double* __restrict__ L, int j0, int n, in
     b[r] -= s;
 }
 
-// x_j = L_jj^{-T} y_j (backward) for the diagonal block at j0; one CTA.
+// x_j = L_jj^{-T} y_j (backward) for the diagonal block at j0; one CTA of NB threads.
 __global__ void trsv_upper_diag(const double* __restrict__ L, int j0, int lda, double* __restrict__ b,
                                 const int* __restrict__ info) {
     __shared__ double x[NB];
+    __shared__ double t[NB][NB + 1];  // t[col][row]
+    __shared__ double rinv[NB];
     if (*info) return;
-    const int t = threadIdx.x;
-    x[t] = b[j0 + t];
+    const int tr = threadIdx.x;
+    load_diag_tile(L, j0, lda, t, rinv);
+    x[tr] = b[j0 + tr];
     __syncthreads();
     for (int k = NB - 1; k >= 0; --k) {
-        if (t == k) x[k] /= L[(j0 + k) + (long long)(j0 + k) * lda];
+        if (tr == k) x[k] *= rinv[k];
         __syncthreads();
-        // row t of L^T is column t of L: (L^T)(t, k) = L(k, t), k > t
-        if (t < k) x[t] -= L[(j0 + k) + (long long)(j0 + t) * lda] * x[k];
+        // row tr of L^T is column tr of L: (L^T)(tr, k) = L(k, tr), k > tr
+        if (tr < k) x[tr] -= t[tr][k] * x[k];
         __syncthreads();
     }
-    b[j0 + t] = x[t];
+    b[j0 + tr] = x[tr];
 }
 
 // y[i0 : j0) -= L[j0:j0+NB, i0:j0]^T x_j; one warp per output row i (reads column i of L).
