@@ -211,34 +211,41 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(double* __restrict__ A,
 }
 
 // Panel solve: rows [j0+NB, n) of columns [j0, j0+NB) := B L_jj^{-T}.
-__global__ void __launch_bounds__(256) trsm_panel_kernel(double* __restrict__ A, int j0, int lda,
+// Rows are independent in X L^T = B: a CTA takes `rows` (a divisor of NB) rows
+// of one panel tile, so that a narrow panel (a band's few tiles) still spreads
+// over NB / rows CTAs per tile.
+__global__ void __launch_bounds__(256) trsm_panel_kernel(double* __restrict__ A, int j0, int lda, int rows,
                                                         const int* __restrict__ info) {
     extern __shared__ double tsm[];
     double(*L)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(tsm);                  // L[col][row]
-    double(*X)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(tsm + NB * (NB + 1));  // X[col][row]
+    double(*X)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(tsm + NB * (NB + 1));  // X[col][row < rows]
     if (*info) return;
     const int tid = threadIdx.x;
-    const long long r0 = j0 + NB + (long long)NB * blockIdx.x;
+    const int parts = NB / rows;
+    const long long r0 = j0 + NB + (long long)NB * (blockIdx.x / parts) + (long long)rows * (blockIdx.x % parts);
     __shared__ double rinv[NB];  // 1 / L_kk, one division per column
     for (int idx = tid; idx < NB * NB; idx += 256) {
         const int r = idx % NB, c = idx / NB;
         L[c][r] = r >= c ? A[(j0 + r) + (long long)(j0 + c) * lda] : 0.0;
+    }
+    for (int idx = tid; idx < rows * NB; idx += 256) {
+        const int r = idx % rows, c = idx / rows;
         X[c][r] = A[(r0 + r) + (long long)(j0 + c) * lda];
     }
     if (tid < NB) rinv[tid] = 1.0 / A[(j0 + tid) + (long long)(j0 + tid) * lda];
     __syncthreads();
     for (int k = 0; k < NB; ++k) {
         const double d = rinv[k];
-        for (int r = tid; r < NB; r += 256) X[k][r] *= d;
+        for (int r = tid; r < rows; r += 256) X[k][r] *= d;
         __syncthreads();
-        for (int idx = tid; idx < NB * NB; idx += 256) {
-            const int r = idx % NB, c = idx / NB;
+        for (int idx = tid; idx < rows * NB; idx += 256) {
+            const int r = idx % rows, c = idx / rows;
             if (c > k) X[c][r] -= X[k][r] * L[k][c];
         }
         __syncthreads();
     }
-    for (int idx = tid; idx < NB * NB; idx += 256) {
-        const int r = idx % NB, c = idx / NB;
+    for (int idx = tid; idx < rows * NB; idx += 256) {
+        const int r = idx % rows, c = idx / rows;
         A[(r0 + r) + (long long)(j0 + c) * lda] = X[c][r];
     }
 }
@@ -303,6 +310,51 @@ __global__ void __launch_bounds__(256) syrk_update_kernel(double* __restrict__ A
             A[row + col * lda] -= acc[m][n][0];
             A[row + (col + 1) * lda] -= acc[m][n][1];
         }
+}
+
+// The trailing update by 32 x 32 quadrants (four CTAs per 64 x 64 tile, the
+// upper quadrant of a diagonal tile skipped): for steps with few tiles (a
+// band's bt(bt+1)/2), so that the update spreads over four times as many SMs.
+// 8 warps per quadrant, each warp 8 x 16 = 1 x 2 DMMA tiles.
+constexpr int kSPq = 32 + 8;  // shared-memory stride (doubles) of the quadrant's K-major operands
+__global__ void __launch_bounds__(256) syrk_update_quad_kernel(double* __restrict__ A, int j0, int ntiles, int lda,
+                                                              const int* __restrict__ info) {
+    __shared__ double As[NB * kSPq];  // [k][row]
+    __shared__ double Bs[NB * kSPq];  // [k][col]
+    if (*info) return;
+    const long long bidx = blockIdx.x >> 2;
+    const int quad = blockIdx.x & 3, qr = quad >> 1, qc = quad & 1;
+    int ti = static_cast<int>((sqrt(8.0 * (double)bidx + 1.0) - 1.0) * 0.5);
+    while ((long long)(ti + 1) * (ti + 2) / 2 <= bidx) ++ti;
+    while ((long long)ti * (ti + 1) / 2 > bidx) --ti;
+    const int tj = static_cast<int>(bidx - (long long)ti * (ti + 1) / 2);
+    if (ti >= ntiles || (ti == tj && qr < qc)) return;
+    const long long R0 = j0 + NB + (long long)NB * ti + 32 * qr, C0 = j0 + NB + (long long)NB * tj + 32 * qc;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < 32 * NB; idx += 256) {
+        const int r = idx % 32, k = idx / 32;
+        As[k * kSPq + r] = A[(R0 + r) + (long long)(j0 + k) * lda];
+        Bs[k * kSPq + r] = A[(C0 + r) + (long long)(j0 + k) * lda];
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    const int wm = (warp & 3) * 8, wn = (warp >> 2) * 16;
+    const int fr = lane >> 2, fk = lane & 3;
+    double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+#pragma unroll 4
+    for (int kk = 0; kk < NB; kk += 4) {
+        const double af = As[(kk + fk) * kSPq + wm + fr];
+        const double* bk = Bs + (kk + fk) * kSPq + wn + fr;
+        dmma_m8n8k4(acc[0], af, bk[0]);
+        dmma_m8n8k4(acc[1], af, bk[8]);
+    }
+#pragma unroll
+    for (int n = 0; n < 2; ++n) {
+        const long long row = R0 + wm + fr;
+        const long long col = C0 + wn + 8 * n + 2 * fk;
+        A[row + col * lda] -= acc[n][0];
+        A[row + (col + 1) * lda] -= acc[n][1];
+    }
 }
 
 // ---------------------------------------------------------------- triangular solves
@@ -418,10 +470,17 @@ void dense_potrf(double* A, int n, int lda, int bt, int* info, cudaStream_t s) {
             if (jb == nt - 1) break;
             continue;
         }
-        trsm_panel_kernel<<<below, 256, tsmem, s>>>(A, j0, lda, info);
+        // few panel tiles (a band, or the last steps of a dense matrix): split
+        // them over more CTAs
+        const int sms = device_sm_count();
+        const int rows = below * 4 <= sms ? 16 : NB;
+        trsm_panel_kernel<<<below * (NB / rows), 256, tsmem, s>>>(A, j0, lda, rows, info);
         GBA_LAUNCH_CHECK();
         const long long tiles = (long long)below * (below + 1) / 2;
-        syrk_update_kernel<<<static_cast<unsigned>(tiles), 256, smem, s>>>(A, j0, below, lda, info);
+        if (tiles * 2 <= sms)
+            syrk_update_quad_kernel<<<static_cast<unsigned>(4 * tiles), 256, 0, s>>>(A, j0, below, lda, info);
+        else
+            syrk_update_kernel<<<static_cast<unsigned>(tiles), 256, smem, s>>>(A, j0, below, lda, info);
         GBA_LAUNCH_CHECK();
     }
 }
