@@ -3,16 +3,22 @@
 //   S x   = U_lambda x - sum_p W_p V'_p^-1 W_p^T x,   W_e = Jc_e^T Jp_e
 //   rhs   = bc - sum_p W_p V'_p^-1 bp_p
 //
-// computed implicitly from the per-slot FP32 Jacobian rows (Jc32, Jp32, slot order):
+// computed implicitly from the per-slot FP32 Jacobian rows (Jc32, Jp32, slot
+// order, component-major):
 //   point pass   (slots sorted by point)  w_p = V'^-1 (a bp_p + sum_e Jp_e^T (Jc_e x_c)),
 //                                         u_e = Jp_e w_p          (2 values per slot)
 //   camera pass  (camera-major chunks)    partial_c = sum_e Jc_e^T u_e
 //   finalize                              y = U_lambda x - sum partials   (or rhs = bc - ...)
 // templated on the arithmetic type: FP32 inside PCG, float-float (ff.cuh) for
 // the right-hand side and the refinement residual when the Schur target is
-// tight. Chunk partials are summed in FP64 in a fixed order, so every product
-// is deterministic. The right-hand side pass also produces the block-Jacobi
+// tight. Chunk partials are summed in FP64 in a fixed order, so these products
+// are deterministic. The right-hand side pass also produces the block-Jacobi
 // diagonal-block sums (G = Jp V'^-1 Jp^T per slot, summed by the camera pass).
+// The FP32 product inside PCG runs by default as one pass (schur_matvec_warp,
+// schur_matvec_long): the point pass adds Jc_e^T u_e into per-camera
+// accumulators with device atomics instead of storing u_e, so each slot's
+// Jacobian rows are read once; its sums are then ordered only up to the
+// atomics (gba_solver_set_matvec selects the two-pass product).
 //
 // Solve: iterative refinement (dc += e, r = rhs - S dc with float-float
 // products, until ||r|| <= refine_tol ||rhs||) around inner block-Jacobi PCG
