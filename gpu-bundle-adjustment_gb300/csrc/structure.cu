@@ -218,7 +218,6 @@ __global__ void gather_cm_kernel(const int* __restrict__ cam_slots, const int* _
     }
 }
 
-// offsets[k] = first position i with keys[i] >= k, for k = 0..nk (keys sorted).
 // acc_id[s] = acc_off[cam(s)] + (camera-major position of s - cam_off[cam(s)]) / per
 __global__ void acc_id_kernel(const int* __restrict__ s_cam, const int* __restrict__ cam_pos,
                               const int* __restrict__ cam_off, const int* __restrict__ acc_off, int E, int per,
@@ -229,6 +228,7 @@ __global__ void acc_id_kernel(const int* __restrict__ s_cam, const int* __restri
     }
 }
 
+// offsets[k] = first position i with keys[i] >= k, for k = 0..nk (keys sorted).
 __global__ void csr_offsets_kernel(const int* __restrict__ keys, int n, int nk, int* __restrict__ off) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int prev = i == 0 ? -1 : keys[i - 1];
