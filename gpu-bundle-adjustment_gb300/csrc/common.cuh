@@ -14,12 +14,49 @@ namespace gba {
 // passes: 9 used, padded to 48 B so that a gather is two float4 and a float.
 constexpr int kX32 = 12;
 
-// The mixed forms' FP32 Jacobian rows are stored component-major: component k
-// of slot s at Jc32[k js + s] (k < 18: row 0 then row 1 of the 2 x 9 camera
-// block) and Jp32[k js + s] (k < 6), js = the slot count rounded up to 32.
-// A warp's load or store of one component is then 128 contiguous bytes (the
+// The mixed forms' FP32 Jacobian rows are stored in component groups: the 18
+// Jc components (row 0 then row 1 of the 2 x 9 camera block) as four float4
+// planes and a float2 plane, Jc32[(q js + s) 4 + i] = Jc[4q + i] (q < 4) and
+// Jc32[16 js + 2 s + i] = Jc[16 + i]; the 6 Jp components as a float4 plane
+// and a float2 plane, Jp32[4 s + i] = Jp[i], Jp32[4 js + 2 s + i] = Jp[4 + i];
+// js = the slot count rounded up to 32. A warp's access to one plane is 512 or
+// 256 contiguous bytes, and a slot's rows are 7 vector accesses (the
 // row-major 72- and 24-byte records cost 4x the L1 wavefronts).
 inline long long jacobian_stride(long long E) { return (E + 31) / 32 * 32; }
+
+__device__ __forceinline__ void store_jacobian_rows(float* __restrict__ Jc32, float* __restrict__ Jp32, long long js,
+                                                    long long s, const float* J) {
+    float4* c4 = reinterpret_cast<float4*>(Jc32);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c4[q * js + s] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+    reinterpret_cast<float2*>(Jc32 + 16 * js)[s] = make_float2(J[16], J[17]);
+    reinterpret_cast<float4*>(Jp32)[s] = make_float4(J[18], J[19], J[20], J[21]);
+    reinterpret_cast<float2*>(Jp32 + 4 * js)[s] = make_float2(J[22], J[23]);
+}
+__device__ __forceinline__ void load_jc_rows(const float* __restrict__ Jc32, long long js, long long s, float* Jc) {
+    const float4* c4 = reinterpret_cast<const float4*>(Jc32);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float4 v = c4[q * js + s];
+        Jc[4 * q] = v.x;
+        Jc[4 * q + 1] = v.y;
+        Jc[4 * q + 2] = v.z;
+        Jc[4 * q + 3] = v.w;
+    }
+    const float2 v = reinterpret_cast<const float2*>(Jc32 + 16 * js)[s];
+    Jc[16] = v.x;
+    Jc[17] = v.y;
+}
+__device__ __forceinline__ void load_jp_rows(const float* __restrict__ Jp32, long long js, long long s, float* jp) {
+    const float4 a = reinterpret_cast<const float4*>(Jp32)[s];
+    const float2 b = reinterpret_cast<const float2*>(Jp32 + 4 * js)[s];
+    jp[0] = a.x;
+    jp[1] = a.y;
+    jp[2] = a.z;
+    jp[3] = a.w;
+    jp[4] = b.x;
+    jp[5] = b.y;
+}
 
 // Thrown by the host driver on CUDA failure (the C-ABI layer converts it to a
 // status code; nothing throws across the ABI).

@@ -271,11 +271,8 @@ __global__ void __launch_bounds__(kPT) point_pass_f32(
                 for (int q = 0; q < 24; ++q) J[q] = 0.f;
                 r[0] = r[1] = 0.f;
             }
-            // component-major rows: lane-contiguous stores
-#pragma unroll
-            for (int k = 0; k < 18; ++k) Jc32[k * js + s] = J[k];
-#pragma unroll
-            for (int k = 0; k < 6; ++k) Jp32[k * js + s] = J[18 + k];
+            // component planes: lane-contiguous vector stores
+            store_jacobian_rows(Jc32, Jp32, js, s, J);
             float4* st = reinterpret_cast<float4*>(stg + kStg * threadIdx.x);
 #pragma unroll
             for (int k = 0; k < 4; ++k) st[k] = make_float4(J[4 * k], J[4 * k + 1], J[4 * k + 2], J[4 * k + 3]);

@@ -166,17 +166,14 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// J = [Jc(18), Jp(6)] of slot s (component-major rows, stride js)
+// J = [Jc(18), Jp(6)] of slot s (component planes, stride js)
 __device__ __forceinline__ void load_j(const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long js,
                                        long long s, float* J) {
-#pragma unroll
-    for (int k = 0; k < 18; ++k) J[k] = Jc32[k * js + s];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) J[18 + k] = Jp32[k * js + s];
+    load_jc_rows(Jc32, js, s, J);
+    load_jp_rows(Jp32, js, s, J + 18);
 }
 __device__ __forceinline__ void load_jp(const float* __restrict__ Jp32, long long js, long long s, float* jp) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) jp[k] = Jp32[k * js + s];
+    load_jp_rows(Jp32, js, s, jp);
 }
 
 // w = V'^-1 z (3x3 packed symmetric)
@@ -239,8 +236,7 @@ __device__ __forceinline__ void accumulate_jct_u(const float* __restrict__ Jc32,
                                                  T u1, T* y) {
     if constexpr (sizeof(T) == 4) {
         float Jc[18];
-#pragma unroll
-        for (int t = 0; t < 18; ++t) Jc[t] = Jc32[t * js + s];
+        load_jc_rows(Jc32, js, s, Jc);
         float r[9];
 #pragma unroll
         for (int t = 0; t < 9; ++t) r[t] = fmaf(Jc[t], u0, Jc[9 + t] * u1);

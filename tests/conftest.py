@@ -121,8 +121,11 @@ def shuffle_cameras(prob, seed):
 
 def jacobian_rows(s):
     """The mixed form's FP32 Jacobian rows as (E, 24) = [Jc (2 x 9 row-major), Jp
-    (2 x 3)] per slot, from their component-major device layout."""
+    (2 x 3)] per slot, from their device layout in component planes (Jc: four
+    float4 planes and a float2 plane; Jp: a float4 and a float2 plane)."""
     E = s.dims()[2]
-    jc = s.download("Jc32").reshape(18, -1)[:, :E]
-    jp = s.download("Jp32").reshape(6, -1)[:, :E]
-    return np.vstack([jc, jp]).T
+    a, b = s.download("Jc32"), s.download("Jp32")
+    js = a.size // 18
+    jc = np.hstack([a[:16 * js].reshape(4, js, 4).transpose(1, 0, 2).reshape(js, 16), a[16 * js:].reshape(js, 2)])
+    jp = np.hstack([b[:4 * js].reshape(js, 4), b[4 * js:].reshape(js, 2)])
+    return np.hstack([jc, jp])[:E]
