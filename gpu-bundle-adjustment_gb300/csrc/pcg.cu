@@ -1075,6 +1075,23 @@ __global__ void __launch_bounds__(kUT) coarse_z(const double* __restrict__ r, co
 // kCoarse single products): the Jacobian rows are read once per slot.
 
 constexpr int kZs = 88;  // BF16 values per camera of the basis copy Zb (9 x 9, padded to 16-byte multiples)
+constexpr int kU9 = 20;  // floats per u record of the coarse product (18 used; 80 B, 16-byte aligned)
+
+// u_j = Jp w_j for the nine columns, stored as one kU9 record: four float4
+// and a float2 (the records are scattered to camera-major positions, so fewer,
+// wider stores).
+__device__ __forceinline__ void store_u9(float* __restrict__ rec, const float* jp, const float* w) {
+    float u[18];
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) {
+        u[2 * j] = fmaf(jp[0], w[3 * j], fmaf(jp[1], w[3 * j + 1], jp[2] * w[3 * j + 2]));
+        u[2 * j + 1] = fmaf(jp[3], w[3 * j], fmaf(jp[4], w[3 * j + 1], jp[5] * w[3 * j + 2]));
+    }
+    float4* r4 = reinterpret_cast<float4*>(rec);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) r4[m] = make_float4(u[4 * m], u[4 * m + 1], u[4 * m + 2], u[4 * m + 3]);
+    reinterpret_cast<float2*>(rec)[8] = make_float2(u[16], u[17]);
+}
 
 // The basis is used at BF16 precision: Zb[c][i][j] = bf16(Z[j][9c + i]), the
 // per-camera rows the point pass gathers (176 B per camera), and Z itself is
@@ -1096,7 +1113,7 @@ __global__ void __launch_bounds__(kVT) coarse_zb_kernel(double* __restrict__ Zc,
 // a_j = Jc Z_c(:, j) for all columns (the camera's 9 x 9 rows read as float4
 // runs) and v_j = Jp^T a_j (27 values); per point t_j = sum over its slots (one
 // warp segmented scan of the 27 values and ordered segment sums), w_j = V'^-1 t_j;
-// per slot u_j = Jp w_j, 18 floats stored at the slot's camera-major position.
+// per slot u_j = Jp w_j, one kU9 record at the slot's camera-major position.
 __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restrict__ prange,
                                                             const int* __restrict__ pt_off,
                                                             const int* __restrict__ s_cam,
@@ -1200,13 +1217,7 @@ __global__ void __launch_bounds__(kPT, 2) coarse_point_pass9(const int4* __restr
         const int pl = s_pt[s] - p0;
         float jp[6];
         load_jp(Jp32, js, s, jp);
-        const float* w = wsh + pl * (KV + 1);
-        float2* out = reinterpret_cast<float2*>(u9 + 18ll * cam_pos[s]);
-#pragma unroll
-        for (int j = 0; j < kCoarse; ++j) {
-            const float w0 = w[3 * j], w1 = w[3 * j + 1], w2 = w[3 * j + 2];
-            out[j] = make_float2(jp[0] * w0 + jp[1] * w1 + jp[2] * w2, jp[3] * w0 + jp[4] * w1 + jp[5] * w2);
-        }
+        store_u9(u9 + static_cast<long long>(kU9) * cam_pos[s], jp, wsh + pl * (KV + 1));
     }
 }
 
@@ -1287,13 +1298,7 @@ __global__ void __launch_bounds__(32 * kMWarps) coarse_point_pass9_warp(
     const int last = 31 - __clz(__match_any_sync(0xffffffffu, key));
 #pragma unroll
     for (int k = 0; k < KV; ++k) v[k] = __shfl_sync(0xffffffffu, v[k], last);
-    if (has) {
-        float2* out = reinterpret_cast<float2*>(u9 + 18 * q);
-#pragma unroll
-        for (int j = 0; j < kCoarse; ++j)
-            out[j] = make_float2(fmaf(J[18], v[3 * j], fmaf(J[19], v[3 * j + 1], J[20] * v[3 * j + 2])),
-                                 fmaf(J[21], v[3 * j], fmaf(J[22], v[3 * j + 1], J[23] * v[3 * j + 2])));
-    }
+    if (has) store_u9(u9 + kU9 * q, J + 18, v);
 }
 
 // Point pass of S Z for points with 33 to 256 observations: a CTA takes a
@@ -1374,12 +1379,7 @@ __global__ void __launch_bounds__(kPT) coarse_point_pass9_list(
     }
     __syncthreads();
     if (tid < n) {
-        const float* w = wsh[key];
-        float2* out = reinterpret_cast<float2*>(u9 + 18ll * cam_pos[sl]);
-#pragma unroll
-        for (int j = 0; j < kCoarse; ++j)
-            out[j] = make_float2(fmaf(J[18], w[3 * j], fmaf(J[19], w[3 * j + 1], J[20] * w[3 * j + 2])),
-                                 fmaf(J[21], w[3 * j], fmaf(J[22], w[3 * j + 1], J[23] * w[3 * j + 2])));
+        store_u9(u9 + static_cast<long long>(kU9) * cam_pos[sl], J + 18, wsh[key]);
     }
 }
 
@@ -1402,7 +1402,7 @@ __global__ void __launch_bounds__(kC9) coarse_camera_pass9(const int* __restrict
     for (int i = 0; i < 9; ++i) acc[i] = 0.f;
     for (int q = b + g; q < e; q += 16) {
         const float* rec = J32c + 20ll * q;
-        const float2 u = reinterpret_cast<const float2*>(u9 + 18ll * q)[j];
+        const float2 u = reinterpret_cast<const float2*>(u9 + static_cast<long long>(kU9) * q)[j];
 #pragma unroll
         for (int i = 0; i < 9; ++i) acc[i] = fmaf(__ldg(rec + i), u.x, fmaf(__ldg(rec + 9 + i), u.y, acc[i]));
     }
@@ -2202,7 +2202,7 @@ void Solver::coarse_prepare(double lambda) {
         ceinv_.alloc(kCoarse * kCoarse + 1);
         cred_.alloc(need_red);
         czb_.alloc(1ull * kZs * C_);
-        cu9_.alloc(18ull * E_);
+        cu9_.alloc(static_cast<size_t>(kU9) * E_);
         cpart9_.alloc(81ull * std::max(n_cchunk_, 1));
     }
     cudaEvent_t ev = prof_start();

@@ -277,7 +277,7 @@ public:
     // and the partial sums of the balancing preconditioner and of E
     DevBuf<double> cz_, csz_, ceinv_, cred_, cpart9_;
     DevBuf<__nv_bfloat16> czb_;  // BF16 per-camera basis rows (the basis is used at BF16 precision)
-    DevBuf<float> cu9_;          // per-slot u of the product S Z (18 floats)
+    DevBuf<float> cu9_;          // per-slot u of the product S Z (18 floats in a 20-float record)
     void coarse_prepare(double lambda);  // pcg.cu
     // Learned form, per solve: 0 = not judged yet, 1 = the learned coarse
     // correction won the first inner solve, 2 = block-Jacobi won (used for the
