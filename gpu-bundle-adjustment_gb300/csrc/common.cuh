@@ -108,6 +108,25 @@ __device__ __forceinline__ double block_sum(double v, double* shared) {
     return r;
 }
 
+// The same for one float per thread: FP32 shuffle tree within each warp, the
+// warp sums widened to FP64 and added in warp order by thread 0 (one FP64 add
+// per warp: on GB300 the FP64 pipe is 1/64 of the FP32 one).
+template <int kThreads>
+__device__ __forceinline__ double block_sum_f(float v, double* shared) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) shared[warp] = static_cast<double>(v);
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) r += shared[w];
+    }
+    __syncthreads();
+    return r;
+}
+
 // Deterministic sum of part[0, n) by one block of kThreads threads (result in
 // thread 0): four interleaved accumulators per thread keep four independent
 // loads in flight instead of one dependent load per add; they are combined in

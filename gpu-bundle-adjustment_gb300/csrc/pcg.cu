@@ -833,23 +833,36 @@ __global__ void __launch_bounds__(kVT) residual_finalize(const int* __restrict__
     if (threadIdx.x == 0) red[blockIdx.x] = t;
 }
 
-// q = S p (finalize) and partial p.q.
+// Row k of the damped camera block times the camera's FP32 direction: Ul holds
+// U_lambda = U + lambda max(diag U, 1e-12) in FP32 (81 per camera), p32 the
+// padded direction (kX32 per camera).
+__device__ __forceinline__ float damped_u_row_dot32(const float* __restrict__ Ul, const float* __restrict__ pc, int k) {
+    const float* u = Ul + 9 * k;
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) s = fmaf(u[j], pc[j], s);
+    return s;
+}
+
+// q = S p (finalize of the two-pass product) and partial p.q: FP32 vectors,
+// the chunk partials summed in FP64.
 __global__ void __launch_bounds__(kVT) pcg_q_finalize(const int* __restrict__ cam_chunk_off,
-                                                     const double* __restrict__ part, const double* __restrict__ U,
-                                                     double lambda, const double* __restrict__ p, int C,
-                                                     double* __restrict__ q, double* __restrict__ red,
-                                                     const double* __restrict__ sc) {
+                                                     const double* __restrict__ part, const float* __restrict__ Ul,
+                                                     const float* __restrict__ p32, int C, float* __restrict__ q,
+                                                     double* __restrict__ red, const double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
     if (sc[S_DONE] != 0.0) return;
     const int i = blockIdx.x * kVT + threadIdx.x;
-    double v = 0.0;
+    float v = 0.f;
     if (i < 9 * C) {
         const int c = i / 9, k = i % 9;
-        const double qi = damped_u_row_dot(U + 81ll * c, k, lambda, p + 9ll * c) - chunk_sum(cam_chunk_off, part, c, k);
+        const float* pc = p32 + static_cast<long long>(kX32) * c;
+        const float qi = damped_u_row_dot32(Ul + 81ll * c, pc, k) -
+                         static_cast<float>(chunk_sum(cam_chunk_off, part, c, k));
         q[i] = qi;
-        v = p[i] * qi;
+        v = pc[k] * qi;
     }
-    const double t = block_sum<kVT>(v, sh);
+    const double t = block_sum_f<kVT>(v, sh);
     if (threadIdx.x == 0) red[blockIdx.x] = t;
 }
 
@@ -858,19 +871,19 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize(const int* __restrict__ ca
 // acc_off[c + 1])), which it clears for the next product. One warp per camera
 // (cameras strided over the grid's warps; the grid has one warp per camera):
 // lanes take the accumulators in turn as float4 runs, then a warp reduction;
-// one p.q partial per block.
+// one p.q partial per block. All FP32 but the block partial.
 __global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y, const int* __restrict__ acc_off,
-                                                         const double* __restrict__ U, double lambda,
-                                                         const double* __restrict__ p, int C,
-                                                         double* __restrict__ q, double* __restrict__ red,
+                                                         const float* __restrict__ Ul,
+                                                         const float* __restrict__ p32, int C,
+                                                         float* __restrict__ q, double* __restrict__ red,
                                                          const double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
     if (sc[S_DONE] != 0.0) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double pq = 0.0;
+    float pq = 0.f;
     for (int c = blockIdx.x * (kVT / 32) + warp; c < C; c += gridDim.x * (kVT / 32)) {
-        // FP32 sums (a lane's accumulators, then the warp tree: as few terms
-        // per sum as the two-pass camera pass), FP64 from the total on
+        // a lane's accumulators, then the warp tree: as few terms per sum as
+        // the two-pass camera pass
         float a[9];
 #pragma unroll
         for (int t = 0; t < 9; ++t) a[t] = 0.f;
@@ -891,19 +904,20 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y,
             reinterpret_cast<float4*>(yr)[1] = make_float4(0.f, 0.f, 0.f, 0.f);
             yr[8] = 0.f;
         }
-        double mine = 0.0;
+        float mine = 0.f;
 #pragma unroll
         for (int t = 0; t < 9; ++t) {
             const float v = warp_sum(a[t]);
-            if (lane == t) mine = static_cast<double>(v);
+            if (lane == t) mine = v;
         }
         if (lane < 9) {
-            const double qi = damped_u_row_dot(U + 81ll * c, lane, lambda, p + 9ll * c) - mine;
+            const float* pc = p32 + static_cast<long long>(kX32) * c;
+            const float qi = damped_u_row_dot32(Ul + 81ll * c, pc, lane) - mine;
             q[9ll * c + lane] = qi;
-            pq += p[9ll * c + lane] * qi;
+            pq = fmaf(pc[lane], qi, pq);
         }
     }
-    const double t = block_sum<kVT>(pq, sh);
+    const double t = block_sum_f<kVT>(pq, sh);
     if (threadIdx.x == 0) red[blockIdx.x] = t;
 }
 
@@ -940,11 +954,11 @@ __device__ __forceinline__ double ordered_sum_all(const double* __restrict__ red
 // substitution, then row a of M = L^-T L^-1. Once per inner solve; the PCG
 // update then applies M_c as a 9x9 product without divisions.
 // z_i = (M_c r_c)_k for entry i = 9c + k; rs holds the block's r entries.
-__device__ __forceinline__ double apply_minv_row(const double* __restrict__ Minv, long long c, int k, const double* rs) {
-    const double* m = Minv + 81 * c + 9 * k;
-    double z = 0.0;
+__device__ __forceinline__ float apply_minv_row(const float* __restrict__ Minv, long long c, int k, const float* rs) {
+    const float* m = Minv + 81 * c + 9 * k;
+    float z = 0.f;
 #pragma unroll
-    for (int j = 0; j < 9; ++j) z += m[j] * rs[j];
+    for (int j = 0; j < 9; ++j) z = fmaf(m[j], rs[j], z);
     return z;
 }
 
@@ -955,18 +969,18 @@ __device__ __forceinline__ double apply_minv_row(const double* __restrict__ Minv
 // its SPD flag live in einv[0, kCoarse^2) and einv[kCoarse^2]; a flag of 0 (E not
 // SPD) zeroes c1 and c2, which leaves block-Jacobi.
 
-// Block partials of V^T v for the kCoarse columns of V (entry i of this
-// thread, vi its value; i past the end contributes 0): red[block * kCoarse + j].
-__device__ __forceinline__ void coarse_partials(const double* __restrict__ V, long long n, long long i, double vi,
-                                                double* sh, double* __restrict__ red) {
+// Block partials of V^T v for the kCoarse columns of V (FP32, entry i of this
+// thread, vi its value; i past the end contributes 0): red[block * kCoarse + j]
+// in FP64.
+__device__ __forceinline__ void coarse_partials(const float* __restrict__ V, long long n, long long i, float vi,
+                                                double* __restrict__ red) {
     // the nine block sums at once: warp shuffle trees (independent, so they
     // interleave), one barrier, then the warps' sums in warp order
-    __shared__ double wpart[kUT / 32][kCoarse];
-    (void)sh;
+    __shared__ float wpart[kUT / 32][kCoarse];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double v[kCoarse];
+    float v[kCoarse];
 #pragma unroll
-    for (int j = 0; j < kCoarse; ++j) v[j] = i < n ? V[j * n + i] * vi : 0.0;
+    for (int j = 0; j < kCoarse; ++j) v[j] = i < n ? V[j * n + i] * vi : 0.f;
 #pragma unroll
     for (int j = 0; j < kCoarse; ++j) v[j] = warp_sum(v[j]);
     if (lane == 0) {
@@ -975,18 +989,19 @@ __device__ __forceinline__ void coarse_partials(const double* __restrict__ V, lo
     }
     __syncthreads();
     if (threadIdx.x < kCoarse) {
-        double t = 0.0;
+        float t = 0.f;
 #pragma unroll
         for (int w = 0; w < kUT / 32; ++w) t += wpart[w][threadIdx.x];
-        red[static_cast<long long>(blockIdx.x) * kCoarse + threadIdx.x] = t;
+        red[static_cast<long long>(blockIdx.x) * kCoarse + threadIdx.x] = static_cast<double>(t);
     }
 }
 
 // c = E^-1 (sum over nb blocks of red[b * kCoarse + j]) in shared cs[kCoarse],
 // every block in the same order (warp j sums column j); 0 if E is not SPD.
-// Needs kUT / 32 == kCoarse warps.
+// Also an FP32 copy in csf[kCoarse] when given. Needs kUT / 32 == kCoarse warps.
 __device__ __forceinline__ void coarse_coeffs(const double* __restrict__ red, int nb,
-                                              const double* __restrict__ einv, double* tsum, double* cs) {
+                                              const double* __restrict__ einv, double* tsum, double* cs,
+                                              float* csf) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double v = 0.0;
     for (int b = lane; b < nb; b += 32) v += red[static_cast<long long>(b) * kCoarse + warp];
@@ -1000,6 +1015,7 @@ __device__ __forceinline__ void coarse_coeffs(const double* __restrict__ red, in
             for (int k = 0; k < kCoarse; ++k) c += einv[threadIdx.x * kCoarse + k] * tsum[k];
         }
         cs[threadIdx.x] = c;
+        if (csf) csf[threadIdx.x] = static_cast<float>(c);
     }
     __syncthreads();
 }
@@ -1007,67 +1023,68 @@ __device__ __forceinline__ void coarse_coeffs(const double* __restrict__ red, in
 // w = B^-1 (r - SZ c1) into w; block partials of SZ^T w. c1 from the Z^T r
 // partials (block 0 also stores it for coarse_z). At init (init != 0) the PCG
 // done flag is not consulted (it is set afterwards by pcg_init_finalize).
-__global__ void __launch_bounds__(kUT) coarse_w(const double* __restrict__ r, const double* __restrict__ SZ,
-                                               const double* __restrict__ Minv, const double* __restrict__ einv,
+// Vectors and SZ in FP32; the coarse coefficients in FP64.
+__global__ void __launch_bounds__(kUT) coarse_w(const float* __restrict__ r, const float* __restrict__ SZ,
+                                               const float* __restrict__ Minv, const double* __restrict__ einv,
                                                int C, const double* __restrict__ red_zr, int nb,
-                                               double* __restrict__ c1_out, double* __restrict__ w,
+                                               double* __restrict__ c1_out, float* __restrict__ w,
                                                double* __restrict__ red_szw, const double* __restrict__ sc, int init) {
     static_assert(kUT / 32 == kCoarse, "one warp per coarse column");
-    __shared__ double sh[kUT / 32];
-    __shared__ double rs[kUT];
+    __shared__ float rs[kUT];
     __shared__ double tsum[kCoarse], c1[kCoarse];
+    __shared__ float c1f[kCoarse];
     __shared__ double bc;
     if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
-    coarse_coeffs(red_zr, nb, einv, tsum, c1);
+    coarse_coeffs(red_zr, nb, einv, tsum, c1, c1f);
     if (blockIdx.x == 0 && threadIdx.x < kCoarse) c1_out[threadIdx.x] = c1[threadIdx.x];
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
-    double yi = 0.0;
+    float yi = 0.f;
     if (c < C) {
         yi = r[i];
 #pragma unroll
-        for (int j = 0; j < kCoarse; ++j) yi -= SZ[j * n + i] * c1[j];
+        for (int j = 0; j < kCoarse; ++j) yi = fmaf(-SZ[j * n + i], c1f[j], yi);
     }
     rs[threadIdx.x] = yi;
     __syncthreads();
-    double wi = 0.0;
+    float wi = 0.f;
     if (c < C) {
         wi = apply_minv_row(Minv, c, k, rs + 9 * cl);
         w[i] = wi;
     }
-    coarse_partials(SZ, n, i, wi, sh, red_szw);
+    coarse_partials(SZ, n, i, wi, red_szw);
 }
 
 // z = w + Z (c1 - c2) in place of w, c2 = E^-1 SZ^T w from the partials; the
-// partials of r.z; at init also p = z and its FP32 copy.
-__global__ void __launch_bounds__(kUT) coarse_z(const double* __restrict__ r, const double* __restrict__ Zc,
+// partials of r.z; at init also p = z (FP32 padded direction).
+__global__ void __launch_bounds__(kUT) coarse_z(const float* __restrict__ r, const float* __restrict__ Zc,
                                                const double* __restrict__ einv, int C,
                                                const double* __restrict__ red_szw, int nb,
-                                               const double* __restrict__ c1_in, double* __restrict__ z,
-                                               double* __restrict__ p, float* __restrict__ p32,
-                                               double* __restrict__ red_rz, const double* __restrict__ sc, int init) {
+                                               const double* __restrict__ c1_in, float* __restrict__ z,
+                                               float* __restrict__ p32, double* __restrict__ red_rz,
+                                               const double* __restrict__ sc, int init) {
     __shared__ double sh[kUT / 32];
     __shared__ double tsum[kCoarse], c2[kCoarse];
+    __shared__ float d[kCoarse];
     __shared__ double bc;
     if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
-    coarse_coeffs(red_szw, nb, einv, tsum, c2);
+    coarse_coeffs(red_szw, nb, einv, tsum, c2, nullptr);
+    if (threadIdx.x < kCoarse) d[threadIdx.x] = static_cast<float>(c1_in[threadIdx.x] - c2[threadIdx.x]);
+    __syncthreads();
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
-    double rz = 0.0;
+    float rz = 0.f;
     if (c < C) {
-        double zi = z[i];
+        float zi = z[i];
 #pragma unroll
-        for (int j = 0; j < kCoarse; ++j) zi += Zc[j * n + i] * (c1_in[j] - c2[j]);
+        for (int j = 0; j < kCoarse; ++j) zi = fmaf(Zc[j * n + i], d[j], zi);
         z[i] = zi;
-        if (init) {
-            p[i] = zi;
-            p32[kX32 * c + k] = static_cast<float>(zi);
-        }
+        if (init) p32[kX32 * c + k] = zi;
         rz = r[i] * zi;
     }
-    const double t = block_sum<kUT>(rz, sh);
+    const double t = block_sum_f<kUT>(rz, sh);
     if (threadIdx.x == 0) red_rz[blockIdx.x] = t;
 }
 
@@ -1094,19 +1111,21 @@ __device__ __forceinline__ void store_u9(float* __restrict__ rec, const float* j
 }
 
 // The basis is used at BF16 precision: Zb[c][i][j] = bf16(Z[j][9c + i]), the
-// per-camera rows the point pass gathers (176 B per camera), and Z itself is
-// overwritten by the same rounded values, so that S Z, E = Z^T S Z and the
-// preconditioner all use one basis (any full-rank basis is valid; the rounding
+// per-camera rows the point pass gathers (176 B per camera), and Z itself (and
+// its FP32 copy Zc32, for the PCG) is overwritten by the same rounded values,
+// so that S Z, E = Z^T S Z and the preconditioner all use one basis (any full-rank basis is valid; the rounding
 // moves its span by ~4e-3 relative).
 __global__ void __launch_bounds__(kVT) coarse_zb_kernel(double* __restrict__ Zc, int C,
-                                                       __nv_bfloat16* __restrict__ Zb) {
+                                                       __nv_bfloat16* __restrict__ Zb, float* __restrict__ Zc32) {
     const int t = blockIdx.x * kVT + threadIdx.x;
     if (t >= 81 * C) return;
     const int c = t / 81, r = t - 81 * c, i = r / 9, j = r - 9 * i;
-    double* z = Zc + static_cast<long long>(j) * 9 * C + 9ll * c + i;
-    const __nv_bfloat16 b = __float2bfloat16_rn(static_cast<float>(*z));
+    const long long at = static_cast<long long>(j) * 9 * C + 9ll * c + i;
+    const __nv_bfloat16 b = __float2bfloat16_rn(static_cast<float>(Zc[at]));
     Zb[static_cast<long long>(kZs) * c + r] = b;
-    *z = static_cast<double>(__bfloat162float(b));
+    const float v = __bfloat162float(b);
+    Zc[at] = static_cast<double>(v);
+    Zc32[at] = v;
 }
 
 // Point pass of S Z (FP32, as schur_point_pass for one vector): per slot,
@@ -1417,19 +1436,22 @@ __global__ void __launch_bounds__(kC9) coarse_camera_pass9(const int* __restrict
     }
 }
 
-// SZ[j][9c + i] = (U_lambda Z_j)_(c, i) - sum over the camera's chunks of part[81 q + 9 i + j] (FP64).
+// SZ[j][9c + i] = (U_lambda Z_j)_(c, i) - sum over the camera's chunks of part[81 q + 9 i + j] (FP64),
+// and its FP32 copy SZ32 (for the PCG).
 __global__ void __launch_bounds__(kVT) coarse_sz_finalize(const int* __restrict__ cam_chunk_off,
                                                          const double* __restrict__ part,
                                                          const double* __restrict__ U, double lambda,
                                                          const double* __restrict__ Zc, int C,
-                                                         double* __restrict__ SZ) {
+                                                         double* __restrict__ SZ, float* __restrict__ SZ32) {
     const int t = blockIdx.x * kVT + threadIdx.x;
     if (t >= 81 * C) return;
     const int c = t / 81, r = t - 81 * c, i = r / 9, j = r - 9 * i;
     const long long n = 9ll * C;
     double sum = 0.0;
     for (int q = cam_chunk_off[c]; q < cam_chunk_off[c + 1]; ++q) sum += part[81ll * q + r];
-    SZ[j * n + 9ll * c + i] = damped_u_row_dot(U + 81ll * c, i, lambda, Zc + j * n + 9ll * c) - sum;
+    const double v = damped_u_row_dot(U + 81ll * c, i, lambda, Zc + j * n + 9ll * c) - sum;
+    SZ[j * n + 9ll * c + i] = v;
+    SZ32[j * n + 9ll * c + i] = static_cast<float>(v);
 }
 
 // Block partials of E = Z^T SZ: red[block * kCoarse^2 + a kCoarse + b] over the
@@ -1532,27 +1554,34 @@ __global__ void __launch_bounds__(kEinvT) coarse_einv_kernel(const double* __res
 }
 
 // Block partials of a . b (FP64).
-__global__ void __launch_bounds__(kVT) dot_partials(const double* __restrict__ a, const double* __restrict__ b, int n,
+// Block partials of a . b, a FP64 and b FP32 (b . x of the inner solution).
+__global__ void __launch_bounds__(kVT) dot_partials(const double* __restrict__ a, const float* __restrict__ b, int n,
                                                    double* __restrict__ red) {
     __shared__ double sh[kVT / 32];
     const int i = blockIdx.x * kVT + threadIdx.x;
-    const double t = block_sum<kVT>(i < n ? a[i] * b[i] : 0.0, sh);
+    const double t = block_sum<kVT>(i < n ? a[i] * static_cast<double>(b[i]) : 0.0, sh);
     if (threadIdx.x == 0) red[blockIdx.x] = t;
 }
+
+// The inner PCG's vectors are FP32 (x, r, z, q: 9 per camera; the direction p
+// in the padded product layout p32, kX32 per camera): it solves the FP32
+// operator's system to a relative residual of 1e-4 or looser, and the
+// refinement around it carries the accuracy. Its scalars (p.q, r.r, r.z, alpha,
+// beta) and the sums of block partials stay FP64.
 
 // alpha = rz / p.q (every block sums the p.q partials in the same order);
 // x += alpha p, r -= alpha q, z = M r; partials r.r and r.z. Nine threads per camera.
 // With a coarse basis Z (learned form; Zc non-null) z is left to coarse_w /
 // coarse_z: this kernel writes the partials of Z^T r (kCoarse per block) instead.
-__global__ void __launch_bounds__(kUT) pcg_update(double* __restrict__ x, double* __restrict__ r,
-                                                 double* __restrict__ z, const double* __restrict__ p,
-                                                 const double* __restrict__ q, const double* __restrict__ Minv, int C,
+__global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* __restrict__ r,
+                                                 float* __restrict__ z, const float* __restrict__ p32,
+                                                 const float* __restrict__ q, const float* __restrict__ Minv, int C,
                                                  const double* __restrict__ red_pq, int n_pq,
                                                  double* __restrict__ red_rr, double* __restrict__ red_rz,
-                                                 double* __restrict__ sc, const double* __restrict__ Zc,
+                                                 double* __restrict__ sc, const float* __restrict__ Zc,
                                                  double* __restrict__ red_zr) {
     __shared__ double sh[kUT / 32];
-    __shared__ double rs[kUT];
+    __shared__ float rs[kUT];
     __shared__ double bc;
     if (block_flag(sc + S_DONE, &bc) != 0.0) return;
     const double pq = ordered_sum_all<kUT>(red_pq, n_pq, sh, &bc);
@@ -1568,31 +1597,32 @@ __global__ void __launch_bounds__(kUT) pcg_update(double* __restrict__ x, double
         sc[S_RZPREV] = rz_old;
         sc[S_ITERS] += 1.0;
     }
+    const float af = static_cast<float>(alpha);
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long i = 9 * c + k;
-    double ri = 0.0;
+    float ri = 0.f;
     if (c < C) {
-        x[i] += alpha * p[i];
-        ri = r[i] - alpha * q[i];
+        x[i] = fmaf(af, p32[kX32 * c + k], x[i]);
+        ri = fmaf(-af, q[i], r[i]);
         r[i] = ri;
     }
     if (Zc) {
-        coarse_partials(Zc, 9ll * C, i, c < C ? ri : 0.0, sh, red_zr);
-        const double a = block_sum<kUT>(ri * ri, sh);
+        coarse_partials(Zc, 9ll * C, i, ri, red_zr);
+        const double a = block_sum_f<kUT>(ri * ri, sh);
         if (threadIdx.x == 0) red_rr[blockIdx.x] = a;
         return;
     }
     rs[threadIdx.x] = ri;
     __syncthreads();
-    double rr = ri * ri, rz = 0.0;
+    float rz = 0.f;
     if (c < C) {
-        const double zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+        const float zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
         z[i] = zi;
         rz = ri * zi;
     }
-    const double a = block_sum<kUT>(rr, sh);
-    const double b = block_sum<kUT>(rz, sh);
+    const double a = block_sum_f<kUT>(ri * ri, sh);
+    const double b = block_sum_f<kUT>(rz, sh);
     if (threadIdx.x == 0) {
         red_rr[blockIdx.x] = a;
         red_rz[blockIdx.x] = b;
@@ -1600,9 +1630,8 @@ __global__ void __launch_bounds__(kUT) pcg_update(double* __restrict__ x, double
 }
 
 // Convergence test and beta = rz / rz_prev (every block sums the partials in
-// the same order), then p = z + beta p and its FP32 copy.
-__global__ void __launch_bounds__(kVT) pcg_direction(double* __restrict__ p, float* __restrict__ p32,
-                                                    const double* __restrict__ z, int n,
+// the same order), then p = z + beta p (FP32, padded layout).
+__global__ void __launch_bounds__(kVT) pcg_direction(float* __restrict__ p32, const float* __restrict__ z, int n,
                                                     const double* __restrict__ red_rr,
                                                     const double* __restrict__ red_rz, int n_red, int max_iters,
                                                     double* __restrict__ sc) {
@@ -1628,52 +1657,51 @@ __global__ void __launch_bounds__(kVT) pcg_direction(double* __restrict__ p, flo
         }
     }
     if (done != 0.0) return;
+    const float bf = static_cast<float>(beta);
     const int i = blockIdx.x * kVT + threadIdx.x;
     if (i < n) {
-        const double v = z[i] + beta * p[i];
-        p[i] = v;
         const int c = i / 9;
-        p32[kX32 * c + (i - 9 * c)] = static_cast<float>(v);
+        float* pp = p32 + static_cast<long long>(kX32) * c + (i - 9 * c);
+        *pp = fmaf(bf, *pp, z[i]);
     }
 }
 
-// x = 0, r = b, z = M b, p = z; partials b.b and r.z. Nine threads per camera.
-// With a coarse basis (Zc non-null): x = 0, r = b and the partials b.b and Z^T b;
-// coarse_w / coarse_z then form z = p and the r.z partials.
-__global__ void __launch_bounds__(kUT) pcg_init(double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
-                                               double* __restrict__ p, float* __restrict__ p32,
-                                               const double* __restrict__ b, const double* __restrict__ Minv, int C,
-                                               double* __restrict__ red_rr, double* __restrict__ red_rz,
-                                               const double* __restrict__ Zc, double* __restrict__ red_zr) {
+// x = 0, r = b (rounded to FP32), z = M r, p = z; partials b.b and r.z. Nine
+// threads per camera. With a coarse basis (Zc non-null): x = 0, r = b and the
+// partials b.b and Z^T b; coarse_w / coarse_z then form z = p and the r.z partials.
+__global__ void __launch_bounds__(kUT) pcg_init(float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
+                                               float* __restrict__ p32, const double* __restrict__ b,
+                                               const float* __restrict__ Minv, int C, double* __restrict__ red_rr,
+                                               double* __restrict__ red_rz, const float* __restrict__ Zc,
+                                               double* __restrict__ red_zr) {
     __shared__ double sh[kUT / 32];
-    __shared__ double rs[kUT];
+    __shared__ float rs[kUT];
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long i = 9 * c + k;
-    double ri = 0.0;
+    float ri = 0.f;
     if (c < C) {
-        ri = b[i];
-        x[i] = 0.0;
+        ri = static_cast<float>(b[i]);
+        x[i] = 0.f;
         r[i] = ri;
     }
     if (Zc) {
-        coarse_partials(Zc, 9ll * C, i, c < C ? ri : 0.0, sh, red_zr);
-        const double a = block_sum<kUT>(ri * ri, sh);
+        coarse_partials(Zc, 9ll * C, i, ri, red_zr);
+        const double a = block_sum_f<kUT>(ri * ri, sh);
         if (threadIdx.x == 0) red_rr[blockIdx.x] = a;
         return;
     }
     rs[threadIdx.x] = ri;
     __syncthreads();
-    double rz = 0.0;
+    float rz = 0.f;
     if (c < C) {
-        const double zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+        const float zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
         z[i] = zi;
-        p[i] = zi;
-        p32[kX32 * c + k] = static_cast<float>(zi);
+        p32[kX32 * c + k] = zi;
         rz = ri * zi;
     }
-    const double a = block_sum<kUT>(ri * ri, sh);
-    const double bb = block_sum<kUT>(rz, sh);
+    const double a = block_sum_f<kUT>(ri * ri, sh);
+    const double bb = block_sum_f<kUT>(rz, sh);
     if (threadIdx.x == 0) {
         red_rr[blockIdx.x] = a;
         red_rz[blockIdx.x] = bb;
@@ -1714,16 +1742,33 @@ __global__ void __launch_bounds__(kVT) split_kernel(const double* __restrict__ y
     }
 }
 
-// y += x, and the float-float split of the new y (hi, lo interleaved).
-__global__ void __launch_bounds__(kVT) axpy_split_kernel(double* __restrict__ y, const double* __restrict__ x, int n,
+// y += x (x: the inner PCG's FP32 solution), and the float-float split of the
+// new y (hi, lo interleaved).
+__global__ void __launch_bounds__(kVT) axpy_split_kernel(double* __restrict__ y, const float* __restrict__ x, int n,
                                                         float* __restrict__ yff) {
     const int i = blockIdx.x * kVT + threadIdx.x;
     if (i < n) {
-        const double v = y[i] + x[i];
+        const double v = y[i] + static_cast<double>(x[i]);
         y[i] = v;
         const ff f = ffa::from_double(v);
         reinterpret_cast<float2*>(yff)[i] = make_float2(f.hi, f.lo);
     }
+}
+
+// Ul = U + lambda max(diag U, 1e-12) in FP32 (81 per camera): the camera
+// blocks of the inner PCG's operator, once per Schur solve.
+__global__ void __launch_bounds__(kVT) damped_u32_kernel(const double* __restrict__ U, double lambda, int C,
+                                                        float* __restrict__ Ul) {
+    const long long t = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x;
+    if (t >= 81ll * C) return;
+    const long long c = t / 81;
+    const int r = static_cast<int>(t - 81 * c), k = r / 9, j = r - 9 * k;
+    double v = U[t];
+    if (k == j) {
+        const double d = U[81 * c + 10 * k];
+        v += lambda * (d > 0.0 ? d : 1e-12);
+    }
+    Ul[t] = static_cast<float>(v);
 }
 
 // ---- block-Jacobi blocks S_cc = U_lambda,c - sum_{e in c} Jc^T (Jp V'^-1 Jp^T) Jc
@@ -1774,8 +1819,9 @@ __device__ __forceinline__ void chol9_lane(double (&a)[45]) {
 // Explicit block inverse M_c = (L L^T)^-1 = X^T X with X = L^-1, from the
 // factor in registers (one camera per lane). X overwrites L column by column
 // (column j of X needs L_ij only for its own entry X_ij, and L's later
-// columns); sums run in increasing k.
-__device__ __forceinline__ void inverse_from_factor_lane(double (&x)[45], double* __restrict__ M) {
+// columns); sums run in increasing k. M is stored in FP32: it is the inner
+// PCG's block-Jacobi preconditioner, applied to FP32 vectors.
+__device__ __forceinline__ void inverse_from_factor_lane(double (&x)[45], float* __restrict__ M) {
     double rd[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) rd[i] = 1.0 / x[blk::tri(i, i)];
@@ -1797,20 +1843,19 @@ __device__ __forceinline__ void inverse_from_factor_lane(double (&x)[45], double
             double m = 0.0;
 #pragma unroll
             for (int k = a; k < 9; ++k) m += x[blk::tri(k, a)] * x[blk::tri(k, b)];
-            M[9 * a + b] = m;
-            M[9 * b + a] = m;
+            M[9 * a + b] = static_cast<float>(m);
+            M[9 * b + a] = static_cast<float>(m);
         }
 }
 
 // One camera per lane: S_cc = U_lambda,c - (chunk sums from the right-hand
-// side pass, in chunk order), stored full FP64, its block-Jacobi factor and,
-// when Minv is given (no learned correction of the factor follows), the
-// explicit inverse as well.
+// side pass, in chunk order), stored full FP64, its block-Jacobi factor and
+// the explicit inverse (FP32).
 __global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict__ cam_chunk_off,
                                                           const double* __restrict__ part,
                                                           const double* __restrict__ U, double lambda, int C,
                                                           double* __restrict__ Sdiag, double* __restrict__ L,
-                                                          double* __restrict__ Minv) {
+                                                          float* __restrict__ Minv) {
     const int c = blockIdx.x * kSL + threadIdx.x;
     if (c >= C) return;
     const double* Uc = U + 81ll * c;
@@ -1840,7 +1885,7 @@ __global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict
     double* Lc = L + 45ll * c;
 #pragma unroll
     for (int t = 0; t < 45; ++t) Lc[t] = a[t];
-    if (Minv) inverse_from_factor_lane(a, Minv + 81ll * c);
+    inverse_from_factor_lane(a, Minv + 81ll * c);
 }
 
 }  // namespace
@@ -1971,6 +2016,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     sdiag_finalize_lane<<<ceil_div(C_, kSL), kSL, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
                                                                C_, Sdiag_.get(), Pfac_.get(), Pinv_.get());
     GBA_LAUNCH_CHECK();
+    damped_u32_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(U_.get(), lambda, C_, ul32_.get());
+    GBA_LAUNCH_CHECK();
     prof_stop("bj_blocks", bj_ev);
     if (learned && !model_) throw std::invalid_argument("learned form: no model loaded");
     if (learned && precond_force_ != 0) learned_choice_ = precond_force_;
@@ -1996,7 +2043,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     // The learned coarse space (basis, S Z, E^-1) is formed once per trial, when
     // an inner solve first needs it.
     bool coarse_ready = false;
-    // Inner PCG on the FP32 operator, S32 e = r (e in pcg_x_), preconditioned by
+    // Inner PCG on the FP32 operator, S32 e = r (e in pcg_e_, FP32), preconditioned by
     // block-Jacobi, or by the balancing two-level form with the learned coarse
     // basis (coarse). Returns the iteration count; *ok = reached the inner
     // tolerance without breakdown; inner_rel2 = its final ||r||^2 / ||b||^2.
@@ -2006,19 +2053,19 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             coarse_prepare(lambda);
             coarse_ready = true;
         }
-        const double* Zc = coarse ? cz_.get() : nullptr;
+        const float* Zc = coarse ? cz32_.get() : nullptr;
         double* red_zr = cred_.get();
         double* red_szw = red_zr + 1ll * nub * kCoarse;
         double* c1 = red_szw + 1ll * nub * kCoarse;
-        pcg_init<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(), pcg_p32_.get(),
-                                           ref_r_.get(), Pinv_.get(), C_, red, red2, Zc, red_zr);
+        pcg_init<<<nub, kUT, 0, stream_>>>(pcg_e_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p32_.get(), ref_r_.get(),
+                                           Pinv_.get(), C_, red, red2, Zc, red_zr);
         GBA_LAUNCH_CHECK();
         if (coarse) {
-            coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz_.get(), Pinv_.get(), ceinv_.get(), C_, red_zr, nub, c1,
-                                               pcg_z_.get(), red_szw, sc, 1);
+            coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz32_.get(), Pinv_.get(), ceinv_.get(), C_, red_zr, nub,
+                                               c1, pcg_z_.get(), red_szw, sc, 1);
             GBA_LAUNCH_CHECK();
             coarse_z<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), Zc, ceinv_.get(), C_, red_szw, nub, c1, pcg_z_.get(),
-                                               pcg_p_.get(), pcg_p32_.get(), red2, sc, 1);
+                                               pcg_p32_.get(), red2, sc, 1);
             GBA_LAUNCH_CHECK();
         }
         pcg_init_finalize<<<1, 256, 0, stream_>>>(red, red2, nub, opts.pcg_tol, sc);
@@ -2040,34 +2087,34 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                 if (one_pass_) {
                     implicit_parts_acc(*this, pcg_p32_.get(), done);
                     cudaEvent_t fev = prof_start();
-                    pcg_q_finalize_acc<<<npq, kVT, 0, stream_>>>(y_acc_.get(), acc_off_.get(), U_.get(), lambda,
-                                                                 pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                    pcg_q_finalize_acc<<<npq, kVT, 0, stream_>>>(y_acc_.get(), acc_off_.get(), ul32_.get(),
+                                                                 pcg_p32_.get(), C_, pcg_q_.get(), red_pq, sc);
                     GBA_LAUNCH_CHECK();
                     prof_stop("pcg_q_finalize", fev);
                 } else {
                     implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
                     cudaEvent_t fev = prof_start();
-                    pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(),
-                                                             lambda, pcg_p_.get(), C_, pcg_q_.get(), red_pq, sc);
+                    pcg_q_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), ul32_.get(),
+                                                             pcg_p32_.get(), C_, pcg_q_.get(), red_pq, sc);
                     GBA_LAUNCH_CHECK();
                     prof_stop("pcg_q_finalize", fev);
                 }
-                pcg_update<<<nub, kUT, 0, stream_>>>(pcg_x_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p_.get(),
+                pcg_update<<<nub, kUT, 0, stream_>>>(pcg_e_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p32_.get(),
                                                      pcg_q_.get(), Pinv_.get(), C_, red_pq, npq, red, red2, sc, Zc,
                                                      red_zr);
                 GBA_LAUNCH_CHECK();
                 if (coarse) {
                     cudaEvent_t cev = prof_start();
-                    coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz_.get(), Pinv_.get(), ceinv_.get(), C_, red_zr,
-                                                       nub, c1, pcg_z_.get(), red_szw, sc, 0);
+                    coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz32_.get(), Pinv_.get(), ceinv_.get(), C_,
+                                                       red_zr, nub, c1, pcg_z_.get(), red_szw, sc, 0);
                     GBA_LAUNCH_CHECK();
                     coarse_z<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), Zc, ceinv_.get(), C_, red_szw, nub, c1,
-                                                       pcg_z_.get(), nullptr, nullptr, red2, sc, 0);
+                                                       pcg_z_.get(), nullptr, red2, sc, 0);
                     GBA_LAUNCH_CHECK();
                     prof_stop("coarse_apply", cev);
                 }
-                pcg_direction<<<nvb, kVT, 0, stream_>>>(pcg_p_.get(), pcg_p32_.get(), pcg_z_.get(), n, red, red2,
-                                                        nub, max_iters, sc);
+                pcg_direction<<<nvb, kVT, 0, stream_>>>(pcg_p32_.get(), pcg_z_.get(), n, red, red2, nub, max_iters,
+                                                        sc);
                 GBA_LAUNCH_CHECK();
             }
             read_back({{h, sc, sizeof h}});
@@ -2078,9 +2125,9 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         prev_inner_ = static_cast<int>(h[S_ITERS]);
         return static_cast<long long>(h[S_ITERS]);
     };
-    // b . x of the inner solution pcg_x_ (b = ref_r_, the inner right-hand side) into sc[slot]
+    // b . x of the inner solution pcg_e_ (b = ref_r_, the inner right-hand side) into sc[slot]
     auto btx = [&](int slot) {
-        dot_partials<<<nvb, kVT, 0, stream_>>>(ref_r_.get(), pcg_x_.get(), n, red);
+        dot_partials<<<nvb, kVT, 0, stream_>>>(ref_r_.get(), pcg_e_.get(), n, red);
         GBA_LAUNCH_CHECK();
         sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, slot);
         GBA_LAUNCH_CHECK();
@@ -2103,7 +2150,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
             const long long it_l = inner_pcg(&ok_l, true, opts.pcg_max_iters);
             const double rel2_l = inner_rel2;
             btx(S_BTX1);
-            GBA_CUDA_CHECK(cudaMemcpyAsync(judge_x_.get(), pcg_x_.get(), n * sizeof(double),
+            GBA_CUDA_CHECK(cudaMemcpyAsync(judge_e_.get(), pcg_e_.get(), n * sizeof(float),
                                            cudaMemcpyDeviceToDevice, stream_));
             const long long cap =
                 ok_l ? std::min<long long>(opts.pcg_max_iters, (it_l * kLearnedWinDen + kLearnedWinNum - 1) / kLearnedWinNum)
@@ -2130,13 +2177,13 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                 learned_choice_ = 1;
                 use_learned = true;
                 inner_rel2 = rel2_l;
-                GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_x_.get(), judge_x_.get(), n * sizeof(double),
+                GBA_CUDA_CHECK(cudaMemcpyAsync(pcg_e_.get(), judge_e_.get(), n * sizeof(float),
                                                cudaMemcpyDeviceToDevice, stream_));
                 st.pcg_iterations += it_bj;
                 it_count = it_l;
                 ok = ok_l;
             } else {
-                // block-Jacobi's solve is in pcg_x_ (it ran last, and was not
+                // block-Jacobi's solve is in pcg_e_ (it ran last, and was not
                 // stopped early: a stopped run leaves ok_bj false, and the
                 // learned solve, converged, wins then)
                 learned_choice_ = (decisive || judge_attempts_ >= attempts) ? 2 : 0;
@@ -2159,16 +2206,17 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         }
         const double iters = static_cast<double>(it_count);
         if (fast && step == 0 && ok && inner_rel2 <= tol2 / bnorm2) {
-            // dc = e, with the inner solve's residual as the check
-            GBA_CUDA_CHECK(cudaMemcpyAsync(dc_.get(), pcg_x_.get(), n * sizeof(double), cudaMemcpyDeviceToDevice,
-                                           stream_));
+            // dc = e (dc is 0 before the first step), with the inner solve's
+            // residual as the check
+            axpy_split_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_e_.get(), n, dcff_.get());
+            GBA_LAUNCH_CHECK();
             rnorm2 = inner_rel2 * bnorm2;
             st.pcg_iterations += static_cast<long long>(iters);
             ++st.refine_steps;
             break;
         }
         // dc += e; residual r = rhs - S dc in float-float products, FP64 sums
-        axpy_split_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_x_.get(), n, dcff_.get());
+        axpy_split_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_e_.get(), n, dcff_.get());
         GBA_LAUNCH_CHECK();
         implicit_parts<ff>(*this, reinterpret_cast<const ff*>(dcff_.get()), 0.0, nullptr);
         residual_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
@@ -2188,7 +2236,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
 
 // Learned coarse space for this trial: the basis Z from the network at the
 // current cameras, SZ = S Z (one FP32 implicit product for all kCoarse columns,
-// FP64 finalize), and
+// FP64 finalize; Z and SZ also in FP32 for the PCG), and
 // E^-1 = (Z^T S Z)^-1 (FP64 Cholesky on the device; flagged off if E is not SPD).
 void Solver::coarse_prepare(double lambda) {
     const int n = 9 * C_;
@@ -2199,6 +2247,8 @@ void Solver::coarse_prepare(double lambda) {
         StreamAllocScope scope(stream_);
         cz_.alloc(1ull * kCoarse * n);
         csz_.alloc(1ull * kCoarse * n);
+        cz32_.alloc(1ull * kCoarse * n);
+        csz32_.alloc(1ull * kCoarse * n);
         ceinv_.alloc(kCoarse * kCoarse + 1);
         cred_.alloc(need_red);
         czb_.alloc(1ull * kZs * C_);
@@ -2208,7 +2258,7 @@ void Solver::coarse_prepare(double lambda) {
     cudaEvent_t ev = prof_start();
     cudaEvent_t ev1 = prof_start();
     model_->coarse_basis(*this, lambda, cz_.get());
-    coarse_zb_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, czb_.get());
+    coarse_zb_kernel<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cz_.get(), C_, czb_.get(), cz32_.get());
     GBA_LAUNCH_CHECK();
     prof_stop("coarse_basis", ev1);
     ev1 = prof_start();
@@ -2241,7 +2291,8 @@ void Solver::coarse_prepare(double lambda) {
     }
     ev1 = prof_start();
     coarse_sz_finalize<<<ceil_div(81ll * C_, kVT), kVT, 0, stream_>>>(cam_chunk_off_.get(), cpart9_.get(), U_.get(),
-                                                                      lambda, cz_.get(), C_, csz_.get());
+                                                                      lambda, cz_.get(), C_, csz_.get(),
+                                                                      csz32_.get());
     GBA_LAUNCH_CHECK();
     double* gram = cred_.get() + 2ll * nub * kCoarse + kCoarse;
     coarse_gram_partials<<<nvb, kVT, 0, stream_>>>(cz_.get(), csz_.get(), n, gram);

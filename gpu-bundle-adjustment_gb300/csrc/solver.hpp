@@ -267,8 +267,13 @@ public:
     DevBuf<int> info_;
     // mixed Schur
     DevBuf<double> Sdiag_, Pfac_;  // S diagonal blocks (81C), preconditioner factors (packed, 45 per camera)
-    DevBuf<double> Pinv_;          // explicit preconditioner blocks M_c = (L L^T)^-1 (81C)
-    DevBuf<double> pcg_x_, pcg_r_, pcg_z_, pcg_p_, pcg_q_, ref_r_, judge_x_;
+    DevBuf<float> Pinv_;           // explicit preconditioner blocks M_c = (L L^T)^-1 (81C, FP32)
+    DevBuf<double> pcg_x_;         // plain form: the dense solve's work vector
+    DevBuf<double> ref_r_;         // mixed forms: the refinement residual, the inner solve's right-hand side
+    // mixed forms: the inner PCG's FP32 vectors (9 per camera; its direction is
+    // pcg_p32_), the learned step kept while block-Jacobi is judged, and the
+    // damped camera blocks U_lambda in FP32 (81 per camera)
+    DevBuf<float> pcg_e_, pcg_r_, pcg_z_, pcg_q_, judge_e_, ul32_;
     DevBuf<double> u_;       // per-slot 2-vectors u_e = Jp_e w_p (matvec intermediate; FP32 or float-float)
     DevBuf<float> g_cm_;     // per-slot G_e = Jp V'^-1 Jp^T (00, 01, 11, pad) at camera-major positions
     DevBuf<double> pcg_s_;   // PCG device scalars (see pcg.cu)
@@ -276,6 +281,7 @@ public:
     // learned form: coarse basis Z (kCoarse columns of 9C), S Z, E^-1 (+ SPD flag),
     // and the partial sums of the balancing preconditioner and of E
     DevBuf<double> cz_, csz_, ceinv_, cred_, cpart9_;
+    DevBuf<float> cz32_, csz32_;  // Z and S Z in FP32 (the PCG's coarse correction)
     DevBuf<__nv_bfloat16> czb_;  // BF16 per-camera basis rows (the basis is used at BF16 precision)
     DevBuf<float> cu9_;          // per-slot u of the product S Z (18 floats in a 20-float record)
     void coarse_prepare(double lambda);  // pcg.cu

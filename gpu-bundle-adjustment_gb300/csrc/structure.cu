@@ -374,7 +374,7 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         Jc32_.alloc(18ull * js_);
         Jp32_.alloc(6ull * js_);
         J32c_.alloc(20ull * E);
-        judge_x_.alloc(9ull * C);
+        judge_e_.alloc(9ull * C);
         Vinv32_.alloc(6ull * P);
         cam_pre_ff_.alloc(32ull * C);
         pts_ff_.alloc(6ull * P);
@@ -389,11 +389,11 @@ Solver::Solver(int C, int P, int E, const double* cams, const double* pts, const
         Pfac_.alloc(81ull * C);
         Pinv_.alloc(81ull * C);
         rhs_.alloc(9ull * C);
-        pcg_x_.alloc(9ull * C);
+        pcg_e_.alloc(9ull * C);
         pcg_r_.alloc(9ull * C);
         pcg_z_.alloc(9ull * C);
-        pcg_p_.alloc(9ull * C);
         pcg_q_.alloc(9ull * C);
+        ul32_.alloc(81ull * C);
         ref_r_.alloc(9ull * C);
         u_.alloc(2ull * E);
         g_cm_.alloc(4ull * E);

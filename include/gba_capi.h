@@ -296,13 +296,18 @@ enum {
     GBA_BUF_DC = 8,       /* double[9 C] */
     GBA_BUF_DP = 9,       /* double[3 P] */
     GBA_BUF_ORDER = 10,   /* int[E]  original observation index of each slot */
-    GBA_BUF_JC32 = 11,    /* float[18 E] Jc (2x9 row-major) per slot (mixed forms) */
+    GBA_BUF_JC32 = 11,    /* float[18 js] Jc per slot (mixed forms), js = E rounded up to a multiple of 32:
+                             component planes, float4 plane q (q = 0..3) at [4 q js, 4 (q + 1) js) holding
+                             entries 4q..4q+3 of the 2x9 row-major Jc of slot s at 4 s, then a float2 plane
+                             at [16 js, 18 js) holding entries 16, 17 */
     GBA_BUF_SDIAG = 12,   /* double[81 C] S diagonal blocks (mixed form) */
     GBA_BUF_CAMS = 13,    /* double[9 C] current cameras */
     GBA_BUF_PTS = 14,     /* double[3 P] current points */
     GBA_BUF_TRIAL_CAMS = 15,
     GBA_BUF_TRIAL_PTS = 16,
-    GBA_BUF_JP32 = 17     /* float[6 E]  Jp (2x3 row-major) per slot (mixed forms) */
+    GBA_BUF_JP32 = 17     /* float[6 js] Jp per slot (mixed forms): a float4 plane at [0, 4 js) holding
+                             entries 0..3 of the 2x3 row-major Jp of slot s at 4 s, then a float2 plane at
+                             [4 js, 6 js) holding entries 4, 5 */
 };
 /* Size in bytes of a solver buffer (0 if the form does not hold it). */
 int gba_solver_buffer_size(gba_solver* s, int buffer, size_t* out_bytes);
