@@ -869,53 +869,101 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize(const int* __restrict__ ca
 // pcg_q_finalize for the one-pass product: q = U_lambda p - the sum of the
 // camera's accumulators (12 floats each, 9 used; camera c's at [acc_off[c],
 // acc_off[c + 1])), which it clears for the next product. One warp per camera
-// (cameras strided over the grid's warps; the grid has one warp per camera):
-// lanes take the accumulators in turn as float4 runs, then a warp reduction;
-// one p.q partial per block. All FP32 but the block partial.
+// (the grid has ceil(C / 8) blocks of 8 warps): lanes take the accumulators in
+// turn as float4 runs, two per lane per round with both loads issued before
+// the stores, then a warp reduction; one p.q partial per block. The loads that
+// do not depend on the product (offsets, U_lambda row, p) go out with the done
+// flag's, so that a warp waits for two memory round trips, not five. All FP32
+// but the block partial.
 __global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y, const int* __restrict__ acc_off,
                                                          const float* __restrict__ Ul,
                                                          const float* __restrict__ p32, int C,
                                                          float* __restrict__ q, double* __restrict__ red,
                                                          const double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
-    if (sc[S_DONE] != 0.0) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float pq = 0.f;
-    for (int c = blockIdx.x * (kVT / 32) + warp; c < C; c += gridDim.x * (kVT / 32)) {
-        // a lane's accumulators, then the warp tree: as few terms per sum as
-        // the two-pass camera pass
-        float a[9];
+    const int c = blockIdx.x * (kVT / 32) + warp;
+    const bool cam = c < C;
+    const double done = sc[S_DONE];
+    int r0 = 0, r1 = 0;
+    float u[9], pc[9], pown = 0.f;
 #pragma unroll
-        for (int t = 0; t < 9; ++t) a[t] = 0.f;
-        for (int r = acc_off[c] + lane; r < acc_off[c + 1]; r += 32) {
-            float* yr = y + static_cast<long long>(kX32) * r;
-            const float4 A = reinterpret_cast<float4*>(yr)[0], B = reinterpret_cast<float4*>(yr)[1];
-            const float c8 = yr[8];
-            a[0] += A.x;
-            a[1] += A.y;
-            a[2] += A.z;
-            a[3] += A.w;
-            a[4] += B.x;
-            a[5] += B.y;
-            a[6] += B.z;
-            a[7] += B.w;
-            a[8] += c8;
-            reinterpret_cast<float4*>(yr)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-            reinterpret_cast<float4*>(yr)[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-            yr[8] = 0.f;
-        }
-        float mine = 0.f;
-#pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const float v = warp_sum(a[t]);
-            if (lane == t) mine = v;
-        }
+    for (int j = 0; j < 9; ++j) u[j] = pc[j] = 0.f;
+    if (cam) {
+        r0 = acc_off[c];
+        r1 = acc_off[c + 1];
         if (lane < 9) {
-            const float* pc = p32 + static_cast<long long>(kX32) * c;
-            const float qi = damped_u_row_dot32(Ul + 81ll * c, pc, lane) - mine;
-            q[9ll * c + lane] = qi;
-            pq = fmaf(pc[lane], qi, pq);
+            const float* ur = Ul + 81ll * c + 9 * lane;
+            const float* pr = p32 + static_cast<long long>(kX32) * c;
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                u[j] = ur[j];
+                pc[j] = pr[j];
+            }
+            pown = pr[lane];
         }
+    }
+    if (done != 0.0) return;  // the same value in every thread of the grid
+    float a[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) a[t] = 0.f;
+    // a lane's accumulators (r, r + 32, r + 64, ... in order), then the warp
+    // tree: as few terms per sum as the two-pass camera pass
+    for (int r = r0 + lane; r < r1; r += 64) {
+        const bool two = r + 32 < r1;
+        float4* ya = reinterpret_cast<float4*>(y + static_cast<long long>(kX32) * r);
+        float4* yb = reinterpret_cast<float4*>(y + static_cast<long long>(kX32) * (r + 32));
+        const float4 A0 = ya[0], B0 = ya[1];
+        const float e0 = reinterpret_cast<const float*>(ya)[8];
+        float4 A1 = make_float4(0.f, 0.f, 0.f, 0.f), B1 = A1;
+        float e1 = 0.f;
+        if (two) {
+            A1 = yb[0];
+            B1 = yb[1];
+            e1 = reinterpret_cast<const float*>(yb)[8];
+        }
+        a[0] += A0.x;
+        a[1] += A0.y;
+        a[2] += A0.z;
+        a[3] += A0.w;
+        a[4] += B0.x;
+        a[5] += B0.y;
+        a[6] += B0.z;
+        a[7] += B0.w;
+        a[8] += e0;
+        a[0] += A1.x;
+        a[1] += A1.y;
+        a[2] += A1.z;
+        a[3] += A1.w;
+        a[4] += B1.x;
+        a[5] += B1.y;
+        a[6] += B1.z;
+        a[7] += B1.w;
+        a[8] += e1;
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        ya[0] = z4;
+        ya[1] = z4;
+        reinterpret_cast<float*>(ya)[8] = 0.f;
+        if (two) {
+            yb[0] = z4;
+            yb[1] = z4;
+            reinterpret_cast<float*>(yb)[8] = 0.f;
+        }
+    }
+    float mine = 0.f;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const float v = warp_sum(a[t]);
+        if (lane == t) mine = v;
+    }
+    float pq = 0.f;
+    if (cam && lane < 9) {
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) s = fmaf(u[j], pc[j], s);
+        const float qi = s - mine;
+        q[9ll * c + lane] = qi;
+        pq = pown * qi;
     }
     const double t = block_sum_f<kVT>(pq, sh);
     if (threadIdx.x == 0) red[blockIdx.x] = t;
@@ -938,11 +986,19 @@ __device__ __forceinline__ double block_flag(const double* flag, double* sh) {
     return v;
 }
 
-// Fixed-order sum of n partials, result in every thread of the block.
+// Fixed-order sum of n partials in two phases, so that a kernel can issue the
+// loads of the first together with its other independent loads: this
+// thread's share (elements threadIdx.x + m kThreads, in order), then the block
+// sum, result in every thread of the block.
 template <int kThreads>
-__device__ __forceinline__ double ordered_sum_all(const double* __restrict__ red, int n, double* sh, double* out) {
+__device__ __forceinline__ double thread_partial_sum(const double* __restrict__ red, int n) {
     double s = 0.0;
+#pragma unroll 4
     for (int i = threadIdx.x; i < n; i += kThreads) s += red[i];
+    return s;
+}
+template <int kThreads>
+__device__ __forceinline__ double finish_sum_all(double s, double* sh, double* out) {
     s = block_sum<kThreads>(s, sh);
     if (threadIdx.x == 0) *out = s;
     __syncthreads();
@@ -969,18 +1025,17 @@ __device__ __forceinline__ float apply_minv_row(const float* __restrict__ Minv, 
 // its SPD flag live in einv[0, kCoarse^2) and einv[kCoarse^2]; a flag of 0 (E not
 // SPD) zeroes c1 and c2, which leaves block-Jacobi.
 
-// Block partials of V^T v for the kCoarse columns of V (FP32, entry i of this
-// thread, vi its value; i past the end contributes 0): red[block * kCoarse + j]
-// in FP64.
-__device__ __forceinline__ void coarse_partials(const float* __restrict__ V, long long n, long long i, float vi,
-                                                double* __restrict__ red) {
+// Block partials of V^T v for the kCoarse columns of V (FP32): col holds this
+// thread's row of V (zeros past the end), vi its entry of v;
+// red[block * kCoarse + j] in FP64.
+__device__ __forceinline__ void coarse_partials(const float (&col)[kCoarse], float vi, double* __restrict__ red) {
     // the nine block sums at once: warp shuffle trees (independent, so they
     // interleave), one barrier, then the warps' sums in warp order
     __shared__ float wpart[kUT / 32][kCoarse];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float v[kCoarse];
 #pragma unroll
-    for (int j = 0; j < kCoarse; ++j) v[j] = i < n ? V[j * n + i] * vi : 0.f;
+    for (int j = 0; j < kCoarse; ++j) v[j] = col[j] * vi;
 #pragma unroll
     for (int j = 0; j < kCoarse; ++j) v[j] = warp_sum(v[j]);
     if (lane == 0) {
@@ -996,23 +1051,47 @@ __device__ __forceinline__ void coarse_partials(const float* __restrict__ V, lon
     }
 }
 
+// Row i of the kCoarse columns of V (entry i = 9c + k of camera c; zeros for c >= C).
+__device__ __forceinline__ void coarse_row(const float* __restrict__ V, long long n, long long i, bool in,
+                                           float (&col)[kCoarse]) {
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) col[j] = in ? V[j * n + i] : 0.f;
+}
+
 // c = E^-1 (sum over nb blocks of red[b * kCoarse + j]) in shared cs[kCoarse],
 // every block in the same order (warp j sums column j); 0 if E is not SPD.
 // Also an FP32 copy in csf[kCoarse] when given. Needs kUT / 32 == kCoarse warps.
-__device__ __forceinline__ void coarse_coeffs(const double* __restrict__ red, int nb,
-                                              const double* __restrict__ einv, double* tsum, double* cs,
-                                              float* csf) {
+// Two phases: the loads (coarse_coeff_loads: this lane's share of its warp's
+// column, and for threads < kCoarse their row of E^-1 and the SPD flag), then
+// the sums (coarse_coeffs).
+struct CoarseLoads {
+    double v;
+    double e[kCoarse];
+    bool spd;
+};
+__device__ __forceinline__ CoarseLoads coarse_coeff_loads(const double* __restrict__ red, int nb,
+                                                          const double* __restrict__ einv) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double v = 0.0;
-    for (int b = lane; b < nb; b += 32) v += red[static_cast<long long>(b) * kCoarse + warp];
-    v = warp_sum(v);
+    CoarseLoads L;
+    L.v = 0.0;
+#pragma unroll 4
+    for (int b = lane; b < nb; b += 32) L.v += red[static_cast<long long>(b) * kCoarse + warp];
+    const bool row = threadIdx.x < kCoarse;
+    L.spd = row && einv[kCoarse * kCoarse] != 0.0;
+#pragma unroll
+    for (int k = 0; k < kCoarse; ++k) L.e[k] = row ? einv[threadIdx.x * kCoarse + k] : 0.0;
+    return L;
+}
+__device__ __forceinline__ void coarse_coeffs(const CoarseLoads& L, double* tsum, double* cs, float* csf) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double v = warp_sum(L.v);
     if (lane == 0) tsum[warp] = v;
     __syncthreads();
     if (threadIdx.x < kCoarse) {
         double c = 0.0;
-        if (einv[kCoarse * kCoarse] != 0.0) {
+        if (L.spd) {
 #pragma unroll
-            for (int k = 0; k < kCoarse; ++k) c += einv[threadIdx.x * kCoarse + k] * tsum[k];
+            for (int k = 0; k < kCoarse; ++k) c += L.e[k] * tsum[k];
         }
         cs[threadIdx.x] = c;
         if (csf) csf[threadIdx.x] = static_cast<float>(c);
@@ -1023,7 +1102,8 @@ __device__ __forceinline__ void coarse_coeffs(const double* __restrict__ red, in
 // w = B^-1 (r - SZ c1) into w; block partials of SZ^T w. c1 from the Z^T r
 // partials (block 0 also stores it for coarse_z). At init (init != 0) the PCG
 // done flag is not consulted (it is set afterwards by pcg_init_finalize).
-// Vectors and SZ in FP32; the coarse coefficients in FP64.
+// Vectors and SZ in FP32; the coarse coefficients in FP64. Every load is
+// issued before the flag test and the coefficient sums.
 __global__ void __launch_bounds__(kUT) coarse_w(const float* __restrict__ r, const float* __restrict__ SZ,
                                                const float* __restrict__ Minv, const double* __restrict__ einv,
                                                int C, const double* __restrict__ red_zr, int nb,
@@ -1034,30 +1114,37 @@ __global__ void __launch_bounds__(kUT) coarse_w(const float* __restrict__ r, con
     __shared__ double tsum[kCoarse], c1[kCoarse];
     __shared__ float c1f[kCoarse];
     __shared__ double bc;
-    if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
-    coarse_coeffs(red_zr, nb, einv, tsum, c1, c1f);
-    if (blockIdx.x == 0 && threadIdx.x < kCoarse) c1_out[threadIdx.x] = c1[threadIdx.x];
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
-    float yi = 0.f;
-    if (c < C) {
-        yi = r[i];
+    const bool in = c < C;
+    const CoarseLoads L = coarse_coeff_loads(red_zr, nb, einv);
+    float sz[kCoarse], m[9], rv = 0.f;
+    coarse_row(SZ, n, i, in, sz);
 #pragma unroll
-        for (int j = 0; j < kCoarse; ++j) yi = fmaf(-SZ[j * n + i], c1f[j], yi);
-    }
-    rs[threadIdx.x] = yi;
+    for (int j = 0; j < 9; ++j) m[j] = in ? Minv[81 * c + 9 * k + j] : 0.f;
+    if (in) rv = r[i];
+    if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
+    coarse_coeffs(L, tsum, c1, c1f);
+    if (blockIdx.x == 0 && threadIdx.x < kCoarse) c1_out[threadIdx.x] = c1[threadIdx.x];
+    float yi = rv;
+#pragma unroll
+    for (int j = 0; j < kCoarse; ++j) yi = fmaf(-sz[j], c1f[j], yi);
+    rs[threadIdx.x] = in ? yi : 0.f;
     __syncthreads();
     float wi = 0.f;
-    if (c < C) {
-        wi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+    if (in) {
+        const float* y9 = rs + 9 * cl;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) wi = fmaf(m[j], y9[j], wi);
         w[i] = wi;
     }
-    coarse_partials(SZ, n, i, wi, red_szw);
+    coarse_partials(sz, wi, red_szw);
 }
 
 // z = w + Z (c1 - c2) in place of w, c2 = E^-1 SZ^T w from the partials; the
-// partials of r.z; at init also p = z (FP32 padded direction).
+// partials of r.z; at init also p = z (FP32 padded direction). Every load is
+// issued before the flag test and the coefficient sums.
 __global__ void __launch_bounds__(kUT) coarse_z(const float* __restrict__ r, const float* __restrict__ Zc,
                                                const double* __restrict__ einv, int C,
                                                const double* __restrict__ red_szw, int nb,
@@ -1068,21 +1155,30 @@ __global__ void __launch_bounds__(kUT) coarse_z(const float* __restrict__ r, con
     __shared__ double tsum[kCoarse], c2[kCoarse];
     __shared__ float d[kCoarse];
     __shared__ double bc;
-    if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
-    coarse_coeffs(red_szw, nb, einv, tsum, c2, nullptr);
-    if (threadIdx.x < kCoarse) d[threadIdx.x] = static_cast<float>(c1_in[threadIdx.x] - c2[threadIdx.x]);
-    __syncthreads();
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
+    const bool in = c < C;
+    const CoarseLoads L = coarse_coeff_loads(red_szw, nb, einv);
+    const double c1v = threadIdx.x < kCoarse ? c1_in[threadIdx.x] : 0.0;
+    float zc[kCoarse], zv = 0.f, rv = 0.f;
+    coarse_row(Zc, n, i, in, zc);
+    if (in) {
+        zv = z[i];
+        rv = r[i];
+    }
+    if (!init && block_flag(sc + S_DONE, &bc) != 0.0) return;
+    coarse_coeffs(L, tsum, c2, nullptr);
+    if (threadIdx.x < kCoarse) d[threadIdx.x] = static_cast<float>(c1v - c2[threadIdx.x]);
+    __syncthreads();
     float rz = 0.f;
-    if (c < C) {
-        float zi = z[i];
+    if (in) {
+        float zi = zv;
 #pragma unroll
-        for (int j = 0; j < kCoarse; ++j) zi = fmaf(Zc[j * n + i], d[j], zi);
+        for (int j = 0; j < kCoarse; ++j) zi = fmaf(zc[j], d[j], zi);
         z[i] = zi;
         if (init) p32[kX32 * c + k] = zi;
-        rz = r[i] * zi;
+        rz = rv * zi;
     }
     const double t = block_sum_f<kUT>(rz, sh);
     if (threadIdx.x == 0) red_rz[blockIdx.x] = t;
@@ -1573,6 +1669,8 @@ __global__ void __launch_bounds__(kVT) dot_partials(const double* __restrict__ a
 // x += alpha p, r -= alpha q, z = M r; partials r.r and r.z. Nine threads per camera.
 // With a coarse basis Z (learned form; Zc non-null) z is left to coarse_w /
 // coarse_z: this kernel writes the partials of Z^T r (kCoarse per block) instead.
+// Every load (partials, scalars, vectors, the M_c row or Z row) is issued
+// before the flag test.
 __global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* __restrict__ r,
                                                  float* __restrict__ z, const float* __restrict__ p32,
                                                  const float* __restrict__ q, const float* __restrict__ Minv, int C,
@@ -1583,14 +1681,32 @@ __global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* 
     __shared__ double sh[kUT / 32];
     __shared__ float rs[kUT];
     __shared__ double bc;
+    const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
+    const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
+    const long long n = 9ll * C, i = 9 * c + k;
+    const bool in = c < C;
+    const double pq_part = thread_partial_sum<kUT>(red_pq, n_pq);
+    const double rz_old = sc[S_RZ];
+    float m[9], xv = 0.f, pv = 0.f, qv = 0.f, rv = 0.f;
+    if (Zc) {
+        coarse_row(Zc, n, i, in, m);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) m[j] = in ? Minv[81 * c + 9 * k + j] : 0.f;
+    }
+    if (in) {
+        xv = x[i];
+        pv = p32[kX32 * c + k];
+        qv = q[i];
+        rv = r[i];
+    }
     if (block_flag(sc + S_DONE, &bc) != 0.0) return;
-    const double pq = ordered_sum_all<kUT>(red_pq, n_pq, sh, &bc);
+    const double pq = finish_sum_all<kUT>(pq_part, sh, &bc);
     const bool first = blockIdx.x == 0 && threadIdx.x == 0;
     if (!(pq > 0.0) || !isfinite(pq)) {
         if (first) sc[S_DONE] = 2.0;  // breakdown: keep the current iterate
         return;
     }
-    const double rz_old = sc[S_RZ];
     const double alpha = rz_old / pq;
     if (first) {
         sc[S_ALPHA] = alpha;
@@ -1598,17 +1714,14 @@ __global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* 
         sc[S_ITERS] += 1.0;
     }
     const float af = static_cast<float>(alpha);
-    const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
-    const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
-    const long long i = 9 * c + k;
     float ri = 0.f;
-    if (c < C) {
-        x[i] = fmaf(af, p32[kX32 * c + k], x[i]);
-        ri = fmaf(-af, q[i], r[i]);
+    if (in) {
+        x[i] = fmaf(af, pv, xv);
+        ri = fmaf(-af, qv, rv);
         r[i] = ri;
     }
     if (Zc) {
-        coarse_partials(Zc, 9ll * C, i, ri, red_zr);
+        coarse_partials(m, ri, red_zr);
         const double a = block_sum_f<kUT>(ri * ri, sh);
         if (threadIdx.x == 0) red_rr[blockIdx.x] = a;
         return;
@@ -1616,8 +1729,11 @@ __global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* 
     rs[threadIdx.x] = ri;
     __syncthreads();
     float rz = 0.f;
-    if (c < C) {
-        const float zi = apply_minv_row(Minv, c, k, rs + 9 * cl);
+    if (in) {
+        const float* r9 = rs + 9 * cl;
+        float zi = 0.f;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) zi = fmaf(m[j], r9[j], zi);
         z[i] = zi;
         rz = ri * zi;
     }
@@ -1630,23 +1746,36 @@ __global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* 
 }
 
 // Convergence test and beta = rz / rz_prev (every block sums the partials in
-// the same order), then p = z + beta p (FP32, padded layout).
+// the same order), then p = z + beta p (FP32, padded layout). Every load is
+// issued before the flag test.
 __global__ void __launch_bounds__(kVT) pcg_direction(float* __restrict__ p32, const float* __restrict__ z, int n,
                                                     const double* __restrict__ red_rr,
                                                     const double* __restrict__ red_rz, int n_red, int max_iters,
                                                     double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
     __shared__ double bc;
+    const double rr_part = thread_partial_sum<kVT>(red_rr, n_red);
+    const double rz_part = thread_partial_sum<kVT>(red_rz, n_red);
+    const double tol2 = sc[S_TOL2], bb = sc[S_BB], iters = sc[S_ITERS], rz_prev = sc[S_RZPREV];
+    const int i = blockIdx.x * kVT + threadIdx.x;
+    float* pp = nullptr;
+    float zv = 0.f, pv = 0.f;
+    if (i < n) {
+        const int c = i / 9;
+        pp = p32 + static_cast<long long>(kX32) * c + (i - 9 * c);
+        zv = z[i];
+        pv = *pp;
+    }
     if (block_flag(sc + S_DONE, &bc) != 0.0) return;
-    const double rr = ordered_sum_all<kVT>(red_rr, n_red, sh, &bc);
-    const double rz = ordered_sum_all<kVT>(red_rz, n_red, sh, &bc);
+    const double rr = finish_sum_all<kVT>(rr_part, sh, &bc);
+    const double rz = finish_sum_all<kVT>(rz_part, sh, &bc);
     double done = 0.0;
-    if (rr <= sc[S_TOL2] * sc[S_BB] || sc[S_ITERS] >= max_iters) {
+    if (rr <= tol2 * bb || iters >= max_iters) {
         done = 1.0;
     } else if (!(rz > 0.0) || !isfinite(rz)) {
         done = 2.0;
     }
-    const double beta = rz / sc[S_RZPREV];
+    const double beta = rz / rz_prev;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         sc[S_RR] = rr;
         if (done != 0.0) {
@@ -1657,13 +1786,7 @@ __global__ void __launch_bounds__(kVT) pcg_direction(float* __restrict__ p32, co
         }
     }
     if (done != 0.0) return;
-    const float bf = static_cast<float>(beta);
-    const int i = blockIdx.x * kVT + threadIdx.x;
-    if (i < n) {
-        const int c = i / 9;
-        float* pp = p32 + static_cast<long long>(kX32) * c + (i - 9 * c);
-        *pp = fmaf(bf, *pp, z[i]);
-    }
+    if (i < n) *pp = fmaf(static_cast<float>(beta), pv, zv);
 }
 
 // x = 0, r = b (rounded to FP32), z = M r, p = z; partials b.b and r.z. Nine
@@ -1686,7 +1809,9 @@ __global__ void __launch_bounds__(kUT) pcg_init(float* __restrict__ x, float* __
         r[i] = ri;
     }
     if (Zc) {
-        coarse_partials(Zc, 9ll * C, i, ri, red_zr);
+        float zc[kCoarse];
+        coarse_row(Zc, 9ll * C, i, c < C, zc);
+        coarse_partials(zc, ri, red_zr);
         const double a = block_sum_f<kUT>(ri * ri, sh);
         if (threadIdx.x == 0) red_rr[blockIdx.x] = a;
         return;
