@@ -89,6 +89,16 @@ inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b -
 int device_sm_count();
 
 #ifdef __CUDACC__
+// Programmatic dependent launch (sm_90 and later). A kernel launched with the
+// programmatic stream serialization attribute may start while the kernel
+// before it in the stream is still finishing; pdl_wait() blocks until that
+// kernel has completed and its memory is visible, so every chained kernel
+// calls it before its first access to memory. pdl_trigger() lets the next
+// chained kernel be scheduled now (it then waits in its own pdl_wait()). In a
+// kernel launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Deterministic block-wide sum of one double per thread. Fixed shuffle tree
 // within each warp, then warp partials summed in warp order by warp 0.
 // `shared` holds at least blockDim.x/32 doubles. Result valid in thread 0.

@@ -616,6 +616,7 @@ __global__ void __launch_bounds__(32 * kMWarps) schur_matvec_warp(
     const int* __restrict__ acc_id, const float* __restrict__ Jc32, const float* __restrict__ Jp32, long long js,
     const float* __restrict__ vinv, const float* __restrict__ x, float* __restrict__ y,
     const double* __restrict__ done) {
+    pdl_wait();  // x: the previous kernel's direction
     if (done && *done != 0.0) return;
     const int wid = blockIdx.x * kMWarps + (threadIdx.x >> 5);
     if (wid >= n_wchunk) return;  // whole warps leave together
@@ -689,6 +690,7 @@ __global__ void __launch_bounds__(kPT) schur_matvec_long(
     __shared__ int pb[kMaxPts + 1], ps[kMaxPts], pid[kMaxPts];  // virtual begin, first real slot, point
     __shared__ float seg[kPT][3];
     __shared__ float wsh[kMaxPts][3];
+    pdl_wait();
     if (done && *done != 0.0) return;
     const int2 lc = lchunk[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31;
@@ -881,6 +883,8 @@ __global__ void __launch_bounds__(kVT) pcg_q_finalize_acc(float* __restrict__ y,
                                                          float* __restrict__ q, double* __restrict__ red,
                                                          const double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
+    pdl_wait();
+    pdl_trigger();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * (kVT / 32) + warp;
     const bool cam = c < C;
@@ -1114,6 +1118,8 @@ __global__ void __launch_bounds__(kUT) coarse_w(const float* __restrict__ r, con
     __shared__ double tsum[kCoarse], c1[kCoarse];
     __shared__ float c1f[kCoarse];
     __shared__ double bc;
+    pdl_wait();
+    pdl_trigger();
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
@@ -1155,6 +1161,8 @@ __global__ void __launch_bounds__(kUT) coarse_z(const float* __restrict__ r, con
     __shared__ double tsum[kCoarse], c2[kCoarse];
     __shared__ float d[kCoarse];
     __shared__ double bc;
+    pdl_wait();
+    pdl_trigger();
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
@@ -1681,6 +1689,8 @@ __global__ void __launch_bounds__(kUT) pcg_update(float* __restrict__ x, float* 
     __shared__ double sh[kUT / 32];
     __shared__ float rs[kUT];
     __shared__ double bc;
+    pdl_wait();
+    pdl_trigger();
     const int cl = threadIdx.x / 9, k = threadIdx.x % 9;
     const long long c = static_cast<long long>(blockIdx.x) * kUC + cl;
     const long long n = 9ll * C, i = 9 * c + k;
@@ -1754,6 +1764,8 @@ __global__ void __launch_bounds__(kVT) pcg_direction(float* __restrict__ p32, co
                                                     double* __restrict__ sc) {
     __shared__ double sh[kVT / 32];
     __shared__ double bc;
+    pdl_wait();
+    pdl_trigger();
     const double rr_part = thread_partial_sum<kVT>(red_rr, n_red);
     const double rz_part = thread_partial_sum<kVT>(red_rz, n_red);
     const double tol2 = sc[S_TOL2], bb = sc[S_BB], iters = sc[S_ITERS], rz_prev = sc[S_RZPREV];
@@ -2015,6 +2027,25 @@ __global__ void __launch_bounds__(kSL) sdiag_finalize_lane(const int* __restrict
 
 }  // namespace
 
+// Launch of a kernel of the PCG iteration chain with programmatic stream
+// serialization: it may be scheduled while the kernel before it finishes, and
+// waits for it in pdl_wait().
+template <typename... KArgs, typename... Args>
+static void launch_chained(void (*kernel)(KArgs...), int grid, int block, cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(grid));
+    cfg.blockDim = dim3(static_cast<unsigned>(block));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GBA_CUDA_CHECK(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...));
+    count_launch();
+}
+
 // Implicit product partials for a given x (FP32 or float-float arithmetic). x
 // is in the arithmetic type (FP32: the PCG direction copy; float-float: dc) or
 // null (then a = 1: the right-hand side). Partials in cam_part_ (9 per chunk).
@@ -2052,16 +2083,16 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
 static void implicit_parts_acc(Solver& s, const float* x, const double* done) {
     cudaEvent_t ev = s.prof_start();
     if (s.n_wchunk_ > 0) {
-        schur_matvec_warp<<<ceil_div(s.n_wchunk_, kMWarps), 32 * kMWarps, 0, s.stream_>>>(
-            reinterpret_cast<const int2*>(s.wchunk_.get()), s.n_wchunk_, s.s_cam_.get(), s.s_pt_.get(),
-            s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), x, s.y_acc_.get(), done);
-        GBA_LAUNCH_CHECK();
+        launch_chained(schur_matvec_warp, ceil_div(s.n_wchunk_, kMWarps), 32 * kMWarps, s.stream_,
+                       reinterpret_cast<const int2*>(s.wchunk_.get()), s.n_wchunk_, s.s_cam_.get(), s.s_pt_.get(),
+                       s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), x, s.y_acc_.get(),
+                       done);
     }
     if (s.n_lchunk_ > 0) {  // points with 33 to 256 observations, packed per CTA
-        schur_matvec_long<<<s.n_lchunk_, kPT, 0, s.stream_>>>(
-            reinterpret_cast<const int2*>(s.lchunk_.get()), s.lpts_.get(), s.pt_off_.get(), s.s_cam_.get(),
-            s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), x, s.y_acc_.get(), done);
-        GBA_LAUNCH_CHECK();
+        launch_chained(schur_matvec_long, s.n_lchunk_, kPT, s.stream_,
+                       reinterpret_cast<const int2*>(s.lchunk_.get()), s.lpts_.get(), s.pt_off_.get(),
+                       s.s_cam_.get(), s.acc_id_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_, s.Vinv32_.get(), x,
+                       s.y_acc_.get(), done);
     }
     if (s.n_huge_ > 0) {  // points with more than 256 observations, one range each
         schur_point_pass<float, false, false, true><<<s.n_huge_, kPT, 0, s.stream_>>>(
@@ -2212,9 +2243,8 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                 if (one_pass_) {
                     implicit_parts_acc(*this, pcg_p32_.get(), done);
                     cudaEvent_t fev = prof_start();
-                    pcg_q_finalize_acc<<<npq, kVT, 0, stream_>>>(y_acc_.get(), acc_off_.get(), ul32_.get(),
-                                                                 pcg_p32_.get(), C_, pcg_q_.get(), red_pq, sc);
-                    GBA_LAUNCH_CHECK();
+                    launch_chained(pcg_q_finalize_acc, npq, kVT, stream_, y_acc_.get(), acc_off_.get(),
+                                   ul32_.get(), pcg_p32_.get(), C_, pcg_q_.get(), red_pq, sc);
                     prof_stop("pcg_q_finalize", fev);
                 } else {
                     implicit_parts<float>(*this, pcg_p32_.get(), 0.0, done);
@@ -2224,23 +2254,18 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
                     GBA_LAUNCH_CHECK();
                     prof_stop("pcg_q_finalize", fev);
                 }
-                pcg_update<<<nub, kUT, 0, stream_>>>(pcg_e_.get(), pcg_r_.get(), pcg_z_.get(), pcg_p32_.get(),
-                                                     pcg_q_.get(), Pinv_.get(), C_, red_pq, npq, red, red2, sc, Zc,
-                                                     red_zr);
-                GBA_LAUNCH_CHECK();
+                launch_chained(pcg_update, nub, kUT, stream_, pcg_e_.get(), pcg_r_.get(), pcg_z_.get(),
+                               pcg_p32_.get(), pcg_q_.get(), Pinv_.get(), C_, red_pq, npq, red, red2, sc, Zc, red_zr);
                 if (coarse) {
                     cudaEvent_t cev = prof_start();
-                    coarse_w<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), csz32_.get(), Pinv_.get(), ceinv_.get(), C_,
-                                                       red_zr, nub, c1, pcg_z_.get(), red_szw, sc, 0);
-                    GBA_LAUNCH_CHECK();
-                    coarse_z<<<nub, kUT, 0, stream_>>>(pcg_r_.get(), Zc, ceinv_.get(), C_, red_szw, nub, c1,
-                                                       pcg_z_.get(), nullptr, red2, sc, 0);
-                    GBA_LAUNCH_CHECK();
+                    launch_chained(coarse_w, nub, kUT, stream_, pcg_r_.get(), csz32_.get(), Pinv_.get(),
+                                   ceinv_.get(), C_, red_zr, nub, c1, pcg_z_.get(), red_szw, sc, 0);
+                    launch_chained(coarse_z, nub, kUT, stream_, pcg_r_.get(), Zc, ceinv_.get(), C_, red_szw, nub,
+                                   c1, pcg_z_.get(), static_cast<float*>(nullptr), red2, sc, 0);
                     prof_stop("coarse_apply", cev);
                 }
-                pcg_direction<<<nvb, kVT, 0, stream_>>>(pcg_p32_.get(), pcg_z_.get(), n, red, red2, nub, max_iters,
-                                                        sc);
-                GBA_LAUNCH_CHECK();
+                launch_chained(pcg_direction, nvb, kVT, stream_, pcg_p32_.get(), pcg_z_.get(), n, red, red2, nub,
+                               max_iters, sc);
             }
             read_back({{h, sc, sizeof h}});
             if (h[S_DONE] != 0.0) break;
