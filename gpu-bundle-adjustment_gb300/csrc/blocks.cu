@@ -300,8 +300,10 @@ double Solver::back_substitute(double lambda) {
     return denom;
 }
 
+double* Solver::backsub_part() { return red_part_.get() + ceil_div(9ll * C_, kTB); }
+
 // dp, trial parameters and the gain denominator into scal_[2], without a host read.
-void Solver::backsub_launch(double lambda) {
+void Solver::backsub_launch(double lambda, bool reuse) {
     const int ncam = ceil_div(9ll * C_, kTB);
     double* part = red_part_.get();
     const bool mixed = form_ != SolverForm::Plain;
@@ -317,9 +319,10 @@ void Solver::backsub_launch(double lambda) {
                                                              lambda, dp_.get(), tpts_.get(), part + ncam);
         GBA_LAUNCH_CHECK();
         pts_ff_trial_ = false;
-    } else {
+    } else if (!(reuse && backsub_ready_ && !fast_solve_)) {
         mixed_back_substitute(*this, lambda, part + ncam);
-    }
+    }  // else: the last refinement check ran the point pass at this dc (dp, trial points, partials)
+    backsub_ready_ = false;
     prof_stop("backsub", ev);
     denom_finalize<<<1, kSumT, 0, stream_>>>(part, ncam, n_pchunk_, scal_.get() + 2);
     GBA_LAUNCH_CHECK();

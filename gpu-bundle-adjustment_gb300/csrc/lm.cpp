@@ -94,7 +94,7 @@ LMResult run_lm(Solver& s, const LMOptions& opts, Clock::time_point t0) {
                 }
                 double denom = 0.0, trial_sse = 0.0;
                 unsigned long long cost_anom = 0;
-                phase(res.t_backsub, [&] { s.backsub_launch(lambda); return 0; });
+                phase(res.t_backsub, [&] { s.backsub_launch(lambda, true); return 0; });
                 phase(res.t_cost, [&] {
                     s.zero_cost_scratch();
                     s.trial_cost_launch(s.counters_.get() + 2);

@@ -263,7 +263,8 @@ struct BacksubOut {
 // null for the right-hand side; z = sum_e Jp^T Jc x + a bp. V'^-1 from its FP32
 // copy (+ low parts for float-float). u is written at the slot's camera-major
 // position so that the camera pass reads it contiguously. With kBack (a = -1,
-// xt = dc): w = -dp, and the pass ends with the back-substitution outputs.
+// xt = dc): w = -dp, and the pass ends with the back-substitution outputs
+// (and, when u_cm is given, also stores u = Jp w = -Jp dp).
 // kRhs: the right-hand side instantiation (xt = null, a = 1, also G).
 template <typename T, bool kBack = false, bool kRhs = false, bool kAcc = false>
 __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack ? 4 : 5)) schur_point_pass(const int4* __restrict__ prange, const int* __restrict__ pchunk, const int* __restrict__ pt_off,
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(kPT, sizeof(T) == 4 ? (kBack ? 6 : 8) : (kBack
             bk.tpts[3ll * p0 + i] = bout[3 * kPT + i];
             bk.tpts_ff[3ll * p0 + i] = bff[i];
         }
-        return;
+        if (!u_cm) return;
     }
     __syncthreads();
     // u_e = Jp_e w_p for every slot of the chunk, stored camera-major (kAcc:
@@ -2078,6 +2079,19 @@ static void implicit_parts(Solver& s, const T* x, double a, const double* done) 
     }
 }
 
+// Camera pass of a float-float product whose u the point pass has stored:
+// partials of sum Jc^T u per camera chunk in cam_part_.
+static void camera_parts_ff(Solver& s) {
+    if (s.n_cchunk_ == 0) return;
+    cudaEvent_t ev = s.prof_start();
+    schur_camera_pass<ff><<<s.n_cchunk_, kCT, 0, s.stream_>>>(s.cchunk_begin_.get(), s.cchunk_cam_.get(),
+                                                             s.cam_off_.get(), s.J32c_.get(),
+                                                             reinterpret_cast<const ff*>(s.u_.get()),
+                                                             s.cam_part_.get(), nullptr, nullptr);
+    GBA_LAUNCH_CHECK();
+    s.prof_stop("schur_camera_pass_ff", ev);
+}
+
 // The one-pass FP32 product (schur_point_pass with kAcc): y = sum over slots of
 // Jc^T u, accumulated in device memory (acc_id_: the slot's accumulator).
 static void implicit_parts_acc(Solver& s, const float* x, const double* done) {
@@ -2113,9 +2127,10 @@ void launch_split_ff(const double* x, long long n, float* out, cudaStream_t s) {
 // Mixed-form back-substitution: the point pass in back-substitution mode (dp,
 // trial points and their float-float split, denominator partials per chunk),
 // in the arithmetic of the last Schur solve: FP32 after a loose solve,
-// float-float otherwise. The camera step kernel has written dc in that
-// arithmetic (pcg_p32_ padded FP32, or dcff_).
-void mixed_back_substitute(Solver& s, double lambda, double* part) {
+// float-float otherwise. dc is in that arithmetic (pcg_p32_ padded FP32, or
+// dcff_). with_u (float-float only): also u = -Jp dp per slot into u_, for the
+// camera pass of the refinement check.
+void mixed_back_substitute(Solver& s, double lambda, double* part, bool with_u) {
     const BacksubOut bk{s.V_.get(), s.pts_.get(),
                         make_float2(static_cast<float>(lambda), static_cast<float>(lambda - static_cast<float>(lambda))),
                         s.dp_.get(), s.tpts_.get(), reinterpret_cast<float2*>(s.pts_ff_.get()), part};
@@ -2127,7 +2142,7 @@ void mixed_back_substitute(Solver& s, double lambda, double* part) {
         schur_point_pass<ff, true><<<s.n_pchunk_, kPT, 0, s.stream_>>>(
             reinterpret_cast<const int4*>(s.pchunk4_.get()), s.pchunk_.get(), s.pt_off_.get(), s.s_cam_.get(), s.s_pt_.get(), s.cam_pos_.get(), s.Jc32_.get(), s.Jp32_.get(), s.js_,
             s.Vinv32_.get(), s.Vinv32lo_.get(), s.bp_.get(), reinterpret_cast<const ff*>(s.dcff_.get()), -1.0,
-            nullptr, nullptr, bk, nullptr);
+            with_u ? reinterpret_cast<ff*>(s.u_.get()) : nullptr, nullptr, bk, nullptr);
     }
     GBA_LAUNCH_CHECK();
     s.ff_holds_ = Solver::kFfNone;  // pts_ff_ holds the trial points now
@@ -2155,6 +2170,7 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
     // targets use float-float products for both and an explicit residual.
     const bool fast = opts.refine_tol >= kLooseTol;
     fast_solve_ = fast;
+    backsub_ready_ = false;
     if (fast) {
         implicit_parts<float>(*this, static_cast<const float*>(nullptr), 1.0, nullptr);
     } else {
@@ -2368,10 +2384,29 @@ PcgStats Solver::schur_pcg(double lambda, const LMOptions& opts, bool learned, u
         // dc += e; residual r = rhs - S dc in float-float products, FP64 sums
         axpy_split_kernel<<<nvb, kVT, 0, stream_>>>(dc_.get(), pcg_e_.get(), n, dcff_.get());
         GBA_LAUNCH_CHECK();
-        implicit_parts<ff>(*this, reinterpret_cast<const ff*>(dcff_.get()), 0.0, nullptr);
-        residual_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
-                                                    dc_.get(), rhs_.get(), C_, ref_r_.get(), red);
-        GBA_LAUNCH_CHECK();
+        if (step == 0 || fast) {
+            implicit_parts<ff>(*this, reinterpret_cast<const ff*>(dcff_.get()), 0.0, nullptr);
+            residual_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
+                                                        dc_.get(), rhs_.get(), C_, ref_r_.get(), red);
+            GBA_LAUNCH_CHECK();
+            backsub_ready_ = false;
+        } else {
+            // A later step usually ends the refinement (float-float targets),
+            // so its check runs the back-substitution: with
+            // dp = V'^-1 (bp - W^T dc) the residual rhs - S dc equals
+            // bc - U_lambda dc - W dp, and the point pass of the
+            // back-substitution (dp, trial points, denominator partials) also
+            // stores u = -Jp dp, whose camera pass sums are -W dp. The
+            // back-substitution of the trial then reuses this pass.
+            cudaEvent_t bev = prof_start();
+            mixed_back_substitute(*this, lambda, backsub_part(), true);
+            prof_stop("backsub", bev);
+            camera_parts_ff(*this);
+            residual_finalize<<<nvb, kVT, 0, stream_>>>(cam_chunk_off_.get(), cam_part_.get(), U_.get(), lambda,
+                                                        dc_.get(), bc_.get(), C_, ref_r_.get(), red);
+            GBA_LAUNCH_CHECK();
+            backsub_ready_ = true;
+        }
         sum_to_scalar<<<1, 256, 0, stream_>>>(red, nvb, sc, S_NORM);
         GBA_LAUNCH_CHECK();
         read_back({{&rnorm2, sc + S_NORM, sizeof rnorm2}});

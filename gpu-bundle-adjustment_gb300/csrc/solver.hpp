@@ -147,7 +147,12 @@ public:
     // read_trial() of the denominator, the SSE and that count.
     void damp_launch(double lambda);
     PcgStats schur_pcg(double lambda, const LMOptions& opts, bool learned, unsigned long long* nonspd_out);
-    void backsub_launch(double lambda);
+    // reuse: the LM driver's trial, where schur_pcg's last refinement check may
+    // already have run the point pass at this dc and lambda (backsub_ready_).
+    void backsub_launch(double lambda, bool reuse = false);
+    // Where the point pass writes its denominator partials (after the camera ones).
+    double* backsub_part();
+    bool backsub_ready_ = false;
     void trial_cost_launch(unsigned long long* anomalies);
     void read_trial(double* denom, double* sse, unsigned long long* cost_anomalies);
     void add_nonspd(unsigned long long n);     // adds to the cumulative non-SPD count
@@ -351,7 +356,7 @@ void launch_split_ff(const double* x, long long n, float* out, cudaStream_t s);
 
 // Mixed-form back-substitution (pcg.cu): dp, trial points and the point terms
 // of the gain denominator (one partial per point chunk in part).
-void mixed_back_substitute(Solver& s, double lambda, double* part);
+void mixed_back_substitute(Solver& s, double lambda, double* part, bool with_u = false);
 
 void launch_batch_chol9_factor_solve(const double* A, const double* b, double* x, int* ok, int n,
                                      cudaStream_t s);
