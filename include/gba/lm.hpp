@@ -21,12 +21,13 @@ enum class SolverForm {
     // factored by the blocked FP64 tensor-core (DMMA) Cholesky. The drop-in.
     Plain = 0,
     // FP32 residuals/Jacobians with FP64 accumulation; S never formed: FP32
-    // implicit matvecs inside block-Jacobi PCG, wrapped in iterative
-    // refinement to LMOptions::refine_tol. Where the plain form is FP64 the
-    // cost evaluation (accept / reject), the refinement residual, the
-    // right-hand side and the 3x3 point inverses V'^-1 run in float-float
-    // arithmetic (unevaluated sums of two FP32 numbers, ~48-bit significands,
-    // on GB300's FP32 pipe) with FP64 sums: the cost agrees with the FP64 cost
+    // implicit matvecs inside block-Jacobi PCG (FP32 vectors, FP64 scalars),
+    // wrapped in iterative refinement to LMOptions::refine_tol. Where the
+    // plain form is FP64 the cost evaluation (accept / reject), the
+    // refinement residual, the right-hand side, the back-substitution and the
+    // 3x3 point inverses V'^-1 run in float-float arithmetic (unevaluated sums
+    // of two FP32 numbers, ~48-bit significands, on GB300's FP32 pipe) with
+    // FP64 sums: the cost agrees with the FP64 cost
     // to ~1e-12 relative and a cost term whose residual leaves FP32's range is
     // recomputed in FP64 (tests/test_gpu_mixed.py). With refine_tol >= 1e-3
     // (inexact Newton steps) the right-hand side and back-substitution are FP32.

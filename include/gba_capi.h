@@ -195,7 +195,10 @@ int gba_solver_set_schur_layout(gba_solver* s, int layout);
  * a band, the camera order (perm[c] = position of camera c). [host] band_rows,
  * band_tiles (may be NULL), perm (C ints, may be NULL). */
 int gba_solver_schur_band(gba_solver* s, int* band_rows, int* band_tiles, int* perm);
-/* Mixed forms: PCG + FP64 refinement (no reference counterpart). */
+/* Mixed forms: PCG + FP64 refinement (no reference counterpart). Its last
+ * refinement check of a float-float target runs the back-substitution's point
+ * pass; gba_solver_back_substitute recomputes it (only the solver's own LM
+ * loop reuses it). */
 int gba_solver_schur_pcg(gba_solver* s, double lambda, const gba_lm_options* opts, int learned,
                          long long* out_pcg_iters, int* out_refine_steps, double* out_rel_residual);
 /* Back-substitution, gain denominator, trial parameters (reference src/lm.cu:606-654). */
