@@ -79,6 +79,32 @@ def test_pcg_deterministic(gba, small):
     assert np.array_equal(out[0], out[1])
 
 
+def test_lm_trial_reuses_the_refinement_back_substitution(gba, small):
+    """The LM driver's trial skips the back-substitution's point pass when the
+    last refinement check already ran it at the same dc. The trial is the same
+    as the stage functions' (which always recompute it): bit-identical trial
+    parameters and cost, in the deterministic two-pass product."""
+    lam = 1e-3
+    opts = dict(refine_tol=1e-10, pcg_tol=1e-3, pcg_max_iters=500, refine_max_steps=12)
+    with gba.Solver(small, "mixed") as s:
+        res = s.run(max_iterations=1, initial_lambda=lam, deterministic=1, **opts)
+        cams_lm, pts_lm = s.get_params()
+    assert res.iterations == 1 and res.trials == 1  # the first trial was accepted
+    assert res.refine_steps >= 2  # a later step's check ran the back-substitution
+    with gba.Solver(small, "mixed") as s:
+        assert not s.set_matvec("two-pass")
+        s.accumulate()
+        assert s.damp_invert_v(lam) == 0
+        _, steps, relres = s.schur_pcg(lam, **opts)
+        s.back_substitute(lam)
+        trial = s.trial_cost()
+        s.accept()
+        cams, pts = s.get_params()
+    assert steps == res.refine_steps and relres <= 1e-10
+    assert np.array_equal(cams, cams_lm) and np.array_equal(pts, pts_lm)
+    assert trial / 2.0 == res.final_cost  # trial_cost() is the SSE, final_cost SSE / 2
+
+
 def test_mixed_lm_reaches_oracle_cost_workload1(gba, oracle):
     prob = gba.synthetic(1)
     ref, _, _ = oracle.solve(prob, max_iterations=20)
