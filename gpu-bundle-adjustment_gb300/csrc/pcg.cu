@@ -27,9 +27,13 @@
 // are the 9x9 diagonal blocks S_cc (FP32 products, FP64 sums, FP64 Cholesky,
 // explicit inverses); the learned form adds a coarse-space correction whose
 // basis the MLP predicts (mlp.cu; the balancing two-level preconditioner
-// below). PCG vectors and dot products are FP64 with
-// deterministic reductions; all PCG control scalars live on the device and the
-// host polls a convergence flag after batches of iterations.
+// below). The PCG vectors are FP32; its scalars and the sums of block
+// partials are FP64, reduced in a fixed order; all PCG control scalars live on
+// the device and the host polls a convergence flag after batches of
+// iterations. The kernels of an iteration are chained with programmatic
+// dependent launch. The last refinement check of a trial (float-float
+// targets) runs the back-substitution's point pass, which the trial then
+// reuses.
 //
 // No reference counterpart: the reference solves S densely on the host.
 
@@ -1658,7 +1662,6 @@ __global__ void __launch_bounds__(kEinvT) coarse_einv_kernel(const double* __res
     if (threadIdx.x == 0) einv[KK] = 1.0;
 }
 
-// Block partials of a . b (FP64).
 // Block partials of a . b, a FP64 and b FP32 (b . x of the inner solution).
 __global__ void __launch_bounds__(kVT) dot_partials(const double* __restrict__ a, const float* __restrict__ b, int n,
                                                    double* __restrict__ red) {
