@@ -177,6 +177,42 @@ def test_oracle_schur_step_matches_dense_normal_equations(gba, oracle):
     assert rel_err(st["dp"], x[9 * C:]) < 1e-8
 
 
+def test_back_substitution_residual_identity(gba, oracle):
+    """The identity behind the mixed forms' last refinement check: for any dc,
+    with dp = V'^-1 (bp - W^T dc), the Schur residual rhs - S dc equals
+    bc - U_lambda dc - W dp (numpy FP64 on the oracle's normal equations)."""
+    prob = gba.synthetic_custom(5, 200, 2, 5, 1.5, seed=11)
+    lam = 1e-3
+    ne = oracle.accumulate(prob)
+    C, P = prob.num_cameras, prob.num_points
+    U = ne["U"].copy()
+    V = ne["V"].copy()
+    for c in range(C):
+        d = np.diag(U[c]).copy()
+        U[c][np.diag_indices(9)] += lam * np.where(d > 0, d, 1e-12)
+    for q in range(P):
+        d = np.diag(V[q]).copy()
+        V[q][np.diag_indices(3)] += lam * np.where(d > 0, d, 1e-12)
+    Vinv = np.linalg.inv(V)
+    W = np.zeros((9 * C, 3 * P))
+    for e in range(prob.num_observations):
+        c, q = prob.obs_camera[e], prob.obs_point[e]
+        W[9 * c:9 * c + 9, 3 * q:3 * q + 3] += ne["W"][e]
+    Ub = np.zeros((9 * C, 9 * C))
+    Vb = np.zeros((3 * P, 3 * P))
+    for c in range(C):
+        Ub[9 * c:9 * c + 9, 9 * c:9 * c + 9] = U[c]
+    for q in range(P):
+        Vb[3 * q:3 * q + 3, 3 * q:3 * q + 3] = Vinv[q]
+    S = Ub - W @ Vb @ W.T
+    rhs = ne["bc"] - W @ Vb @ ne["bp"]
+    dc = np.random.default_rng(2).standard_normal(9 * C) * 1e-3
+    dp = Vb @ (ne["bp"] - W.T @ dc)
+    lhs = rhs - S @ dc
+    rhs_form = ne["bc"] - Ub @ dc - W @ dp
+    assert np.linalg.norm(lhs - rhs_form) <= 1e-12 * max(np.linalg.norm(ne["bc"]), np.linalg.norm(Ub @ dc))
+
+
 def test_oracle_lm_converges_on_small_problem(gba, oracle):
     prob = gba.synthetic_custom(6, 400, 2, 6, 1.5, seed=4)
     res, _, _ = oracle.solve(prob, max_iterations=30, threads=2)
